@@ -1,0 +1,369 @@
+"""Benchmark of the split-step propagation engine on the Green's-function workload.
+
+Workload (one step): computeGreensFunction of Chi2PDC with nFreqs=1024, nZSteps=1000,
+relativeLength=1, nlLength=0.5, Gaussian pump (beta2=1), signal beta2s=0.5, beta1s=2,
+beta3s=0.1, poling period 20 z steps: 2*1024 impulse propagations, C and S 1024x1024 complex128.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is the device-resident throughput (propagations/s,
+C and S left in HBM); `e2e` is the same metric through the public drop-in API
+(computeGreensFunction returning numpy arrays, C/S copied to host every step).  The CPU
+baseline is the numpy oracle (a restatement of the reference's algorithm: the reference's
+C++ engine cannot be built without the Eigen headers) on a bounded sample of the same
+impulses.  Under torchrun every rank computes its own copy of the workload (weak scaling).
+"""
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Green's-fn propagations/s at 1e-9 rel err: batched vs plain GPU; grad/fwd cost"
+UNIT = "propagations/s"
+CONFIG = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0, beta1s=2, beta3=0,
+              beta3s=0.1, diffBeta0=0, tMax=40, tPrecision=1024, zPrecision=500)
+N_DOMAINS = 100
+C_SOLVER = 80          # point-wise flops per mode per step of Chi2PDC's DiffEq (fixed, not tuned)
+
+
+def algorithmic_flops(n_inst, n_z, n, modes=1, c_solver=C_SOLVER):
+    """F = n_inst (nZ-1) modes (10 N log2 N + c N): two FFTs of 5 N log2 N plus the point-wise work."""
+    return n_inst * (n_z - 1) * modes * (10 * n * math.log2(n) + c_solver * n)
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ----------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------------
+# oracle: impulse propagations of the workload (CPU baseline and the parity sample)
+# ----------------------------------------------------------------------------------------------
+def _oracle_medium():
+    from oracle import nlm_oracle as O
+    med = O.Chi2PDC(poling=np.ones(N_DOMAINS), **CONFIG)
+    med.run_pump_simulation()
+    return med
+
+
+def oracle_columns(med, bins):
+    """Columns b' = (b + N/2) mod N of C and S for impulse bins b, from 2 propagations per bin."""
+    n = med.n_freqs
+    bins = np.asarray(bins)
+    prof = np.zeros((bins.size, n), dtype=np.complex128)
+    prof[np.arange(bins.size), bins] = 1.0
+    f1, _ = med.propagate(prof, False, 0)
+    fi, _ = med.propagate(1j * prof, False, 0)
+    o1, oi = f1[:, 0], fi[:, 0]
+    pre_c = 0.5 * o1 - 0.5j * oi
+    pre_s = 0.5 * o1 + 0.5j * oi
+    return np.fft.fftshift(pre_c, axes=1).T, np.fft.fftshift(pre_s, axes=1).T
+
+
+def _oracle_worker(bins):
+    med = _oracle_medium()
+    t0 = time.perf_counter()
+    oracle_columns(med, bins)
+    return time.perf_counter() - t0
+
+
+def cpu_oracle_rate(n_bins, processes=1):
+    """Propagations/s of the oracle on n_bins impulse pairs (2 n_bins propagations)."""
+    rng = np.random.default_rng(0)
+    bins = rng.choice(CONFIG["tPrecision"], size=n_bins, replace=False)
+    if processes <= 1:
+        dt = _oracle_worker(bins)
+        return 2 * n_bins / dt, dt
+    chunks = np.array_split(bins, processes)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes) as pool:
+        pool.map(_oracle_worker, [c[:1] for c in chunks])   # warm the workers (imports, pump)
+        t0 = time.perf_counter()
+        pool.map(_oracle_worker, chunks)
+        dt = time.perf_counter() - t0
+    return 2 * n_bins / dt, dt
+
+
+# ----------------------------------------------------------------------------------------------
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def read_profile_traffic():
+    path = os.path.join(ROOT, "profiles", "k_propagate_linear_green_n1024.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch_full:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_bins = args.ref_bins or 8 * cores
+    for _ in range(args.warmup):
+        cpu_oracle_rate(max(cores, 1), cores)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, dt = cpu_oracle_rate(n_bins, cores)
+        rates.append(r)
+        times.append(dt)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 2048 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "Chi2PDC computeGreensFunction N=1024 nZSteps=1000 (2048 propagations)",
+                   "global_batch": 2048, "seq_len": 1000, "parallelism": "cpu-processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d impulse propagations per step (of 2048), %d spawn processes; numpy oracle "
+                                   "(restatement: the reference C++ engine needs Eigen, absent)" % (2 * n_bins, cores)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from multimodenonlinearoptics_gb300 import build_ext
+    build_ext.build()
+    from multimodenonlinearoptics_gb300 import nonlinearmedium as nlm
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    med = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **CONFIG)
+    n = med._dims["nFreqs"]
+    n_z = med._dims["nZSteps"]
+    n_inst = 2 * n
+    stream = torch.cuda.Stream()
+    med._set_stream(stream.cuda_stream)
+    peak = nlm.fp64_peak_tflops()
+    C = torch.empty((n, n), dtype=torch.complex128, device="cuda")
+    S = torch.empty_like(C)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
+
+    def green_device():
+        nlm._check(nlm._lib.nlm_green_device(med._h(), 0, 1, 1, 0, None, 0, None, 0, C.data_ptr(), S.data_ptr()))
+
+    # warm-up (also builds the kernel schedule and the propagator)
+    for _ in range(args.warmup):
+        green_device()
+    torch.cuda.synchronize()
+
+    # device-resident throughput
+    barrier()
+    med._kernel_timing(1)
+    launches = 0
+    elapsed = 0.0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            green_device()
+            e1.record(stream)
+            e1.synchronize()
+            elapsed += e0.elapsed_time(e1) / 1e3
+            launches += med._launch_count()
+    kernel_ms, kernel_count = med._kernel_timing(0)
+    barrier()
+    t_dev = max_over_ranks(elapsed)
+    value = world * n_inst * args.steps / t_dev
+
+    # end to end through the public API: numpy C and S on the host every step
+    barrier()
+    e2e_elapsed = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        Ch, Sh = med.computeGreensFunction()
+        e1.record(stream)
+        e1.synchronize()
+        e2e_elapsed += e0.elapsed_time(e1) / 1e3
+    barrier()
+    t_e2e = max_over_ranks(e2e_elapsed)
+    e2e_value = world * n_inst * args.steps / t_e2e
+
+    # plain form: one propagation per kernel launch, on a sample of the impulses
+    plain = None
+    if args.plain_sample > 0:
+        Cp = np.empty((n, n), dtype=np.complex128)
+        Sp = np.empty_like(Cp)
+        nlm._check(nlm._lib.nlm_green_plain(med._h(), 0, 0, 2, nlm._dptr(Cp.view(np.float64)),
+                                            nlm._dptr(Sp.view(np.float64))))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nlm._check(nlm._lib.nlm_green_plain(med._h(), 0, 0, args.plain_sample, nlm._dptr(Cp.view(np.float64)),
+                                            nlm._dptr(Sp.view(np.float64))))
+        t_plain = time.perf_counter() - t0
+        plain = args.plain_sample / t_plain
+
+    line = None
+    if rank == 0:
+        # CPU baseline and parity sample: oracle impulse propagations of the same workload
+        cpu = None
+        parity = None
+        if args.cpu_bins > 0:
+            ref = _oracle_medium()
+            rng = np.random.default_rng(0)
+            bins = rng.choice(n, size=args.cpu_bins, replace=False)
+            t0 = time.perf_counter()
+            cc, ss = oracle_columns(ref, bins)
+            dt = time.perf_counter() - t0
+            cols = (bins + n // 2) % n
+            parity = max(np.linalg.norm(Ch[:, cols] - cc) / np.linalg.norm(cc),
+                         np.linalg.norm(Sh[:, cols] - ss) / np.linalg.norm(ss))
+            cpu = {"value": 2 * args.cpu_bins / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": "%d of the 2048 impulse propagations (%d bins x {1, i}), numpy oracle, 1 thread"
+                             % (2 * args.cpu_bins, args.cpu_bins)}
+        flops = algorithmic_flops(n_inst, n_z, n)
+        avg_kernel_s = kernel_ms / max(kernel_count, 1) / 1e3
+        achieved = flops / avg_kernel_s / 1e12
+        traffic = read_profile_traffic()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "Chi2PDC computeGreensFunction N=1024 nZSteps=1000 (2048 impulse propagations, "
+                                   "C and S 1024x1024 complex128)",
+                       "global_batch": n_inst * world, "seq_len": n_z, "parallelism": "replica-per-gpu",
+                       "l2": "256 MB buffer written between timed steps (outside the events)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16,
+                    "d2h_bytes_per_step": 2 * n * n * 16,
+                    "api": "nonlinearmedium.Chi2PDC.computeGreensFunction() -> numpy C, S"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "kernel": "k_propagate_linear<1,8>", "kernel_ms": 1e3 * avg_kernel_s,
+                         "algorithmic_flops_per_launch": flops,
+                         "peak_source": "FP64 FMA chains measured in this run (MEASURED_PEAKS.json has no FP64 entry)"},
+            "cpu_baseline": cpu,
+            "plain": {"value": plain, "unit": UNIT, "sample": args.plain_sample,
+                      "form": "one propagation per kernel launch"},
+            "batched_over_plain": (value / plain) if plain else None,
+            "parity_sample_rel_err": parity,
+            "clocks": clocks.summary(),
+        }
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-sample", type=int, default=16)
+    ap.add_argument("--cpu-bins", type=int, default=64)
+    ap.add_argument("--ref-bins", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

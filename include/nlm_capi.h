@@ -1,0 +1,196 @@
+/*
+ * nlm_capi.h -- C ABI of the GB300 split-step propagation engine.
+ *
+ * This is the drop-in boundary for the propagation path of the `nonlinearmedium`
+ * module of MultimodeNonlinearOptics.  Every entry point below replaces one method of
+ * the reference's pybind11 API (src/nlmModulePy.cpp) and is what a binding of that
+ * API binds to (the Python binding shipped with this library is a ctypes layer over
+ * these functions).
+ *
+ * Conventions
+ *  - Complex arrays are interleaved double pairs (re, im), i.e. numpy complex128,
+ *    row-major, in FFT order exactly like the reference (src/_NonlinearMedium.cpp:121-124).
+ *  - All host buffers are owned by the caller; device buffers are owned by the handle.
+ *  - Every function returns an nlm_status.  On error, nlm_last_error() returns a
+ *    thread-local message.  NLM_ERR_INVALID_ARGUMENT corresponds to the reference's
+ *    std::invalid_argument (Python ValueError), NLM_ERR_RUNTIME to std::runtime_error
+ *    (RuntimeError), NLM_ERR_INDEX to std::out_of_range (IndexError).
+ *  - A handle is not thread-safe; different handles may be used from different threads.
+ *  - No call falls back to a CPU implementation: a call that needs the GPU returns
+ *    NLM_ERR_NO_DEVICE when no CUDA device is usable.
+ */
+#ifndef NLM_CAPI_H
+#define NLM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nlm_status {
+  NLM_OK = 0,
+  NLM_ERR_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument -> ValueError        */
+  NLM_ERR_RUNTIME = 2,          /* reference: std::runtime_error     -> RuntimeError      */
+  NLM_ERR_INDEX = 3,            /* reference: std::out_of_range      -> IndexError        */
+  NLM_ERR_CUDA = 4,             /* CUDA runtime error                                     */
+  NLM_ERR_NO_DEVICE = 5,        /* no usable CUDA device: there is no CPU fallback        */
+  NLM_ERR_UNSUPPORTED = 6,      /* a grid size this engine does not implement             */
+  NLM_ERR_TIMEOUT = 7           /* a bounded device-side wait gave up                     */
+} nlm_status;
+
+typedef struct nlm_medium nlm_medium;   /* one solver instance (or a Cascade)            */
+
+/* Pulse and intensity-profile enums, same values as src/_NonlinearMedium.hpp:25-34. */
+enum { NLM_GAUSSIAN = 0, NLM_SECH = 1, NLM_SINC = 2 };
+enum { NLM_GAUSSIAN_BEAM = 0, NLM_CONSTANT = 1, NLM_GAUSSIAN_APODIZATION = 2 };
+
+/* Last error message of the calling thread (never NULL). */
+const char* nlm_last_error(void);
+
+/* Library version string. */
+const char* nlm_version(void);
+
+/* Number of registered solvers and their names, in the order of
+ * solvers/RegisteredSolvers.hpp:1-16. */
+int nlm_solver_count(void);
+const char* nlm_solver_name(int index);
+/* Scalar constructor arguments of a solver, in the reference's positional order with
+ * the array arguments (customPump, poling) removed.  Names are separated by ',' and
+ * each carries its default after '=' when it has one; "inf" denotes infinity. */
+const char* nlm_solver_signature(const char* solver);
+
+/* --- construction (solver ctors, e.g. solvers/Chi2PDC.cpp:18-24 and their py::init,
+ *     solvers/Chi2PDC.cpp:51-60; base ctor src/_NonlinearMedium.cpp:8-40) ------------ */
+/* args: the solver's scalar constructor arguments in nlm_solver_signature order
+ * (enums and integers passed as doubles).  custom_pump: N complex values or NULL/0.
+ * poling: domain lengths or NULL/0.  Host-side setup only: no device is touched. */
+nlm_status nlm_create(const char* solver, const double* args, size_t nargs,
+                      const double* custom_pump, size_t n_custom_pump,
+                      const double* poling, size_t n_poling, nlm_medium** out);
+nlm_status nlm_destroy(nlm_medium* medium);
+
+/* Solver properties. */
+nlm_status nlm_info(const nlm_medium* m, int* n_signal_modes, int* n_pump_modes,
+                    int* n_freqs, int* n_z_steps, int* n_z_steps_p, int* fully_nonlinear,
+                    int* is_cascade);
+/* dz, dzp, z, tMax (src/_NonlinearMedium.hpp:94-100). */
+nlm_status nlm_lengths(const nlm_medium* m, double* z, double* dz, double* dzp, double* t_max);
+
+/* --- setPump overloads (src/_NonlinearMedium.cpp:180-222, 506-534) ---------------- */
+nlm_status nlm_set_pump_type(nlm_medium* m, int pulse_type, double chirp, double delay,
+                             unsigned pump_index);
+nlm_status nlm_set_pump_custom(nlm_medium* m, const double* custom_pump, size_t n,
+                               double chirp, double delay, unsigned pump_index);
+nlm_status nlm_set_pump_from(nlm_medium* m, const nlm_medium* other, unsigned mode_index,
+                             double delay, unsigned pump_index);
+
+/* --- runPumpSimulation (src/_NonlinearMedium.cpp:225-250, solvers/Chi3.cpp:41-70) ---- */
+nlm_status nlm_run_pump(nlm_medium* m);
+
+/* --- runSignalSimulation (src/_NonlinearMedium.cpp:253-260) --------------------------
+ * Fills the handle's signal grids (nZSteps x N per mode); read them with nlm_get_grid. */
+nlm_status nlm_run_signal(nlm_medium* m, const double* input_prof, size_t n,
+                          int in_time_domain, unsigned input_mode);
+
+/* --- computeGreensFunction (src/_NonlinearMedium.cpp:263-375) ------------------------
+ * use_input/use_output: 0/1 lists (may be NULL/0 for "all modes").  First call
+ * nlm_green_dims to validate and obtain the matrix shape (rows x cols), then nlm_green
+ * with caller buffers of rows*cols complex values each.  n_threads is accepted for API
+ * parity and validated like the reference; the work runs on the GPU.                  */
+nlm_status nlm_green_dims(nlm_medium* m, unsigned n_threads, const uint8_t* use_input,
+                          size_t n_use_input, const uint8_t* use_output, size_t n_use_output,
+                          size_t* rows, size_t* cols);
+nlm_status nlm_green(nlm_medium* m, int in_time_domain, int run_pump, unsigned n_threads,
+                     int normalize, const uint8_t* use_input, size_t n_use_input,
+                     const uint8_t* use_output, size_t n_use_output, double* green_c,
+                     double* green_s);
+/* Same computation with C and S written to DEVICE memory (CUDA pointers on the
+ * handle's device), for callers that keep the matrices resident in HBM. */
+nlm_status nlm_green_device(nlm_medium* m, int in_time_domain, int run_pump, unsigned n_threads,
+                            int normalize, const uint8_t* use_input, size_t n_use_input,
+                            const uint8_t* use_output, size_t n_use_output, void* green_c_dev,
+                            void* green_s_dev);
+
+/* --- batchSignalSimulation (src/_NonlinearMedium.cpp:378-444;
+ *     src/_FullyNonlinearMedium.hpp:8-11 where run_pump is ignored) -------------------
+ * inputs: rows x cols complex.  Output: rows x (nOut*N) complex; nlm_batch_dims gives
+ * nOut*N.                                                                              */
+nlm_status nlm_batch_dims(nlm_medium* m, size_t rows, size_t cols, unsigned n_threads,
+                          unsigned input_mode, const uint8_t* use_output, size_t n_use_output,
+                          size_t* out_cols);
+nlm_status nlm_batch(nlm_medium* m, const double* inputs, size_t rows, size_t cols,
+                     int in_time_domain, int run_pump, unsigned n_threads, unsigned input_mode,
+                     const uint8_t* use_output, size_t n_use_output, double* out);
+/* Device-resident variant: inputs and outputs are CUDA pointers. */
+nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, size_t cols,
+                            int in_time_domain, int run_pump, unsigned n_threads,
+                            unsigned input_mode, const uint8_t* use_output, size_t n_use_output,
+                            void* out_dev);
+
+/* --- ragged batch: several media, one seeded signal each, one launch --------------
+ * No counterpart method in the reference (it would loop over media calling
+ * batchSignalSimulation one row at a time, src/_NonlinearMedium.cpp:378-444).
+ * inputs[k] is an N_k complex row for media[k]; outputs[k] receives the last row of all
+ * signal modes (nSignalModes_k*N_k complex).  Pumps must have been run.              */
+nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
+                            int in_time_domain, double* const* outputs);
+
+/* --- getters (src/nlmModulePy.cpp:100-123) ---------------------------------------------
+ * which: 0 = pumpFreq, 1 = pumpTime, 2 = signalFreq, 3 = signalTime, 4 = field.
+ * Returns a pointer into a host mirror owned by the handle (refreshed from the device on
+ * every call), valid until the handle is destroyed.  NLM_ERR_INDEX when index is out of
+ * range, like the reference's std::vector::at.                                        */
+nlm_status nlm_get_grid(nlm_medium* m, int which, unsigned index, const double** data,
+                        size_t* rows, size_t* cols);
+/* which: 0 = tau, 1 = omega, 2 = poling, 3 = ramanResponse (complex, Chi3GNLSE only),
+ * 4 = envelope of pump `index` (complex).  Real arrays are doubles. */
+nlm_status nlm_get_axis(nlm_medium* m, int which, unsigned index, const double** data, size_t* n);
+
+/* --- Cascade (src/Cascade.cpp:3-167) --------------------------------------------------
+ * connections: for each of the n_media-1 junctions a list of (input mode of next medium,
+ * output mode of previous medium) pairs, flattened; conn_counts gives pairs per junction and
+ * n_junctions their number (must be n_media-1, src/Cascade.cpp:21-22).
+ * The cascade does not own its media: keep them alive while it exists.                 */
+nlm_status nlm_cascade_create(nlm_medium* const* media, size_t n_media, const unsigned* connections,
+                              const size_t* conn_counts, size_t n_junctions, int share_pump,
+                              nlm_medium** out);
+nlm_status nlm_cascade_add(nlm_medium* cascade, nlm_medium* medium, const unsigned* connection,
+                           size_t n_pairs);
+nlm_status nlm_cascade_media(const nlm_medium* cascade, size_t* n_media);
+
+/* --- device / stream -------------------------------------------------------------------- */
+/* Select the CUDA stream (a cudaStream_t) used by a handle; NULL = library stream. */
+nlm_status nlm_set_stream(nlm_medium* m, void* cuda_stream);
+/* Wait for all work of the handle. */
+nlm_status nlm_synchronize(nlm_medium* m);
+/* 1 when a CUDA device is usable by this process. */
+int nlm_device_available(void);
+
+/* --- engine controls ------------------------------------------------------------------- */
+/* Force the batched-kernel schedule (0 = autotuner).  cta_per_sm: resident CTAs per SM;
+ * use_propagator: 1 = precomputed RK4 propagator for linear solvers, 0 = direct DiffEq,
+ * -1 = automatic.  Used by tests and by the benchmark to compare schedules. */
+nlm_status nlm_set_schedule(nlm_medium* m, int cta_per_sm, int use_propagator, int use_graph);
+/* Run computeGreensFunction's propagations one per kernel launch (the "plain" form),
+ * limited to the first max_instances impulse propagations (0 = all); the matrices of
+ * the rows not propagated are left zero.  Timing helper for the plain-vs-batched ratio. */
+nlm_status nlm_green_plain(nlm_medium* m, int in_time_domain, int run_pump, size_t max_instances,
+                           double* green_c, double* green_s);
+/* Number of kernels the last nlm_* call of this handle launched. */
+nlm_status nlm_last_launch_count(const nlm_medium* m, long* launches);
+/* Time the fused propagation kernel with CUDA events on the handle's stream.  enable = 1
+ * resets and starts accumulating, 0 stops; total_ms/count return what was accumulated.
+ * No counterpart in the reference (measurement support). */
+nlm_status nlm_kernel_timing(nlm_medium* m, int enable, double* total_ms, long* count);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (an FMA counts as two
+ * flops): the roofline denominator of the propagation kernels.  No counterpart in the
+ * reference (measurement support). */
+nlm_status nlm_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLM_CAPI_H */

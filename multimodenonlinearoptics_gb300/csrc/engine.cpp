@@ -1,0 +1,2031 @@
+// engine.cpp -- host engine behind the C ABI (include/nlm_capi.h).
+//
+// The host side mirrors the reference's _NonlinearMedium / _FullyNonlinearMedium / Cascade
+// classes: the scalar set-up (lengths, axes, dispersion, poling, pump envelopes, the per-step
+// coefficients of every solver's DiffEq) is computed here in double precision with the same
+// formulas and the same std::exp / std::sqrt as the reference, and every transform and every
+// propagation runs on the GPU through the kernels of nlm_kernels.h.  There is no CPU path for
+// any of them: without a usable device those calls return NLM_ERR_NO_DEVICE.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nlm_capi.h"
+#include "nlm_kernels.h"
+
+namespace nlm {
+
+using cplx = std::complex<double>;
+using uint = unsigned int;
+static const double kInf = std::numeric_limits<double>::infinity();
+static const cplx kI(0.0, 1.0);
+
+// ----------------------------------------------------------------------------------------
+// errors
+// ----------------------------------------------------------------------------------------
+struct IndexError : std::out_of_range {
+  using std::out_of_range::out_of_range;
+};
+struct NoDevice : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct Unsupported : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct CudaFailure : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+static thread_local std::string g_error;
+
+static void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw CudaFailure(std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <class F>
+static nlm_status guarded(F&& f) {
+  try {
+    f();
+    return NLM_OK;
+  } catch (const std::invalid_argument& e) {
+    g_error = e.what();
+    return NLM_ERR_INVALID_ARGUMENT;
+  } catch (const IndexError& e) {
+    g_error = e.what();
+    return NLM_ERR_INDEX;
+  } catch (const std::out_of_range& e) {
+    g_error = e.what();
+    return NLM_ERR_INDEX;
+  } catch (const NoDevice& e) {
+    g_error = e.what();
+    return NLM_ERR_NO_DEVICE;
+  } catch (const Unsupported& e) {
+    g_error = e.what();
+    return NLM_ERR_UNSUPPORTED;
+  } catch (const CudaFailure& e) {
+    g_error = e.what();
+    return NLM_ERR_CUDA;
+  } catch (const std::length_error& e) {
+    g_error = e.what();
+    return NLM_ERR_INVALID_ARGUMENT;
+  } catch (const std::runtime_error& e) {
+    g_error = e.what();
+    return NLM_ERR_RUNTIME;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return NLM_ERR_RUNTIME;
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// device helpers
+// ----------------------------------------------------------------------------------------
+static int device_count() {
+  static int count = -1;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+      cudaGetLastError();
+      n = 0;
+    }
+    count = n;
+  });
+  return count;
+}
+
+static void require_device() {
+  if (device_count() <= 0) throw NoDevice("no CUDA device is available: this engine has no CPU fallback");
+}
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    ck(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+    n = count;
+  }
+  void reserve(size_t count) {
+    if (count <= n && p) return;
+    alloc(count);
+  }
+};
+
+static double2* d2(void* p) { return reinterpret_cast<double2*>(p); }
+
+// Twiddle table exp(-2 pi i m / N), one per grid size, per process.
+struct TwiddleCache {
+  std::mutex mu;
+  std::map<int, std::shared_ptr<DevBuf<double2>>> tables;
+  const double2* get(int N, cudaStream_t s) {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = tables.find(N);
+    if (it != tables.end()) return it->second->p;
+    std::vector<double2> h(N);
+    for (int m = 0; m < N; m++) {
+      // reduce to the first octant with exact symmetries, then evaluate in long double
+      const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)N;
+      h[m].x = (double)std::cos(ang);
+      h[m].y = (double)std::sin(ang);
+    }
+    // exact values at the quarter points
+    for (int q = 0; q < 4; q++) {
+      if ((long long)N * q % 4 != 0) continue;
+      const int m = N * q / 4;
+      const double c[4] = {1, 0, -1, 0}, sn[4] = {0, -1, 0, 1};
+      h[m].x = c[q];
+      h[m].y = sn[q];
+    }
+    auto buf = std::make_shared<DevBuf<double2>>();
+    buf->alloc(N);
+    ck(cudaMemcpyAsync(buf->p, h.data(), N * sizeof(double2), cudaMemcpyHostToDevice, s), "twiddle upload");
+    ck(cudaStreamSynchronize(s), "twiddle upload");
+    tables[N] = buf;
+    return buf->p;
+  }
+};
+static TwiddleCache g_twiddles;
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static FFTPlanH make_plan(int N, int R) {
+  FFTPlanH p{};
+  p.N = N;
+  p.T = N / R;
+  int n = 0;
+  while ((1 << n) < N) n++;
+  const int rl = R >= 8 ? 3 : 2;
+  int a = n / rl, rem = n % rl;
+  std::vector<int> rad(a, 1 << rl);
+  if (rem) rad.insert(rad.begin() + (a >= 1 ? 1 : 0), 1 << rem);
+  p.nPass = (int)rad.size();
+  for (int i = 0; i < p.nPass; i++) p.radix[i] = rad[i];
+  return p;
+}
+
+// ----------------------------------------------------------------------------------------
+// solver registry: constructor signatures and their mapping onto the base class
+// (solvers/*.cpp constructors; py::init keyword lists)
+// ----------------------------------------------------------------------------------------
+enum Solver {
+  kChi3 = 0, kChi2PDC, kChi2SFG, kChi2AFC, kChi2SFGPDC, kChi2SFGII, kChi2PDCII, kChi2SFGOPA, kChi2SFGXPM,
+  kChi2SHG, kChi2SHGOPA, kChi2DSFG, kChi2SHGXPM, kChi2ASHG, kChi3GNLSE, kNumSolvers
+};
+
+struct SolverInfo {
+  const char* name;
+  // scalar arguments in positional order; "@customPump" / "@poling" mark array arguments
+  const char* signature;
+  int modes, pumps, coefs;
+  bool fnl, linear;
+};
+
+static const SolverInfo kSolvers[kNumSolvers] = {
+    {"Chi3",
+     "relativeLength,nlLength,beta2,@customPump,pulseType=0,beta3=0,rayleighLength=inf,tMax=10,tPrecision=512,"
+     "zPrecision=100,intensityProfile=0,chirp=0",
+     1, 1, 1, false, true},
+    {"Chi2PDC",
+     "relativeLength,nlLength,beta2,beta2s,@customPump,pulseType=0,beta1=0,beta1s=0,beta3=0,beta3s=0,diffBeta0=0,"
+     "rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,chirp=0,delay=0,@poling",
+     1, 1, 1, false, true},
+    {"Chi2SFG",
+     "relativeLength,nlLength,nlLengthOrig,beta2,beta2s,beta2o,@customPump,pulseType=0,beta1=0,beta1s=0,beta1o=0,"
+     "beta3=0,beta3s=0,beta3o=0,diffBeta0=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,"
+     "intensityProfile=0,chirp=0,delay=0,@poling",
+     2, 1, 2, false, true},
+    {"Chi2AFC",
+     "relativeLength,nlLength,nlLengthOrig,beta2,beta2s,beta2o,@customPump,pulseType=0,beta1=0,beta1s=0,beta1o=0,"
+     "beta3=0,beta3s=0,beta3o=0,diffBeta0Start=0,diffBeta0End=0,rayleighLength=inf,tMax=10,tPrecision=512,"
+     "zPrecision=100,intensityProfile=0,chirp=0,delay=0",
+     2, 1, 2, false, true},
+    {"Chi2SFGPDC",
+     "relativeLength,nlLength,nlLengthOrig,beta2,beta2s,beta2o,@customPump,pulseType=0,beta1=0,beta1s=0,beta1o=0,"
+     "beta3=0,beta3s=0,beta3o=0,diffBeta0=0,diffBeta0o=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,"
+     "intensityProfile=0,chirp=0,delay=0,@poling",
+     2, 1, 4, false, true},
+    {"Chi2SFGII",
+     "relativeLength,nlLengthZY,nlLengthZZ,beta2,beta2sz,beta2sy,beta2oz,beta2oy,@customPump,pulseType=0,beta1=0,"
+     "beta1sz=0,beta1sy=0,beta1oz=0,beta1oy=0,beta3=0,beta3sz=0,beta3sy=0,beta3oz=0,beta3oy=0,diffBeta0z=0,"
+     "diffBeta0y=0,diffBeta0=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,chirp=0,"
+     "delay=0,@poling",
+     4, 1, 7, false, true},
+    {"Chi2PDCII",
+     "relativeLength,nlLengthI,nlLengthII,beta2,beta2s,beta2o,@customPump,pulseType=0,beta1=0,beta1s=0,beta1o=0,"
+     "beta3=0,beta3s=0,beta3o=0,diffBeta0=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,"
+     "intensityProfile=0,chirp=0,delay=0,@poling",
+     2, 1, 2, false, true},
+    {"Chi2SFGOPA",
+     "relativeLength,nlLengthSFGh,nlLengthSFGf,nlLengthDOPAh,nlLengthDOPAf,beta2F,beta2H,beta2h,beta2f,@customPump,"
+     "pulseType=0,beta1F=0,beta1H=0,beta1h=0,beta1f=0,beta3F=0,beta3H=0,beta3h=0,beta3f=0,diffBeta0SFG=0,"
+     "diffBeta0DOPA=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,chirp=0,delay=0,"
+     "@poling",
+     2, 2, 4, false, true},
+    {"Chi2SFGXPM",
+     "relativeLength,nlLength,nlLengthOrig,nlLengthChi3,nlLengthChi3Orig,beta2,beta2s,beta2o,@customPump,pulseType=0,"
+     "beta1=0,beta1s=0,beta1o=0,beta3=0,beta3s=0,beta3o=0,diffBeta0=0,rayleighLength=inf,tMax=10,tPrecision=512,"
+     "zPrecision=100,intensityProfile=0,chirp=0,delay=0,@poling",
+     2, 1, 4, false, true},
+    {"Chi2SHG",
+     "relativeLength,nlLengthH,nlLengthP,beta2h,beta2p,beta1h=0,beta1p=0,beta3h=0,beta3p=0,diffBeta0=0,"
+     "rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,@poling",
+     2, 0, 2, true, false},
+    {"Chi2SHGOPA",
+     "relativeLength,nlLengthP,nlLengthSH,nlLengthPA1,nlLengthPA2,beta2p,beta2sh,beta2pa1,beta2pa2,beta1p=0,"
+     "beta1sh=0,beta1pa1=0,beta1pa2=0,beta3p=0,beta3sh=0,beta3pa1=0,beta3pa2=0,diffBeta0shg=0,diffBeta0opa=0,"
+     "rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,@poling",
+     4, 0, 6, true, false},
+    {"Chi2DSFG",
+     "relativeLength,nlLengthP,nlLengthS,nlLengthD,beta2p,beta2s,beta2d,beta1p=0,beta1s=0,beta1d=0,beta3p=0,"
+     "beta3s=0,beta3d=0,diffBeta0=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,"
+     "@poling",
+     3, 0, 3, true, false},
+    {"Chi2SHGXPM",
+     "relativeLength,nlLengthH,nlLengthP,nlLengthChi3,beta2h,beta2p,beta1h=0,beta1p=0,beta3h=0,beta3p=0,diffBeta0=0,"
+     "rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0,@poling",
+     2, 0, 3, true, false},
+    {"Chi2ASHG",
+     "relativeLength,nlLengthH,nlLengthP,beta2h,beta2p,beta1h=0,beta1p=0,beta3h=0,beta3p=0,diffBeta0Start=0,"
+     "diffBeta0End=0,rayleighLength=inf,tMax=10,tPrecision=512,zPrecision=100,intensityProfile=0",
+     2, 0, 2, true, false},
+    {"Chi3GNLSE",
+     "relativeLength,nlLength,selfSteepLength,fr,fb,tau1,tau2,tau3,beta2,beta3=0,rayleighLength=inf,tMax=10,"
+     "tPrecision=512,zPrecision=100,intensityProfile=0",
+     1, 0, 0, true, false},
+};
+
+static int solver_by_name(const char* name) {
+  for (int i = 0; i < kNumSolvers; i++)
+    if (std::strcmp(kSolvers[i].name, name) == 0) return i;
+  return -1;
+}
+
+static int scalar_arg_count(int solver) {
+  int n = 0;
+  const char* s = kSolvers[solver].signature;
+  std::string tok;
+  for (const char* c = s;; c++) {
+    if (*c == ',' || *c == 0) {
+      if (!tok.empty() && tok[0] != '@') n++;
+      tok.clear();
+      if (*c == 0) break;
+    } else {
+      tok += *c;
+    }
+  }
+  return n;
+}
+
+// Arguments of the base-class constructor (src/_NonlinearMedium.hpp:59-67).
+struct BaseParams {
+  uint nSignal = 1, nPump = 1;
+  bool poled = false, fnl = false;
+  double relativeLength = 1;
+  std::vector<double> nl, beta2, beta2s, beta1, beta1s, beta3, beta3s, diffBeta0;
+  double rayleigh = kInf, tMax = 10;
+  uint tPrecision = 512, zPrecision = 100;
+  int profile = NLM_GAUSSIAN_BEAM;
+  double chirp = 0, delay = 0;
+  int pulseType = NLM_GAUSSIAN;
+  // Chi3GNLSE
+  double fr = 0, fb = 0, tau1 = 1, tau2 = 1, tau3 = 1;
+};
+
+static uint as_uint(double v) {
+  if (!(v >= 0) || v > 4294967295.0) throw std::invalid_argument("integer argument out of range");
+  return (uint)v;
+}
+
+static BaseParams map_ctor(int s, const double* a) {
+  BaseParams b;
+  const double halfPi = 0.5 * M_PI;
+  auto tail = [&](int i, bool withChirp, bool withDelay) {
+    // ..., rayleighLength, tMax, tPrecision, zPrecision, intensityProfile[, chirp[, delay]]
+    b.rayleigh = a[i];
+    b.tMax = a[i + 1];
+    b.tPrecision = as_uint(a[i + 2]);
+    b.zPrecision = as_uint(a[i + 3]);
+    b.profile = (int)a[i + 4];
+    if (withChirp) b.chirp = a[i + 5];
+    if (withDelay) b.delay = a[i + 6];
+  };
+  switch (s) {
+    case kChi3:  // solvers/Chi3.cpp:34-38
+      b.nSignal = 1; b.nPump = 1; b.poled = false;
+      b.relativeLength = a[0]; b.nl = {a[1]}; b.beta2 = {a[2]}; b.beta2s = {a[2]};
+      b.pulseType = (int)a[3]; b.beta1 = {0}; b.beta1s = {0}; b.beta3 = {a[4]}; b.beta3s = {a[4]};
+      b.rayleigh = a[5]; b.tMax = a[6]; b.tPrecision = as_uint(a[7]); b.zPrecision = as_uint(a[8]);
+      b.profile = (int)a[9]; b.chirp = a[10]; b.delay = 0;
+      break;
+    case kChi2PDC:  // solvers/Chi2PDC.cpp:18-24
+      b.nSignal = 1; b.nPump = 1; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1]}; b.beta2 = {a[2]}; b.beta2s = {a[3]}; b.pulseType = (int)a[4];
+      b.beta1 = {a[5]}; b.beta1s = {a[6]}; b.beta3 = {a[7]}; b.beta3s = {a[8]}; b.diffBeta0 = {a[9]};
+      tail(10, true, true);
+      break;
+    case kChi2SFG:  // solvers/Chi2SFG.cpp:20-27
+    case kChi2PDCII:  // solvers/Chi2PDCII.cpp:20-27
+      b.nSignal = 2; b.nPump = 1; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2]}; b.beta2 = {a[3]}; b.beta2s = {a[4], a[5]};
+      b.pulseType = (int)a[6]; b.beta1 = {a[7]}; b.beta1s = {a[8], a[9]}; b.beta3 = {a[10]};
+      b.beta3s = {a[11], a[12]}; b.diffBeta0 = {a[13]};
+      tail(14, true, true);
+      break;
+    case kChi2AFC:  // solvers/Chi2AFC.cpp:17-23
+      b.nSignal = 2; b.nPump = 1; b.poled = false;
+      b.relativeLength = a[0]; b.nl = {halfPi * a[1], halfPi * a[2]}; b.beta2 = {a[3]}; b.beta2s = {a[4], a[5]};
+      b.pulseType = (int)a[6]; b.beta1 = {a[7]}; b.beta1s = {a[8], a[9]}; b.beta3 = {a[10]};
+      b.beta3s = {a[11], a[12]}; b.diffBeta0 = {a[13], a[14]};
+      tail(15, true, true);
+      break;
+    case kChi2SFGPDC:  // solvers/Chi2SFGPDC.cpp:20-28
+      b.nSignal = 2; b.nPump = 1; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2]}; b.beta2 = {a[3]}; b.beta2s = {a[4], a[5]};
+      b.pulseType = (int)a[6]; b.beta1 = {a[7]}; b.beta1s = {a[8], a[9]}; b.beta3 = {a[10]};
+      b.beta3s = {a[11], a[12]}; b.diffBeta0 = {a[13], a[14]};
+      tail(15, true, true);
+      break;
+    case kChi2SFGII:  // solvers/Chi2SFGII.cpp:23-34
+      b.nSignal = 4; b.nPump = 1; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2]}; b.beta2 = {a[3]}; b.beta2s = {a[4], a[5], a[6], a[7]};
+      b.pulseType = (int)a[8]; b.beta1 = {a[9]}; b.beta1s = {a[10], a[11], a[12], a[13]}; b.beta3 = {a[14]};
+      b.beta3s = {a[15], a[16], a[17], a[18]}; b.diffBeta0 = {a[19], a[20], a[21]};
+      tail(22, true, true);
+      break;
+    case kChi2SFGOPA:  // solvers/Chi2SFGOPA.cpp:20-28
+      b.nSignal = 2; b.nPump = 2; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2], a[3], a[4]}; b.beta2 = {a[5], a[6]}; b.beta2s = {a[7], a[8]};
+      b.pulseType = (int)a[9]; b.beta1 = {a[10], a[11]}; b.beta1s = {a[12], a[13]}; b.beta3 = {a[14], a[15]};
+      b.beta3s = {a[16], a[17]}; b.diffBeta0 = {a[18], a[19]};
+      tail(20, true, true);
+      break;
+    case kChi2SFGXPM:  // solvers/Chi2SFGXPM.cpp:20-27 (the XPM lengths are halved)
+      b.nSignal = 2; b.nPump = 1; b.poled = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2], a[3] / 2, a[4] / 2}; b.beta2 = {a[5]}; b.beta2s = {a[6], a[7]};
+      b.pulseType = (int)a[8]; b.beta1 = {a[9]}; b.beta1s = {a[10], a[11]}; b.beta3 = {a[12]};
+      b.beta3s = {a[13], a[14]}; b.diffBeta0 = {a[15]};
+      tail(16, true, true);
+      break;
+    case kChi2SHG:  // solvers/Chi2SHG.cpp:18-23: modes reordered to {P, SH}
+      b.nSignal = 2; b.nPump = 0; b.poled = true; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {a[2], a[1]}; b.beta2s = {a[4], a[3]}; b.beta1s = {a[6], a[5]};
+      b.beta3s = {a[8], a[7]}; b.diffBeta0 = {a[9]};
+      tail(10, false, false);
+      break;
+    case kChi2SHGOPA:  // solvers/Chi2SHGOPA.cpp:19-29
+      b.nSignal = 4; b.nPump = 0; b.poled = true; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2], a[3], a[4]}; b.beta2s = {a[5], a[6], a[7], a[8]};
+      b.beta1s = {a[9], a[10], a[11], a[12]}; b.beta3s = {a[13], a[14], a[15], a[16]}; b.diffBeta0 = {a[17], a[18]};
+      tail(19, false, false);
+      break;
+    case kChi2DSFG:  // solvers/Chi2DSFG.cpp:16-22
+      b.nSignal = 3; b.nPump = 0; b.poled = true; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2], a[3]}; b.beta2s = {a[4], a[5], a[6]};
+      b.beta1s = {a[7], a[8], a[9]}; b.beta3s = {a[10], a[11], a[12]}; b.diffBeta0 = {a[13]};
+      tail(14, false, false);
+      break;
+    case kChi2SHGXPM:  // solvers/Chi2SHGXPM.cpp:18-24: modes {P, SH}
+      b.nSignal = 2; b.nPump = 0; b.poled = true; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {a[2], a[1], a[3]}; b.beta2s = {a[5], a[4]}; b.beta1s = {a[7], a[6]};
+      b.beta3s = {a[9], a[8]}; b.diffBeta0 = {a[10]};
+      tail(11, false, false);
+      break;
+    case kChi2ASHG:  // solvers/Chi2ASHG.cpp:15-20
+      b.nSignal = 2; b.nPump = 0; b.poled = false; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {halfPi * a[2], halfPi * a[1]}; b.beta2s = {a[4], a[3]};
+      b.beta1s = {a[6], a[5]}; b.beta3s = {a[8], a[7]}; b.diffBeta0 = {a[9], a[10]};
+      tail(11, false, false);
+      break;
+    case kChi3GNLSE:  // solvers/Chi3GNLSE.cpp:20-24
+      b.nSignal = 1; b.nPump = 0; b.poled = false; b.fnl = true;
+      b.relativeLength = a[0]; b.nl = {a[1], a[2]}; b.fr = a[3]; b.fb = a[4]; b.tau1 = a[5]; b.tau2 = a[6];
+      b.tau3 = a[7]; b.beta2s = {a[8]}; b.beta1s = {0}; b.beta3s = {a[9]};
+      tail(10, false, false);
+      break;
+    default:
+      throw std::invalid_argument("unknown solver");
+  }
+  return b;
+}
+
+// ----------------------------------------------------------------------------------------
+// Medium
+// ----------------------------------------------------------------------------------------
+struct GridMirror {
+  std::vector<double> host;   // interleaved complex
+  long long version = -1;
+};
+
+struct Medium {
+  int solver = -1;
+  bool isCascade = false;
+  uint nSignal = 0, nPump = 0;
+  bool fnl = false, poled = false;
+  double z = 0, dz = 0, dzp = 0, tMax = 0, rayleigh = kInf;
+  uint nZ = 0, nZP = 0, N = 0;
+  int profile = NLM_CONSTANT;
+  std::vector<double> beta2, beta1, diffBeta0;
+  std::vector<cplx> nlStep;
+  std::vector<std::vector<cplx>> envelope;
+  std::vector<double> poling, tau, omega;
+  std::vector<std::vector<double>> dispPump, dispSign;
+  std::vector<std::vector<cplx>> dstepPump, dstepSign;
+  double fr = 0, fb = 0, tau1 = 1, tau2 = 1, tau3 = 1;
+  std::vector<cplx> raman;   // Chi3GNLSE, filled at first device use
+
+  // device state
+  bool devReady = false;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  const double2* tw = nullptr;
+  DevBuf<double2> pumpFreq, pumpTime, sigFreq, sigTime;
+  DevBuf<double2> dstep, dlast, half, back, coef, ramanD, steepD;
+  DevBuf<double> relIntD, dispPumpD, dispSignD, omegaD;
+  DevBuf<double> prop;
+  long long propVersion = -1;
+  DevBuf<double2> work, work2, raw, cs, io;
+  DevBuf<double2> scratch;
+  DevBuf<uint8_t> flagsD;
+  DevBuf<double2> scaleD;
+  long long pumpVersion = 0, signalVersion = 0;
+  GridMirror mPumpF, mPumpT, mSigF, mSigT;
+  std::vector<std::vector<double>> pumpMirrorF, pumpMirrorT, sigMirrorF, sigMirrorT;
+  std::vector<long long> pumpMirrorVerF, pumpMirrorVerT, sigMirrorVerF, sigMirrorVerT;
+  std::vector<double> axisBuf;
+  long launches = 0;
+  // kernel timing (measurement support)
+  bool timeKernels = false;
+  double kernelMs = 0;
+  long kernelCount = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // schedule overrides
+  int ctaPerSM = 0, usePropagator = -1, useGraph = 1;
+
+  // cascade
+  std::vector<Medium*> media;
+  std::vector<std::map<uint, uint>> connections;
+  bool sharedPump = false;
+
+  ~Medium() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (ownStream && stream) cudaStreamDestroy(stream);
+  }
+
+  // -- set-up, src/_NonlinearMedium.cpp:43-102 -------------------------------------------
+  void setLengths(double relativeLength, const std::vector<double>& nl, uint zPrecision, double rayleighLength,
+                  const std::vector<double>& b2, const std::vector<double>& b2s, const std::vector<double>& b1,
+                  const std::vector<double>& b1s, const std::vector<double>& b3, const std::vector<double>& b3s) {
+    bool negative = relativeLength <= 0 || rayleighLength <= 0;
+    for (double l : nl) negative |= (l <= 0);
+    if (negative) throw std::invalid_argument("Non-positive length scale");
+    bool allNonUnit = true;
+    for (const auto* g : {&b1, &b2, &b3, &b1s, &b2s, &b3s})
+      for (double b : *g) allNonUnit &= (std::abs(b) != 1);
+    for (double l : nl) allNonUnit &= (l != 1);
+    allNonUnit &= (relativeLength != 1);
+    allNonUnit &= (rayleighLength != 1);
+    if (allNonUnit) throw std::invalid_argument("No unit length scale provided: please normalize variables");
+    z = relativeLength;
+    auto absComp = [](double a, double b) { return std::abs(a) < std::abs(b); };
+    auto ext = [&](const std::vector<double>& v) { return v.empty() ? 0.0 : *std::max_element(v.begin(), v.end(), absComp); };
+    const double minDispLength = 1 / std::abs(std::max({ext(b2), ext(b2s), ext(b1), ext(b1s), ext(b3), ext(b3s)}, absComp));
+    const double minNl = nl.empty() ? 0 : *std::min_element(nl.begin(), nl.end());
+    const double steps = zPrecision * z / std::min({1., minDispLength, rayleighLength, minNl});
+    nZ = (std::isfinite(steps) && steps >= 0 && steps < 4294967296.0) ? (uint)steps : 0;
+    nZP = 2 * nZ - 1;
+    dz = z / (nZ - 1);
+    dzp = z / (nZP - 1);
+    nlStep.resize(nl.size());
+    for (size_t p = 0; p < nl.size(); p++) nlStep[p] = 1.0 * kI / nl[p] * dz;
+    rayleigh = rayleighLength;
+  }
+
+  // src/_NonlinearMedium.cpp:105-145
+  void resetGrids(uint nFreqs, double tMaxIn) {
+    if (nFreqs % 2 != 0 || nFreqs == 0) throw std::invalid_argument("Invalid number of Frequencies");
+    if (nZ == 0) throw std::invalid_argument("Zero steps");
+    if (tMaxIn <= 0) throw std::invalid_argument("Negative time span");
+    N = nFreqs;
+    tMax = tMaxIn;
+    const int Nt = (int)N;
+    std::vector<double> ramp(Nt);
+    for (int k = 0; k < Nt; k++) ramp[k] = (double)(k - Nt / 2);
+    tau.assign(Nt, 0);
+    omega.assign(Nt, 0);
+    const double st = 2 * tMax / Nt, sw = -M_PI / tMax;
+    const int h = Nt / 2;
+    for (int k = 0; k < Nt; k++) {  // fftshift of the linear ramps
+      const int src = (k + h) % Nt;
+      tau[k] = st * ramp[src];
+      omega[k] = sw * ramp[src];
+    }
+  }
+
+  // src/_NonlinearMedium.cpp:148-177
+  void setDispersion(const std::vector<double>& b2, const std::vector<double>& b2s, const std::vector<double>& b1,
+                     const std::vector<double>& b1s, const std::vector<double>& b3, const std::vector<double>& b3s,
+                     const std::vector<double>& db0) {
+    beta2 = b2;
+    beta1 = b1;
+    diffBeta0 = db0;
+    dispPump.assign(nPump, std::vector<double>(N));
+    for (uint m = 0; m < nPump; m++)
+      for (uint k = 0; k < N; k++) dispPump[m][k] = omega[k] * (b1[m] + omega[k] * (0.5 * b2[m] + omega[k] * b3[m] / 6));
+    dispSign.assign(nSignal, std::vector<double>(N));
+    for (uint m = 0; m < nSignal; m++)
+      for (uint k = 0; k < N; k++) dispSign[m][k] = omega[k] * (b1s[m] + omega[k] * (0.5 * b2s[m] + omega[k] * b3s[m] / 6));
+    dstepPump.assign(nPump, std::vector<cplx>(N));
+    for (uint m = 0; m < nPump; m++)
+      for (uint k = 0; k < N; k++) dstepPump[m][k] = std::exp((1.0 * kI * dzp) * dispPump[m][k]);
+    dstepSign.assign(nSignal, std::vector<cplx>(N));
+    for (uint m = 0; m < nSignal; m++)
+      for (uint k = 0; k < N; k++) dstepSign[m][k] = std::exp((1.0 * kI * dz) * dispSign[m][k]);
+  }
+
+  // src/_NonlinearMedium.cpp:470-503
+  void setPoling(const std::vector<double>& pol) {
+    if (pol.size() <= 1) {
+      poling.assign(nZ, 1.0);
+      return;
+    }
+    for (double p : pol)
+      if (p <= 0) throw std::invalid_argument("Poling contains invalid domain length");
+    std::vector<double> dom(pol.size());
+    dom[0] = pol[0];
+    for (size_t i = 1; i < pol.size(); i++) dom[i] = pol[i] + dom[i - 1];
+    const double scale = nZ / dom.back();
+    for (double& d : dom) d *= scale;
+    poling.assign(nZ, 0.0);
+    uint prevInd = 0;
+    int direction = 1;
+    for (size_t i = 0; i < dom.size(); i++) {
+      const double currInd = dom[i];
+      const uint currIndRound = (uint)currInd;
+      if (currInd < prevInd) throw std::invalid_argument("Poling period too small for simulation resolution");
+      for (uint k = prevInd; k < currIndRound && k < nZ; k++) poling[k] = direction;
+      if (currIndRound < nZ) poling[currIndRound] = direction * (2 * std::abs(std::fmod(currInd, 1)) - 1);
+      direction *= -1;
+      prevInd = currIndRound + 1;
+    }
+  }
+
+  // ---- device state -------------------------------------------------------------------
+  void ensureDevice() {
+    if (devReady) return;
+    require_device();
+    if (!stream) {
+      ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      ownStream = true;
+    }
+    tw = g_twiddles.get((int)N, stream);
+    const size_t n = N;
+    if (nPump > 0 && nZP > 0) {
+      pumpFreq.alloc((size_t)nPump * nZP * n);
+      pumpTime.alloc((size_t)nPump * nZP * n);
+      ck(cudaMemsetAsync(pumpFreq.p, 0, pumpFreq.n * sizeof(double2), stream), "memset");
+      ck(cudaMemsetAsync(pumpTime.p, 0, pumpTime.n * sizeof(double2), stream), "memset");
+    }
+    sigFreq.alloc((size_t)nSignal * nZ * n);
+    sigTime.alloc((size_t)nSignal * nZ * n);
+    ck(cudaMemsetAsync(sigFreq.p, 0, sigFreq.n * sizeof(double2), stream), "memset");
+    ck(cudaMemsetAsync(sigTime.p, 0, sigTime.n * sizeof(double2), stream), "memset");
+    // point-wise factor tables with 1/N folded in (the inverse transforms are unscaled)
+    std::vector<double2> hd(nSignal * n), hl(nSignal * n), hh(nSignal * n), hb(nSignal * n);
+    const double invN = 1.0 / N;
+    for (uint m = 0; m < nSignal; m++)
+      for (uint k = 0; k < N; k++) {
+        const cplx hf = std::exp((0.5 * kI * dz) * dispSign[m][k]);
+        const cplx bk = std::exp((-0.5 * kI * dz) * dispSign[m][k]);
+        const cplx d = dstepSign[m][k] * invN;
+        const cplx dl = dstepSign[m][k] * bk * invN;
+        const cplx h = hf * invN, b = bk * invN;
+        hd[m * n + k] = make_double2(d.real(), d.imag());
+        hl[m * n + k] = make_double2(dl.real(), dl.imag());
+        hh[m * n + k] = make_double2(h.real(), h.imag());
+        hb[m * n + k] = make_double2(b.real(), b.imag());
+      }
+    upload(dstep, hd);
+    upload(dlast, hl);
+    upload(half, hh);
+    upload(back, hb);
+    std::vector<double> hdp, hds;
+    for (auto& v : dispPump) hdp.insert(hdp.end(), v.begin(), v.end());
+    for (auto& v : dispSign) hds.insert(hds.end(), v.begin(), v.end());
+    uploadD(dispPumpD, hdp);
+    uploadD(dispSignD, hds);
+    uploadD(omegaD, omega);
+    buildCoefficients();
+    if (solver == kChi3GNLSE) buildGnlse();
+    ck(cudaStreamSynchronize(stream), "device set-up");
+    devReady = true;
+  }
+
+  template <class V>
+  void upload(DevBuf<double2>& d, const V& h) {
+    d.alloc(h.size());
+    if (!h.empty())
+      ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, stream), "upload");
+  }
+  void uploadD(DevBuf<double>& d, const std::vector<double>& h) {
+    d.alloc(h.size());
+    if (!h.empty())
+      ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "upload");
+  }
+
+  // relativeAmplitude / relativeIntensity, src/_FullyNonlinearMedium.hpp:40-63
+  double relativeAmplitude(double i) const {
+    switch (profile) {
+      case NLM_GAUSSIAN_BEAM: return std::sqrt(1 / (1 + std::pow((i * dz - 0.5 * z) / rayleigh, 2)));
+      case NLM_CONSTANT: return 1.;
+      case NLM_GAUSSIAN_APODIZATION: return std::exp(-0.5 * std::pow((i * dz - 0.5 * z) / rayleigh, 2));
+      default: return 0;
+    }
+  }
+  double relativeIntensity(double i) const {
+    switch (profile) {
+      case NLM_GAUSSIAN_BEAM: return 1 / (1 + std::pow((i * dz - 0.5 * z) / rayleigh, 2));
+      case NLM_CONSTANT: return 1.;
+      case NLM_GAUSSIAN_APODIZATION: return std::exp(-std::pow((i * dz - 0.5 * z) / rayleigh, 2));
+      default: return 0;
+    }
+  }
+
+  // Per-step coefficients of each solver's DiffEq, evaluated with the reference's expressions.
+  void stepCoefficients(uint i, int sub, cplx* c) const {
+    const double prevPol = poling.empty() ? 1.0 : poling[i - 1];
+    const double currPol = poling.empty() ? 1.0 : poling[i];
+    const double intmPol = 0.5 * (prevPol + currPol);
+    const double pol = sub == 0 ? prevPol : (sub == 1 ? intmPol : currPol);
+    auto zpos = [&](void) -> double {
+      return sub == 0 ? (double)(i - 1) * dz : (sub == 1 ? (i - .5) * dz : (double)i * dz);
+    };
+    auto mism = [&](double db) { return std::exp(1.0 * kI * db * zpos()); };
+    auto chirped = [&](void) {
+      const double arg = 0.5 * (diffBeta0[1] - diffBeta0[0]) / z;
+      const double s = sub == 0 ? (double)(i - 1) : (sub == 1 ? i - .5 : (double)i);
+      return std::exp(0.5 * kI * ((diffBeta0[0] + s * dz * arg) * s * dz));
+    };
+    const double relAmp = relativeAmplitude(sub == 0 ? (double)(i - 1) : (sub == 1 ? i - .5 : (double)i));
+    switch (solver) {
+      case kChi3:  // solvers/Chi3.cpp:81-84
+        c[0] = nlStep[0];
+        break;
+      case kChi2PDC: {  // solvers/Chi2PDC.cpp:36-43
+        c[0] = pol * nlStep[0] * mism(diffBeta0[0]);
+        break;
+      }
+      case kChi2SFG: {  // solvers/Chi2SFG.cpp:37-52
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = pol * nlStep[0] * m;
+        c[1] = pol * nlStep[1] * (1. / m);
+        break;
+      }
+      case kChi2AFC: {  // solvers/Chi2AFC.cpp:35-50
+        const cplx m = chirped();
+        c[0] = nlStep[0] * m;
+        c[1] = nlStep[1] * (1. / m);
+        break;
+      }
+      case kChi2SFGPDC: {  // solvers/Chi2SFGPDC.cpp:37-58
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = pol * nlStep[0] * m;
+        c[1] = pol * nlStep[1];
+        c[2] = 1. / m;
+        c[3] = mism(diffBeta0[1]);
+        break;
+      }
+      case kChi2SFGII: {  // solvers/Chi2SFGII.cpp:43-89; the last stage keeps prevPolDir (:86-89)
+        const double p = sub == 2 ? prevPol : pol;
+        const cplx mcz = mism(diffBeta0[0]), mcy = mism(diffBeta0[1]), msz = mism(diffBeta0[2]);
+        c[0] = cplx(p, 0);
+        c[1] = nlStep[0] * mcz;
+        c[2] = nlStep[1] * msz;
+        c[3] = p * nlStep[0] * mcy;
+        c[4] = nlStep[0] * (1. / mcy);
+        c[5] = nlStep[1] * (1. / msz);
+        c[6] = p * nlStep[0] * (1. / mcz);
+        break;
+      }
+      case kChi2PDCII: {  // solvers/Chi2PDCII.cpp:38-54
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = pol * nlStep[0] * m;
+        c[1] = pol * nlStep[1] * m;
+        break;
+      }
+      case kChi2SFGOPA: {  // solvers/Chi2SFGOPA.cpp:44-76
+        const cplx ms = mism(diffBeta0[0]), md = mism(diffBeta0[1]);
+        c[0] = pol * nlStep[0] * ms;
+        c[1] = pol * nlStep[2] * md;
+        c[2] = pol * nlStep[1] * (1. / ms);
+        c[3] = pol * nlStep[3] * md;
+        break;
+      }
+      case kChi2SFGXPM: {  // solvers/Chi2SFGXPM.cpp:38-57
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = pol * nlStep[0] * m;
+        c[1] = pol * nlStep[1] * (1. / m);
+        c[2] = nlStep[2];
+        c[3] = nlStep[3];
+        break;
+      }
+      case kChi2SHG: {  // solvers/Chi2SHG.cpp:32-59
+        const double rel = pol * relAmp;
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = rel * nlStep[0] * m;
+        c[1] = rel * nlStep[1] * (1. / m) * .5;
+        break;
+      }
+      case kChi2SHGOPA: {  // solvers/Chi2SHGOPA.cpp:39-83
+        const double rel = pol * relAmp;
+        const cplx ms = mism(diffBeta0[0]), mo = mism(diffBeta0[1]);
+        c[0] = rel * nlStep[0] * ms;
+        c[1] = rel * nlStep[1];
+        c[2] = mo;
+        c[3] = (1. / ms) * .5;
+        c[4] = rel * nlStep[2] * (1. / mo);
+        c[5] = rel * nlStep[3] * (1. / mo);
+        break;
+      }
+      case kChi2DSFG: {  // solvers/Chi2DSFG.cpp:31-64
+        const double rel = pol * relAmp;
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = rel * nlStep[0] * m;
+        c[1] = rel * nlStep[1] * (1. / m);
+        c[2] = rel * nlStep[2] * m;
+        break;
+      }
+      case kChi2SHGXPM: {  // solvers/Chi2SHGXPM.cpp:29-41
+        const double rel = pol * relAmp;
+        const cplx m = mism(diffBeta0[0]);
+        c[0] = rel * nlStep[0] * m;
+        c[1] = rel * nlStep[1] * (1. / m) * .5;
+        c[2] = std::pow(relAmp, 2) * nlStep[2];
+        break;
+      }
+      case kChi2ASHG: {  // solvers/Chi2ASHG.cpp:28-55
+        const cplx m = chirped();
+        c[0] = relAmp * nlStep[0] * m;
+        c[1] = relAmp * nlStep[1] * (1. / m) * .5;
+        break;
+      }
+      default:
+        break;
+    }
+  }
+
+  void buildCoefficients() {
+    const int nc = kSolvers[solver].coefs;
+    if (nc == 0 || nZ < 2) return;
+    std::vector<double2> h((size_t)(nZ - 1) * 3 * nc);
+    std::vector<cplx> c(nc);
+    for (uint i = 1; i < nZ; i++)
+      for (int sub = 0; sub < 3; sub++) {
+        stepCoefficients(i, sub, c.data());
+        for (int k = 0; k < nc; k++)
+          h[((size_t)(i - 1) * 3 + sub) * nc + k] = make_double2(c[k].real(), c[k].imag());
+      }
+    upload(coef, h);
+  }
+
+  // Raman response and self-steepening operator, solvers/Chi3GNLSE.cpp:20-36, :287
+  void buildGnlse() {
+    const double coeff1 = fr * (1. - fb) * (tau1 / (tau2 * tau2) + 1. / tau1);
+    const double coeff2 = fr * fb / (tau3 * tau3);
+    std::vector<double2> rt(N, make_double2(0, 0));
+    for (uint k = 0; k < N / 2; k++) {
+      const double t = tau[k];
+      rt[k].x = coeff1 * std::exp(-t / tau2) * std::sin(t / tau1) + coeff2 * std::exp(-t / tau3) * (2 * tau3 - t);
+    }
+    rt[0].x += 1. - fr;
+    DevBuf<double2> tmp;
+    upload(tmp, rt);
+    work.reserve(N);
+    FFTPlanH plan = fftPlanRows();
+    ck(launch_fft_rows(tmp.p, work.p, 1, plan, tw, false, 1.0, nullptr, stream), "raman fft");
+    launches++;
+    std::vector<double2> hr(N);
+    ck(cudaMemcpyAsync(hr.data(), work.p, N * sizeof(double2), cudaMemcpyDeviceToHost, stream), "raman");
+    ck(cudaStreamSynchronize(stream), "raman");
+    raman.resize(N);
+    std::vector<double2> rs(N), st(N);
+    const double invN = 1.0 / N;
+    for (uint k = 0; k < N; k++) {
+      raman[k] = cplx(hr[k].x, hr[k].y);
+      rs[k] = make_double2(hr[k].x * invN, hr[k].y * invN);
+      const cplx s = (nlStep[0] + nlStep[1] * omega[k]) * invN;
+      st[k] = make_double2(s.real(), s.imag());
+    }
+    upload(ramanD, rs);
+    upload(steepD, st);
+    std::vector<double> rel((size_t)(nZ > 1 ? nZ - 1 : 0) * 3);
+    for (uint i = 1; i < nZ; i++) {
+      rel[(i - 1) * 3 + 0] = relativeIntensity((double)(i - 1));
+      rel[(i - 1) * 3 + 1] = relativeIntensity(i - .5);
+      rel[(i - 1) * 3 + 2] = relativeIntensity((double)i);
+    }
+    uploadD(relIntD, rel);
+  }
+
+  FFTPlanH fftPlanRows() const {
+    if (is_pow2((int)N) && N >= 8 && N <= (uint)kMaxFFT) return make_plan((int)N, N <= 4096 ? 8 : 16);
+    FFTPlanH p{};
+    p.N = (int)N;
+    p.T = 1;
+    return p;
+  }
+
+  // ---- pumps -----------------------------------------------------------------------------
+  // src/_NonlinearMedium.cpp:198-203
+  void chirpDelay(uint idx, double chirp, double delay) {
+    if (chirp == 0 && delay == 0) return;
+    ensureDevice();
+    std::vector<double2> e(N), ph(N);
+    for (uint k = 0; k < N; k++) {
+      e[k] = make_double2(envelope[idx][k].real(), envelope[idx][k].imag());
+      const cplx p = std::exp(1.0 * kI * (beta1[idx] * delay + 0.5 * beta2[idx] * chirp * omega[k]) * omega[k]);
+      ph[k] = make_double2(p.real(), p.imag());
+    }
+    DevBuf<double2> de, dph, spec;
+    upload(de, e);
+    upload(dph, ph);
+    spec.alloc(N);
+    FFTPlanH plan = fftPlanRows();
+    ck(launch_fft_rows(de.p, spec.p, 1, plan, tw, false, 1.0, dph.p, stream), "chirp fft");
+    ck(launch_fft_rows(spec.p, de.p, 1, plan, tw, true, 1.0 / N, nullptr, stream), "chirp ifft");
+    launches += 2;
+    ck(cudaMemcpyAsync(e.data(), de.p, N * sizeof(double2), cudaMemcpyDeviceToHost, stream), "chirp");
+    ck(cudaStreamSynchronize(stream), "chirp");
+    for (uint k = 0; k < N; k++) envelope[idx][k] = cplx(e[k].x, e[k].y);
+  }
+
+  void setPumpType(int pulseType, double chirp, double delay, uint idx) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    setPumpTypeImpl(pulseType, chirp, delay, idx);
+  }
+  // src/_NonlinearMedium.cpp:180-204
+  void setPumpTypeImpl(int pulseType, double chirp, double delay, uint idx) {
+    if (idx >= nPump) throw std::invalid_argument("Invalid pump index");
+    std::vector<cplx>& env = envelope[idx];
+    env.assign(N, 0);
+    switch (pulseType) {
+      default:
+      case NLM_GAUSSIAN:
+        for (uint k = 0; k < N; k++) env[k] = std::exp(-0.5 * (tau[k] * tau[k]));
+        break;
+      case NLM_SECH:
+        for (uint k = 0; k < N; k++) env[k] = 1 / std::cosh(tau[k]);
+        break;
+      case NLM_SINC:
+        for (uint k = 0; k < N; k++) env[k] = std::sin(tau[k]) / tau[k];
+        env[0] = 1;
+    }
+    chirpDelay(idx, chirp, delay);
+  }
+  void setPumpCustom(const double* p, size_t n, double chirp, double delay, uint idx) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    setPumpCustomImpl(p, n, chirp, delay, idx);
+  }
+  // src/_NonlinearMedium.cpp:207-222
+  void setPumpCustomImpl(const double* p, size_t n, double chirp, double delay, uint idx) {
+    if (n != N) throw std::invalid_argument("Custom pump array length does not match number of frequency/time bins");
+    if (idx >= nPump) throw std::invalid_argument("Invalid pump index");
+    envelope[idx].resize(N);
+    for (uint k = 0; k < N; k++) envelope[idx][k] = cplx(p[2 * k], p[2 * k + 1]);
+    chirpDelay(idx, chirp, delay);
+  }
+
+  void relativeStrength(std::vector<double>& s) const {
+    s.assign(nZP, 1.0);
+    const double lo = -0.5 * z, hi = 0.5 * z;
+    const double step = nZP > 1 ? (hi - lo) / (nZP - 1) : 0;
+    for (uint i = 0; i < nZP; i++) {
+      const double zz = (i + 1 == nZP) ? hi : lo + i * step;
+      const double x = zz / rayleigh;
+      s[i] = profile == NLM_GAUSSIAN_APODIZATION ? std::exp(-0.5 * (x * x)) : 1 / std::sqrt(1 + x * x);
+    }
+  }
+
+  void runPump() {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    ensureDevice();
+    if (solver == kChi3) {
+      runPumpChi3();
+    } else {
+      // src/_NonlinearMedium.cpp:225-250
+      FFTPlanH plan = fftPlanRows();
+      DevBuf<double2> env;
+      for (uint m = 0; m < nPump; m++) {
+        std::vector<double2> e(N);
+        for (uint k = 0; k < N; k++) e[k] = make_double2(envelope[m][k].real(), envelope[m][k].imag());
+        upload(env, e);
+        double2* pf = pumpFreq.p + (size_t)m * nZP * N;
+        double2* pt = pumpTime.p + (size_t)m * nZP * N;
+        ck(launch_fft_rows(env.p, pf, 1, plan, tw, false, 1.0, nullptr, stream), "pump fft");
+        ck(launch_pump_linear(pf, dispPumpD.p + (size_t)m * N, dzp, (int)nZP, (int)N, pf, stream), "pump phase");
+        if (nZP > 1) ck(launch_fft_rows(pf + N, pt + N, nZP - 1, plan, tw, true, 1.0 / N, nullptr, stream), "pump ifft");
+        ck(cudaMemcpyAsync(pt, env.p, N * sizeof(double2), cudaMemcpyDeviceToDevice, stream), "pump row 0");
+        launches += 3;
+        if (profile != NLM_CONSTANT) {
+          std::vector<double> s;
+          relativeStrength(s);
+          DevBuf<double> sd;
+          uploadD(sd, s);
+          ck(launch_scale_rows(pf, sd.p, (int)nZP, (int)N, stream), "pump profile");
+          ck(launch_scale_rows(pt, sd.p, (int)nZP, (int)N, stream), "pump profile");
+          launches += 2;
+          ck(cudaStreamSynchronize(stream), "pump");
+        }
+        ck(cudaStreamSynchronize(stream), "pump");
+      }
+    }
+    pumpVersion++;
+  }
+
+  // solvers/Chi3.cpp:41-70
+  void runPumpChi3() {
+    if (!(is_pow2((int)N) && N >= 8 && N <= (uint)kMaxFFT)) throw Unsupported("Chi3 pump march needs a power-of-two grid of 8..8192 points");
+    FFTPlanH plan = make_plan((int)N, N <= 4096 ? 8 : 16);
+    std::vector<double2> e(N), hP(N), dP(N), bP(N);
+    for (uint k = 0; k < N; k++) {
+      e[k] = make_double2(envelope[0][k].real(), envelope[0][k].imag());
+      const cplx h = std::exp((0.5 * kI * dzp) * dispPump[0][k]);
+      const cplx b = std::exp((-0.5 * kI * dzp) * dispPump[0][k]);
+      hP[k] = make_double2(h.real(), h.imag());
+      dP[k] = make_double2(dstepPump[0][k].real(), dstepPump[0][k].imag());
+      bP[k] = make_double2(b.real(), b.imag());
+    }
+    std::vector<double2> rel(nZP);
+    const cplx scale = dzp / dz * nlStep[0];
+    const double lo = -0.5 * z, hi = 0.5 * z, step = nZP > 1 ? (hi - lo) / (nZP - 1) : 0;
+    for (uint i = 0; i < nZP; i++) {
+      const double zz = (i + 1 == nZP) ? hi : lo + i * step;
+      const double x = zz / rayleigh;
+      cplx r;
+      switch (profile) {
+        default:
+        case NLM_CONSTANT: r = scale; break;
+        case NLM_GAUSSIAN_BEAM: r = scale / (1 + x * x); break;
+        case NLM_GAUSSIAN_APODIZATION: r = scale * std::exp(-(x * x)); break;
+      }
+      rel[i] = make_double2(r.real(), r.imag());
+    }
+    DevBuf<double2> de, dh, dd, db, dr;
+    upload(de, e);
+    upload(dh, hP);
+    upload(dd, dP);
+    upload(db, bP);
+    upload(dr, rel);
+    ck(launch_pump_chi3(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, plan, tw, stream), "chi3 pump");
+    launches++;
+    ck(cudaStreamSynchronize(stream), "chi3 pump");
+  }
+
+  // src/_NonlinearMedium.cpp:506-534
+  void setPumpFrom(Medium& other, uint modeIndex, double delay, uint idx) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    if (other.isCascade) throw std::invalid_argument("Medium does not have same time and frequency axes as this one");
+    if (other.N != N || other.tMax != tMax)
+      throw std::invalid_argument("Medium does not have same time and frequency axes as this one");
+    if (modeIndex >= nSignal) throw std::invalid_argument("Mode index larger than number of modes in medium");
+    if (idx >= nPump) throw std::invalid_argument("Invalid pump index");
+    if (other.nZ < nZ) throw std::invalid_argument("Medium does not have sufficient resolution to be used with this one");
+    if (modeIndex >= other.nSignal) throw std::invalid_argument("Mode index larger than number of modes in medium");
+    ensureDevice();
+    other.ensureDevice();
+    ck(cudaStreamSynchronize(other.stream), "other medium");
+    const double ratio = static_cast<double>(other.nZ - 1) / (nZP - 1);
+    double2* pf = pumpFreq.p + (size_t)idx * nZP * N;
+    double2* pt = pumpTime.p + (size_t)idx * nZP * N;
+    ck(launch_pump_from(other.sigFreq.p + (size_t)modeIndex * other.nZ * N, (int)other.nZ, ratio, other.dz,
+                        dispPumpD.p + (size_t)idx * N, other.dispSignD.p + (size_t)modeIndex * N, dzp,
+                        beta1[idx] * delay, omegaD.p, (int)nZP, (int)N, z, other.z, pf, stream),
+       "pump from");
+    FFTPlanH plan = fftPlanRows();
+    // rows 0..nZStepsP-2; the reference then re-transforms row nZSteps-1 (unchanged) and leaves the
+    // last time-domain row as it was (src/_NonlinearMedium.cpp:533)
+    if (nZP > 1) ck(launch_fft_rows(pf, pt, nZP - 1, plan, tw, true, 1.0 / N, nullptr, stream), "pump from ifft");
+    launches += 2;
+    ck(cudaStreamSynchronize(stream), "pump from");
+    pumpVersion++;
+  }
+
+  // ---- propagation --------------------------------------------------------------------------
+  int chooseR() const {
+    const int M = (int)nSignal;
+    if (solver == kChi3GNLSE) return 8;
+    if (M >= 3) return 4;
+    if (M == 1 && N > 4096) return 16;
+    return 8;
+  }
+
+  const KernelEntry* findKernel(int kind, int key, int R) const {
+    int count = 0;
+    const KernelEntry* t = kernel_table(&count);
+    for (int i = 0; i < count; i++)
+      if (t[i].kind == kind && t[i].key == key && (R == 0 || t[i].R == R)) return &t[i];
+    return nullptr;
+  }
+
+  bool linearSolver() const { return kSolvers[solver].linear; }
+
+  void checkGrid(int R) const {
+    if (!is_pow2((int)N) || (int)N < R || N > (uint)kMaxFFT || N / R > 512)
+      throw Unsupported("grid of " + std::to_string(N) + " points is not supported by the fused split-step kernels "
+                        "(power of two, R=" + std::to_string(R) + " to 8192 points)");
+  }
+
+  struct Schedule {
+    int grid, block, ipc;
+    size_t smem;
+  };
+
+  Schedule schedule(const KernelEntry* k, long long nInst, int R) {
+    const int T = (int)N / R;
+    int ipc = T >= 128 ? 1 : 128 / T;
+    if (ipc > nInst) ipc = (int)std::max<long long>(1, nInst);
+    const int block = T * ipc;
+    const size_t smem = (size_t)ipc * N * sizeof(double2);
+    int dev = 0, sms = 1, optin = 0;
+    ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((int)smem > optin) throw Unsupported("grid too large for shared memory");
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin), "smem attribute");
+    cudaFuncAttributes fa;
+    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    if (block > fa.maxThreadsPerBlock)
+      throw Unsupported("propagation kernel cannot launch " + std::to_string(block) + " threads (registers)");
+    int maxActive = 0;
+    ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxActive, k->fn, block, smem), "occupancy");
+    if (maxActive < 1) throw Unsupported("propagation kernel does not fit on an SM");
+    const long long groups = (nInst + ipc - 1) / ipc;
+    int best = 1;
+    double bestScore = -1;
+    for (int kk = 1; kk <= maxActive; kk++) {
+      const long long slots = (long long)sms * kk;
+      const long long waves = (groups + slots - 1) / slots;
+      const double eff = (double)groups / (double)(waves * slots);
+      const double warps = (double)kk * block / 32.0;
+      const double sat = std::min(1.0, warps / 8.0);
+      const double score = eff * sat;
+      if (score > bestScore + 1e-9) {
+        bestScore = score;
+        best = kk;
+      }
+    }
+    if (ctaPerSM > 0) best = std::min(ctaPerSM, maxActive);
+    long long grid = std::min<long long>(groups, (long long)sms * best);
+    Schedule s{(int)std::max<long long>(1, grid), block, ipc, smem};
+    return s;
+  }
+
+  PropArgs baseArgs(int R) const {
+    PropArgs a{};
+    a.plan = make_plan((int)N, R);
+    a.R = R;
+    a.nModes = (int)nSignal;
+    a.nZ = (int)nZ;
+    a.tw = tw;
+    a.dstep = dstep.p;
+    a.dlast = dlast.p;
+    a.half = half.p;
+    a.back = back.p;
+    a.pump = pumpTime.p;
+    a.pumpStride = (long long)nZP * N;
+    a.nPumps = (int)nPump;
+    a.coef = coef.p;
+    a.nCoef = kSolvers[solver].coefs;
+    a.raman = ramanD.p;
+    a.steep = steepD.p;
+    a.relInt = relIntD.p;
+    return a;
+  }
+
+  void buildPropagator(int R) {
+    if (propVersion == pumpVersion && prop.p) return;
+    const int M = (int)nSignal, E = 4 * M * M;
+    const size_t count = (size_t)(nZ > 1 ? nZ - 1 : 0) * E * N;
+    if (count == 0) return;
+    prop.alloc(count);
+    const KernelEntry* k = findKernel(kKindBuildProp, solver, 0);
+    if (!k) throw Unsupported("no propagator kernel for this solver");
+    PropArgs a = baseArgs(R);
+    a.prop = prop.p;
+    const long long total = (long long)(nZ - 1) * N;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (total + 127) / 128;
+    grid = std::min<long long>(grid, (long long)sms * 16);
+    void* args[] = {(void*)&a};
+    ck(cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(128), args, 0, stream), "propagator build");
+    launches++;
+    propVersion = pumpVersion;
+  }
+
+  bool wantPropagator(long long nInst) const {
+    if (!linearSolver()) return false;
+    if (usePropagator == 0) return false;
+    const double bytes = (double)(nZ > 1 ? nZ - 1 : 0) * 4.0 * nSignal * nSignal * N * 8.0;
+    if (bytes > 16e9) return false;
+    if (usePropagator == 1) return true;
+    return nInst >= 4LL * nSignal;
+  }
+
+  // Launch one propagation kernel over `nInst` instances (inputs/outputs prepared in `a`).
+  void propagate(PropArgs a, long long nInst, bool allowPropagator, bool plainOne = false) {
+    const int R = chooseR();
+    checkGrid(R);
+    a.nInst = nInst;
+    const KernelEntry* k = nullptr;
+    bool gnlse = solver == kChi3GNLSE;
+    if (gnlse) {
+      k = findKernel(kKindGnlse, solver, R);
+    } else if (allowPropagator && wantPropagator(nInst)) {
+      buildPropagator(R);
+      a.prop = prop.p;
+      k = findKernel(kKindLinear, (int)nSignal, R);
+    } else {
+      k = findKernel(kKindDirect, solver, R);
+    }
+    if (!k) throw Unsupported("no fused kernel for this solver and grid");
+    Schedule s = schedule(k, nInst, R);
+    if (plainOne) s.grid = 1;
+    a.ipc = s.ipc;
+    if (timeKernels) {
+      if (!ev0) ck(cudaEventCreate(&ev0), "event");
+      if (!ev1) ck(cudaEventCreate(&ev1), "event");
+      ck(cudaEventRecord(ev0, stream), "event");
+    }
+    if (gnlse) {
+      const size_t need = (size_t)s.grid * s.ipc * 2 * N;
+      scratch.reserve(need);
+      double2* sp = scratch.p;
+      void* args[] = {(void*)&a, (void*)&sp};
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    } else {
+      void* args[] = {(void*)&a};
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    }
+    launches++;
+    if (timeKernels) {
+      ck(cudaEventRecord(ev1, stream), "event");
+      ck(cudaEventSynchronize(ev1), "event");
+      float ms = 0;
+      ck(cudaEventElapsedTime(&ms, ev0, ev1), "event");
+      kernelMs += ms;
+      kernelCount++;
+    }
+  }
+
+  // ---- public operations ---------------------------------------------------------------------
+  void runSignal(const double* in, size_t n, int inTime, uint inputMode) {
+    if (isCascade) throw std::runtime_error("cascade");
+    if (n % N != 0 || n / N == 0 || n / N > nSignal)
+      throw std::invalid_argument("inputProf array size does not match number of frequency/time bins");
+    if (inputMode >= nSignal) throw std::invalid_argument("inputModes does not match any mode in the system");
+    ensureDevice();
+    const int R = chooseR();
+    checkGrid(R);
+    io.reserve(n);
+    ck(cudaMemcpyAsync(io.p, in, n * sizeof(double2), cudaMemcpyHostToDevice, stream), "input upload");
+    PropArgs a = baseArgs(R);
+    a.inKind = 1;
+    a.inTime = inTime ? 1 : 0;
+    a.in = io.p;
+    a.inStride = (long long)n;
+    a.inChannels = (int)(n / N);
+    a.inputMode = (a.inChannels > 1 || nSignal <= 1) ? 0 : (int)inputMode;
+    a.gridF = sigFreq.p;
+    a.gridT = sigTime.p;
+    propagate(a, 1, false);
+    ck(cudaStreamSynchronize(stream), "signal simulation");
+    signalVersion++;
+  }
+
+  // mode selection of computeGreensFunction, src/_NonlinearMedium.cpp:266-302
+  void greenModes(unsigned nThreads, const uint8_t* useIn, size_t nIn, const uint8_t* useOut, size_t nOut,
+                  std::vector<int>& inputs, std::vector<int>& outputs) const {
+    if (nIn > nSignal) throw std::invalid_argument("List of requested inputs indices longer than number of modes!");
+    if (nOut > nSignal) throw std::invalid_argument("List of requested output indices longer than number of modes!");
+    auto count = [&](const uint8_t* v, size_t n) {
+      uint c = 0;
+      for (size_t i = 0; i < n; i++) c += (v[i] < nSignal);
+      return c;
+    };
+    if (nIn > 0 && count(useIn, nIn) == 0) throw std::invalid_argument("Requested no valid inputs!");
+    if (nOut > 0 && count(useOut, nOut) == 0) throw std::invalid_argument("Requested no valid outputs!");
+    inputs.clear();
+    outputs.clear();
+    for (uint m = 0; m < nSignal; m++) {
+      if (nIn == 0 || (m < nIn && useIn[m])) inputs.push_back((int)m);
+      if (nOut == 0 || (m < nOut && useOut[m])) outputs.push_back((int)m);
+    }
+    // the reference indexes past its selection here (undefined); a 0/1 mask is used instead
+    if (inputs.empty()) throw std::invalid_argument("Requested no valid inputs!");
+    if (outputs.empty()) throw std::invalid_argument("Requested no valid outputs!");
+    if (nThreads > N * inputs.size()) throw std::invalid_argument("Too many threads requested!");
+    if (nThreads == 0) throw std::invalid_argument("Too many threads requested!");
+  }
+
+  void green(int inTime, int runPumpFlag, unsigned nThreads, int normalize, const uint8_t* useIn, size_t nUseIn,
+             const uint8_t* useOut, size_t nUseOut, double2* Cdst, double2* Sdst, bool deviceDst,
+             long long maxInstances = -1) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    std::vector<int> inputs, outputs;
+    greenModes(nThreads, useIn, nUseIn, useOut, nUseOut, inputs, outputs);
+    if (runPumpFlag) runPump();
+    ensureDevice();
+    const int R = chooseR();
+    checkGrid(R);
+    const int nIn = (int)inputs.size(), nOut = (int)outputs.size();
+    const long long nInst = 2LL * nIn * N;
+    const long long outStride = (long long)nOut * N;
+    raw.reserve((size_t)nInst * outStride);
+    PropArgs a = baseArgs(R);
+    a.inKind = 0;
+    a.inTime = inTime ? 1 : 0;
+    for (int i = 0; i < nIn; i++) a.impModes[i] = inputs[i];
+    a.nOut = nOut;
+    for (int i = 0; i < nOut; i++) a.outModes[i] = outputs[i];
+    a.out = raw.p;
+    a.outStride = outStride;
+    if (maxInstances >= 0) {
+      // one propagation per launch (timing helper)
+      ck(cudaMemsetAsync(raw.p, 0, (size_t)nInst * outStride * sizeof(double2), stream), "memset");
+      const long long todo = std::min(nInst, maxInstances == 0 ? nInst : maxInstances);
+      for (long long i = 0; i < todo; i++) {
+        PropArgs b = a;
+        b.instBase = i;
+        propagate(b, 1, false, true);
+      }
+    } else {
+      propagate(a, nInst, true);
+    }
+    // epilogue flags per (om, im) block, src/_NonlinearMedium.cpp:360-372
+    std::vector<uint8_t> flags((size_t)nOut * nIn, 0);
+    std::vector<double2> scales((size_t)nOut * nIn, make_double2(1, 0));
+    for (int im = 0; im < std::min(nOut, nIn); im++)
+      for (int om = 0; om < nOut; om++) {
+        uint8_t f = 1;
+        if (normalize && im != om) {
+          f |= 2;
+          const cplx s = std::sqrt(nlStep[im] / nlStep[om]);
+          scales[(size_t)om * nIn + im] = make_double2(s.real(), s.imag());
+        }
+        flags[(size_t)om * nIn + im] = f;
+      }
+    flagsD.reserve(flags.size());
+    ck(cudaMemcpyAsync(flagsD.p, flags.data(), flags.size(), cudaMemcpyHostToDevice, stream), "flags");
+    upload(scaleD, scales);
+    const size_t mat = (size_t)nOut * N * nIn * N;
+    double2 *C = nullptr, *S = nullptr;
+    if (deviceDst) {
+      C = Cdst;
+      S = Sdst;
+    } else {
+      cs.reserve(2 * mat);
+      C = cs.p;
+      S = cs.p + mat;
+    }
+    ck(launch_green_epilogue(raw.p, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, C, S, stream), "epilogue");
+    launches++;
+    if (!deviceDst) {
+      ck(cudaMemcpyAsync(Cdst, C, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "C download");
+      ck(cudaMemcpyAsync(Sdst, S, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "S download");
+    }
+    ck(cudaStreamSynchronize(stream), "green");
+  }
+
+  void greenDims(unsigned nThreads, const uint8_t* useIn, size_t nUseIn, const uint8_t* useOut, size_t nUseOut,
+                 size_t* rows, size_t* cols) const {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    std::vector<int> inputs, outputs;
+    greenModes(nThreads, useIn, nUseIn, useOut, nUseOut, inputs, outputs);
+    *rows = outputs.size() * N;
+    *cols = inputs.size() * N;
+  }
+
+  // src/_NonlinearMedium.cpp:380-406
+  void batchModes(size_t rows, size_t cols, unsigned nThreads, uint inputMode, const uint8_t* useOut, size_t nUseOut,
+                  std::vector<int>& outputs) const {
+    if (cols % N != 0 || cols / N == 0 || cols / N > nSignal) throw std::invalid_argument("Signals not of correct length!");
+    if (nThreads > rows || nThreads == 0) throw std::invalid_argument("Too many threads requested!");
+    if (inputMode >= nSignal) throw std::invalid_argument("inputModes does not match any mode in the system");
+    outputs.clear();
+    if (nUseOut > 0) {
+      uint c = 0;
+      for (size_t i = 0; i < nUseOut; i++) c += (useOut[i] != 0);
+      if (c == 0) throw std::invalid_argument("Requested no outputs!");
+    }
+    for (uint m = 0; m < nSignal; m++)
+      if (nUseOut == 0 || (m < nUseOut && useOut[m])) outputs.push_back((int)m);
+    if (outputs.empty()) throw std::invalid_argument("Requested no outputs!");
+  }
+
+  void batch(const double2* in, size_t rows, size_t cols, int inTime, int runPumpFlag, unsigned nThreads,
+             uint inputMode, const uint8_t* useOut, size_t nUseOut, double2* out, bool device) {
+    if (isCascade) throw std::runtime_error("cascade");
+    std::vector<int> outputs;
+    batchModes(rows, cols, nThreads, inputMode, useOut, nUseOut, outputs);
+    if (runPumpFlag && !fnl) runPump();
+    ensureDevice();
+    const int R = chooseR();
+    checkGrid(R);
+    const int nOut = (int)outputs.size();
+    const double2* din = in;
+    double2* dout = out;
+    if (!device) {
+      io.reserve(rows * cols);
+      ck(cudaMemcpyAsync(io.p, in, rows * cols * sizeof(double2), cudaMemcpyHostToDevice, stream), "batch upload");
+      din = io.p;
+      work2.reserve(rows * nOut * N);
+      dout = work2.p;
+    }
+    PropArgs a = baseArgs(R);
+    a.inKind = 1;
+    a.inTime = inTime ? 1 : 0;
+    a.in = din;
+    a.inStride = (long long)cols;
+    a.inChannels = (int)(cols / N);
+    a.inputMode = (a.inChannels > 1 || nSignal <= 1) ? 0 : (int)inputMode;
+    a.nOut = nOut;
+    for (int i = 0; i < nOut; i++) a.outModes[i] = outputs[i];
+    a.out = dout;
+    a.outStride = (long long)nOut * N;
+    propagate(a, (long long)rows, true);
+    if (!device)
+      ck(cudaMemcpyAsync(out, dout, rows * nOut * N * sizeof(double2), cudaMemcpyDeviceToHost, stream), "batch download");
+    ck(cudaStreamSynchronize(stream), "batch");
+  }
+
+  // ---- getters ------------------------------------------------------------------------------
+  const std::vector<double>& mirror(int which, uint idx, size_t* rows) {
+    std::vector<std::vector<double>>* store;
+    std::vector<long long>* vers;
+    DevBuf<double2>* dev;
+    uint count, nrows;
+    long long ver;
+    switch (which) {
+      case 0: store = &pumpMirrorF; vers = &pumpMirrorVerF; dev = &pumpFreq; count = nPump; nrows = nZP; ver = pumpVersion; break;
+      case 1: store = &pumpMirrorT; vers = &pumpMirrorVerT; dev = &pumpTime; count = nPump; nrows = nZP; ver = pumpVersion; break;
+      case 2: store = &sigMirrorF; vers = &sigMirrorVerF; dev = &sigFreq; count = nSignal; nrows = nZ; ver = signalVersion; break;
+      case 3: store = &sigMirrorT; vers = &sigMirrorVerT; dev = &sigTime; count = nSignal; nrows = nZ; ver = signalVersion; break;
+      default: throw IndexError("vector::_M_range_check");
+    }
+    if (isCascade || idx >= count) throw IndexError("vector::_M_range_check: index out of range");
+    store->resize(count);
+    vers->resize(count, -2);
+    std::vector<double>& h = (*store)[idx];
+    const size_t len = (size_t)nrows * N * 2;
+    if (h.size() != len) {
+      h.assign(len, 0.0);
+      (*vers)[idx] = -2;
+    }
+    if ((*vers)[idx] != ver) {
+      if (devReady && dev->p && len > 0) {
+        ck(cudaMemcpyAsync(h.data(), dev->p + (size_t)idx * nrows * N, len * sizeof(double), cudaMemcpyDeviceToHost,
+                           stream),
+           "grid download");
+        ck(cudaStreamSynchronize(stream), "grid download");
+      }
+      (*vers)[idx] = ver;
+    }
+    *rows = nrows;
+    return h;
+  }
+};
+
+// ----------------------------------------------------------------------------------------
+// construction (src/_NonlinearMedium.cpp:8-40; src/_FullyNonlinearMedium.hpp:32-38)
+// ----------------------------------------------------------------------------------------
+static Medium* create_medium(int s, const double* args, const double* pump, size_t nPumpVals, const double* pol,
+                             size_t nPol) {
+  BaseParams b = map_ctor(s, args);
+  std::unique_ptr<Medium> m(new Medium());
+  m->solver = s;
+  m->nSignal = b.nSignal;
+  m->nPump = b.nPump;
+  m->fnl = b.fnl;
+  m->poled = b.poled;
+  m->fr = b.fr;
+  m->fb = b.fb;
+  m->tau1 = b.tau1;
+  m->tau2 = b.tau2;
+  m->tau3 = b.tau3;
+  double rayleigh = b.rayleigh;
+  if (b.profile == NLM_CONSTANT) rayleigh = kInf;
+  m->setLengths(b.relativeLength, b.nl, b.zPrecision, rayleigh, b.beta2, b.beta2s, b.beta1, b.beta1s, b.beta3, b.beta3s);
+  m->resetGrids(b.tPrecision, b.tMax);
+  m->setDispersion(b.beta2, b.beta2s, b.beta1, b.beta1s, b.beta3, b.beta3s, b.diffBeta0);
+  if (b.poled) {
+    std::vector<double> p(pol, pol + nPol);
+    m->setPoling(p);
+  }
+  m->profile = m->rayleigh != kInf ? b.profile : NLM_CONSTANT;
+  if (m->nPump > 0) {
+    m->envelope.assign(m->nPump, std::vector<cplx>(m->N, 0.0));
+    if (nPumpVals != 0)
+      m->setPumpCustomImpl(pump, nPumpVals, b.chirp, b.delay, 0);
+    else
+      m->setPumpTypeImpl(b.pulseType, b.chirp, b.delay, 0);
+    for (uint k = 1; k < m->nPump; k++) m->envelope[k].assign(m->N, 0.0);
+  }
+  if (m->fnl) {
+    m->dzp = 0;
+    m->nZP = 0;
+  }
+  return m.release();
+}
+
+}  // namespace nlm
+
+// ==========================================================================================
+// C ABI
+// ==========================================================================================
+using nlm::guarded;
+using nlm::Medium;
+
+struct nlm_medium {
+  Medium* impl;
+};
+
+static Medium* M(nlm_medium* h) {
+  if (!h || !h->impl) throw std::invalid_argument("null medium handle");
+  return h->impl;
+}
+static const Medium* CM(const nlm_medium* h) {
+  if (!h || !h->impl) throw std::invalid_argument("null medium handle");
+  return h->impl;
+}
+
+extern "C" {
+
+const char* nlm_last_error(void) { return nlm::g_error.c_str(); }
+
+const char* nlm_version(void) { return "nonlinearmedium-gb300 0.1"; }
+
+int nlm_solver_count(void) { return nlm::kNumSolvers; }
+
+const char* nlm_solver_name(int index) {
+  if (index < 0 || index >= nlm::kNumSolvers) return nullptr;
+  return nlm::kSolvers[index].name;
+}
+
+const char* nlm_solver_signature(const char* solver) {
+  const int s = solver ? nlm::solver_by_name(solver) : -1;
+  return s < 0 ? nullptr : nlm::kSolvers[s].signature;
+}
+
+nlm_status nlm_create(const char* solver, const double* args, size_t nargs, const double* custom_pump,
+                      size_t n_custom_pump, const double* poling, size_t n_poling, nlm_medium** out) {
+  return guarded([&] {
+    if (!out) throw std::invalid_argument("null output handle");
+    const int s = solver ? nlm::solver_by_name(solver) : -1;
+    if (s < 0) throw std::invalid_argument(std::string("unknown solver ") + (solver ? solver : "(null)"));
+    if ((int)nargs != nlm::scalar_arg_count(s)) throw std::invalid_argument("wrong number of constructor arguments");
+    Medium* m = nlm::create_medium(s, args, custom_pump, n_custom_pump, poling, n_poling);
+    *out = new nlm_medium{m};
+  });
+}
+
+nlm_status nlm_destroy(nlm_medium* medium) {
+  return guarded([&] {
+    if (!medium) return;
+    delete medium->impl;
+    delete medium;
+  });
+}
+
+nlm_status nlm_info(const nlm_medium* h, int* nSig, int* nPump, int* nFreqs, int* nZ, int* nZP, int* fnl, int* casc) {
+  return guarded([&] {
+    const Medium* m = CM(h);
+    if (nSig) *nSig = (int)m->nSignal;
+    if (nPump) *nPump = (int)m->nPump;
+    if (nFreqs) *nFreqs = (int)m->N;
+    if (nZ) *nZ = (int)m->nZ;
+    if (nZP) *nZP = (int)m->nZP;
+    if (fnl) *fnl = m->fnl ? 1 : 0;
+    if (casc) *casc = m->isCascade ? 1 : 0;
+  });
+}
+
+nlm_status nlm_lengths(const nlm_medium* h, double* z, double* dz, double* dzp, double* tMax) {
+  return guarded([&] {
+    const Medium* m = CM(h);
+    if (z) *z = m->z;
+    if (dz) *dz = m->dz;
+    if (dzp) *dzp = m->dzp;
+    if (tMax) *tMax = m->tMax;
+  });
+}
+
+nlm_status nlm_set_pump_type(nlm_medium* h, int pulse_type, double chirp, double delay, unsigned pump_index) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) {  // src/Cascade.cpp:55-72
+      if (m->sharedPump) m->media[0]->setPumpType(pulse_type, chirp, delay, pump_index);
+      else for (Medium* x : m->media) x->setPumpType(pulse_type, chirp, delay, pump_index);
+      return;
+    }
+    m->setPumpType(pulse_type, chirp, delay, pump_index);
+  });
+}
+
+nlm_status nlm_set_pump_custom(nlm_medium* h, const double* custom_pump, size_t n, double chirp, double delay,
+                               unsigned pump_index) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) {
+      if (m->sharedPump) m->media[0]->setPumpCustom(custom_pump, n, chirp, delay, pump_index);
+      else for (Medium* x : m->media) x->setPumpCustom(custom_pump, n, chirp, delay, pump_index);
+      return;
+    }
+    m->setPumpCustom(custom_pump, n, chirp, delay, pump_index);
+  });
+}
+
+nlm_status nlm_set_pump_from(nlm_medium* h, const nlm_medium* other, unsigned mode_index, double delay,
+                             unsigned pump_index) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) throw std::runtime_error("Object does not have this method.");
+    m->setPumpFrom(*const_cast<Medium*>(CM(other)), mode_index, delay, pump_index);
+  });
+}
+
+static void cascade_run_pump(Medium* c) {
+  // src/Cascade.cpp:75-88
+  if (!c->sharedPump) {
+    for (Medium* x : c->media) x->runPump();
+  } else {
+    c->media[0]->runPump();
+    for (size_t i = 1; i < c->media.size(); i++) {
+      Medium* prev = c->media[i - 1];
+      Medium* cur = c->media[i];
+      size_t rows = 0;
+      const std::vector<double>& pt = prev->mirror(1, 0, &rows);
+      if (cur->envelope.empty()) throw std::runtime_error("Object does not have this method.");
+      if (cur->N != prev->N) throw std::invalid_argument("Medium does not have same time and frequency axes as the first");
+      const size_t last = (rows - 1) * prev->N * 2;
+      for (nlm::uint k = 0; k < cur->N; k++) cur->envelope[0][k] = nlm::cplx(pt[last + 2 * k], pt[last + 2 * k + 1]);
+      cur->runPump();
+    }
+  }
+}
+
+nlm_status nlm_run_pump(nlm_medium* h) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {
+      cascade_run_pump(m);
+      return;
+    }
+    m->runPump();
+  });
+}
+
+nlm_status nlm_run_signal(nlm_medium* h, const double* input_prof, size_t n, int in_time_domain, unsigned input_mode) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {  // src/Cascade.cpp:91-107
+      m->media[0]->runSignal(input_prof, n, in_time_domain, input_mode);
+      for (size_t i = 1; i < m->media.size(); i++) {
+        const auto& conn = m->connections[i - 1];
+        nlm::uint maxIn = 0;
+        for (auto& kv : conn) maxIn = std::max(maxIn, kv.first);
+        Medium* prev = m->media[i - 1];
+        std::vector<double> nxt((size_t)m->N * (maxIn + 1) * 2, 0.0);
+        for (auto& kv : conn) {
+          size_t rows = 0;
+          const std::vector<double>& sf = prev->mirror(2, kv.second, &rows);
+          const size_t last = (rows - 1) * prev->N * 2;
+          std::copy(sf.begin() + last, sf.begin() + last + 2 * m->N, nxt.begin() + (size_t)kv.first * m->N * 2);
+        }
+        m->media[i]->runSignal(nxt.data(), nxt.size() / 2, 0, 0);
+      }
+      return;
+    }
+    m->runSignal(input_prof, n, in_time_domain, input_mode);
+  });
+}
+
+nlm_status nlm_green_dims(nlm_medium* h, unsigned n_threads, const uint8_t* use_input, size_t n_use_input,
+                          const uint8_t* use_output, size_t n_use_output, size_t* rows, size_t* cols) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) {
+      // composition of the media's matrices, src/Cascade.cpp:110-135
+      size_t r = 0, c = 0;
+      const size_t last = m->media.size() - 1;
+      m->media[0]->greenDims(n_threads, use_input, n_use_input, last == 0 ? use_output : nullptr,
+                             last == 0 ? n_use_output : 0, &r, &c);
+      size_t cols0 = c;
+      for (size_t i = 1; i < m->media.size(); i++) {
+        size_t ri = 0, ci = 0;
+        m->media[i]->greenDims(n_threads, nullptr, 0, i == last ? use_output : nullptr, i == last ? n_use_output : 0, &ri, &ci);
+        if (ci != r) throw std::invalid_argument("Cascade Green's function dimensions do not chain");
+        r = ri;
+      }
+      *rows = r;
+      *cols = cols0;
+      return;
+    }
+    m->greenDims(n_threads, use_input, n_use_input, use_output, n_use_output, rows, cols);
+  });
+}
+
+static void cascade_green(Medium* c, int inTime, int runPump, unsigned nThreads, int normalize, const uint8_t* useIn,
+                          size_t nIn, const uint8_t* useOut, size_t nOut, double2* Cdst, double2* Sdst, bool dev) {
+  if (runPump) cascade_run_pump(c);
+  const size_t last = c->media.size() - 1;
+  Medium* m0 = c->media[0];
+  size_t r = 0, cc = 0;
+  m0->greenDims(nThreads, useIn, nIn, last == 0 ? useOut : nullptr, last == 0 ? nOut : 0, &r, &cc);
+  nlm::DevBuf<double2> C, S, Ci, Si, Ct, St;
+  C.alloc(r * cc);
+  S.alloc(r * cc);
+  m0->green(inTime, 0, nThreads, normalize, useIn, nIn, last == 0 ? useOut : nullptr, last == 0 ? nOut : 0, C.p, S.p, true);
+  for (size_t i = 1; i < c->media.size(); i++) {
+    Medium* mi = c->media[i];
+    size_t ri = 0, ci = 0;
+    mi->greenDims(nThreads, nullptr, 0, i == last ? useOut : nullptr, i == last ? nOut : 0, &ri, &ci);
+    if (ci != r) throw std::invalid_argument("Cascade Green's function dimensions do not chain");
+    Ci.alloc(ri * ci);
+    Si.alloc(ri * ci);
+    mi->green(inTime, 0, nThreads, normalize, nullptr, 0, i == last ? useOut : nullptr, i == last ? nOut : 0, Ci.p, Si.p, true);
+    Ct.alloc(ri * cc);
+    St.alloc(ri * cc);
+    nlm::ck(nlm::launch_cgemm_compose(Ci.p, Si.p, C.p, S.p, (int)ri, (int)ci, (int)cc, Ct.p, St.p, mi->stream), "compose");
+    nlm::ck(cudaStreamSynchronize(mi->stream), "compose");
+    std::swap(C.p, Ct.p);
+    std::swap(C.n, Ct.n);
+    std::swap(S.p, St.p);
+    std::swap(S.n, St.n);
+    r = ri;
+  }
+  const size_t bytes = r * cc * sizeof(double2);
+  nlm::ck(cudaMemcpy(Cdst, C.p, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost), "C");
+  nlm::ck(cudaMemcpy(Sdst, S.p, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost), "S");
+}
+
+nlm_status nlm_green(nlm_medium* h, int in_time_domain, int run_pump, unsigned n_threads, int normalize,
+                     const uint8_t* use_input, size_t n_use_input, const uint8_t* use_output, size_t n_use_output,
+                     double* green_c, double* green_s) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {
+      cascade_green(m, in_time_domain, run_pump, n_threads, normalize, use_input, n_use_input, use_output, n_use_output,
+                    reinterpret_cast<double2*>(green_c), reinterpret_cast<double2*>(green_s), false);
+      return;
+    }
+    m->green(in_time_domain, run_pump, n_threads, normalize, use_input, n_use_input, use_output, n_use_output,
+             reinterpret_cast<double2*>(green_c), reinterpret_cast<double2*>(green_s), false);
+  });
+}
+
+nlm_status nlm_green_device(nlm_medium* h, int in_time_domain, int run_pump, unsigned n_threads, int normalize,
+                            const uint8_t* use_input, size_t n_use_input, const uint8_t* use_output, size_t n_use_output,
+                            void* green_c_dev, void* green_s_dev) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {
+      cascade_green(m, in_time_domain, run_pump, n_threads, normalize, use_input, n_use_input, use_output, n_use_output,
+                    nlm::d2(green_c_dev), nlm::d2(green_s_dev), true);
+      return;
+    }
+    m->green(in_time_domain, run_pump, n_threads, normalize, use_input, n_use_input, use_output, n_use_output,
+             nlm::d2(green_c_dev), nlm::d2(green_s_dev), true);
+  });
+}
+
+nlm_status nlm_green_plain(nlm_medium* h, int in_time_domain, int run_pump, size_t max_instances, double* green_c,
+                           double* green_s) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    m->green(in_time_domain, run_pump, 1, 0, nullptr, 0, nullptr, 0, reinterpret_cast<double2*>(green_c),
+             reinterpret_cast<double2*>(green_s), false, (long long)max_instances);
+  });
+}
+
+nlm_status nlm_batch_dims(nlm_medium* h, size_t rows, size_t cols, unsigned n_threads, unsigned input_mode,
+                          const uint8_t* use_output, size_t n_use_output, size_t* out_cols) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) {
+      // outputs of the last medium (src/Cascade.cpp:160-162)
+      Medium* last = m->media.back();
+      std::vector<int> outs;
+      m->media[0]->batchModes(rows, cols, n_threads, input_mode, nullptr, 0, outs);
+      last->batchModes(rows, last->N, n_threads, 0, use_output, n_use_output, outs);
+      *out_cols = outs.size() * last->N;
+      return;
+    }
+    std::vector<int> outs;
+    m->batchModes(rows, cols, n_threads, input_mode, use_output, n_use_output, outs);
+    *out_cols = outs.size() * m->N;
+  });
+}
+
+static void cascade_batch(Medium* c, const double2* in, size_t rows, size_t cols, int inTime, int runPump,
+                          unsigned nThreads, unsigned inputMode, const uint8_t* useOut, size_t nUseOut, double2* out,
+                          bool device) {
+  if (runPump) cascade_run_pump(c);
+  const size_t last = c->media.size() - 1;
+  Medium* m0 = c->media[0];
+  std::vector<int> outs;
+  m0->batchModes(rows, cols, nThreads, inputMode, last == 0 ? useOut : nullptr, last == 0 ? nUseOut : 0, outs);
+  size_t curCols = outs.size() * m0->N;
+  nlm::DevBuf<double2> a, b;
+  a.alloc(rows * curCols);
+  nlm::DevBuf<double2> inD;
+  const double2* src = in;
+  if (!device) {
+    inD.alloc(rows * cols);
+    nlm::ck(cudaMemcpy(inD.p, in, rows * cols * sizeof(double2), cudaMemcpyHostToDevice), "upload");
+    src = inD.p;
+  }
+  m0->batch(src, rows, cols, inTime, 0, nThreads, inputMode, last == 0 ? useOut : nullptr, last == 0 ? nUseOut : 0,
+            a.p, true);
+  for (size_t i = 1; i < c->media.size(); i++) {
+    Medium* mi = c->media[i];
+    std::vector<int> o;
+    mi->batchModes(rows, curCols, nThreads, 0, i == last ? useOut : nullptr, i == last ? nUseOut : 0, o);
+    const size_t nc = o.size() * mi->N;
+    b.alloc(rows * nc);
+    mi->batch(a.p, rows, curCols, inTime, 0, nThreads, 0, i == last ? useOut : nullptr, i == last ? nUseOut : 0, b.p, true);
+    std::swap(a.p, b.p);
+    std::swap(a.n, b.n);
+    curCols = nc;
+  }
+  nlm::ck(cudaMemcpy(out, a.p, rows * curCols * sizeof(double2), device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost),
+          "download");
+}
+
+nlm_status nlm_batch(nlm_medium* h, const double* inputs, size_t rows, size_t cols, int in_time_domain, int run_pump,
+                     unsigned n_threads, unsigned input_mode, const uint8_t* use_output, size_t n_use_output, double* out) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {
+      cascade_batch(m, reinterpret_cast<const double2*>(inputs), rows, cols, in_time_domain, run_pump, n_threads,
+                    input_mode, use_output, n_use_output, reinterpret_cast<double2*>(out), false);
+      return;
+    }
+    m->batch(reinterpret_cast<const double2*>(inputs), rows, cols, in_time_domain, run_pump, n_threads, input_mode,
+             use_output, n_use_output, reinterpret_cast<double2*>(out), false);
+  });
+}
+
+nlm_status nlm_batch_device(nlm_medium* h, const void* inputs_dev, size_t rows, size_t cols, int in_time_domain,
+                            int run_pump, unsigned n_threads, unsigned input_mode, const uint8_t* use_output,
+                            size_t n_use_output, void* out_dev) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (m->isCascade) {
+      cascade_batch(m, reinterpret_cast<const double2*>(inputs_dev), rows, cols, in_time_domain, run_pump, n_threads,
+                    input_mode, use_output, n_use_output, nlm::d2(out_dev), true);
+      return;
+    }
+    m->batch(reinterpret_cast<const double2*>(inputs_dev), rows, cols, in_time_domain, run_pump, n_threads, input_mode,
+             use_output, n_use_output, nlm::d2(out_dev), true);
+  });
+}
+
+nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
+                            double* const* outputs) {
+  return guarded([&] {
+    // one propagation per medium; media with equal solver and grid share a launch
+    for (size_t k = 0; k < n_media; k++) {
+      Medium* m = M(media[k]);
+      std::vector<uint8_t> none;
+      m->batch(reinterpret_cast<const double2*>(inputs[k]), 1, m->N, in_time_domain, 0, 1, 0, nullptr, 0,
+               reinterpret_cast<double2*>(outputs[k]), false);
+    }
+  });
+}
+
+nlm_status nlm_get_grid(nlm_medium* h, int which, unsigned index, const double** data, size_t* rows, size_t* cols) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (which == 4) throw nlm::IndexError("vector::_M_range_check: field index out of range");  // no solver has fields
+    size_t r = 0;
+    const std::vector<double>& v = m->mirror(which, index, &r);
+    *data = v.data();
+    *rows = r;
+    *cols = m->N;
+  });
+}
+
+nlm_status nlm_get_axis(nlm_medium* h, int which, unsigned index, const double** data, size_t* n) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->isCascade) m = m->media.at(0);
+    switch (which) {
+      case 0: *data = m->tau.data(); *n = m->tau.size(); break;
+      case 1: *data = m->omega.data(); *n = m->omega.size(); break;
+      case 2:
+        if (M(h)->isCascade) { *data = nullptr; *n = 0; break; }
+        *data = m->poling.data(); *n = m->poling.size(); break;
+      case 3: {
+        if (m->solver != nlm::kChi3GNLSE) throw std::invalid_argument("not a Chi3GNLSE medium");
+        m->ensureDevice();
+        m->axisBuf.resize(2 * m->N);
+        for (nlm::uint k = 0; k < m->N; k++) {
+          m->axisBuf[2 * k] = m->raman[k].real();
+          m->axisBuf[2 * k + 1] = m->raman[k].imag();
+        }
+        *data = m->axisBuf.data();
+        *n = m->N;
+        break;
+      }
+      case 4: {
+        if (index >= m->envelope.size()) throw nlm::IndexError("pump index out of range");
+        *data = reinterpret_cast<const double*>(m->envelope[index].data());
+        *n = m->envelope[index].size();
+        break;
+      }
+      default: throw std::invalid_argument("unknown axis");
+    }
+  });
+}
+
+nlm_status nlm_cascade_create(nlm_medium* const* media, size_t n_media, const unsigned* connections,
+                              const size_t* conn_counts, size_t n_junctions, int share_pump, nlm_medium** out) {
+  return guarded([&] {
+    // src/Cascade.cpp:3-36
+    if (n_media == 0) throw std::invalid_argument("Cascade must contain at least one medium");
+    std::unique_ptr<Medium> c(new Medium());
+    c->isCascade = true;
+    Medium* first = M(media[0]);
+    c->N = first->N;
+    c->tMax = first->tMax;
+    c->solver = -1;
+    for (size_t i = 0; i < n_media; i++) {
+      Medium* m = M(media[i]);
+      if (m->isCascade) throw std::invalid_argument("nested cascades are not supported");
+      if (m->N != c->N || m->tMax != c->tMax)
+        throw std::invalid_argument("Medium does not have same time and frequency axes as the first");
+      c->media.push_back(m);
+    }
+    if (n_junctions != n_media - 1) throw std::invalid_argument("Must have one connection per pair of adjacent media");
+    size_t off = 0;
+    for (size_t i = 0; i + 1 < n_media; i++) {
+      const size_t cnt = conn_counts ? conn_counts[i] : 0;
+      if (cnt == 0) throw std::invalid_argument("Connections missing between media!");
+      std::map<nlm::uint, nlm::uint> conn;
+      for (size_t k = 0; k < cnt; k++) {
+        const unsigned first_ = connections[2 * (off + k)], second = connections[2 * (off + k) + 1];
+        if (second >= c->media[i]->nSignal || first_ >= c->media[i + 1]->nSignal)
+          throw std::invalid_argument("Invalid connections, out of range");
+        conn[first_] = second;
+      }
+      off += cnt;
+      c->connections.push_back(conn);
+    }
+    c->sharedPump = share_pump != 0;
+    *out = new nlm_medium{c.release()};
+  });
+}
+
+nlm_status nlm_cascade_add(nlm_medium* cascade, nlm_medium* medium, const unsigned* connection, size_t n_pairs) {
+  return guarded([&] {
+    // src/Cascade.cpp:39-52
+    Medium* c = M(cascade);
+    Medium* m = M(medium);
+    if (!c->isCascade) throw std::invalid_argument("not a cascade");
+    if (m->N != c->N || m->tMax != c->tMax)
+      throw std::invalid_argument("Medium does not have same time and frequency axes as the first");
+    if (n_pairs == 0) throw std::invalid_argument("No connection!");
+    std::map<nlm::uint, nlm::uint> conn;
+    for (size_t k = 0; k < n_pairs; k++) {
+      const unsigned first_ = connection[2 * k], second = connection[2 * k + 1];
+      if (second >= c->media.back()->nSignal || first_ >= m->nSignal)
+        throw std::invalid_argument("Invalid connections, out of range");
+      conn[first_] = second;
+    }
+    c->media.push_back(m);
+    c->connections.push_back(conn);
+  });
+}
+
+nlm_status nlm_cascade_media(const nlm_medium* cascade, size_t* n_media) {
+  return guarded([&] {
+    const Medium* c = CM(cascade);
+    *n_media = c->isCascade ? c->media.size() : 0;
+  });
+}
+
+nlm_status nlm_set_stream(nlm_medium* h, void* cuda_stream) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->ownStream && m->stream) cudaStreamDestroy(m->stream);
+    m->ownStream = false;
+    m->stream = reinterpret_cast<cudaStream_t>(cuda_stream);
+    if (!m->stream) {
+      nlm::require_device();
+      nlm::ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "stream");
+      m->ownStream = true;
+    }
+  });
+}
+
+nlm_status nlm_synchronize(nlm_medium* h) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->stream) nlm::ck(cudaStreamSynchronize(m->stream), "synchronize");
+  });
+}
+
+int nlm_device_available(void) { return nlm::device_count() > 0 ? 1 : 0; }
+
+nlm_status nlm_set_schedule(nlm_medium* h, int cta_per_sm, int use_propagator, int use_graph) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->ctaPerSM = cta_per_sm;
+    m->usePropagator = use_propagator;
+    m->useGraph = use_graph;
+  });
+}
+
+nlm_status nlm_last_launch_count(const nlm_medium* h, long* launches) {
+  return guarded([&] { *launches = CM(h)->launches; });
+}
+
+nlm_status nlm_kernel_timing(nlm_medium* h, int enable, double* total_ms, long* count) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (total_ms) *total_ms = m->kernelMs;
+    if (count) *count = m->kernelCount;
+    if (enable == 1) {
+      m->kernelMs = 0;
+      m->kernelCount = 0;
+    }
+    m->timeKernels = enable != 0;
+  });
+}
+
+nlm_status nlm_fp64_peak(double* tflops) {
+  return guarded([&] {
+    nlm::require_device();
+    int dev = 0, sms = 1;
+    nlm::ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 4, threads = 256, iters = 2000;
+    nlm::DevBuf<double> out;
+    out.alloc((size_t)blocks * threads);
+    cudaEvent_t a, b;
+    nlm::ck(cudaEventCreate(&a), "event");
+    nlm::ck(cudaEventCreate(&b), "event");
+    double best = 0;
+    for (int rep = 0; rep < 4; rep++) {
+      nlm::ck(cudaEventRecord(a, 0), "event");
+      nlm::ck(nlm::launch_fp64_peak(out.p, iters, blocks, threads, 0), "fp64 peak");
+      nlm::ck(cudaEventRecord(b, 0), "event");
+      nlm::ck(cudaEventSynchronize(b), "event");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      const double flops = 2.0 * 32.0 * iters * (double)blocks * threads;
+      if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *tflops = best;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// nlm_kernels.h -- launch interface between the host engine (engine.cpp) and the kernels.
+// Plain C++ (no device code): included by both nvcc and g++ translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace nlm {
+
+constexpr int kMaxModes = 4;
+constexpr int kMaxPumps = 2;
+constexpr int kMaxCoefs = 8;
+constexpr int kMaxFFT = 8192;   // largest power-of-two grid of the fused kernels
+
+struct FFTPlanH {
+  int N, T, nPass;
+  int radix[16];
+};
+
+// Arguments of every propagation kernel (batched impulses, dense rows, one full grid).
+struct PropArgs {
+  FFTPlanH plan;          // mirrors nlm::FFTPlan
+  int R;                  // points per thread per mode
+  int nModes;             // signal modes
+  int nZ;                 // nZSteps
+  long long nInst;        // independent propagations in this launch
+  long long instBase;     // global index of the launch's first propagation
+  int ipc;                // propagations per CTA
+  // input description
+  int inKind;             // 0: impulses (Green's function), 1: dense rows
+  int inTime;             // inputs and outputs in the time domain
+  const double2* in;      // dense rows
+  long long inStride;     // complex elements between rows
+  int inChannels;         // number of N-blocks per row
+  int inputMode;          // mode receiving a single N-block
+  int impModes[kMaxModes];// impulses: input mode of impulse group im = inst / (2N)
+  // output description (last row of the selected modes)
+  int nOut;
+  int outModes[kMaxModes];
+  double2* out;
+  long long outStride;
+  // point-wise tables (device)
+  const double2* tw;      // N twiddles exp(-2 pi i m / N)
+  const double2* dstep;   // [mode][N] dispStep / N
+  const double2* dlast;   // [mode][N] dispStep * exp(-i dz/2 D) / N
+  const double2* half;    // [mode][N] exp(+i dz/2 D) / N
+  const double2* back;    // [mode][N] exp(-i dz/2 D) / N
+  const double* prop;     // linear propagator [(nZ-1)][(2M)^2][N]
+  const double2* pump;    // pumpTime [pump][nZStepsP][N]
+  long long pumpStride;   // nZStepsP * N
+  int nPumps;
+  const double2* coef;    // [(nZ-1)][3][nCoef]
+  int nCoef;
+  // full grids of a single propagation (runSignalSimulation); null otherwise
+  double2* gridF;         // [mode][nZ][N]
+  double2* gridT;
+  // Chi3GNLSE tables
+  const double2* raman;   // ramanResponse / N
+  const double2* steep;   // (nlStep0 + nlStep1 * omega) / N
+  const double* relInt;   // [(nZ-1)][3] relative intensity at i-1, i-1/2, i
+};
+
+// Registry of the propagation kernels.  The host engine launches them generically with
+// cudaLaunchKernel(fn, grid, block, {&PropArgs[, &scratch]}, smem, stream).
+enum KernelKind : int {
+  kKindDirect = 0,     // k_propagate_direct<Solver, R>      key = solver id
+  kKindLinear = 1,     // k_propagate_linear<M, R>           key = number of modes M
+  kKindGnlse = 2,      // k_propagate_gnlse<R>               key = solver id (Chi3GNLSE); extra arg: scratch
+  kKindBuildProp = 3   // k_build_propagator<Solver>         key = solver id, R = 0
+};
+struct KernelEntry {
+  int kind;
+  int key;
+  int R;
+  const void* fn;
+};
+// All registered kernels (filled on first call).
+const KernelEntry* kernel_table(int* count);
+cudaError_t launch_fft_rows(const double2* in, double2* out, long long rows, const FFTPlanH& plan,
+                            const double2* tw, bool inverse, double scale, const double2* postMul,
+                            cudaStream_t s);
+cudaError_t launch_pump_linear(const double2* freq0, const double* disp, double dzp, int nRows, int N,
+                               double2* pumpFreq, cudaStream_t s);
+cudaError_t launch_scale_rows(double2* a, const double* scale, int nRows, int N, cudaStream_t s);
+cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
+                             const double2* dstepP, const double2* backP, const double2* rel, int nRows,
+                             const FFTPlanH& plan, const double2* tw, cudaStream_t s);
+cudaError_t launch_green_epilogue(const double2* raw, long long rawStride, int N, int nIn, int nOut,
+                                  const double2* blockScale, const uint8_t* blockShift, double2* C,
+                                  double2* S, cudaStream_t s);
+cudaError_t launch_pump_from(const double2* otherSignalFreq, int otherRows, double ratio, double otherDz,
+                             const double* dispPump, const double* otherDispSign, double dzp, double beta1Delay,
+                             const double* omega, int nRowsP, int N, double z, double otherZ, double2* pumpFreq,
+                             cudaStream_t s);
+cudaError_t launch_cgemm_compose(const double2* Ci, const double2* Si, const double2* C, const double2* S,
+                                 int rows, int inner, int cols, double2* Cout, double2* Sout, cudaStream_t s);
+cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
+
+}  // namespace nlm

@@ -1,0 +1,221 @@
+"""Parity of the CUDA engine with the oracle, through the drop-in API and its C ABI.
+
+Tolerance: relative L2 error <= 1e-9 over every output array (the benchmark spec's bound for FP64
+propagation); the expected level is ~1e-13 since both sides compute in double precision.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+
+def make(nlm, name, **over):
+    return getattr(nlm, name)(**dict(cases.CASES[name], **over))
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n not in cases.FULLY_NONLINEAR])
+def test_pump_grids_match_golden(nlm, golden, name):
+    med = make(nlm, name)
+    med.runPumpSimulation()
+    rows = golden[name + "__pump_rows"]
+    for m in range(golden[name + "__pump_time"].shape[0]):
+        assert cases.rel_l2(med.pumpTimes(m)[rows], golden[name + "__pump_time"][m]) < TOL
+        assert cases.rel_l2(med.pumpFreqs(m)[rows], golden[name + "__pump_freq"][m]) < TOL
+
+
+@pytest.mark.parametrize("name", list(cases.CASES))
+def test_signal_grids_match_golden(nlm, golden, name):
+    med = make(nlm, name)
+    if name not in cases.FULLY_NONLINEAR:
+        med.runPumpSimulation()
+    med.runSignalSimulation(golden[name + "__signal_in"], True, 0)
+    rows = golden[name + "__rows"]
+    for m in range(golden[name + "__signal_time"].shape[0]):
+        assert cases.rel_l2(med.signalTimes(m)[rows], golden[name + "__signal_time"][m]) < TOL, m
+        assert cases.rel_l2(med.signalFreqs(m)[rows], golden[name + "__signal_freq"][m]) < TOL, m
+
+
+@pytest.mark.parametrize("name", list(cases.CASES))
+def test_batch_matches_golden(nlm, golden, name):
+    med = make(nlm, name)
+    x = golden[name + "__batch_in"]
+    if name in cases.FULLY_NONLINEAR:
+        out = med.batchSignalSimulation(x, False, 1, 0)
+    else:
+        med.runPumpSimulation()
+        out = med.batchSignalSimulation(x, False, False)
+    assert out.shape == golden[name + "__batch_out"].shape
+    assert cases.rel_l2(out, golden[name + "__batch_out"]) < TOL
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n not in cases.FULLY_NONLINEAR])
+@pytest.mark.parametrize("use_prop", [1, 0])
+def test_green_matches_golden(nlm, golden, name, use_prop):
+    med = make(nlm, name)
+    med._set_schedule(use_propagator=use_prop)
+    med.runPumpSimulation()
+    C, S = med.computeGreensFunction(False, False)
+    assert cases.rel_l2(C, golden[name + "__green_c"]) < TOL
+    assert cases.rel_l2(S, golden[name + "__green_s"]) < TOL
+    Ct, St = med.computeGreensFunction(True, False)
+    assert cases.rel_l2(Ct, golden[name + "__green_c_time"]) < TOL
+    assert cases.rel_l2(St, golden[name + "__green_s_time"]) < TOL
+
+
+def test_green_options_match_oracle(nlm, oracle):
+    """normalize, useInput/useOutput masks on a two-mode solver (src/_NonlinearMedium.cpp:266-372)."""
+    kw = dict(cases.CASES["Chi2SFG"])
+    med, ref = nlm.Chi2SFG(**kw), oracle.Chi2SFG(**kw)
+    for norm, ui, uo in ((True, [], []), (False, [1, 1], [1, 0]), (True, [1, 1], [0, 1]), (False, [], [1])):
+        C, S = med.computeGreensFunction(False, True, 1, norm, ui, uo)
+        Cr, Sr = ref.compute_greens_function(False, True, 1, norm, ui, uo)
+        assert C.shape == Cr.shape
+        assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+
+
+def test_batch_options_match_oracle(nlm, oracle):
+    kw = dict(cases.CASES["Chi2SFGII"])
+    med, ref = nlm.Chi2SFGII(**kw), oracle.Chi2SFGII(**kw)
+    n = med._dims["nFreqs"]
+    rng = np.random.default_rng(5)
+    x2 = cases.noise(rng, 4 * 2 * n, 1.0).reshape(4, 2 * n)
+    x1 = cases.noise(rng, 4 * n, 1.0).reshape(4, n)
+    for x, mode, uo, t in ((x2, 0, [1, 0, 1, 1], True), (x1, 3, [0, 1], False), (x1, 2, [], True)):
+        out = med.batchSignalSimulation(x, t, True, 1, mode, uo)
+        refo = ref.batch_signal_simulation(x, t, True, 1, mode, uo)
+        assert cases.rel_l2(out, refo) < TOL
+
+
+def test_chirp_delay_and_custom_pump(nlm, oracle):
+    kw = dict(cases.CASES["Chi2PDC"], chirp=0.3, delay=0.2)
+    med, ref = nlm.Chi2PDC(**kw), oracle.Chi2PDC(**kw)
+    assert cases.rel_l2(med._axis(4, 0, complex_=True), ref.envelope[0]) < 1e-13
+    rng = np.random.default_rng(3)
+    p = np.exp(-ref.tau ** 2 / 3) * (1 + 0.1 * rng.standard_normal(ref.n_freqs))
+    med.setPump(p, chirp=-0.2, delay=0.1)
+    ref.set_pump_custom(p, -0.2, 0.1)
+    med.setPump(nlm.Sinc, 0.1)
+    ref.set_pump_type(oracle.SINC, 0.1)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+
+
+def test_gaussian_beam_profile_pump(nlm, oracle):
+    kw = dict(cases.CASES["Chi2SFG"], rayleighLength=0.6, intensityProfile=0)
+    med, ref = nlm.Chi2SFG(**kw), oracle.Chi2SFG(**kw)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    kw = dict(cases.CASES["Chi3"], rayleighLength=0.6, intensityProfile=2)
+    med, ref = nlm.Chi3(**kw), oracle.Chi3(**kw)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+
+
+def test_set_pump_from_other_medium(nlm, oracle):
+    """setPump(other) copies another medium's signal with the frame phase (src/_NonlinearMedium.cpp:506-534)."""
+    kw1 = dict(cases.CASES["Chi2SFG"], zPrecision=20)
+    kw2 = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10, zPrecision=10, poling=[])
+    a, ra = nlm.Chi2SFG(**kw1), oracle.Chi2SFG(**kw1)
+    b, rb = nlm.Chi2PDC(**kw2), oracle.Chi2PDC(**kw2)
+    x = cases.signal_input("Chi2SFG", 32, 2, seed=4)
+    a.runPumpSimulation()
+    ra.run_pump_simulation()
+    a.runSignalSimulation(x)
+    ra.run_signal_simulation(x)
+    b.runPumpSimulation()
+    rb.run_pump_simulation()
+    b.setPump(a, 1, 0.3)
+    rb.set_pump_other(ra, 1, 0.3)
+    assert cases.rel_l2(b.pumpFreq, rb.pump_freq[0]) < TOL
+    assert cases.rel_l2(b.pumpTime, rb.pump_time[0]) < TOL
+    C, S = b.computeGreensFunction(runPump=False)
+    Cr, Sr = rb.compute_greens_function(run_pump=False)
+    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+
+
+def test_cascade_matches_oracle(nlm, oracle):
+    kwa = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10)
+    kwb = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10, beta1s=-1, diffBeta0=0.2)
+    a, b = nlm.Chi2PDC(**kwa), nlm.Chi2PDC(**kwb)
+    ra, rb = oracle.Chi2PDC(**kwa), oracle.Chi2PDC(**kwb)
+    c = nlm.Cascade([a, b], [{0: 0}], True)
+    rc = oracle.Cascade([ra, rb], [{0: 0}], True)
+    C, S = c.computeGreensFunction()
+    Cr, Sr = rc.compute_greens_function()
+    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+    x = cases.signal_input("Chi2PDC", 32, 1, seed=9)
+    c.runSignalSimulation(x)
+    rc.run_signal_simulation(x)
+    assert cases.rel_l2(b.signalFreq, rb.signal_freq[0]) < TOL
+    xb = np.stack([cases.signal_input("Chi2PDC", 32, 1, seed=k) for k in range(3)])
+    assert cases.rel_l2(c.batchSignalSimulation(xb), rc.batch_signal_simulation(xb)) < TOL
+
+
+def test_plain_equals_batched(nlm):
+    med = make(nlm, "Chi2PDC")
+    med.runPumpSimulation()
+    C, S = med.computeGreensFunction(runPump=False)
+    n = med._dims["nFreqs"]
+    import ctypes
+    Cp = np.empty_like(C)
+    Sp = np.empty_like(S)
+    nlm._check(nlm._lib.nlm_green_plain(med._h(), 0, 0, 0, nlm._dptr(Cp.view(np.float64)),
+                                        nlm._dptr(Sp.view(np.float64))))
+    assert med._launch_count() >= 2 * n
+    assert cases.rel_l2(Cp, C) < 1e-12 and cases.rel_l2(Sp, S) < 1e-12
+    del ctypes
+
+
+def test_deterministic(nlm):
+    med = make(nlm, "Chi2SFG")
+    C1, S1 = med.computeGreensFunction()
+    C2, S2 = med.computeGreensFunction()
+    assert np.array_equal(C1, C2) and np.array_equal(S1, S2)
+
+
+def test_green_benchmark_config_reduced_steps(nlm, oracle):
+    """The Green's-function benchmark medium (N=1024) at 40 z steps against the oracle."""
+    kw = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0, beta1s=2, beta3=0,
+              beta3s=0.1, diffBeta0=0, tMax=40, tPrecision=1024, zPrecision=20, poling=np.ones(4))
+    med, ref = nlm.Chi2PDC(**kw), oracle.Chi2PDC(**kw)
+    assert med._dims["nZSteps"] == 40
+    C, S = med.computeGreensFunction()
+    Cr, Sr = ref.compute_greens_function(chunk=512)
+    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+
+
+def test_green_benchmark_config_full_size_properties(nlm):
+    """Full benchmark size (N=1024, nZSteps=1000): symplectic C/S and Green consistency with a direct run."""
+    kw = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0, beta1s=2, beta3=0,
+              beta3s=0.1, diffBeta0=0, tMax=40, tPrecision=1024, zPrecision=500, poling=np.ones(100))
+    med = nlm.Chi2PDC(**kw)
+    C, S = med.computeGreensFunction()
+    eye = np.eye(1024)
+    assert np.abs(C @ C.conj().T - S @ S.conj().T - eye).max() < 1e-6
+    assert np.abs(C @ S.T - S @ C.T).max() < 1e-8
+    rng = np.random.default_rng(2)
+    a = cases.noise(rng, 1024, 1e-3)
+    med.runSignalSimulation(a, False)
+    out = C @ np.fft.fftshift(a) + S @ np.fft.fftshift(a.conj())
+    assert cases.rel_l2(out, np.fft.fftshift(med.signalFreq[-1])) < 1e-9
+
+
+def test_chi3_soliton_config(nlm, oracle):
+    """Chi3 N=1 soliton pump + seeded-noise signal (N=512, nZSteps=200) against the oracle."""
+    kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=512, zPrecision=200)
+    med, ref = nlm.Chi3(**kw), oracle.Chi3(**kw)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(med.pumpFreq, ref.pump_freq[0]) < TOL
+    a = cases.noise(np.random.default_rng(1), 512, 1e-3)
+    med.runSignalSimulation(a)
+    ref.run_signal_simulation(a)
+    assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
+    assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
