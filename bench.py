@@ -123,28 +123,41 @@ def oracle_columns(med, bins):
     return np.fft.fftshift(pre_c, axes=1).T, np.fft.fftshift(pre_s, axes=1).T
 
 
+_WORKER_MEDIUM = None
+
+
+def _init_worker():
+    global _WORKER_MEDIUM
+    _WORKER_MEDIUM = _oracle_medium()
+
+
 def _oracle_worker(bins):
-    med = _oracle_medium()
+    med = _WORKER_MEDIUM if _WORKER_MEDIUM is not None else _oracle_medium()
     t0 = time.perf_counter()
     oracle_columns(med, bins)
     return time.perf_counter() - t0
 
 
-def cpu_oracle_rate(n_bins, processes=1):
-    """Propagations/s of the oracle on n_bins impulse pairs (2 n_bins propagations)."""
-    rng = np.random.default_rng(0)
-    bins = rng.choice(CONFIG["tPrecision"], size=n_bins, replace=False)
-    if processes <= 1:
-        dt = _oracle_worker(bins)
-        return 2 * n_bins / dt, dt
-    chunks = np.array_split(bins, processes)
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(processes) as pool:
-        pool.map(_oracle_worker, [c[:1] for c in chunks])   # warm the workers (imports, pump)
+class OraclePool:
+    """Oracle impulse propagations on every host core (spawned processes, one medium each)."""
+
+    def __init__(self, processes):
+        self.processes = processes
+        self.pool = mp.get_context("spawn").Pool(processes, initializer=_init_worker)
+        self.pool.map(_oracle_worker, [np.array([0])] * processes)   # imports and pump done
+
+    def rate(self, n_bins, seed=0):
+        rng = np.random.default_rng(seed)
+        bins = rng.choice(CONFIG["tPrecision"], size=n_bins, replace=False)
+        chunks = [c for c in np.array_split(bins, self.processes) if c.size]
         t0 = time.perf_counter()
-        pool.map(_oracle_worker, chunks)
+        self.pool.map(_oracle_worker, chunks)
         dt = time.perf_counter() - t0
-    return 2 * n_bins / dt, dt
+        return 2 * n_bins / dt, dt
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
 
 
 # ----------------------------------------------------------------------------------------------
@@ -174,14 +187,16 @@ def run_reference(args):
         return
     cores = os.cpu_count() or 1
     n_bins = args.ref_bins or 8 * cores
-    for _ in range(args.warmup):
-        cpu_oracle_rate(max(cores, 1), cores)
+    pool = OraclePool(cores)
+    for k in range(args.warmup):
+        pool.rate(cores, seed=100 + k)
     rates, times = [], []
-    for _ in range(args.steps):
-        r, dt = cpu_oracle_rate(n_bins, cores)
+    for k in range(args.steps):
+        r, dt = pool.rate(n_bins, seed=k)
         rates.append(r)
         times.append(dt)
-    value = float(np.mean(rates))
+    pool.close()
+    value = 2 * n_bins * args.steps / float(np.sum(times))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * 2048 / value,
@@ -221,7 +236,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    med = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **CONFIG)
+    med = nlm.Chi2PDC(poling=np.ones(N_DOMAINS if CONFIG["zPrecision"] == 500 else 5), **CONFIG)
     n = med._dims["nFreqs"]
     n_z = med._dims["nZSteps"]
     n_inst = 2 * n
@@ -319,8 +334,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "Chi2PDC computeGreensFunction N=1024 nZSteps=1000 (2048 impulse propagations, "
-                                   "C and S 1024x1024 complex128)",
+            "config": {"workload": "Chi2PDC computeGreensFunction N=1024 nZSteps=%d (2048 impulse propagations, "
+                                   "C and S 1024x1024 complex128)" % n_z,
                        "global_batch": n_inst * world, "seq_len": n_z, "parallelism": "replica-per-gpu",
                        "l2": "256 MB buffer written between timed steps (outside the events)"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16,
@@ -356,7 +371,11 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--cpu-bins", type=int, default=64)
     ap.add_argument("--ref-bins", type=int, default=0)
+    ap.add_argument("--zprecision", type=int, default=0,
+                    help="override zPrecision (smaller captures for the profiler; the benchmark uses 500)")
     args = ap.parse_args()
+    if args.zprecision:
+        CONFIG["zPrecision"] = args.zprecision
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

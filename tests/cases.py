@@ -57,14 +57,9 @@ CASES = {
 
 FULLY_NONLINEAR = {"Chi2SHG", "Chi2SHGOPA", "Chi2DSFG", "Chi2SHGXPM", "Chi2ASHG", "Chi3GNLSE"}
 
-# Chi2SFGII's keywords "intensityProfile" and "zPrecision" are bound to each other's slot in the
-# reference (solvers/Chi2SFGII.cpp:98-106); the oracle takes them by meaning.
-ORACLE_RENAMES = {}
-
-
 def oracle_kwargs(name):
-    kw = dict(CASES[name])
-    return kw
+    """Keyword arguments of the oracle's constructor (the same as the engine's for these cases)."""
+    return dict(CASES[name])
 
 
 def noise(rng, n, sigma):
@@ -87,3 +82,11 @@ def rel_l2(a, b):
     b = np.asarray(b)
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+def rel_l2_pair(c, s, cr, sr):
+    """Joint relative L2 error of a (C, S) pair: S vanishes identically for processes without
+    conjugate coupling (sum-frequency generation), where a per-matrix ratio is meaningless."""
+    num = np.linalg.norm(np.asarray(c) - cr) ** 2 + np.linalg.norm(np.asarray(s) - sr) ** 2
+    den = np.linalg.norm(cr) ** 2 + np.linalg.norm(sr) ** 2
+    return float(np.sqrt(num / (den if den > 0 else 1.0)))

@@ -58,11 +58,9 @@ def test_green_matches_golden(nlm, golden, name, use_prop):
     med._set_schedule(use_propagator=use_prop)
     med.runPumpSimulation()
     C, S = med.computeGreensFunction(False, False)
-    assert cases.rel_l2(C, golden[name + "__green_c"]) < TOL
-    assert cases.rel_l2(S, golden[name + "__green_s"]) < TOL
+    assert cases.rel_l2_pair(C, S, golden[name + "__green_c"], golden[name + "__green_s"]) < TOL
     Ct, St = med.computeGreensFunction(True, False)
-    assert cases.rel_l2(Ct, golden[name + "__green_c_time"]) < TOL
-    assert cases.rel_l2(St, golden[name + "__green_s_time"]) < TOL
+    assert cases.rel_l2_pair(Ct, St, golden[name + "__green_c_time"], golden[name + "__green_s_time"]) < TOL
 
 
 def test_green_options_match_oracle(nlm, oracle):
@@ -73,7 +71,7 @@ def test_green_options_match_oracle(nlm, oracle):
         C, S = med.computeGreensFunction(False, True, 1, norm, ui, uo)
         Cr, Sr = ref.compute_greens_function(False, True, 1, norm, ui, uo)
         assert C.shape == Cr.shape
-        assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+        assert cases.rel_l2_pair(C, S, Cr, Sr) < TOL
 
 
 def test_batch_options_match_oracle(nlm, oracle):
@@ -120,9 +118,10 @@ def test_gaussian_beam_profile_pump(nlm, oracle):
 def test_set_pump_from_other_medium(nlm, oracle):
     """setPump(other) copies another medium's signal with the frame phase (src/_NonlinearMedium.cpp:506-534)."""
     kw1 = dict(cases.CASES["Chi2SFG"], zPrecision=20)
-    kw2 = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10, zPrecision=10, poling=[])
+    kw2 = dict(cases.CASES["Chi2PDCII"])
     a, ra = nlm.Chi2SFG(**kw1), oracle.Chi2SFG(**kw1)
-    b, rb = nlm.Chi2PDC(**kw2), oracle.Chi2PDC(**kw2)
+    b, rb = nlm.Chi2PDCII(**kw2), oracle.Chi2PDCII(**kw2)
+    assert a._dims["nZSteps"] >= b._dims["nZSteps"]
     x = cases.signal_input("Chi2SFG", 32, 2, seed=4)
     a.runPumpSimulation()
     ra.run_pump_simulation()
@@ -136,7 +135,9 @@ def test_set_pump_from_other_medium(nlm, oracle):
     assert cases.rel_l2(b.pumpTime, rb.pump_time[0]) < TOL
     C, S = b.computeGreensFunction(runPump=False)
     Cr, Sr = rb.compute_greens_function(run_pump=False)
-    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+    assert cases.rel_l2_pair(C, S, Cr, Sr) < TOL
+    with pytest.raises(ValueError, match="Mode index larger"):
+        nlm.Chi2PDC(**dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10)).setPump(a, 1)   # this medium's modes
 
 
 def test_cascade_matches_oracle(nlm, oracle):
@@ -148,7 +149,7 @@ def test_cascade_matches_oracle(nlm, oracle):
     rc = oracle.Cascade([ra, rb], [{0: 0}], True)
     C, S = c.computeGreensFunction()
     Cr, Sr = rc.compute_greens_function()
-    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+    assert cases.rel_l2_pair(C, S, Cr, Sr) < TOL
     x = cases.signal_input("Chi2PDC", 32, 1, seed=9)
     c.runSignalSimulation(x)
     rc.run_signal_simulation(x)
@@ -187,7 +188,7 @@ def test_green_benchmark_config_reduced_steps(nlm, oracle):
     assert med._dims["nZSteps"] == 40
     C, S = med.computeGreensFunction()
     Cr, Sr = ref.compute_greens_function(chunk=512)
-    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL   # both matrices are O(1) for PDC
 
 
 def test_green_benchmark_config_full_size_properties(nlm):
