@@ -137,6 +137,20 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
 
+/* --- allocation-free Chi3GNLSE batch ----------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory where they
+ * propagate (memory owned by another allocator with a fixed budget, or loops where cudaMalloc /
+ * cudaFree would synchronise the device): the same propagation as nlm_batch_device for a Chi3GNLSE
+ * medium (rows x N complex inputs on the device, one N-point output row each, frequency or time
+ * domain as in_time_domain), with the kernel's scratch taken from one 16 MiB file-scope device array
+ * instead of an allocation.  The medium must have run one GPU call before (its device tables are
+ * built there).  Grids needing more than the array per CTA are rejected.  The call is asynchronous
+ * on cuda_stream (a cudaStream_t; NULL is the legacy default stream).  All calls share the array: calls that overlap on the
+ * GPU race.  The first call on a device looks up the array's address; make it before any stream
+ * capture. */
+nlm_status nlm_batch_gnlse_noalloc(nlm_medium* m, const void* inputs_dev, size_t rows,
+                                   int in_time_domain, void* out_dev, void* cuda_stream);
+
 /* --- getters (src/nlmModulePy.cpp:100-123) ---------------------------------------------
  * which: 0 = pumpFreq, 1 = pumpTime, 2 = signalFreq, 3 = signalTime, 4 = field.
  * Returns a pointer into a host mirror owned by the handle (refreshed from the device on

@@ -18,7 +18,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libnlm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_gnlse.cu", "kernels_misc.cu"]
+CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_gnlse.cu", "kernels_misc.cu",
+                "nlm_noalloc.cu"]
 CXX_SOURCES = ["engine.cpp"]
 
 

@@ -49,6 +49,8 @@ struct CudaFailure : std::runtime_error {
 
 static thread_local std::string g_error;
 
+void set_error_message(const std::string& msg) { g_error = msg; }
+
 static void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1466,6 +1468,12 @@ static Medium* create_medium(int s, const double* args, const double* pump, size
   return m.release();
 }
 
+// Launch description of a Chi3GNLSE batch whose scratch memory the caller provides: validates and
+// schedules without allocating device memory (used by nlm_batch_gnlse_noalloc, nlm_noalloc.cu).
+nlm_status prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows, int inTime, void* out,
+                                 size_t scratchElems, PropArgs* args, int* grid, int* block, size_t* smem,
+                                 const void** fn, cudaStream_t* stream);
+
 }  // namespace nlm
 
 // ==========================================================================================
@@ -1485,6 +1493,53 @@ static Medium* M(nlm_medium* h) {
 static const Medium* CM(const nlm_medium* h) {
   if (!h || !h->impl) throw std::invalid_argument("null medium handle");
   return h->impl;
+}
+
+nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows, int inTime, void* out,
+                                      size_t scratchElems, PropArgs* args, int* grid, int* block, size_t* smem,
+                                      const void** fn, cudaStream_t* stream) {
+  return guarded([&] {
+    Medium* m = M(h);
+    if (m->solver != kChi3GNLSE)
+      throw std::invalid_argument("the allocation-free batch entry point propagates Chi3GNLSE media only");
+    if (!m->devReady || (m->relIntD.p == nullptr && m->nZ > 1))
+      throw std::runtime_error("medium has no device tables yet: run one GPU call of it (e.g. batchSignalSimulation) "
+                               "before the allocation-free entry point");
+    if (!in || !out) throw std::invalid_argument("null input or output pointer");
+    if (rows == 0) throw std::invalid_argument("Too many threads requested!");
+    const int R = m->chooseR();
+    m->checkGrid(R);
+    const KernelEntry* k = m->findKernel(kKindGnlse, m->solver, R);
+    if (!k) throw Unsupported("no fused kernel for this grid");
+    Medium::Schedule s = m->schedule(k, (long long)rows, R);
+    const size_t perSlot = 2 * (size_t)m->N;
+    const size_t slots = scratchElems / perSlot;
+    if (slots < (size_t)s.ipc)
+      throw std::invalid_argument("grid of " + std::to_string(m->N) + " points needs " +
+                                  std::to_string(perSlot * s.ipc * sizeof(double2)) +
+                                  " bytes of scratch per CTA; the allocation-free entry point holds " +
+                                  std::to_string(scratchElems * sizeof(double2)) + " bytes");
+    s.grid = (int)std::min<size_t>((size_t)s.grid, slots / (size_t)s.ipc);
+    PropArgs a = m->baseArgs(R);
+    a.inKind = 1;
+    a.inTime = inTime ? 1 : 0;
+    a.in = reinterpret_cast<const double2*>(in);
+    a.inStride = (long long)m->N;
+    a.inChannels = 1;
+    a.inputMode = 0;
+    a.nOut = 1;
+    a.outModes[0] = 0;
+    a.out = reinterpret_cast<double2*>(out);
+    a.outStride = (long long)m->N;
+    a.nInst = (long long)rows;
+    a.ipc = s.ipc;
+    *args = a;
+    *grid = s.grid;
+    *block = s.block;
+    *smem = s.smem;
+    *fn = k->fn;
+    *stream = m->stream;
+  });
 }
 
 extern "C" {
