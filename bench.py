@@ -37,6 +37,34 @@ N_DOMAINS = 100
 C_SOLVER = 80          # point-wise flops per mode per step of Chi2PDC's DiffEq (fixed, not tuned)
 
 
+def ragged_media_params(seed=3, count=64):
+    """The ragged workload: Chi2SFG media with N in {128..2048}, beta1s ~ U[-3,3], beta2, beta2s ~ U[-1,1],
+    beta3s ~ U[-0.2,0.2], Gaussian pump of width U[0.5,3], poling domains of U{5..50} z steps with
+    alternating sign, nZSteps ~ U[200,2000] (realised through zPrecision), relativeLength=1,
+    nlLength=nlLengthOrig=1, beta2o=beta1o=beta3o=0, diffBeta0=0, tMax=10."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice([128, 256, 512, 1024, 2048]))
+        b1s, b2, b2s, b3s = rng.uniform(-3, 3), rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-0.2, 0.2)
+        w = rng.uniform(0.5, 3)
+        target = int(rng.integers(200, 2001))
+        min_len = min(1.0, 1.0 / max(abs(b1s), abs(b2), abs(b2s), abs(b3s)))
+        zp = int(math.ceil(target * min_len))
+        kw = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=b2, beta2s=b2s, beta2o=0, beta1=0, beta1s=b1s,
+                  beta1o=0, beta3=0, beta3s=b3s, beta3o=0, diffBeta0=0, tMax=10, tPrecision=n, zPrecision=zp)
+        doms, total = [], 0
+        while total < target:
+            d = int(rng.integers(5, 51))
+            doms.append(d)
+            total += d
+        t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
+        pump = np.exp(-t ** 2 / (2 * w * w))
+        sig = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3 / np.sqrt(2)
+        out.append((kw, np.array(doms, dtype=float), pump, sig))
+    return out
+
+
 def algorithmic_flops(n_inst, n_z, n, modes=1, c_solver=C_SOLVER):
     """F = n_inst (nZ-1) modes (10 N log2 N + c N): two FFTs of 5 N log2 N plus the point-wise work."""
     return n_inst * (n_z - 1) * modes * (10 * n * math.log2(n) + c_solver * n)
@@ -211,6 +239,70 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_adjoint(nlm, torch, reps=3):
+    """grad/fwd cost on the gradient configuration: Chi2PDC N=512, nZSteps=2000, one seeded noise signal
+    (sigma 1e-3), continuous poling d(z) ~ U[-1, 1] (seed 4), loss ||X(L) - target||^2.  fwd = one forward
+    propagation with the pump run (batchSignalSimulation); grad = forward with checkpoints + reverse sweep
+    with the pump-spectrum and poling-profile reductions."""
+    import ctypes
+    kw = dict(CONFIG, tPrecision=512, zPrecision=1000)
+    med = nlm.Chi2PDC(**kw)
+    n, nz = med._dims["nFreqs"], med._dims["nZSteps"]
+    rng = np.random.default_rng(4)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3 / np.sqrt(2)
+    d = rng.uniform(-1, 1, nz)
+    target = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    target /= np.linalg.norm(target)
+    stream = torch.cuda.Stream()
+    med._set_stream(stream.cuda_stream)
+    med._set_poling_profile(d)
+    xin = torch.tensor(x.reshape(1, n), dtype=torch.complex128, device="cuda")
+    out = torch.empty_like(xin)
+    gin = torch.empty_like(xin)
+    gp = torch.empty(n, dtype=torch.complex128, device="cuda")
+    gpol = np.zeros(nz)
+    tt = torch.tensor(target.reshape(1, n), dtype=torch.complex128, device="cuda")
+    used = ctypes.c_int()
+
+    def fwd():
+        nlm._check(nlm._lib.nlm_batch_device(med._h(), ctypes.c_void_p(xin.data_ptr()), 1, n, 0, 1, 1, 0, None, 0,
+                                             ctypes.c_void_p(out.data_ptr())))
+
+    def grad(interval):
+        nlm._check(nlm._lib.nlm_run_pump(med._h()))
+        nlm._check(nlm._lib.nlm_adjoint_forward(med._h(), ctypes.c_void_p(xin.data_ptr()), 1,
+                                                ctypes.c_void_p(out.data_ptr()), interval, ctypes.byref(used)))
+        with torch.cuda.stream(stream):
+            g = (2 * (out - tt)).contiguous()
+        nlm._check(nlm._lib.nlm_adjoint_backward(med._h(), ctypes.c_void_p(g.data_ptr()),
+                                                 ctypes.c_void_p(gin.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
+                                                 nlm._dptr(gpol)))
+
+    def timed(fn):
+        best = float("inf")
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    fwd()
+    grad(0)
+    t_fwd = timed(fwd)
+    t_grad = timed(lambda: grad(0))
+    k_auto = used.value
+    k_sqrt = int(math.ceil(math.sqrt(nz - 1)))
+    t_grad_sqrt = timed(lambda: grad(k_sqrt))
+    return {"grad_fwd_cost": t_grad / t_fwd, "fwd_ms": t_fwd, "grad_ms": t_grad, "checkpoint_interval": k_auto,
+            "grad_fwd_cost_sqrt_checkpoints": t_grad_sqrt / t_fwd, "sqrt_checkpoint_interval": k_sqrt,
+            "workload": "Chi2PDC N=512 nZSteps=%d, gradients wrt input spectrum, pump spectrum (512 bins) and "
+                        "poling profile (%d values)" % (nz, nz)}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -308,6 +400,8 @@ def run_ours(args):
         t_plain = time.perf_counter() - t0
         plain = args.plain_sample / t_plain
 
+    adjoint = measure_adjoint(nlm, torch) if args.adjoint else None
+
     line = None
     if rank == 0:
         # CPU baseline and parity sample: oracle impulse propagations of the same workload
@@ -352,6 +446,7 @@ def run_ours(args):
                       "form": "one propagation per kernel launch"},
             "batched_over_plain": (value / plain) if plain else None,
             "parity_sample_rel_err": parity,
+            "adjoint": adjoint,
             "clocks": clocks.summary(),
         }
     if world > 1:
@@ -371,6 +466,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--cpu-bins", type=int, default=64)
     ap.add_argument("--ref-bins", type=int, default=0)
+    ap.add_argument("--adjoint", type=int, default=1, help="measure the grad/fwd cost (1) or not (0)")
     ap.add_argument("--zprecision", type=int, default=0,
                     help="override zPrecision (smaller captures for the profiler; the benchmark uses 500)")
     args = ap.parse_args()

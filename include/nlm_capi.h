@@ -113,6 +113,17 @@ nlm_status nlm_green_device(nlm_medium* m, int in_time_domain, int run_pump, uns
                             const uint8_t* use_output, size_t n_use_output, void* green_c_dev,
                             void* green_s_dev);
 
+/* --- computeGreensFunction split over several GPUs ------------------------------------------
+ * The 2 N nSignalModes impulse propagations of computeGreensFunction (all modes, as with empty
+ * useInput/useOutput) are independent: src/_NonlinearMedium.cpp:350-353 splits them over threads in
+ * contiguous ranges; nlm_green_rows computes the raw last-row outputs (nSignalModes N complex each) of
+ * the range [first, first + count) on this handle's GPU, nlm_green_finish turns the gathered raw
+ * rows of all propagations into C and S (src/_NonlinearMedium.cpp:329-345, 360-372). */
+nlm_status nlm_green_rows(nlm_medium* m, int in_time_domain, int run_pump, size_t first, size_t count,
+                          double* raw_out);
+nlm_status nlm_green_finish(nlm_medium* m, const double* raw, int normalize, double* green_c,
+                            double* green_s);
+
 /* --- batchSignalSimulation (src/_NonlinearMedium.cpp:378-444;
  *     src/_FullyNonlinearMedium.hpp:8-11 where run_pump is ignored) -------------------
  * inputs: rows x cols complex.  Output: rows x (nOut*N) complex; nlm_batch_dims gives
@@ -136,6 +147,25 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
  * signal modes (nSignalModes_k*N_k complex).  Pumps must have been run.              */
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
+
+/* --- gradients (no counterpart in the reference) -------------------------------------------
+ * Reverse-mode gradients of a functional L of the output spectra of a Chi2PDC batch with respect to
+ * the input spectra, the pump spectrum F0 = FFT(envelope) and a continuous poling profile d(z).
+ * Complex gradients use the convention dL/dRe z + i dL/dIm z.
+ *
+ * nlm_set_poling_profile: replace the domain pattern by d(z) on the nZSteps grid (the values the
+ *   reference keeps in its protected _poling array, src/_NonlinearMedium.cpp:470-503).
+ * nlm_adjoint_forward: propagate rows x N input spectra (device) to rows x N output spectra (device),
+ *   storing the states every checkpoint_interval steps (<= 0: every step when that fits in 1 GB,
+ *   else every ceil(sqrt(nZSteps-1)) steps, the segments being recomputed in the reverse sweep).
+ *   The pump must have been run.
+ * nlm_adjoint_backward: given dL/dX (device, rows x N) returns dL/dX_in (device, rows x N), dL/dF0
+ *   (device, N; may be NULL) and dL/dd (host, nZSteps doubles; may be NULL). */
+nlm_status nlm_set_poling_profile(nlm_medium* m, const double* profile, size_t n);
+nlm_status nlm_adjoint_forward(nlm_medium* m, const void* inputs_dev, size_t rows, void* out_dev,
+                               int checkpoint_interval, int* used_interval);
+nlm_status nlm_adjoint_backward(nlm_medium* m, const void* grad_out_dev, void* grad_in_dev,
+                                void* grad_pump_dev, double* grad_poling);
 
 /* --- allocation-free Chi3GNLSE batch ----------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory where they

@@ -1,0 +1,235 @@
+// adjoint.cu -- reverse sweep of the split-step propagation for Chi2PDC (solvers/Chi2PDC.cpp:27-44).
+//
+// The reference has no gradient.  This is the exact discrete adjoint of what the forward kernels
+// compute: for an output functional L of the last-row spectrum X, with g = dL/dRe + i dL/dIm, the
+// sweep runs the z steps backwards,
+//     g <- conj(table_i) * FFT(g),  g <- IFFT(g),  g <- RK4_i^T(g; s_{i-1})
+// where RK4_i^T is the transposed RK4 step at each point, evaluated with the forward state s_{i-1}.
+// s_{i-1} comes from checkpoints stored by the forward kernel every K steps; inside a segment the
+// states are recomputed from its checkpoint (K = 1 stores every state and recomputes nothing).
+// Per step the sweep also accumulates the gradients of the RK4 stage factors a_s = c_s P_s
+// (c_s: poling sign x nonlinear step x phase mismatch of stage s, P_s: pump row 2i-2, 2i-1, 2i),
+// from which the pump-spectrum and poling-profile gradients are reduced afterwards.
+#include <vector>
+
+#include "nlm_propagate.cuh"
+
+namespace nlm {
+
+__device__ __forceinline__ void atomic_add2(double2* p, double2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  __shared__ long long s_group;
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const int g = threadIdx.x / T, j = threadIdx.x - g * T;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
+  double2* segp = d.seg ? d.seg + ((long long)blockIdx.x * a.ipc + g) * (long long)d.K * N : nullptr;
+  const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
+    const long long local = cg * a.ipc + g;
+    const bool active = local < a.nInst;
+    const long long inst = a.instBase + local;
+    const double2* ck = d.ckpt + (active ? inst : 0) * (long long)d.nCk * N;
+    double2 gv[R];
+    {
+      const double2* go = d.gout + (active ? inst : 0) * (long long)N;
+#pragma unroll
+      for (int v = 0; v < R; v++) gv[v] = active ? cscale(go[j + v * T], (double)N) : czero();
+    }
+    int segEnd = a.nZ - 1;
+    while (segEnd >= 1) {
+      const int jseg = (segEnd - 1) / d.K;
+      const int s0 = jseg * d.K;
+      if (d.K > 1) {
+        // recompute the states s_{s0} .. s_{segEnd-1} of this segment from its checkpoint
+        double2 x[1][R];
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          x[0][v] = ck[(long long)jseg * N + j + v * T];
+          segp[j + v * T] = x[0][v];
+        }
+        for (int i = s0 + 1; i < segEnd; i++) {
+          const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
+            double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
+            double2 xm[1] = {x[0][v]};
+            rk4_point<FChi2PDC>(xm, p, c);
+            x[0][v] = xm[0];
+          }
+          fft_regs<R, false>(x[0], buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) x[0][v] = cmul(x[0][v], __ldg(a.dstep + j + v * T));
+          fft_regs<R, true>(x[0], buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) segp[(long long)(i - s0) * N + j + v * T] = x[0][v];
+        }
+      }
+      for (int i = segEnd; i > s0; i--) {
+        const double2* prev = d.K > 1 ? segp + (long long)(i - 1 - s0) * N : ck + (long long)(i - 1) * N;
+        if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
+        const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+#pragma unroll
+        for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
+        fft_regs<R, true>(gv, buf, tw, plan, j);
+        const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+        const double2 c0 = c[0], c1 = c[1], c2 = c[2];
+        double2* gacc = d.ga + (long long)(i - 1) * 3 * N;
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
+          const double2 a0 = cmul(c0, __ldg(pr)), a1 = cmul(c1, __ldg(pr + N)), a2 = cmul(c2, __ldg(pr + 2 * N));
+          const double2 x = prev[t];
+          // forward stages (solvers/Chi2PDC.cpp:40-43)
+          const double2 k1 = cmulc(a0, x);
+          const double2 y1 = caxpy(x, 0.5, k1);
+          const double2 k2 = cmulc(a1, y1);
+          const double2 y2 = caxpy(x, 0.5, k2);
+          const double2 k3 = cmulc(a1, y2);
+          const double2 y3 = cadd(x, k3);
+          // reverse: x' = x + (k1 + 2 k2 + 2 k3 + k4) / 6 with k = a conj(y)
+          const double2 gp = gv[v];
+          double2 gx = gp;
+          double2 gk1 = cscale(gp, 1.0 / 6.0);
+          double2 gk2 = cscale(gp, 1.0 / 3.0);
+          double2 gk3 = gk2;
+          const double2 gk4 = gk1;
+          const double2 ga2 = cmul(y3, gk4);
+          const double2 gy3 = cmulc(a2, gk4);
+          gx = cadd(gx, gy3);
+          gk3 = cadd(gk3, gy3);
+          double2 ga1 = cmul(y2, gk3);
+          const double2 gy2 = cmulc(a1, gk3);
+          gx = cadd(gx, gy2);
+          gk2 = caxpy(gk2, 0.5, gy2);
+          ga1 = cadd(ga1, cmul(y1, gk2));
+          const double2 gy1 = cmulc(a1, gk2);
+          gx = cadd(gx, gy1);
+          gk1 = caxpy(gk1, 0.5, gy1);
+          const double2 ga0 = cmul(x, gk1);
+          gx = cadd(gx, cmulc(a0, gk1));
+          gv[v] = gx;
+          if (active) {
+            atomic_add2(gacc + t, ga0);
+            atomic_add2(gacc + N + t, ga1);
+            atomic_add2(gacc + 2 * N + t, ga2);
+          }
+        }
+      }
+      segEnd = s0;
+    }
+    // gradient of the input spectrum: s_0 = IFFT(half X_in)
+    fft_regs<R, false>(gv, buf, tw, plan, j);
+    if (active) {
+#pragma unroll
+      for (int v = 0; v < R; v++)
+        d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+    }
+    __syncthreads();
+  }
+}
+
+// Pump-row gradients: gP[r] = sum over the stages reading pump row r of conj(c_s) ga_s, times the
+// intensity profile of the row (src/_NonlinearMedium.cpp:235-248).
+__global__ void k_adj_pump_rows(const double2* __restrict__ ga, const double2* __restrict__ coef,
+                                const double* __restrict__ prof, int nZ, int N, double2* __restrict__ gP) {
+  const int nRows = 2 * nZ - 1;
+  const long long total = (long long)nRows * N;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx / N), t = (int)(idx - (long long)r * N);
+    double2 acc = czero();
+    if (r & 1) {
+      const int i = (r + 1) / 2;  // stage 1 (and 2) of step i reads row 2i-1
+      acc = cmul(cconj(coef[(long long)(i - 1) * 3 + 1]), ga[((long long)(i - 1) * 3 + 1) * N + t]);
+    } else {
+      const int m = r / 2;
+      if (m >= 1)  // last stage of step m reads row 2m
+        acc = cmul(cconj(coef[(long long)(m - 1) * 3 + 2]), ga[((long long)(m - 1) * 3 + 2) * N + t]);
+      if (m + 1 <= nZ - 1)  // first stage of step m+1 reads row 2m
+        acc = cadd(acc, cmul(cconj(coef[(long long)m * 3]), ga[((long long)m * 3) * N + t]));
+    }
+    if (prof) acc = cscale(acc, prof[r]);
+    gP[idx] = acc;
+  }
+}
+
+// gF0[t] = (1/N) sum_r exp(-i r dzp D[t]) FFT(gP)[r][t]: the pump rows are IFFT(F0 exp(i r dzp D)).
+__global__ void k_adj_pump_reduce(const double2* __restrict__ fgP, const double* __restrict__ disp, double dzp,
+                                  int nRowsP, int N, double2* __restrict__ gF0) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  double2 acc = czero();
+  for (int r = 0; r < nRowsP; r++) {
+    double sn = 0, cs = 1;
+    if (r > 0) sincos(((double)r * dzp) * disp[t], &sn, &cs);
+    acc = cadd(acc, cmulc(fgP[(long long)r * N + t], make_double2(cs, sn)));
+  }
+  gF0[t] = cscale(acc, 1.0 / N);
+}
+
+// gc[i][s] = sum_t conj(P_row(i,s)[t]) ga[i][s][t]: gradient of the stage coefficient c_s of step i+1.
+__global__ void k_adj_coef_reduce(const double2* __restrict__ ga, const double2* __restrict__ pump, int nZ, int N,
+                                  double2* __restrict__ gc) {
+  __shared__ double2 part[256];
+  const int pair = blockIdx.x;          // (i-1)*3 + s
+  const int i = pair / 3 + 1, s = pair % 3;
+  const int row = 2 * i - 2 + s;
+  double2 acc = czero();
+  for (int t = threadIdx.x; t < N; t += blockDim.x)
+    acc = cadd(acc, cmulc(ga[(long long)pair * N + t], pump[(long long)row * N + t]));
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] = cadd(part[threadIdx.x], part[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) gc[pair] = part[0];
+}
+
+static int sm_count_adj() {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const double* prof, int nZ, int N,
+                                 double2* gP, cudaStream_t s) {
+  const long long total = (long long)(2 * nZ - 1) * N;
+  int grid = (int)((total + 255) / 256);
+  if (grid > 32 * sm_count_adj()) grid = 32 * sm_count_adj();
+  k_adj_pump_rows<<<grid > 0 ? grid : 1, 256, 0, s>>>(ga, coef, prof, nZ, N, gP);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_pump_reduce(const double2* fgP, const double* disp, double dzp, int nRowsP, int N,
+                                   double2* gF0, cudaStream_t s) {
+  k_adj_pump_reduce<<<(N + 127) / 128, 128, 0, s>>>(fgP, disp, dzp, nRowsP, N, gF0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_coef_reduce(const double2* ga, const double2* pump, int nZ, int N, double2* gc,
+                                   cudaStream_t s) {
+  if (nZ < 2) return cudaSuccess;
+  k_adj_coef_reduce<<<3 * (nZ - 1), 256, 0, s>>>(ga, pump, nZ, N, gc);
+  return cudaGetLastError();
+}
+
+void add_kernels_adjoint(std::vector<KernelEntry>& t) {
+  t.push_back({kKindAdjoint, kChi2PDC, 8, (const void*)k_adjoint_pdc<8>});
+  t.push_back({kKindAdjoint, kChi2PDC, 16, (const void*)k_adjoint_pdc<16>});
+}
+
+}  // namespace nlm

@@ -475,6 +475,13 @@ struct Medium {
   DevBuf<double2> work, work2, raw, cs, io;
   DevBuf<double2> scratch;
   DevBuf<uint8_t> flagsD;
+  DevBuf<unsigned long long> workCounter;
+  // adjoint state: forward checkpoints of the last nlm_adjoint_forward
+  DevBuf<double2> ckpt, adjSeg, adjGa, adjGP, adjFGP, adjGc;
+  DevBuf<double> profD;
+  long long adjRows = 0;
+  int adjK = 0, adjNCk = 0;
+  long long adjPumpVersion = -1;
   DevBuf<double2> scaleD;
   long long pumpVersion = 0, signalVersion = 0;
   GridMirror mPumpF, mPumpT, mSigF, mSigT;
@@ -1074,35 +1081,27 @@ struct Medium {
     int ipc = T >= 128 ? 1 : 128 / T;
     if (ipc > nInst) ipc = (int)std::max<long long>(1, nInst);
     const int block = T * ipc;
-    const size_t smem = (size_t)ipc * N * sizeof(double2);
+    // exchange buffers of the ipc propagations, plus the staged twiddle table when R != 16
+    const size_t smem = (size_t)(ipc + (k->R != 16 ? 1 : 0)) * N * sizeof(double2);
     int dev = 0, sms = 1, optin = 0;
     ck(cudaGetDevice(&dev), "device");
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if ((int)smem > optin) throw Unsupported("grid too large for shared memory");
-    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin), "smem attribute");
     cudaFuncAttributes fa;
     ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    const int dynMax = optin - (int)fa.sharedSizeBytes;   // static shared memory counts against the opt-in limit
+    if ((int)smem > dynMax) throw Unsupported("grid too large for shared memory");
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
     if (block > fa.maxThreadsPerBlock)
       throw Unsupported("propagation kernel cannot launch " + std::to_string(block) + " threads (registers)");
     int maxActive = 0;
     ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxActive, k->fn, block, smem), "occupancy");
     if (maxActive < 1) throw Unsupported("propagation kernel does not fit on an SM");
     const long long groups = (nInst + ipc - 1) / ipc;
-    int best = 1;
-    double bestScore = -1;
-    for (int kk = 1; kk <= maxActive; kk++) {
-      const long long slots = (long long)sms * kk;
-      const long long waves = (groups + slots - 1) / slots;
-      const double eff = (double)groups / (double)(waves * slots);
-      const double warps = (double)kk * block / 32.0;
-      const double sat = std::min(1.0, warps / 8.0);
-      const double score = eff * sat;
-      if (score > bestScore + 1e-9) {
-        bestScore = score;
-        best = kk;
-      }
-    }
+    // The kernels claim groups from a work counter, so every SM keeps working until the queue is
+    // empty whatever the number of resident CTAs: take the most resident warps (the FP64 pipe is
+    // shared by all of them and needs several warps per scheduler to stay busy).
+    int best = maxActive;
     if (ctaPerSM > 0) best = std::min(ctaPerSM, maxActive);
     long long grid = std::min<long long>(groups, (long long)sms * best);
     Schedule s{(int)std::max<long long>(1, grid), block, ipc, smem};
@@ -1182,6 +1181,12 @@ struct Medium {
     Schedule s = schedule(k, nInst, R);
     if (plainOne) s.grid = 1;
     a.ipc = s.ipc;
+    a.work = nullptr;
+    if (!plainOne && (long long)s.grid < (nInst + s.ipc - 1) / s.ipc) {
+      workCounter.reserve(1);
+      ck(cudaMemsetAsync(workCounter.p, 0, sizeof(unsigned long long), stream), "work counter");
+      a.work = workCounter.p;
+    }
     if (timeKernels) {
       if (!ev0) ck(cudaEventCreate(&ev0), "event");
       if (!ev1) ck(cudaEventCreate(&ev1), "event");
@@ -1206,6 +1211,124 @@ struct Medium {
       kernelMs += ms;
       kernelCount++;
     }
+  }
+
+  // ---- adjoint (no counterpart in the reference) -------------------------------------------------
+  // Continuous poling d(z) on the nZSteps grid in place of the domain pattern (the reference's
+  // protected _poling array).
+  void setPolingProfile(const double* d, size_t n) {
+    if (isCascade || fnl || !poled) throw std::invalid_argument("medium has no poling");
+    if (n != nZ) throw std::invalid_argument("poling profile must have nZSteps values");
+    poling.assign(d, d + n);
+    if (devReady) {
+      buildCoefficients();
+      ck(cudaStreamSynchronize(stream), "coefficients");
+    }
+    propVersion = -1;
+  }
+
+  void adjointForward(const double2* in, size_t rows, double2* out, int interval) {
+    if (solver != kChi2PDC) throw Unsupported("the adjoint is implemented for Chi2PDC");
+    if (rows == 0) throw std::invalid_argument("Too many threads requested!");
+    if (nZ < 2) throw std::invalid_argument("the adjoint needs at least two z steps");
+    ensureDevice();
+    const int R = chooseR();
+    checkGrid(R);
+    const size_t steps = nZ - 1;
+    int K = interval;
+    if (K <= 0) {
+      const double bytes = (double)rows * steps * N * sizeof(double2);
+      K = bytes <= 1e9 ? 1 : (int)std::ceil(std::sqrt((double)steps));
+    }
+    const int nCk = (int)((steps + K - 1) / K);
+    ckpt.reserve((size_t)rows * nCk * N);
+    PropArgs a = baseArgs(R);
+    a.inKind = 1;
+    a.inTime = 0;
+    a.in = in;
+    a.inStride = (long long)N;
+    a.inChannels = 1;
+    a.inputMode = 0;
+    a.nOut = 1;
+    a.outModes[0] = 0;
+    a.out = out;
+    a.outStride = (long long)N;
+    a.ckpt = ckpt.p;
+    a.ckK = K;
+    a.ckN = nCk;
+    propagate(a, (long long)rows, false);
+    ck(cudaStreamSynchronize(stream), "adjoint forward");
+    adjRows = (long long)rows;
+    adjK = K;
+    adjNCk = nCk;
+    adjPumpVersion = pumpVersion;
+  }
+
+  void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {
+    if (adjRows == 0 || adjPumpVersion != pumpVersion)
+      throw std::runtime_error("no adjoint forward pass to differentiate: run nlm_adjoint_forward first");
+    const int R = chooseR();
+    const KernelEntry* k = findKernel(kKindAdjoint, solver, R);
+    if (!k) throw Unsupported("no adjoint kernel for this grid");
+    const size_t steps = nZ - 1;
+    adjGa.reserve(steps * 3 * N);
+    ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
+    Schedule s = schedule(k, adjRows, R);
+    if (adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * adjK * N);
+    PropArgs a = baseArgs(R);
+    a.nInst = adjRows;
+    a.ipc = s.ipc;
+    a.work = nullptr;
+    AdjArgs d{};
+    d.gout = gout;
+    d.ckpt = ckpt.p;
+    d.K = adjK;
+    d.nCk = adjNCk;
+    d.seg = adjK > 1 ? adjSeg.p : nullptr;
+    d.ga = adjGa.p;
+    d.gin = gin;
+    void* args[] = {(void*)&a, (void*)&d};
+    ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
+    launches++;
+    if (gpump) {
+      const size_t rowsP = nZP;
+      adjGP.reserve(rowsP * N);
+      adjFGP.reserve(rowsP * N);
+      const double* prof = nullptr;
+      if (profile != NLM_CONSTANT) {
+        std::vector<double> sv;
+        relativeStrength(sv);
+        uploadD(profD, sv);
+        prof = profD.p;
+      }
+      ck(launch_adj_pump_rows(adjGa.p, coef.p, prof, (int)nZ, (int)N, adjGP.p, stream), "pump rows");
+      ck(launch_fft_rows(adjGP.p, adjFGP.p, (long long)rowsP, fftPlanRows(), tw, false, 1.0, nullptr, stream), "fft");
+      ck(launch_adj_pump_reduce(adjFGP.p, dispPumpD.p, dzp, (int)rowsP, (int)N, gpump, stream), "pump reduce");
+      launches += 3;
+    }
+    if (gpol) {
+      adjGc.reserve(steps * 3);
+      ck(launch_adj_coef_reduce(adjGa.p, pumpTime.p, (int)nZ, (int)N, adjGc.p, stream), "coef reduce");
+      launches++;
+      std::vector<double2> gc(steps * 3);
+      ck(cudaMemcpyAsync(gc.data(), adjGc.p, gc.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream), "gc");
+      ck(cudaStreamSynchronize(stream), "adjoint");
+      // c_s = pol_s q_s with q_s = nlStep * mismatch(z_s): dL/dpol_s = Re(g_c conj(q_s)),
+      // pol_0 = d[i-1], pol_1 = (d[i-1] + d[i]) / 2, pol_2 = d[i]  (solvers/Chi2PDC.cpp:32-34)
+      for (uint i = 0; i < nZ; i++) gpol[i] = 0;
+      for (uint i = 1; i < nZ; i++) {
+        double gs[3];
+        for (int sub = 0; sub < 3; sub++) {
+          const double zz = sub == 0 ? (double)(i - 1) * dz : (sub == 1 ? (i - .5) * dz : (double)i * dz);
+          const cplx q = nlStep[0] * std::exp(1.0 * kI * diffBeta0[0] * zz);
+          const double2 g = gc[(size_t)(i - 1) * 3 + sub];
+          gs[sub] = (cplx(g.x, g.y) * std::conj(q)).real();
+        }
+        gpol[i - 1] += gs[0] + 0.5 * gs[1];
+        gpol[i] += 0.5 * gs[1] + gs[2];
+      }
+    }
+    ck(cudaStreamSynchronize(stream), "adjoint");
   }
 
   // ---- public operations ---------------------------------------------------------------------
@@ -1325,6 +1448,66 @@ struct Medium {
       ck(cudaMemcpyAsync(Sdst, S, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "S download");
     }
     ck(cudaStreamSynchronize(stream), "green");
+  }
+
+  // Raw outputs of impulse propagations [first, first + count) of the Green's function over all modes
+  // (instance 2 (im N + bin) + {0: impulse 1, 1: impulse i}); the row block of one rank when the
+  // 2 N nIn propagations are split over several GPUs.
+  void greenRows(int inTime, int runPumpFlag, long long first, long long count, double2* rawOut) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    const long long total = 2LL * nSignal * N;
+    if (first < 0 || count < 0 || first + count > total) throw std::invalid_argument("impulse range out of bounds");
+    if (runPumpFlag) runPump();
+    ensureDevice();
+    const int R = chooseR();
+    checkGrid(R);
+    const long long outStride = (long long)nSignal * N;
+    raw.reserve((size_t)std::max<long long>(count, 1) * outStride);
+    PropArgs a = baseArgs(R);
+    a.inKind = 0;
+    a.inTime = inTime ? 1 : 0;
+    for (uint m = 0; m < nSignal; m++) a.impModes[m] = (int)m;
+    a.nOut = (int)nSignal;
+    for (uint m = 0; m < nSignal; m++) a.outModes[m] = (int)m;
+    a.out = raw.p - first * outStride;   // the kernel indexes outputs by the global instance
+    a.outStride = outStride;
+    a.instBase = first;
+    if (count > 0) propagate(a, count, true);
+    if (count > 0)
+      ck(cudaMemcpyAsync(rawOut, raw.p, (size_t)count * outStride * sizeof(double2), cudaMemcpyDeviceToHost, stream),
+         "rows download");
+    ck(cudaStreamSynchronize(stream), "green rows");
+  }
+
+  // C and S from the raw rows of all 2 N nSignal impulse propagations (the epilogue of green()).
+  void greenFinish(const double2* rawIn, int normalize, double2* Cdst, double2* Sdst) {
+    if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    ensureDevice();
+    const int nIn = (int)nSignal, nOut = (int)nSignal;
+    const long long nInst = 2LL * nIn * N, outStride = (long long)nOut * N;
+    raw.reserve((size_t)nInst * outStride);
+    ck(cudaMemcpyAsync(raw.p, rawIn, (size_t)nInst * outStride * sizeof(double2), cudaMemcpyHostToDevice, stream),
+       "rows upload");
+    std::vector<uint8_t> flags((size_t)nOut * nIn, 1);
+    std::vector<double2> scales((size_t)nOut * nIn, make_double2(1, 0));
+    for (int im = 0; im < nIn; im++)
+      for (int om = 0; om < nOut; om++)
+        if (normalize && im != om) {
+          flags[(size_t)om * nIn + im] |= 2;
+          const cplx sc = std::sqrt(nlStep[im] / nlStep[om]);
+          scales[(size_t)om * nIn + im] = make_double2(sc.real(), sc.imag());
+        }
+    flagsD.reserve(flags.size());
+    ck(cudaMemcpyAsync(flagsD.p, flags.data(), flags.size(), cudaMemcpyHostToDevice, stream), "flags");
+    upload(scaleD, scales);
+    const size_t mat = (size_t)nOut * N * nIn * N;
+    cs.reserve(2 * mat);
+    ck(launch_green_epilogue(raw.p, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, cs.p, cs.p + mat, stream),
+       "epilogue");
+    launches++;
+    ck(cudaMemcpyAsync(Cdst, cs.p, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "C download");
+    ck(cudaMemcpyAsync(Sdst, cs.p + mat, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "S download");
+    ck(cudaStreamSynchronize(stream), "green finish");
   }
 
   void greenDims(unsigned nThreads, const uint8_t* useIn, size_t nUseIn, const uint8_t* useOut, size_t nUseOut,
@@ -1533,6 +1716,7 @@ nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows
     a.outStride = (long long)m->N;
     a.nInst = (long long)rows;
     a.ipc = s.ipc;
+    a.work = nullptr;   // static round robin: no counter to allocate
     *args = a;
     *grid = s.grid;
     *block = s.block;
@@ -1881,15 +2065,138 @@ nlm_status nlm_batch_device(nlm_medium* h, const void* inputs_dev, size_t rows, 
   });
 }
 
+// Workspace of the ragged launch (process-wide; the launch is serialised by the mutex).
+struct RaggedWorkspace {
+  std::mutex mu;
+  nlm::DevBuf<double2> in, out;
+  nlm::DevBuf<nlm::PropArgs> items;
+  nlm::DevBuf<unsigned long long> counter;
+};
+static RaggedWorkspace g_ragged;
+
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
                             double* const* outputs) {
   return guarded([&] {
-    // one propagation per medium; media with equal solver and grid share a launch
+    using namespace nlm;
+    if (n_media == 0) return;
+    std::vector<Medium*> ms(n_media);
     for (size_t k = 0; k < n_media; k++) {
-      Medium* m = M(media[k]);
-      std::vector<uint8_t> none;
-      m->batch(reinterpret_cast<const double2*>(inputs[k]), 1, m->N, in_time_domain, 0, 1, 0, nullptr, 0,
-               reinterpret_cast<double2*>(outputs[k]), false);
+      ms[k] = M(media[k]);
+      if (ms[k]->isCascade) throw std::invalid_argument("ragged batches take single media");
+      ms[k]->launches = 0;
+    }
+    // media without a ragged kernel (or with a grid it cannot take) run one launch each
+    std::vector<size_t> fused;
+    for (size_t k = 0; k < n_media; k++) {
+      Medium* m = ms[k];
+      const KernelEntry* ke = m->findKernel(kKindRagged, m->solver, 8);
+      const bool ok = ke && is_pow2((int)m->N) && m->N >= 8 && m->N / 8 <= 512;
+      if (ok) {
+        fused.push_back(k);
+      } else {
+        m->batch(reinterpret_cast<const double2*>(inputs[k]), 1, m->N, in_time_domain, 0, 1, 0, nullptr, 0,
+                 reinterpret_cast<double2*>(outputs[k]), false);
+      }
+    }
+    if (fused.empty()) return;
+    std::lock_guard<std::mutex> lock(g_ragged.mu);
+    // one launch per solver present in the set
+    std::map<int, std::vector<size_t>> bySolver;
+    for (size_t k : fused) bySolver[ms[k]->solver].push_back(k);
+    for (auto& kv : bySolver) {
+      std::vector<size_t>& ks = kv.second;
+      for (size_t k : ks) {
+        ms[k]->ensureDevice();
+        ck(cudaStreamSynchronize(ms[k]->stream), "medium stream");
+      }
+      // largest first (cost ~ nZSteps * modes * N log N)
+      std::sort(ks.begin(), ks.end(), [&](size_t x, size_t y) {
+        auto cost = [&](Medium* m) { return (double)m->nZ * m->nSignal * m->N * std::log2((double)m->N); };
+        return cost(ms[x]) > cost(ms[y]);
+      });
+      size_t inTot = 0, outTot = 0, maxN = 0;
+      for (size_t k : ks) {
+        inTot += ms[k]->N;
+        outTot += (size_t)ms[k]->nSignal * ms[k]->N;
+        maxN = std::max<size_t>(maxN, ms[k]->N);
+      }
+      Medium* lead = ms[ks[0]];
+      cudaStream_t st = lead->stream;
+      g_ragged.in.reserve(inTot);
+      g_ragged.out.reserve(outTot);
+      g_ragged.items.reserve(ks.size());
+      g_ragged.counter.reserve(1);
+      std::vector<PropArgs> items(ks.size());
+      std::vector<size_t> outOff(ks.size());
+      size_t io = 0, oo = 0;
+      for (size_t q = 0; q < ks.size(); q++) {
+        Medium* m = ms[ks[q]];
+        ck(cudaMemcpyAsync(g_ragged.in.p + io, inputs[ks[q]], m->N * sizeof(double2), cudaMemcpyHostToDevice, st),
+           "ragged input");
+        PropArgs a = m->baseArgs(8);
+        a.nInst = 1;
+        a.ipc = 1;
+        a.inKind = 1;
+        a.inTime = in_time_domain ? 1 : 0;
+        a.in = g_ragged.in.p + io;
+        a.inStride = (long long)m->N;
+        a.inChannels = 1;
+        a.inputMode = 0;
+        a.nOut = (int)m->nSignal;
+        for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
+        a.out = g_ragged.out.p + oo;
+        a.outStride = (long long)m->nSignal * m->N;
+        items[q] = a;
+        outOff[q] = oo;
+        io += m->N;
+        oo += (size_t)m->nSignal * m->N;
+      }
+      ck(cudaMemcpyAsync(g_ragged.items.p, items.data(), items.size() * sizeof(PropArgs), cudaMemcpyHostToDevice, st),
+         "ragged items");
+      ck(cudaMemsetAsync(g_ragged.counter.p, 0, sizeof(unsigned long long), st), "ragged counter");
+      const KernelEntry* ke = lead->findKernel(kKindRagged, kv.first, 8);
+      int block = (int)((maxN / 8 + 31) / 32 * 32);
+      const size_t smem = maxN * sizeof(double2);
+      int dev = 0, sms = 1, optin = 0;
+      ck(cudaGetDevice(&dev), "device");
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      cudaFuncAttributes fa;
+      ck(cudaFuncGetAttributes(&fa, ke->fn), "kernel attributes");
+      ck(cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
+         "smem attribute");
+      if (block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
+      int active = 0;
+      ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, ke->fn, block, smem), "occupancy");
+      if (active < 1) throw Unsupported("ragged kernel does not fit on an SM");
+      const int nItems = (int)ks.size();
+      const int grid = std::min(nItems, sms * active);
+      PropArgs* itemsD = g_ragged.items.p;
+      unsigned long long* ctr = g_ragged.counter.p;
+      int nIt = nItems;
+      void* args[] = {(void*)&itemsD, (void*)&nIt, (void*)&ctr};
+      if (lead->timeKernels) {
+        if (!lead->ev0) ck(cudaEventCreate(&lead->ev0), "event");
+        if (!lead->ev1) ck(cudaEventCreate(&lead->ev1), "event");
+        ck(cudaEventRecord(lead->ev0, st), "event");
+      }
+      ck(cudaLaunchKernel(ke->fn, dim3(grid), dim3(block), args, smem, st), "ragged launch");
+      lead->launches++;
+      if (lead->timeKernels) {
+        ck(cudaEventRecord(lead->ev1, st), "event");
+        ck(cudaEventSynchronize(lead->ev1), "event");
+        float ms_ = 0;
+        ck(cudaEventElapsedTime(&ms_, lead->ev0, lead->ev1), "event");
+        lead->kernelMs += ms_;
+        lead->kernelCount++;
+      }
+      for (size_t q = 0; q < ks.size(); q++) {
+        Medium* m = ms[ks[q]];
+        ck(cudaMemcpyAsync(outputs[ks[q]], g_ragged.out.p + outOff[q], (size_t)m->nSignal * m->N * sizeof(double2),
+                           cudaMemcpyDeviceToHost, st),
+           "ragged output");
+      }
+      ck(cudaStreamSynchronize(st), "ragged batch");
     }
   });
 }
@@ -2002,6 +2309,47 @@ nlm_status nlm_cascade_media(const nlm_medium* cascade, size_t* n_media) {
   return guarded([&] {
     const Medium* c = CM(cascade);
     *n_media = c->isCascade ? c->media.size() : 0;
+  });
+}
+
+nlm_status nlm_green_rows(nlm_medium* h, int in_time_domain, int run_pump, size_t first, size_t count, double* raw_out) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    m->greenRows(in_time_domain, run_pump, (long long)first, (long long)count, reinterpret_cast<double2*>(raw_out));
+  });
+}
+
+nlm_status nlm_green_finish(nlm_medium* h, const double* raw, int normalize, double* green_c, double* green_s) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    m->greenFinish(reinterpret_cast<const double2*>(raw), normalize, reinterpret_cast<double2*>(green_c),
+                   reinterpret_cast<double2*>(green_s));
+  });
+}
+
+nlm_status nlm_set_poling_profile(nlm_medium* h, const double* profile, size_t n) {
+  return guarded([&] { M(h)->setPolingProfile(profile, n); });
+}
+
+nlm_status nlm_adjoint_forward(nlm_medium* h, const void* inputs_dev, size_t rows, void* out_dev,
+                               int checkpoint_interval, int* used_interval) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    m->adjointForward(reinterpret_cast<const double2*>(inputs_dev), rows, nlm::d2(out_dev), checkpoint_interval);
+    if (used_interval) *used_interval = m->adjK;
+  });
+}
+
+nlm_status nlm_adjoint_backward(nlm_medium* h, const void* grad_out_dev, void* grad_in_dev, void* grad_pump_dev,
+                                double* grad_poling) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    m->adjointBackward(reinterpret_cast<const double2*>(grad_out_dev), nlm::d2(grad_in_dev), nlm::d2(grad_pump_dev),
+                       grad_poling);
   });
 }
 

@@ -13,6 +13,8 @@ void add_kernels_linear(std::vector<KernelEntry>& t);
 void add_kernels_direct_a(std::vector<KernelEntry>& t);
 void add_kernels_direct_b(std::vector<KernelEntry>& t);
 void add_kernels_gnlse(std::vector<KernelEntry>& t);
+void add_kernels_adjoint(std::vector<KernelEntry>& t);
+void add_kernels_ragged(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -22,6 +24,8 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_direct_a(table);
     add_kernels_direct_b(table);
     add_kernels_gnlse(table);
+    add_kernels_adjoint(table);
+    add_kernels_ragged(table);
   });
   *count = (int)table.size();
   return table.data();
@@ -101,7 +105,10 @@ static cudaError_t smem_optin(const void* fn) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
   if (e == cudaSuccess) done.push_back(fn);
   return e;
 }

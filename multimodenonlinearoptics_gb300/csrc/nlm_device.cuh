@@ -106,15 +106,22 @@ __device__ __forceinline__ void dft_r(double2 (&x)[R], int u, int B) {
 // One Stockham pass.  Every shared-memory store is preceded by a barrier (all earlier
 // loads of the buffer are complete) and every load is preceded by one (all stores are
 // visible).  Barriers are CTA-wide and all branches here are uniform across the CTA.
-template <int R, int r, bool INV>
+template <int R, int r, bool INV, bool GUARD = false>
 __device__ __forceinline__ void stockham_pass(double2 (&x)[R], double2* __restrict__ buf,
                                               const double2* __restrict__ tw, int N, int T, int j,
-                                              int L, bool from_smem, bool to_smem) {
+                                              int L, bool from_smem, bool to_smem, bool act = true) {
+  // GUARD: threads with act == false (j >= T in a CTA sized for a larger grid) take part in the
+  // barriers only and touch no memory.
   constexpr int B = R / r;
   if (from_smem) {
     __syncthreads();
+    if (!GUARD || act) {
 #pragma unroll
-    for (int v = 0; v < R; v++) x[v] = buf[j + v * T];
+      for (int v = 0; v < R; v++) x[v] = buf[j + v * T];
+    } else {
+#pragma unroll
+      for (int v = 0; v < R; v++) x[v] = czero();
+    }
   }
   if (L > 1) {
     const int stride = N / (L * r);
@@ -123,7 +130,8 @@ __device__ __forceinline__ void stockham_pass(double2 (&x)[R], double2* __restri
       const int k = (j + u * T) & (L - 1);
 #pragma unroll
       for (int q = 1; q < r; q++) {
-        const double2 w = __ldg(tw + k * q * stride);
+        double2 w = czero();
+        if (!GUARD || act) w = tw[k * q * stride];   // shared or global table (the caller's choice)
         x[u + q * B] = INV ? cmulc(x[u + q * B], w) : cmul(x[u + q * B], w);
       }
     }
@@ -132,37 +140,40 @@ __device__ __forceinline__ void stockham_pass(double2 (&x)[R], double2* __restri
   for (int u = 0; u < B; u++) dft_r<r, INV>(x, u, B);
   if (to_smem) {
     __syncthreads();
+    if (!GUARD || act) {
 #pragma unroll
-    for (int u = 0; u < B; u++) {
-      const int jp = j + u * T;
-      const int k = jp & (L - 1);
-      const int base = (jp - k) * r + k;
+      for (int u = 0; u < B; u++) {
+        const int jp = j + u * T;
+        const int k = jp & (L - 1);
+        const int base = (jp - k) * r + k;
 #pragma unroll
-      for (int s2 = 0; s2 < r; s2++) buf[base + s2 * L] = x[u + s2 * B];
+        for (int s2 = 0; s2 < r; s2++) buf[base + s2 * L] = x[u + s2 * B];
+      }
     }
   }
 }
 
 // Full transform of the R register points of thread j (ownership j + v*T in and out).
-template <int R, bool INV>
+template <int R, bool INV, bool GUARD = false>
 __device__ __forceinline__ void fft_regs(double2 (&x)[R], double2* __restrict__ buf,
-                                         const double2* __restrict__ tw, const FFTPlanH& plan, int j) {
+                                         const double2* __restrict__ tw, const FFTPlanH& plan, int j,
+                                         bool act = true) {
   int L = 1;
   for (int p = 0; p < plan.nPass; p++) {
     const bool from = p > 0, to = p < plan.nPass - 1;
     const int r = plan.radix[p];
     if constexpr (R >= 8) {
       if (r == 8) {
-        stockham_pass<R, 8, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
+        stockham_pass<R, 8, INV, GUARD>(x, buf, tw, plan.N, plan.T, j, L, from, to, act);
         L *= 8;
         continue;
       }
     }
     if (r == 4) {
-      stockham_pass<R, 4, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
+      stockham_pass<R, 4, INV, GUARD>(x, buf, tw, plan.N, plan.T, j, L, from, to, act);
       L *= 4;
     } else {
-      stockham_pass<R, 2, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
+      stockham_pass<R, 2, INV, GUARD>(x, buf, tw, plan.N, plan.T, j, L, from, to, act);
       L *= 2;
     }
   }

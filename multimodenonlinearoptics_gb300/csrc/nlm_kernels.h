@@ -25,6 +25,7 @@ struct PropArgs {
   long long nInst;        // independent propagations in this launch
   long long instBase;     // global index of the launch's first propagation
   int ipc;                // propagations per CTA
+  unsigned long long* work;  // zeroed work counter for dynamic scheduling of the groups; null: static
   // input description
   int inKind;             // 0: impulses (Green's function), 1: dense rows
   int inTime;             // inputs and outputs in the time domain
@@ -53,10 +54,24 @@ struct PropArgs {
   // full grids of a single propagation (runSignalSimulation); null otherwise
   double2* gridF;         // [mode][nZ][N]
   double2* gridT;
+  // checkpoints of the forward states for the adjoint: state s_i (time domain, all modes) is stored
+  // at ckpt[((inst * ckN) + i / ckK) * nModes + m][N] when i % ckK == 0 and i < nZ - 1
+  double2* ckpt;
+  int ckK, ckN;
   // Chi3GNLSE tables
   const double2* raman;   // ramanResponse / N
   const double2* steep;   // (nlStep0 + nlStep1 * omega) / N
   const double* relInt;   // [(nZ-1)][3] relative intensity at i-1, i-1/2, i
+};
+
+// Arguments of the reverse (adjoint) sweep.
+struct AdjArgs {
+  const double2* gout;   // [nInst][N]: dL/dRe X + i dL/dIm X of the output spectrum
+  const double2* ckpt;   // forward checkpoints (PropArgs::ckpt layout)
+  int K, nCk;            // checkpoint interval and count
+  double2* seg;          // scratch [slot][K][N] for the recomputed states of one segment (K > 1)
+  double2* ga;           // [(nZ-1)][3][N] accumulated gradients of the stage factors a_s = c_s P_s
+  double2* gin;          // [nInst][N]: gradient with respect to the input spectrum
 };
 
 // Registry of the propagation kernels.  The host engine launches them generically with
@@ -65,7 +80,9 @@ enum KernelKind : int {
   kKindDirect = 0,     // k_propagate_direct<Solver, R>      key = solver id
   kKindLinear = 1,     // k_propagate_linear<M, R>           key = number of modes M
   kKindGnlse = 2,      // k_propagate_gnlse<R>               key = solver id (Chi3GNLSE); extra arg: scratch
-  kKindBuildProp = 3   // k_build_propagator<Solver>         key = solver id, R = 0
+  kKindBuildProp = 3,  // k_build_propagator<Solver>         key = solver id, R = 0
+  kKindAdjoint = 4,    // k_adjoint_pdc<R>                   key = solver id; args (PropArgs, AdjArgs)
+  kKindRagged = 5      // k_propagate_ragged<Solver, R>      key = solver id; args (items, nItems, work)
 };
 struct KernelEntry {
   int kind;
@@ -94,5 +111,12 @@ cudaError_t launch_pump_from(const double2* otherSignalFreq, int otherRows, doub
 cudaError_t launch_cgemm_compose(const double2* Ci, const double2* Si, const double2* C, const double2* S,
                                  int rows, int inner, int cols, double2* Cout, double2* Sout, cudaStream_t s);
 cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
+// Post-processing of the adjoint of Chi2PDC (adjoint.cu)
+cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const double* prof, int nZ, int N,
+                                 double2* gP, cudaStream_t s);
+cudaError_t launch_adj_pump_reduce(const double2* fgP, const double* disp, double dzp, int nRowsP, int N,
+                                   double2* gF0, cudaStream_t s);
+cudaError_t launch_adj_coef_reduce(const double2* ga, const double2* pump, int nZ, int N, double2* gc,
+                                   cudaStream_t s);
 
 }  // namespace nlm

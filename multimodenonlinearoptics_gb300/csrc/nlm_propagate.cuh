@@ -19,11 +19,41 @@ namespace nlm {
 
 constexpr int kMaxThreads = 512;   // launch bound of every propagation kernel
 
+// Next group of propagations for this CTA: static round robin, or the next free group of a
+// work counter shared by the grid (first group = blockIdx.x, then atomically claimed ones).
+// Called by all threads of the CTA in uniform control flow.
+__device__ __forceinline__ long long next_group(const PropArgs& a, long long cg, long long* slot) {
+  if (a.work == nullptr) return cg + gridDim.x;
+  __syncthreads();   // everyone has read the previous value of *slot
+  if (threadIdx.x == 0) *slot = (long long)atomicAdd(a.work, 1ULL) + gridDim.x;
+  __syncthreads();
+  return *slot;
+}
+
+// Twiddle table of the transforms: staged in shared memory (in front of the exchange buffers) for
+// R <= 8, i.e. N <= 4096, so that the passes read it with shared-memory loads instead of loading it
+// through the L1/texture path, whose queue otherwise throttles the warps; left in global memory for
+// R = 16 (N = 8192), where the table would not fit next to the buffer.
+template <int R>
+__device__ __forceinline__ const double2* stage_twiddles(const double2* __restrict__ tw, double2* smem, int N,
+                                                         double2** bufs) {
+  if constexpr (R != 16) {
+    for (int k = threadIdx.x; k < N; k += blockDim.x) smem[k] = tw[k];
+    __syncthreads();
+    *bufs = smem + N;
+    return smem;
+  } else {
+    *bufs = smem;
+    return tw;
+  }
+}
+
 // Input of one propagation, in the frequency domain and pre-multiplied by exp(+i dz/2 D)/N
 // (src/_NonlinearMedium.hpp:169-192).
 template <int M, int R>
 __device__ __forceinline__ void load_input(const PropArgs& a, long long inst, bool active, int j,
-                                           double2 (&x)[M][R], double2* buf, const FFTPlanH& plan) {
+                                           double2 (&x)[M][R], double2* buf, const FFTPlanH& plan,
+                                           const double2* tw) {
   const int N = plan.N, T = plan.T;
   if (a.inKind == 0) {
     // impulses: instance = ((im * N) + bin) * 2 + which; value 1 (which 0) or i (which 1)
@@ -50,7 +80,7 @@ __device__ __forceinline__ void load_input(const PropArgs& a, long long inst, bo
   }
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    if (a.inTime) fft_regs<R, false>(x[m], buf, a.tw, plan, j);
+    if (a.inTime) fft_regs<R, false>(x[m], buf, tw, plan, j);
     const double2* h = a.half + (long long)m * N;
 #pragma unroll
     for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(h + j + v * T));
@@ -88,12 +118,13 @@ __device__ __forceinline__ void store_output(const PropArgs& a, long long inst, 
 // Dispersion half of a step for all modes: FFT, multiply, optional inverse FFT and grid rows.
 template <int M, int R>
 __device__ __forceinline__ void dispersion_step(const PropArgs& a, int i, bool last, int j, double2 (&x)[M][R],
-                                                double2* buf, const FFTPlanH& plan, bool active, const double2* table) {
+                                                double2* buf, const FFTPlanH& plan, bool active, const double2* table,
+                                                const double2* tw) {
   const int N = plan.N, T = plan.T;
   const bool wantTime = !last || a.inTime || a.gridT != nullptr;
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    fft_regs<R, false>(x[m], buf, a.tw, plan, j);
+    fft_regs<R, false>(x[m], buf, tw, plan, j);
     const double2* d = table + (long long)m * N;
 #pragma unroll
     for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(d + j + v * T));
@@ -102,7 +133,7 @@ __device__ __forceinline__ void dispersion_step(const PropArgs& a, int i, bool l
   if (a.gridF) store_rows<M, R>(a.gridF, ms, i, N, T, j, x, (double)N, active);
   if (wantTime) {
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, a.tw, plan, j);
+    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
     if (a.gridT) store_rows<M, R>(a.gridT, ms, i, N, T, j, x, 1.0, active);
   }
 }
@@ -149,19 +180,23 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
   const int g = threadIdx.x / T, j = threadIdx.x - g * T;
-  double2* buf = smem + (long long)g * N;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
-  for (long long cg = blockIdx.x; cg < nGroups; cg += gridDim.x) {
+  __shared__ long long s_group;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
     const long long local = cg * a.ipc + g;
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[M][R];
-    load_input<M, R>(a, inst, active, j, x, buf, plan);
+    load_input<M, R>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
     if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, a.tw, plan, j);
+    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
     if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+    if (a.ckpt && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
 #pragma unroll
@@ -187,11 +222,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
         for (int m = 0; m < M; m++) x[m][v] = xm[m];
       }
       const bool last = i == a.nZ - 1;
-      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep);
+      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      if (a.ckpt && !last && i % a.ckK == 0)
+        store_rows<M, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     }
     if (a.nZ == 1) {
 #pragma unroll
-      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, a.tw, plan, j);
+      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, tw, plan, j);
       // x now holds X_in * exp(+i dz/2 D); the factor tables are pre-divided by N
 #pragma unroll
       for (int m = 0; m < M; m++)
@@ -200,7 +237,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
       if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
       if (a.inTime || a.gridT) {
 #pragma unroll
-        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, a.tw, plan, j);
+        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
         if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
       }
     }
@@ -211,7 +248,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
 
 // --------------------------------------------------------------------------------------------
 // Linear kernel: pump-driven solvers with the precomputed per-point RK4 map.
-// prop layout: [step][E = (2M)^2][N], entry e = row * 2M + col over (Re a0, Im a0, Re a1, ...).
+// prop layout: [step][E/2][N] double2, word w = row * M + c holding the entries (row, 2c), (row, 2c+1)
+// of the (2M)x(2M) real matrix over (Re a0, Im a0, Re a1, ...).
 // --------------------------------------------------------------------------------------------
 template <int M, int R>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs a) {
@@ -220,21 +258,25 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
   const int g = threadIdx.x / T, j = threadIdx.x - g * T;
-  double2* buf = smem + (long long)g * N;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
-  for (long long cg = blockIdx.x; cg < nGroups; cg += gridDim.x) {
+  __shared__ long long s_group;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
     const long long local = cg * a.ipc + g;
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[M][R];
-    load_input<M, R>(a, inst, active, j, x, buf, plan);
+    load_input<M, R>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
     if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, a.tw, plan, j);
+    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
     if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
-      const double* mat = a.prop + (long long)(i - 1) * E * N;
+      // entries stored as pairs (row r, columns 2c and 2c+1) so a point loads D*D/2 16-byte words
+      const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (E / 2) * N;
 #pragma unroll
       for (int v = 0; v < R; v++) {
         const int t = j + v * T;
@@ -246,27 +288,32 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs
         }
 #pragma unroll
         for (int r = 0; r < D; r++) {
-          double s = __ldg(mat + (long long)(r * D) * N + t) * in[0];
+          const double2 e0 = __ldg(mat + (long long)(r * (D / 2)) * N + t);
+          double s = fma(e0.y, in[1], e0.x * in[0]);
 #pragma unroll
-          for (int c = 1; c < D; c++) s = fma(__ldg(mat + (long long)(r * D + c) * N + t), in[c], s);
+          for (int c = 1; c < D / 2; c++) {
+            const double2 e = __ldg(mat + (long long)(r * (D / 2) + c) * N + t);
+            s = fma(e.x, in[2 * c], s);
+            s = fma(e.y, in[2 * c + 1], s);
+          }
           outv[r] = s;
         }
 #pragma unroll
         for (int m = 0; m < M; m++) x[m][v] = make_double2(outv[2 * m], outv[2 * m + 1]);
       }
       const bool last = i == a.nZ - 1;
-      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep);
+      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
     }
     if (a.nZ == 1) {
 #pragma unroll
-      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, a.tw, plan, j);
+      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, tw, plan, j);
 #pragma unroll
       for (int m = 0; m < M; m++)
 #pragma unroll
         for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(a.back + (long long)m * N + j + v * T));
       if (a.inTime) {
 #pragma unroll
-        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, a.tw, plan, j);
+        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
       }
     }
     store_output<M, R>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
@@ -296,7 +343,7 @@ __global__ void k_build_propagator(const PropArgs a) {
       p[2][q] = pr[2 * N];
     }
     const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-    double* mat = const_cast<double*>(a.prop) + (long long)(i - 1) * E * N + t;
+    double cols[D][D];   // cols[col][row]
 #pragma unroll
     for (int col = 0; col < D; col++) {
       double2 xm[M];
@@ -306,10 +353,16 @@ __global__ void k_build_propagator(const PropArgs a) {
       rk4_point<S>(xm, p, c);
 #pragma unroll
       for (int m = 0; m < M; m++) {
-        mat[(long long)((2 * m) * D + col) * N] = xm[m].x;
-        mat[(long long)((2 * m + 1) * D + col) * N] = xm[m].y;
+        cols[col][2 * m] = xm[m].x;
+        cols[col][2 * m + 1] = xm[m].y;
       }
     }
+    double2* mat = reinterpret_cast<double2*>(const_cast<double*>(a.prop)) + (long long)(i - 1) * (E / 2) * N + t;
+#pragma unroll
+    for (int r = 0; r < D; r++)
+#pragma unroll
+      for (int cc = 0; cc < D / 2; cc++)
+        mat[(long long)(r * (D / 2) + cc) * N] = make_double2(cols[2 * cc][r], cols[2 * cc + 1][r]);
   }
 }
 

@@ -18,19 +18,22 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
   const int g = threadIdx.x / T, j = threadIdx.x - g * T;
-  double2* buf = smem + (long long)g * N;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
   double2* X = scratch + ((long long)blockIdx.x * a.ipc + g) * 2 * N;   // state (time domain)
   double2* ACC = X + N;                                                 // k1 + 2 k2 + 2 k3 + k4
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
-  for (long long cg = blockIdx.x; cg < nGroups; cg += gridDim.x) {
+  __shared__ long long s_group;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
     const long long local = cg * a.ipc + g;
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[1][R];
-    load_input<1, R>(a, inst, active, j, x, buf, plan);
+    load_input<1, R>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
     if (a.gridF) store_rows<1, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
-    fft_regs<R, true>(x[0], buf, a.tw, plan, j);
+    fft_regs<R, true>(x[0], buf, tw, plan, j);
     if (a.gridT) store_rows<1, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
 #pragma unroll
     for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
@@ -50,17 +53,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
           u[v] = make_double2(ri * cabs2(y[v]), 0.0);
         }
         // Raman convolution R~ * (rel |y|^2)
-        fft_regs<R, false>(u, buf, a.tw, plan, j);
+        fft_regs<R, false>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + j + v * T));
-        fft_regs<R, true>(u, buf, a.tw, plan, j);
+        fft_regs<R, true>(u, buf, tw, plan, j);
         // times the field, then the self-steepening operator (g0 + g1 w)
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], y[v]);
-        fft_regs<R, false>(u, buf, a.tw, plan, j);
+        fft_regs<R, false>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + j + v * T));
-        fft_regs<R, true>(u, buf, a.tw, plan, j);
+        fft_regs<R, true>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) {
           k[v] = u[v];
@@ -71,19 +74,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
 #pragma unroll
       for (int v = 0; v < R; v++) x[0][v] = caxpy(X[j + v * T], 1.0 / 6.0, ACC[j + v * T]);
       const bool last = i == a.nZ - 1;
-      dispersion_step<1, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep);
+      dispersion_step<1, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
       if (!last) {
 #pragma unroll
         for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
       }
     }
     if (a.nZ == 1) {
-      fft_regs<R, false>(x[0], buf, a.tw, plan, j);
+      fft_regs<R, false>(x[0], buf, tw, plan, j);
 #pragma unroll
       for (int v = 0; v < R; v++) x[0][v] = cmul(x[0][v], __ldg(a.back + j + v * T));
       if (a.gridF) store_rows<1, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
       if (a.inTime || a.gridT) {
-        fft_regs<R, true>(x[0], buf, a.tw, plan, j);
+        fft_regs<R, true>(x[0], buf, tw, plan, j);
         if (a.gridT) store_rows<1, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
       }
     }

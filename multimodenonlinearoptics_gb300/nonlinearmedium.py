@@ -73,6 +73,11 @@ def _load():
         "nlm_set_schedule": (i, [vp, i, i, i]),
         "nlm_last_launch_count": (i, [vp, P(ctypes.c_long)]),
         "nlm_kernel_timing": (i, [vp, i, P(d), P(ctypes.c_long)]),
+        "nlm_set_poling_profile": (i, [vp, P(d), sz]),
+        "nlm_green_rows": (i, [vp, i, i, sz, sz, P(d)]),
+        "nlm_green_finish": (i, [vp, P(d), i, P(d), P(d)]),
+        "nlm_adjoint_forward": (i, [vp, vp, sz, vp, i, P(i)]),
+        "nlm_adjoint_backward": (i, [vp, vp, vp, vp, P(d)]),
         "nlm_fp64_peak": (i, [P(d)]),
     }
     for name, (res, args) in sigs.items():
@@ -111,6 +116,32 @@ def _mask(v):
 def device_available():
     """True when a CUDA device is usable by this process."""
     return bool(_lib.nlm_device_available())
+
+
+def ragged_batch(media, inputs, inTimeDomain=False):
+    """Propagate one signal through each medium of a ragged set in one persistent launch.
+
+    No counterpart in the reference, which would call batchSignalSimulation once per medium
+    (src/_NonlinearMedium.cpp:378-444).  media: list of media (pumps already run); inputs: one
+    N-point spectrum (or time profile) per medium for its first mode.  Returns, per medium, the last
+    row of all its signal modes (nSignalModes x N).
+    """
+    media = list(media)
+    ins = [_complex1d(x) for x in inputs]
+    if len(ins) != len(media):
+        raise ValueError("one input per medium")
+    outs = []
+    for m, x in zip(media, ins):
+        d = m._dims
+        if x.size != d["nFreqs"]:
+            raise ValueError("input length does not match the medium's nFreqs")
+        outs.append(np.empty((d["nSignalModes"], d["nFreqs"]), dtype=np.complex128))
+    P = ctypes.POINTER(ctypes.c_double)
+    hs = (ctypes.c_void_p * len(media))(*[m._h() for m in media])
+    ip = (P * len(media))(*[_dptr(x.view(np.float64)) for x in ins])
+    op = (P * len(media))(*[_dptr(o.view(np.float64)) for o in outs])
+    _check(_lib.nlm_ragged_batch(hs, len(media), ip, int(bool(inTimeDomain)), op))
+    return outs
 
 
 def fp64_peak_tflops():
@@ -288,6 +319,11 @@ class _NonlinearMedium:
         ms, cnt = ctypes.c_double(), ctypes.c_long()
         _check(_lib.nlm_kernel_timing(self._h(), int(enable), ctypes.byref(ms), ctypes.byref(cnt)))
         return ms.value, cnt.value
+
+    def _set_poling_profile(self, profile):
+        """Continuous poling d(z) on the nZSteps grid in place of the domain pattern (no reference counterpart)."""
+        p = np.ascontiguousarray(np.asarray(profile, dtype=np.float64).ravel())
+        _check(_lib.nlm_set_poling_profile(self._h(), _dptr(p), p.size))
 
     def _set_stream(self, stream_handle):
         _check(_lib.nlm_set_stream(self._h(), ctypes.c_void_p(stream_handle)))

@@ -1,0 +1,166 @@
+"""Gradients of the reverse sweep (Chi2PDC) against central finite differences of the engine's own
+forward and of the oracle's forward (the reference's algorithm with its poling array replaced by a
+continuous profile)."""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0, beta1s=2, beta3=0,
+          beta3s=0.1, diffBeta0=0.3, tMax=20, tPrecision=64, zPrecision=20)
+
+
+def _problem(n, nz, rows, seed=4):
+    rng = np.random.default_rng(seed)
+    x = cases.noise(rng, rows * n, 0.3).reshape(rows, n)
+    t = np.fft.fftshift(np.linspace(-KW["tMax"], KW["tMax"], n, endpoint=False))
+    f0 = np.fft.fft(np.exp(-t ** 2 / 2)) * (1 + 0.05 * cases.noise(rng, n, 1.0))
+    d = rng.uniform(-1, 1, nz)
+    target = cases.noise(rng, rows * n, 1.0).reshape(rows, n)
+    target /= np.linalg.norm(target)
+    return x, f0, d, target
+
+
+def _oracle_out(oracle, kw, x, f0, d):
+    m = oracle.Chi2PDC(**kw)
+    m.set_pump_custom(np.fft.ifft(f0))
+    m.poling = np.asarray(d, dtype=np.float64)        # continuous profile in place of the domains
+    m.run_pump_simulation()
+    f, _ = m.propagate(x, False, 0)
+    return f[:, 0]
+
+
+def _loss(out, target):
+    """||out - target||^2 without its constant ||target||^2 (same gradient): keeps the value at the
+    scale of the field so the finite-difference round-off (~1e-16 |L| / h) stays below the gradients."""
+    out = np.asarray(out)
+    return float(np.sum(np.abs(out) ** 2) - 2 * np.real(np.vdot(target, out)))
+
+
+def _engine_grads(nlm, kw, x, f0, d, target, interval=0):
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_pdc
+    med = nlm.Chi2PDC(**kw)
+    xt = torch.tensor(x, dtype=torch.complex128, device="cuda", requires_grad=True)
+    ft = torch.tensor(f0, dtype=torch.complex128, device="cuda", requires_grad=True)
+    dt = torch.tensor(d, dtype=torch.float64, requires_grad=True)
+    tt = torch.tensor(target, dtype=torch.complex128, device="cuda")
+    out = propagate_pdc(med, xt, ft, dt, interval)
+    loss = torch.sum(torch.abs(out - tt) ** 2)
+    loss.backward()
+    return (out.detach().cpu().numpy(), xt.grad.cpu().numpy(), ft.grad.cpu().numpy(), dt.grad.numpy(), med)
+
+
+def _fd(fun, base, idx, h, complex_part=None):
+    p, m = base.copy(), base.copy()
+    if complex_part == "im":
+        p.flat[idx] += 1j * h
+        m.flat[idx] -= 1j * h
+    else:
+        p.flat[idx] += h
+        m.flat[idx] -= h
+    return (fun(p) - fun(m)) / (2 * h)
+
+
+def _significant(g, count, rng):
+    """Indices of the largest components and of random ones above 5% of the largest: components far
+    below the loss scale are dominated by the finite-difference round-off (~1e-16 L / h)."""
+    mag = np.abs(g).ravel()
+    top = list(np.argsort(mag)[::-1][:count])
+    big = np.flatnonzero(mag >= 0.05 * mag.max())
+    extra = list(rng.choice(big, min(count, big.size), replace=False))
+    return sorted(set(top + extra))
+
+
+def _rel_vec(adj, fd):
+    adj, fd = np.asarray(adj), np.asarray(fd)
+    return float(np.linalg.norm(adj - fd) / np.linalg.norm(fd))
+
+
+def test_adjoint_matches_finite_differences_of_oracle_and_engine(nlm, oracle):
+    kw = dict(KW)
+    n = 64
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    x, f0, d, target = _problem(n, nz, rows=2)
+    out, gx, gf, gd, med = _engine_grads(nlm, kw, x, f0, d, target)
+    ref = _oracle_out(oracle, kw, x, f0, d)
+    assert cases.rel_l2(out, ref) < 1e-9
+    h = 1e-6
+    rng = np.random.default_rng(0)
+
+    def loss_x(v):
+        return _loss(_oracle_out(oracle, kw, v, f0, d), target)
+
+    def loss_f(v):
+        return _loss(_oracle_out(oracle, kw, x, v, d), target)
+
+    def loss_d(v):
+        return _loss(_oracle_out(oracle, kw, x, f0, v), target)
+
+    ga, gfd = [], []
+    for idx in _significant(gx, 3, rng):
+        ga += [gx.flat[idx].real, gx.flat[idx].imag]
+        gfd += [_fd(loss_x, x, idx, h), _fd(loss_x, x, idx, h, "im")]
+    assert _rel_vec(ga, gfd) < 1e-6
+    ga, gfd = [], []
+    for idx in _significant(gf, 3, rng):
+        ga += [gf[idx].real, gf[idx].imag]
+        gfd += [_fd(loss_f, f0, idx, h), _fd(loss_f, f0, idx, h, "im")]
+    assert _rel_vec(ga, gfd) < 1e-6
+    idx_d = _significant(gd, 4, rng)
+    assert _rel_vec(gd[idx_d], [_fd(loss_d, d, i, h) for i in idx_d]) < 1e-6
+
+    # central differences of the engine's own forward
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_pdc
+
+    def eng_loss_d(v):
+        o = propagate_pdc(med, torch.tensor(x, device="cuda"), torch.tensor(f0, device="cuda"),
+                          torch.tensor(v), 0).cpu().numpy()
+        return _loss(o, target)
+
+    idx_d = _significant(gd, 3, rng)
+    assert _rel_vec(gd[idx_d], [_fd(eng_loss_d, d, i, h) for i in idx_d]) < 1e-6
+
+
+def test_checkpointed_sweep_equals_stored_states(nlm):
+    kw = dict(KW)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    x, f0, d, target = _problem(64, nz, rows=3, seed=9)
+    a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
+    b = _engine_grads(nlm, kw, x, f0, d, target, interval=7)
+    for ga, gb in zip(a[1:4], b[1:4]):
+        assert cases.rel_l2(gb, ga) < 1e-12
+
+
+def test_adjoint_config_size(nlm, oracle):
+    """The gradient configuration: N=512, nZSteps=2000, one noise signal, d(z) ~ U[-1, 1]."""
+    kw = dict(KW, tMax=40, tPrecision=512, zPrecision=1000, diffBeta0=0)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    assert nz == 2000
+    rng = np.random.default_rng(4)
+    x = cases.noise(rng, 512, 1e-3).reshape(1, 512)
+    t = np.fft.fftshift(np.linspace(-40, 40, 512, endpoint=False))
+    f0 = np.fft.fft(np.exp(-t ** 2 / 2))
+    d = rng.uniform(-1, 1, nz)
+    target = cases.noise(rng, 512, 1.0).reshape(1, 512)
+    target /= np.linalg.norm(target)
+    out, gx, gf, gd, _ = _engine_grads(nlm, kw, x, f0, d, target)
+    h = 1e-6
+
+    def loss_f(v):
+        return _loss(_oracle_out(oracle, kw, x, v, d), target)
+
+    def loss_d(v):
+        return _loss(_oracle_out(oracle, kw, x, f0, v), target)
+
+    rng2 = np.random.default_rng(1)
+    ga, gfd = [], []
+    for idx in _significant(gf, 2, rng2):
+        ga += [gf[idx].real, gf[idx].imag]
+        gfd += [_fd(loss_f, f0, idx, h), _fd(loss_f, f0, idx, h, "im")]
+    assert _rel_vec(ga, gfd) < 1e-6
+    idx_d = _significant(gd, 2, rng2)
+    assert _rel_vec(gd[idx_d], [_fd(loss_d, d, i, h) for i in idx_d]) < 1e-6

@@ -1,0 +1,42 @@
+"""One persistent launch over a ragged set of media against the oracle and against one batch per medium."""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+
+def test_ragged_launch_matches_oracle(nlm, oracle):
+    import bench
+    params = bench.ragged_media_params(seed=11, count=6)
+    media, refs, ins = [], [], []
+    for kw, doms, pump, sig in params:
+        kw = dict(kw, zPrecision=max(10, kw["zPrecision"] // 20))   # fewer steps for the oracle
+        doms = doms[: max(2, doms.size // 20)]                      # keep domains longer than a step
+        m = nlm.Chi2SFG(customPump=pump, poling=doms, **kw)
+        r = oracle.Chi2SFG(customPump=pump, poling=doms, **kw)
+        m.runPumpSimulation()
+        r.run_pump_simulation()
+        media.append(m)
+        refs.append(r)
+        ins.append(sig)
+    # a Chi2PDC medium in the same call takes its own launch
+    kw = dict(cases.CASES["Chi2PDC"])
+    media.append(nlm.Chi2PDC(**kw))
+    refs.append(oracle.Chi2PDC(**kw))
+    media[-1].runPumpSimulation()
+    refs[-1].run_pump_simulation()
+    ins.append(cases.signal_input("Chi2PDC", 64, 1, seed=3))
+    outs = nlm.ragged_batch(media, ins)
+    assert media[0]._launch_count() >= 1
+    for m, r, x, o in zip(media, refs, ins, outs):
+        f, _ = r.propagate(x[None, :], False, 0)
+        assert cases.rel_l2(o, f[0]) < TOL
+        b = m.batchSignalSimulation(x[None, :], runPump=False)
+        assert cases.rel_l2(o.reshape(1, -1), b) < 1e-13
+    outs_t = nlm.ragged_batch(media[:3], ins[:3], True)
+    for m, r, x, o in zip(media[:3], refs[:3], ins[:3], outs_t):
+        _, t = r.propagate(x[None, :], True, 0)
+        assert cases.rel_l2(o, t[0]) < TOL
