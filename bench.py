@@ -303,6 +303,135 @@ def measure_adjoint(nlm, torch, reps=3):
                         "poling profile (%d values)" % (nz, nz)}
 
 
+GNLSE_CONFIG = dict(relativeLength=1, nlLength=1.0 / 9, selfSteepLength=6.5, fr=0.18, fb=0.21, tau1=0.244, tau2=0.64,
+                    tau3=1.92, beta2=-1, beta3=0.05, tMax=50, tPrecision=4096, zPrecision=1111)
+
+
+def measure_configs(nlm, torch, cpu=True):
+    """The other workloads of the benchmark configuration list, each bounded to a few seconds."""
+    import ctypes
+    res = {}
+    # 1. Chi3 N=1 soliton pump + seeded-noise signal, N=512, nZSteps=200: latency through the API
+    kw1 = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=512, zPrecision=200)
+    m1 = nlm.Chi3(**kw1)
+    rng = np.random.default_rng(1)
+    sig = (rng.standard_normal(512) + 1j * rng.standard_normal(512)) * 1e-3 / np.sqrt(2)
+    m1.runPumpSimulation()
+    m1.runSignalSimulation(sig)
+    lat = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        m1.runPumpSimulation()
+        m1.runSignalSimulation(sig)
+        _ = m1.signalTime
+        lat.append(time.perf_counter() - t0)
+    res["chi3_pump_signal_n512"] = {"gpu_latency_ms": 1e3 * min(lat)}
+    if cpu:
+        from oracle import nlm_oracle as O
+        o1 = O.Chi3(**kw1)
+        t0 = time.perf_counter()
+        o1.run_pump_simulation()
+        o1.run_signal_simulation(sig)
+        res["chi3_pump_signal_n512"]["cpu_oracle_latency_ms"] = 1e3 * (time.perf_counter() - t0)
+    # 3. 64 ragged Chi2SFG media in one launch
+    params = ragged_media_params()
+    media = []
+    for kw, doms, pump, _ in params:
+        m = nlm.Chi2SFG(customPump=pump, poling=doms, **kw)
+        m.runPumpSimulation()
+        media.append(m)
+    ins = [p[3] for p in params]
+    nlm.ragged_batch(media, ins)
+    wall = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        nlm.ragged_batch(media, ins)
+        wall.append(time.perf_counter() - t0)
+    steps = sum(m._dims["nZSteps"] for m in media)
+    res["ragged_chi2sfg_64_media"] = {"gpu_wall_ms": 1e3 * min(wall), "media": len(media), "total_z_steps": steps,
+                                      "n_freqs": sorted({m._dims["nFreqs"] for m in media})}
+    if cpu:
+        from oracle import nlm_oracle as O
+        t0 = time.perf_counter()
+        done_steps = 0
+        for kw, doms, pump, x in params[:8]:
+            o = O.Chi2SFG(customPump=pump, poling=doms, **kw)
+            o.run_pump_simulation()
+            o.propagate(x[None, :], False, 0)
+            done_steps += o.n_z_steps
+        dt = time.perf_counter() - t0
+        res["ragged_chi2sfg_64_media"]["cpu_oracle_sequential_ms_estimate"] = 1e3 * dt * steps / done_steps
+        res["ragged_chi2sfg_64_media"]["cpu_sample"] = "first 8 media (pump and propagation), scaled by z steps"
+    # 5. Chi3GNLSE batch of seeded noise realisations of 3 sech(t), N=4096 (sample of the rows and steps)
+    kw5 = dict(GNLSE_CONFIG, zPrecision=111)
+    m5 = nlm.Chi3GNLSE(**kw5)
+    nz5 = m5._dims["nZSteps"]
+    rows = 304
+    t = np.fft.fftshift(np.linspace(-50, 50, 4096, endpoint=False))
+    rng = np.random.default_rng(5)
+    x5 = 3 / np.cosh(t)[None, :] + (rng.standard_normal((rows, 4096)) + 1j * rng.standard_normal((rows, 4096))) \
+        * 1e-4 / np.sqrt(2)
+    x5t = torch.tensor(x5, device="cuda")
+    o5 = torch.empty_like(x5t)
+
+    def gn():
+        nlm._check(nlm._lib.nlm_batch_device(m5._h(), ctypes.c_void_p(x5t.data_ptr()), rows, 4096, 1, 0, 1, 0, None, 0,
+                                             ctypes.c_void_p(o5.data_ptr())))
+    gn()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gn()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    full_steps = nlm.Chi3GNLSE(**GNLSE_CONFIG)._dims["nZSteps"]
+    res["gnlse_batch_n4096"] = {"rows": rows, "z_steps_run": nz5, "z_steps_config": full_steps,
+                                "row_steps_per_s": rows * (nz5 - 1) / dt,
+                                "propagations_per_s_at_config_steps": rows * (nz5 - 1) / dt / (full_steps - 1)}
+    if cpu:
+        from oracle import nlm_oracle as O
+        o = O.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=3))
+        t0 = time.perf_counter()
+        o.propagate(x5[:1], True, 0)
+        dt = time.perf_counter() - t0
+        res["gnlse_batch_n4096"]["cpu_oracle_row_steps_per_s"] = (o.n_z_steps - 1) / dt
+    # gradient of the band energy (w in [2, 4]) with respect to the input spectral phase, 16 rows
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    m6 = nlm.Chi3GNLSE(**kw5)
+    w = torch.tensor(m6.omega, device="cuda")
+    band = ((w >= 2) & (w <= 4)).to(torch.float64)
+    p0 = torch.fft.fft(torch.tensor(3 / np.cosh(t), device="cuda"))
+    noise = torch.fft.fft(x5t[:16] - torch.tensor(3 / np.cosh(t), device="cuda")[None, :], dim=1)
+    phi = torch.zeros(4096, dtype=torch.float64, device="cuda", requires_grad=True)
+
+    def fwd_only():
+        with torch.no_grad():
+            a = p0[None, :] * torch.exp(1j * phi)[None, :] + noise
+            xa = a.contiguous()
+            out = torch.empty_like(xa)
+            nlm._check(nlm._lib.nlm_batch_device(m6._h(), ctypes.c_void_p(xa.data_ptr()), 16, 4096, 0, 0, 1, 0, None, 0,
+                                                 ctypes.c_void_p(out.data_ptr())))
+            torch.cuda.synchronize()
+
+    def grad():
+        a = p0[None, :] * torch.exp(1j * phi)[None, :] + noise
+        out = propagate_gnlse(m6, a)
+        e = torch.sum(torch.abs(out) ** 2 * band)
+        phi.grad = None
+        e.backward()
+        torch.cuda.synchronize()
+    fwd_only()
+    grad()
+    t0 = time.perf_counter()
+    fwd_only()
+    t_f = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    grad()
+    t_g = time.perf_counter() - t0
+    res["gnlse_phase_gradient"] = {"rows": 16, "z_steps": nz5, "fwd_ms": 1e3 * t_f, "grad_ms": 1e3 * t_g,
+                                   "grad_fwd_cost": t_g / t_f}
+    return res
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -401,6 +530,7 @@ def run_ours(args):
         plain = args.plain_sample / t_plain
 
     adjoint = measure_adjoint(nlm, torch) if args.adjoint else None
+    configs = measure_configs(nlm, torch, cpu=args.cpu_bins > 0) if args.configs else None
 
     line = None
     if rank == 0:
@@ -447,6 +577,7 @@ def run_ours(args):
             "batched_over_plain": (value / plain) if plain else None,
             "parity_sample_rel_err": parity,
             "adjoint": adjoint,
+            "other_configs": configs,
             "clocks": clocks.summary(),
         }
     if world > 1:
@@ -467,6 +598,7 @@ def main():
     ap.add_argument("--cpu-bins", type=int, default=64)
     ap.add_argument("--ref-bins", type=int, default=0)
     ap.add_argument("--adjoint", type=int, default=1, help="measure the grad/fwd cost (1) or not (0)")
+    ap.add_argument("--configs", type=int, default=1, help="measure the other workloads (1) or not (0)")
     ap.add_argument("--zprecision", type=int, default=0,
                     help="override zPrecision (smaller captures for the profiler; the benchmark uses 500)")
     args = ap.parse_args()

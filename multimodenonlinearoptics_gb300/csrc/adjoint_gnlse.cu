@@ -1,0 +1,183 @@
+// adjoint_gnlse.cu -- reverse sweep of the Chi3GNLSE split-step propagation (solvers/Chi3GNLSE.cpp:39-92).
+//
+// Each RK4 stage of the generalised NLSE is
+//     u1 = r |y|^2,  u2 = F^H(R' F u1),  k = F^H(St' F(u2 y)),   y_s = x + fac_s k_{s-1}
+// (R' = Raman response / N, St' = (g0 + g1 w) / N, F unscaled).  Its adjoint with g = dL/dRe + i dL/dIm:
+//     g_u3 = F^H(conj(St') F g_k),  g_y += conj(u2) g_u3,  g_u2 = conj(y) g_u3,
+//     g_u1 = Re F^H(conj(R') F g_u2),  g_y += 2 r g_u1 y,  g_x += g_y,  g_k_{s-1} += fac_s g_y.
+// For every step the stage inputs y_s and convolutions u2_s are recomputed from the state before the
+// step (16 transforms), then the 16 transforms of the reverse stages and the dispersion pair run.
+// States come from checkpoints every K steps; segments between checkpoints are recomputed.
+// Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and SEG[K][N] when K > 1.
+#include <vector>
+
+#include "nlm_propagate.cuh"
+
+namespace nlm {
+
+// Forward stages of step i from the state in `xs` (global, this thread's points): stores y_s and
+// u2_s, and (when acc != nullptr) the next state x + (k0 + 2 k1 + 2 k2 + k3)/6 into acc.
+template <int R>
+__device__ __forceinline__ void gnlse_stages(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
+                                             const double2* xs, double2* Y, double2* U2, double2* acc) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const double* rel = a.relInt + (long long)(i - 1) * 3;
+  double2 k[R];
+#pragma unroll
+  for (int v = 0; v < R; v++) k[v] = czero();
+  for (int s = 0; s < 4; s++) {
+    const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+    const double wgt = (s == 1 || s == 2) ? 2.0 : 1.0;
+    const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+    double2 y[R], u[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      y[v] = caxpy(xs[j + v * T], fac, k[v]);
+      Y[(long long)s * N + j + v * T] = y[v];
+      u[v] = make_double2(ri * cabs2(y[v]), 0.0);
+    }
+    fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + j + v * T));
+    fft_regs<R, true>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      U2[(long long)s * N + j + v * T] = u[v];
+      u[v] = cmul(u[v], y[v]);
+    }
+    fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + j + v * T));
+    fft_regs<R, true>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      k[v] = u[v];
+      if (acc) {
+        const int t = j + v * T;
+        acc[t] = s == 0 ? u[v] : caxpy(acc[t], wgt, u[v]);
+      }
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  __shared__ long long s_group;
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const int g = threadIdx.x / T, j = threadIdx.x - g * T;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
+  double2* slot = d.seg + ((long long)blockIdx.x * a.ipc + g) * (long long)(10 + (d.K > 1 ? d.K : 0)) * N;
+  double2* Y = slot;
+  double2* U2 = slot + 4LL * N;
+  double2* GX = slot + 8LL * N;
+  double2* GXP = slot + 9LL * N;
+  double2* SEG = slot + 10LL * N;
+  const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
+    const long long local = cg * a.ipc + g;
+    const bool active = local < a.nInst;
+    const long long inst = a.instBase + local;
+    const double2* ck = d.ckpt + (active ? inst : 0) * (long long)d.nCk * N;
+    double2 gv[R];
+    {
+      const double2* go = d.gout + (active ? inst : 0) * (long long)N;
+#pragma unroll
+      for (int v = 0; v < R; v++) gv[v] = active ? cscale(go[j + v * T], (double)N) : czero();
+    }
+    int segEnd = a.nZ - 1;
+    while (segEnd >= 1) {
+      const int jseg = (segEnd - 1) / d.K;
+      const int s0 = jseg * d.K;
+      if (d.K > 1) {
+        // recompute the states of the segment: SEG[q] = s_{s0 + q}
+#pragma unroll
+        for (int v = 0; v < R; v++) SEG[j + v * T] = ck[(long long)jseg * N + j + v * T];
+        for (int i = s0 + 1; i < segEnd; i++) {
+          const double2* xs = SEG + (long long)(i - 1 - s0) * N;
+          gnlse_stages<R>(a, i, j, buf, tw, xs, Y, U2, GX);   // GX holds the stage sum here
+          double2 x[R];
+#pragma unroll
+          for (int v = 0; v < R; v++) x[v] = caxpy(xs[j + v * T], 1.0 / 6.0, GX[j + v * T]);
+          fft_regs<R, false>(x, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+          fft_regs<R, true>(x, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) SEG[(long long)(i - s0) * N + j + v * T] = x[v];
+        }
+      }
+      for (int i = segEnd; i > s0; i--) {
+        const double2* prev = d.K > 1 ? SEG + (long long)(i - 1 - s0) * N : ck + (long long)(i - 1) * N;
+        gnlse_stages<R>(a, i, j, buf, tw, prev, Y, U2, nullptr);
+        // dispersion half: g_x' = F^H(conj(table) F g)
+        if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
+        const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+#pragma unroll
+        for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
+        fft_regs<R, true>(gv, buf, tw, plan, j);
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          GX[j + v * T] = gv[v];
+          GXP[j + v * T] = gv[v];
+        }
+        const double* rel = a.relInt + (long long)(i - 1) * 3;
+        double2 gke[R];
+#pragma unroll
+        for (int v = 0; v < R; v++) gke[v] = czero();
+        for (int s = 3; s >= 0; s--) {
+          const double w = (s == 1 || s == 2) ? 2.0 / 6.0 : 1.0 / 6.0;
+          const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+          const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+          double2 u[R];
+#pragma unroll
+          for (int v = 0; v < R; v++) u[v] = caxpy(gke[v], w, GXP[j + v * T]);   // g_k_s
+          fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
+          fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u3
+          double2 gy[R];
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            const double2 y = Y[(long long)s * N + t], u2 = U2[(long long)s * N + t];
+            gy[v] = cmulc(u[v], u2);     // conj(u2) g_u3
+            u[v] = cmulc(u[v], y);       // g_u2 = conj(y) g_u3
+          }
+          fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.raman + j + v * T));
+          fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u1 (real part)
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            const double2 y = Y[(long long)s * N + t];
+            gy[v] = caxpy(gy[v], 2.0 * ri * u[v].x, y);
+            GX[t] = cadd(GX[t], gy[v]);
+            gke[v] = cscale(gy[v], fac);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < R; v++) gv[v] = GX[j + v * T];
+      }
+      segEnd = s0;
+    }
+    fft_regs<R, false>(gv, buf, tw, plan, j);
+    if (active) {
+#pragma unroll
+      for (int v = 0; v < R; v++)
+        d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+    }
+    __syncthreads();
+  }
+}
+
+void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t) {
+  t.push_back({kKindAdjoint, kChi3GNLSE, 8, (const void*)k_adjoint_gnlse<8>});
+}
+
+}  // namespace nlm

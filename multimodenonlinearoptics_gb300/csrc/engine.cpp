@@ -1228,7 +1228,8 @@ struct Medium {
   }
 
   void adjointForward(const double2* in, size_t rows, double2* out, int interval) {
-    if (solver != kChi2PDC) throw Unsupported("the adjoint is implemented for Chi2PDC");
+    if (solver != kChi2PDC && solver != kChi3GNLSE)
+      throw Unsupported("the adjoint is implemented for Chi2PDC and Chi3GNLSE");
     if (rows == 0) throw std::invalid_argument("Too many threads requested!");
     if (nZ < 2) throw std::invalid_argument("the adjoint needs at least two z steps");
     ensureDevice();
@@ -1274,7 +1275,10 @@ struct Medium {
     adjGa.reserve(steps * 3 * N);
     ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
     Schedule s = schedule(k, adjRows, R);
-    if (adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * adjK * N);
+    const bool gn = solver == kChi3GNLSE;
+    if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
+    const size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
+    if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
     PropArgs a = baseArgs(R);
     a.nInst = adjRows;
     a.ipc = s.ipc;
@@ -1284,7 +1288,7 @@ struct Medium {
     d.ckpt = ckpt.p;
     d.K = adjK;
     d.nCk = adjNCk;
-    d.seg = adjK > 1 ? adjSeg.p : nullptr;
+    d.seg = (gn || adjK > 1) ? adjSeg.p : nullptr;
     d.ga = adjGa.p;
     d.gin = gin;
     void* args[] = {(void*)&a, (void*)&d};

@@ -15,6 +15,7 @@ void add_kernels_direct_b(std::vector<KernelEntry>& t);
 void add_kernels_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_adjoint(std::vector<KernelEntry>& t);
 void add_kernels_ragged(std::vector<KernelEntry>& t);
+void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -26,6 +27,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_gnlse(table);
     add_kernels_adjoint(table);
     add_kernels_ragged(table);
+    add_kernels_adjoint_gnlse(table);
   });
   *count = (int)table.size();
   return table.data();

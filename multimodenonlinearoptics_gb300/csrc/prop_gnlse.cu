@@ -37,6 +37,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
     if (a.gridT) store_rows<1, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
 #pragma unroll
     for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
+    if (a.ckpt && a.nZ > 1) store_rows<1, R>(a.ckpt + inst * a.ckN * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       const double* rel = a.relInt + (long long)(i - 1) * 3;
       double2 k[R];
@@ -78,6 +79,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
       if (!last) {
 #pragma unroll
         for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
+        if (a.ckpt && i % a.ckK == 0)
+          store_rows<1, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * (long long)N, N, 0, N, T, j, x, 1.0, active);
       }
     }
     if (a.nZ == 1) {

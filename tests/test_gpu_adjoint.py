@@ -53,7 +53,9 @@ def _engine_grads(nlm, kw, x, f0, d, target, interval=0):
     return (out.detach().cpu().numpy(), xt.grad.cpu().numpy(), ft.grad.cpu().numpy(), dt.grad.numpy(), med)
 
 
-def _fd(fun, base, idx, h, complex_part=None):
+def _fd(fun, base, idx, h, complex_part=None, relative=False):
+    if relative:   # step relative to the parameter's magnitude
+        h = h * max(1.0, abs(base.flat[idx]))
     p, m = base.copy(), base.copy()
     if complex_part == "im":
         p.flat[idx] += 1j * h
@@ -136,7 +138,9 @@ def test_checkpointed_sweep_equals_stored_states(nlm):
 
 
 def test_adjoint_config_size(nlm, oracle):
-    """The gradient configuration: N=512, nZSteps=2000, one noise signal, d(z) ~ U[-1, 1]."""
+    """The gradient configuration: N=512, nZSteps=2000, one noise signal, d(z) ~ U[-1, 1].  The pump
+    spectrum reaches |F0| ~ 16 while the signal is 1e-3, so its finite differences use a step of 1e-6
+    relative to each component (an absolute 1e-6 leaves the difference at the round-off level)."""
     kw = dict(KW, tMax=40, tPrecision=512, zPrecision=1000, diffBeta0=0)
     nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
     assert nz == 2000
@@ -160,7 +164,68 @@ def test_adjoint_config_size(nlm, oracle):
     ga, gfd = [], []
     for idx in _significant(gf, 2, rng2):
         ga += [gf[idx].real, gf[idx].imag]
-        gfd += [_fd(loss_f, f0, idx, h), _fd(loss_f, f0, idx, h, "im")]
+        gfd += [_fd(loss_f, f0, idx, h, relative=True), _fd(loss_f, f0, idx, h, "im", relative=True)]
     assert _rel_vec(ga, gfd) < 1e-6
     idx_d = _significant(gd, 2, rng2)
     assert _rel_vec(gd[idx_d], [_fd(loss_d, d, i, h) for i in idx_d]) < 1e-6
+
+
+GN = dict(relativeLength=0.5, nlLength=1, selfSteepLength=5, fr=0.18, fb=0.21, tau1=0.0155, tau2=0.2165, tau3=0.4,
+          beta2=-1, beta3=0.05, tMax=10, tPrecision=64, zPrecision=20)
+
+
+def _oracle_gnlse(oracle, x):
+    m = oracle.Chi3GNLSE(**GN)
+    f, _ = m.propagate(x, False, 0)
+    return f[:, 0]
+
+
+def test_gnlse_adjoint_matches_finite_differences(nlm, oracle):
+    """Gradient of the band energy with respect to the input spectrum, and of the spectral phase of the
+    pump part of the input (the gradient configuration of the GNLSE batch, at small size)."""
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    med = nlm.Chi3GNLSE(**GN)
+    n = 64
+    rng = np.random.default_rng(5)
+    t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
+    pump = np.fft.fft(2.0 / np.cosh(t))
+    noise = np.fft.fft(cases.noise(rng, 2 * n, 1e-2).reshape(2, n), axis=1)
+    w = med.omega
+    band = ((w >= 2) & (w <= 4)).astype(float)
+    phi0 = rng.uniform(-0.3, 0.3, n)
+
+    def inputs(phi):
+        return pump[None, :] * np.exp(1j * phi)[None, :] + noise
+
+    phi = torch.tensor(phi0, dtype=torch.float64, device="cuda", requires_grad=True)
+    a_in = torch.tensor(pump, device="cuda")[None, :] * torch.exp(1j * phi)[None, :] + torch.tensor(noise, device="cuda")
+    out = propagate_gnlse(med, a_in)
+    energy = torch.sum(torch.abs(out) ** 2 * torch.tensor(band, device="cuda"))
+    energy.backward()
+    gphi = phi.grad.cpu().numpy()
+    ref_out = _oracle_gnlse(oracle, inputs(phi0))
+    assert cases.rel_l2(out.detach().cpu().numpy(), ref_out) < 1e-9
+
+    def e_oracle(p):
+        return float(np.sum(np.abs(_oracle_gnlse(oracle, inputs(p))) ** 2 * band))
+
+    h = 1e-6
+    idx = _significant(gphi, 4, np.random.default_rng(0))
+    assert _rel_vec(gphi[idx], [_fd(e_oracle, phi0, i, h) for i in idx]) < 1e-6
+
+
+def test_gnlse_checkpointed_sweep(nlm):
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    med = nlm.Chi3GNLSE(**GN)
+    rng = np.random.default_rng(8)
+    x = np.fft.fft(cases.signal_input("Chi3GNLSE", 64, 1, seed=2))[None, :].repeat(3, 0)
+    x = x + np.fft.fft(cases.noise(rng, 3 * 64, 1e-2).reshape(3, 64), axis=1)
+    grads = []
+    for k in (1, 6):
+        xt = torch.tensor(x, device="cuda", requires_grad=True)
+        out = propagate_gnlse(med, xt, k)
+        torch.sum(torch.abs(out) ** 2 * torch.arange(64, device="cuda")).backward()
+        grads.append(xt.grad.cpu().numpy())
+    assert cases.rel_l2(grads[1], grads[0]) < 1e-12

@@ -30,7 +30,7 @@ def test_ragged_launch_matches_oracle(nlm, oracle):
     refs[-1].run_pump_simulation()
     ins.append(cases.signal_input("Chi2PDC", 64, 1, seed=3))
     outs = nlm.ragged_batch(media, ins)
-    assert media[0]._launch_count() >= 1
+    assert sum(m._launch_count() for m in media) == 2     # one launch per solver in the set
     for m, r, x, o in zip(media, refs, ins, outs):
         f, _ = r.propagate(x[None, :], False, 0)
         assert cases.rel_l2(o, f[0]) < TOL
