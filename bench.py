@@ -432,6 +432,44 @@ def measure_configs(nlm, torch, cpu=True):
     return res
 
 
+def measure_ff(nlm, torch, args, stream, flush, C64, S64, f64_value, f64_kernel_ms):
+    """The same Green's function with the double-float kernel (FP32 pairs on the FP32 units): device
+    throughput over the same steps, kernel time, and its distance from the FP64 result."""
+    med = nlm.Chi2PDC(poling=np.ones(N_DOMAINS if CONFIG["zPrecision"] == 500 else 5), **CONFIG)
+    med._set_stream(stream.cuda_stream)
+    med._set_precision("ff")
+    n = med._dims["nFreqs"]
+    C = torch.empty_like(C64)
+    S = torch.empty_like(S64)
+
+    def green_device():
+        nlm._check(nlm._lib.nlm_green_device(med._h(), 0, 1, 1, 0, None, 0, None, 0, C.data_ptr(), S.data_ptr()))
+
+    for _ in range(args.warmup):
+        green_device()
+    torch.cuda.synchronize()
+    med._kernel_timing(1)
+    elapsed = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        green_device()
+        e1.record(stream)
+        e1.synchronize()
+        elapsed += e0.elapsed_time(e1) / 1e3
+    kernel_ms, kernel_count = med._kernel_timing(0)
+    value = 2 * n * args.steps / elapsed
+    err = max(float(torch.linalg.norm(C - C64) / torch.linalg.norm(C64)),
+              float(torch.linalg.norm(S - S64) / torch.linalg.norm(S64)))
+    return {"value": value, "unit": UNIT, "kernel": "k_propagate_linear_ff<8>",
+            "kernel_ms": kernel_ms / max(kernel_count, 1), "speedup_vs_f64": value / f64_value,
+            "kernel_speedup_vs_f64": f64_kernel_ms / max(kernel_ms / max(kernel_count, 1), 1e-12),
+            "rel_err_vs_f64": err, "dtype": "f32x2 (double-float, ~48-bit significand)"}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -529,6 +567,7 @@ def run_ours(args):
         t_plain = time.perf_counter() - t0
         plain = args.plain_sample / t_plain
 
+    ff = measure_ff(nlm, torch, args, stream, flush, C, S, value, kernel_ms / max(kernel_count, 1)) if args.ff else None
     adjoint = measure_adjoint(nlm, torch) if args.adjoint else None
     configs = measure_configs(nlm, torch, cpu=args.cpu_bins > 0) if args.configs else None
 
@@ -576,6 +615,7 @@ def run_ours(args):
                       "form": "one propagation per kernel launch"},
             "batched_over_plain": (value / plain) if plain else None,
             "parity_sample_rel_err": parity,
+            "variant_ff": ff,
             "adjoint": adjoint,
             "other_configs": configs,
             "clocks": clocks.summary(),
@@ -597,6 +637,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--cpu-bins", type=int, default=64)
     ap.add_argument("--ref-bins", type=int, default=0)
+    ap.add_argument("--ff", type=int, default=1, help="measure the double-float variant (1) or not (0)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure the grad/fwd cost (1) or not (0)")
     ap.add_argument("--configs", type=int, default=1, help="measure the other workloads (1) or not (0)")
     ap.add_argument("--zprecision", type=int, default=0,

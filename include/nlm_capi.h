@@ -217,6 +217,11 @@ int nlm_device_available(void);
  * use_propagator: 1 = precomputed RK4 propagator for linear solvers, 0 = direct DiffEq,
  * -1 = automatic.  Used by tests and by the benchmark to compare schedules. */
 nlm_status nlm_set_schedule(nlm_medium* m, int cta_per_sm, int use_propagator, int use_graph);
+/* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
+ * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float
+ * (pairs of FP32 values, ~48-bit significand, on the FP32 units).  Other paths stay FP64.
+ * No counterpart in the reference (its arithmetic is always FP64). */
+nlm_status nlm_set_precision(nlm_medium* m, int precision);
 /* Run computeGreensFunction's propagations one per kernel launch (the "plain" form),
  * limited to the first max_instances impulse propagations (0 = all); the matrices of
  * the rows not propagated are left zero.  Timing helper for the plain-vs-batched ratio. */

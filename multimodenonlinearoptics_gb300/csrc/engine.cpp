@@ -471,7 +471,12 @@ struct Medium {
   DevBuf<double2> dstep, dlast, half, back, coef, ramanD, steepD;
   DevBuf<double> relIntD, dispPumpD, dispSignD, omegaD;
   DevBuf<double> prop;
-  long long propVersion = -1;
+  long long propVersion = -1, propBuilds = 0;
+  // arithmetic of the single-mode propagator path: 0 FP64, 1 double-float on the FP32 units
+  int precision = 0;
+  DevBuf<float4> twF, dstepF, dlastF, halfF, backF, propF;
+  bool ffTables = false;
+  long long propFFBuild = -1;
   DevBuf<double2> work, work2, raw, cs, io;
   DevBuf<double2> scratch;
   DevBuf<uint8_t> flagsD;
@@ -1150,6 +1155,37 @@ struct Medium {
     ck(cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(128), args, 0, stream), "propagator build");
     launches++;
     propVersion = pumpVersion;
+    propBuilds++;
+  }
+
+  // Double-float path: the FP64 tables and propagator are split into float-float copies once
+  // (and again after every rebuild of the propagator).
+  bool wantFF(int R, const PropArgs& a) const {
+    return precision == 1 && nSignal == 1 && R == 8 && !a.gridF && !a.gridT && !a.ckpt;
+  }
+
+  FFTables prepareFF() {
+    std::vector<SplitSeg> segs;
+    if (!ffTables) {
+      for (auto* b : {&twF, &dstepF, &dlastF, &halfF, &backF}) b->alloc(N);
+      segs.push_back({tw, twF.p, (long long)N});
+      segs.push_back({dstep.p, dstepF.p, (long long)N});
+      segs.push_back({dlast.p, dlastF.p, (long long)N});
+      segs.push_back({half.p, halfF.p, (long long)N});
+      segs.push_back({back.p, backF.p, (long long)N});
+      ffTables = true;
+    }
+    if (propFFBuild != propBuilds) {
+      const size_t count = (size_t)(nZ > 1 ? nZ - 1 : 0) * 2 * N;
+      propF.alloc(count);
+      if (count) segs.push_back({d2(prop.p), propF.p, (long long)count});
+      propFFBuild = propBuilds;
+    }
+    if (!segs.empty()) {
+      ck(launch_split_ff(segs.data(), (int)segs.size(), stream), "float-float tables");
+      launches++;
+    }
+    return FFTables{twF.p, dstepF.p, dlastF.p, halfF.p, backF.p, propF.p};
   }
 
   bool wantPropagator(long long nInst) const {
@@ -1167,13 +1203,20 @@ struct Medium {
     checkGrid(R);
     a.nInst = nInst;
     const KernelEntry* k = nullptr;
-    bool gnlse = solver == kChi3GNLSE;
+    bool gnlse = solver == kChi3GNLSE, ff = false;
+    FFTables ffT{};
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
     } else if (allowPropagator && wantPropagator(nInst)) {
       buildPropagator(R);
       a.prop = prop.p;
-      k = findKernel(kKindLinear, (int)nSignal, R);
+      if (wantFF(R, a)) {
+        ff = true;
+        ffT = prepareFF();
+        k = findKernel(kKindLinearFF, 1, R);
+      } else {
+        k = findKernel(kKindLinear, (int)nSignal, R);
+      }
     } else {
       k = findKernel(kKindDirect, solver, R);
     }
@@ -1197,6 +1240,9 @@ struct Medium {
       scratch.reserve(need);
       double2* sp = scratch.p;
       void* args[] = {(void*)&a, (void*)&sp};
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    } else if (ff) {
+      void* args[] = {(void*)&a, (void*)&ffT};
       ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
     } else {
       void* args[] = {(void*)&a};
@@ -2386,6 +2432,15 @@ nlm_status nlm_set_schedule(nlm_medium* h, int cta_per_sm, int use_propagator, i
     m->ctaPerSM = cta_per_sm;
     m->usePropagator = use_propagator;
     m->useGraph = use_graph;
+  });
+}
+
+nlm_status nlm_set_precision(nlm_medium* h, int precision) {
+  return guarded([&] {
+    if (precision != 0 && precision != 1) throw std::invalid_argument("precision must be 0 (FP64) or 1 (double-float)");
+    Medium* m = M(h);
+    m->precision = precision;
+    for (Medium* c : m->media) c->precision = precision;
   });
 }
 

@@ -16,6 +16,7 @@ void add_kernels_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_adjoint(std::vector<KernelEntry>& t);
 void add_kernels_ragged(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t);
+void add_kernels_ff(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -28,6 +29,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_adjoint(table);
     add_kernels_ragged(table);
     add_kernels_adjoint_gnlse(table);
+    add_kernels_ff(table);
   });
   *count = (int)table.size();
   return table.data();

@@ -82,7 +82,19 @@ enum KernelKind : int {
   kKindGnlse = 2,      // k_propagate_gnlse<R>               key = solver id (Chi3GNLSE); extra arg: scratch
   kKindBuildProp = 3,  // k_build_propagator<Solver>         key = solver id, R = 0
   kKindAdjoint = 4,    // k_adjoint_pdc<R>                   key = solver id; args (PropArgs, AdjArgs)
-  kKindRagged = 5      // k_propagate_ragged<Solver, R>      key = solver id; args (items, nItems, work)
+  kKindRagged = 5,     // k_propagate_ragged<Solver, R>      key = solver id; args (items, nItems, work)
+  kKindLinearFF = 6    // k_propagate_linear_ff<R>           key = M (1); args (PropArgs, FFTables)
+};
+
+// Float-float copies (float4 {re.hi, re.lo, im.hi, im.lo} per complex value) of the tables of a
+// single-mode linear propagation, for the double-float kernel on the FP32 pipes.
+struct FFTables {
+  const float4* tw;      // N twiddles
+  const float4* dstep;   // [N]
+  const float4* dlast;
+  const float4* half;
+  const float4* back;
+  const float4* prop;    // [(nZ-1)][2][N]: pairs (M00, M01) and (M10, M11)
 };
 struct KernelEntry {
   int kind;
@@ -110,6 +122,13 @@ cudaError_t launch_pump_from(const double2* otherSignalFreq, int otherRows, doub
                              cudaStream_t s);
 cudaError_t launch_cgemm_compose(const double2* Ci, const double2* Si, const double2* C, const double2* S,
                                  int rows, int inner, int cols, double2* Cout, double2* Sout, cudaStream_t s);
+// dst[k] = float-float split of src[k] for k < n (segments of several arrays in one launch)
+struct SplitSeg {
+  const double2* src;
+  float4* dst;
+  long long n;
+};
+cudaError_t launch_split_ff(const SplitSeg* segs, int nSegs, cudaStream_t s);
 cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
 // Post-processing of the adjoint of Chi2PDC (adjoint.cu)
 cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const double* prof, int nZ, int N,

@@ -71,6 +71,7 @@ def _load():
         "nlm_synchronize": (i, [vp]),
         "nlm_device_available": (i, []),
         "nlm_set_schedule": (i, [vp, i, i, i]),
+        "nlm_set_precision": (i, [vp, i]),
         "nlm_last_launch_count": (i, [vp, P(ctypes.c_long)]),
         "nlm_kernel_timing": (i, [vp, i, P(d), P(ctypes.c_long)]),
         "nlm_set_poling_profile": (i, [vp, P(d), sz]),
@@ -314,6 +315,14 @@ class _NonlinearMedium:
     # -- engine controls (no counterpart in the reference) ------------------------------------
     def _set_schedule(self, cta_per_sm=0, use_propagator=-1, use_graph=1):
         _check(_lib.nlm_set_schedule(self._h(), int(cta_per_sm), int(use_propagator), int(use_graph)))
+
+    def _set_precision(self, precision):
+        """"f64" (default) or "ff": double-float arithmetic (FP32 pairs, ~48-bit significand) for the
+        single-mode precomputed-propagator kernel; every other path stays FP64."""
+        code = {"f64": 0, "ff": 1}.get(precision)
+        if code is None:
+            raise ValueError("precision must be 'f64' or 'ff'")
+        _check(_lib.nlm_set_precision(self._h(), code))
 
     def _kernel_timing(self, enable):
         ms, cnt = ctypes.c_double(), ctypes.c_long()

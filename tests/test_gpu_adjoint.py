@@ -137,10 +137,20 @@ def test_checkpointed_sweep_equals_stored_states(nlm):
         assert cases.rel_l2(gb, ga) < 1e-12
 
 
+def _dir_fd(fun, base, direction, h):
+    """Central difference of fun along `direction` (fun(base + h direction) - fun(base - h direction)) / 2h."""
+    return (fun(base + h * direction) - fun(base - h * direction)) / (2 * h)
+
+
 def test_adjoint_config_size(nlm, oracle):
-    """The gradient configuration: N=512, nZSteps=2000, one noise signal, d(z) ~ U[-1, 1].  The pump
-    spectrum reaches |F0| ~ 16 while the signal is 1e-3, so its finite differences use a step of 1e-6
-    relative to each component (an absolute 1e-6 leaves the difference at the round-off level)."""
+    """The gradient configuration: N=512, nZSteps=2000, one noise signal (1e-3), d(z) ~ U[-1, 1].
+
+    The loss is ~1e-3 and single gradient components reach down to 1e-9, so componentwise finite
+    differences at this size resolve only ~1e-4 (the forward's own round-off over 2000 steps, a few
+    1e-13 of the loss, divided by the step).  The check therefore uses directional derivatives along
+    random directions, which sum all components: Re<g, v> against the central difference of the oracle's
+    forward along v.  Steps of 1e-4 to 1e-3 (relative) agree with each other to a few 1e-8 for the
+    pump and poling directions; the loss is exactly quadratic in the input, so any step is exact there."""
     kw = dict(KW, tMax=40, tPrecision=512, zPrecision=1000, diffBeta0=0)
     nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
     assert nz == 2000
@@ -152,22 +162,23 @@ def test_adjoint_config_size(nlm, oracle):
     target = cases.noise(rng, 512, 1.0).reshape(1, 512)
     target /= np.linalg.norm(target)
     out, gx, gf, gd, _ = _engine_grads(nlm, kw, x, f0, d, target)
-    h = 1e-6
-
-    def loss_f(v):
-        return _loss(_oracle_out(oracle, kw, x, v, d), target)
-
-    def loss_d(v):
-        return _loss(_oracle_out(oracle, kw, x, f0, v), target)
-
-    rng2 = np.random.default_rng(1)
-    ga, gfd = [], []
-    for idx in _significant(gf, 2, rng2):
-        ga += [gf[idx].real, gf[idx].imag]
-        gfd += [_fd(loss_f, f0, idx, h, relative=True), _fd(loss_f, f0, idx, h, "im", relative=True)]
-    assert _rel_vec(ga, gfd) < 1e-6
-    idx_d = _significant(gd, 2, rng2)
-    assert _rel_vec(gd[idx_d], [_fd(loss_d, d, i, h) for i in idx_d]) < 1e-6
+    assert cases.rel_l2(out, _oracle_out(oracle, kw, x, f0, d)) < 1e-9
+    r2 = np.random.default_rng(11)
+    # pump: a perturbation proportional to the spectrum with random phases
+    v = f0 * np.exp(2j * np.pi * r2.uniform(size=512)) * r2.uniform(0.5, 1.5, 512)
+    adj = float(np.sum(gf.real * v.real + gf.imag * v.imag))
+    fd = _dir_fd(lambda f: _loss(_oracle_out(oracle, kw, x, f, d), target), f0, v, 5e-4)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
+    # poling profile
+    u = r2.uniform(-1, 1, nz)
+    adj = float(np.dot(gd, u))
+    fd = _dir_fd(lambda p: _loss(_oracle_out(oracle, kw, x, f0, p), target), d, u, 5e-4)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
+    # input spectrum
+    w = cases.noise(r2, 512, 1e-3).reshape(1, 512)
+    adj = float(np.sum(gx.real * w.real + gx.imag * w.imag))
+    fd = _dir_fd(lambda y: _loss(_oracle_out(oracle, kw, y, f0, d), target), x, w, 0.5)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
 
 
 GN = dict(relativeLength=0.5, nlLength=1, selfSteepLength=5, fr=0.18, fb=0.21, tau1=0.0155, tau2=0.2165, tau3=0.4,

@@ -54,6 +54,15 @@ def test_validation_errors(nlm):
         nlm.Chi2PDC(1, 0.5, 1, 0.5, notAnArgument=3)
 
 
+def test_precision_switch_validation(nlm):
+    m = nlm.Chi2PDC(**cases.CASES["Chi2PDC"])
+    m._set_precision("ff")
+    m._set_precision("f64")
+    with pytest.raises(ValueError):
+        m._set_precision("f16")
+    assert nlm._lib.nlm_set_precision(m._h(), 2) == 1   # NLM_ERR_INVALID_ARGUMENT
+
+
 def test_method_validation_before_any_device_work(nlm):
     m = nlm.Chi2SFG(**cases.CASES["Chi2SFG"])
     n = m._dims["nFreqs"]
