@@ -532,6 +532,7 @@ def run_ours(args):
             elapsed += e0.elapsed_time(e1) / 1e3
             launches += med._launch_count()
     kernel_ms, kernel_count = med._kernel_timing(0)
+    sched = med._last_schedule()
     barrier()
     t_dev = max_over_ranks(elapsed)
     value = world * n_inst * args.steps / t_dev
@@ -615,6 +616,10 @@ def run_ours(args):
                       "form": "one propagation per kernel launch"},
             "batched_over_plain": (value / plain) if plain else None,
             "parity_sample_rel_err": parity,
+            "schedule": {"points_per_thread": sched["R"], "propagations_per_cta": sched["ipc"], "grid": sched["grid"],
+                         "block": sched["block"], "cta_per_sm": sched["cta_per_sm"],
+                         "chosen_by": "autotuner" if sched["tuned"] else "occupancy"},
+            "cuda_graphs": dict(zip(("captures", "replays"), med._graph_stats())),
             "variant_ff": ff,
             "adjoint": adjoint,
             "other_configs": configs,

@@ -213,10 +213,18 @@ nlm_status nlm_synchronize(nlm_medium* m);
 int nlm_device_available(void);
 
 /* --- engine controls ------------------------------------------------------------------- */
-/* Force the batched-kernel schedule (0 = autotuner).  cta_per_sm: resident CTAs per SM;
+/* Schedule controls of the batched kernels.  cta_per_sm: 0 = autotuner (default: the first
+ * batched launch of a shape times the kernel variants, propagations per CTA and resident CTAs per
+ * SM on a few z steps and keeps the fastest for the process; NLM_AUTOTUNE=0 in the environment
+ * turns it off), -1 = occupancy maximum without timing, > 0 = that many resident CTAs per SM;
  * use_propagator: 1 = precomputed RK4 propagator for linear solvers, 0 = direct DiffEq,
- * -1 = automatic.  Used by tests and by the benchmark to compare schedules. */
+ * -1 = automatic; use_graph: 1 = batched launches captured into CUDA graphs and replayed
+ * (default), 0 = direct launches.  No counterpart in the reference. */
 nlm_status nlm_set_schedule(nlm_medium* m, int cta_per_sm, int use_propagator, int use_graph);
+/* Launch shape of the last propagation of this handle: values[0..6] = points per thread R,
+ * propagations per CTA, grid, block, resident CTAs per SM, 1 if chosen by the autotuner, and the
+ * autotuner trials this handle ran.  No counterpart in the reference. */
+nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float
  * (pairs of FP32 values, ~48-bit significand, on the FP32 units).  Other paths stay FP64.
@@ -227,6 +235,11 @@ nlm_status nlm_set_precision(nlm_medium* m, int precision);
  * the rows not propagated are left zero.  Timing helper for the plain-vs-batched ratio. */
 nlm_status nlm_green_plain(nlm_medium* m, int in_time_domain, int run_pump, size_t max_instances,
                            double* green_c, double* green_s);
+/* Propagation launches of this handle (and of a cascade's media) captured into CUDA graphs, and
+ * replays of captured graphs, since creation.  A batched propagation (with the Green's-function
+ * epilogue) is captured once per distinct set of launch arguments and replayed by later calls;
+ * use_graph = 0 in nlm_set_schedule launches directly.  No counterpart in the reference. */
+nlm_status nlm_graph_stats(const nlm_medium* m, long* captures, long* replays);
 /* Number of kernels the last nlm_* call of this handle launched. */
 nlm_status nlm_last_launch_count(const nlm_medium* m, long* launches);
 /* Time the fused propagation kernel with CUDA events on the handle's stream.  enable = 1

@@ -12,7 +12,9 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <memory>
@@ -141,6 +143,98 @@ struct DevBuf {
 };
 
 static double2* d2(void* p) { return reinterpret_cast<double2*>(p); }
+
+// Launch sequences captured into CUDA graphs and replayed.  The key holds the bytes of every
+// host-side value the captured launches read (kernel arguments, grid shape, pointers), so a replay
+// is exactly the launch sequence it stands for; any change of a key byte captures a new graph.
+struct GraphKey {
+  std::vector<unsigned char> bytes;
+  template <class T>
+  GraphKey& add(const T& v) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&v);
+    bytes.insert(bytes.end(), p, p + sizeof(T));
+    return *this;
+  }
+};
+
+// Key bytes of a PropArgs, field by field (the struct has padding, whose bytes are unspecified).
+static void add_prop_key(GraphKey& k, const PropArgs& a) {
+  k.add(a.plan.N).add(a.plan.T).add(a.plan.nPass);
+  for (int i = 0; i < a.plan.nPass && i < 16; i++) k.add(a.plan.radix[i]);
+  k.add(a.R).add(a.nModes).add(a.nZ).add(a.nInst).add(a.instBase).add(a.ipc).add(a.work);
+  k.add(a.inKind).add(a.inTime).add(a.in).add(a.inStride).add(a.inChannels).add(a.inputMode);
+  for (int i = 0; i < kMaxModes; i++) k.add(a.impModes[i]);
+  k.add(a.nOut);
+  for (int i = 0; i < kMaxModes; i++) k.add(a.outModes[i]);
+  k.add(a.out).add(a.outStride).add(a.tw).add(a.dstep).add(a.dlast).add(a.half).add(a.back).add(a.prop);
+  k.add(a.pump).add(a.pumpStride).add(a.nPumps).add(a.coef).add(a.nCoef).add(a.gridF).add(a.gridT);
+  k.add(a.ckpt).add(a.ckK).add(a.ckN).add(a.raman).add(a.steep).add(a.relInt);
+}
+
+struct GraphCache {
+  struct Entry {
+    std::vector<unsigned char> key;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long lastUse = 0;
+  };
+  static constexpr size_t kMaxEntries = 8;
+  std::vector<Entry> entries;
+  unsigned long long clock = 0;
+  long captures = 0, replays = 0;
+
+  GraphCache() = default;
+  GraphCache(const GraphCache&) = delete;
+  GraphCache& operator=(const GraphCache&) = delete;
+  ~GraphCache() { clear(); }
+  void clear() {
+    for (auto& e : entries)
+      if (e.exec) cudaGraphExecDestroy(e.exec);
+    entries.clear();
+  }
+
+  // Enqueue `record` (launches on `stream` only: no allocation, synchronisation or pageable copy) as
+  // a graph: replay of the graph captured for `key`, else capture, instantiate and launch.  Streams
+  // that cannot be captured (the legacy default stream, or one already being captured by the
+  // caller) get the launches directly.
+  void run(const GraphKey& key, cudaStream_t stream, const std::function<void()>& record) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (stream == nullptr || cudaStreamIsCapturing(stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
+      record();
+      return;
+    }
+    clock++;
+    for (auto& e : entries)
+      if (e.key == key.bytes) {
+        e.lastUse = clock;
+        replays++;
+        ck(cudaGraphLaunch(e.exec, stream), "graph launch");
+        return;
+      }
+    cudaGraph_t g = nullptr;
+    ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    try {
+      record();
+    } catch (...) {
+      cudaStreamEndCapture(stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    ck(cudaStreamEndCapture(stream, &g), "graph capture");
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    ck(e, "graph instantiate");
+    if (entries.size() >= kMaxEntries) {
+      auto old = std::min_element(entries.begin(), entries.end(),
+                                  [](const Entry& a, const Entry& b) { return a.lastUse < b.lastUse; });
+      cudaGraphExecDestroy(old->exec);
+      entries.erase(old);
+    }
+    entries.push_back(Entry{key.bytes, ex, clock});
+    captures++;
+    ck(cudaGraphLaunch(ex, stream), "graph launch");
+  }
+};
 
 // Twiddle table exp(-2 pi i m / N), one per grid size, per process.
 struct TwiddleCache {
@@ -501,6 +595,7 @@ struct Medium {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // schedule overrides
   int ctaPerSM = 0, usePropagator = -1, useGraph = 1;
+  GraphCache graphs;
 
   // cascade
   std::vector<Medium*> media;
@@ -1079,11 +1174,15 @@ struct Medium {
   struct Schedule {
     int grid, block, ipc;
     size_t smem;
+    int maxActive, ctas;   // occupancy limit and chosen resident CTAs per SM
   };
 
-  Schedule schedule(const KernelEntry* k, long long nInst, int R) {
+  // Launch shape of a persistent propagation kernel: ipc propagations per CTA (N/R threads each; by
+  // default enough for 128 threads, times ipcMul), `cta` resident CTAs per SM (0: the member
+  // override or the occupancy maximum), grid = SMs x CTAs per SM, capped by the number of groups.
+  Schedule schedule(const KernelEntry* k, long long nInst, int R, int cta = 0, int ipcMul = 1) {
     const int T = (int)N / R;
-    int ipc = T >= 128 ? 1 : 128 / T;
+    int ipc = (T >= 128 ? 1 : 128 / T) * ipcMul;
     if (ipc > nInst) ipc = (int)std::max<long long>(1, nInst);
     const int block = T * ipc;
     // exchange buffers of the ipc propagations, plus the staged twiddle table when R != 16
@@ -1107,10 +1206,125 @@ struct Medium {
     // empty whatever the number of resident CTAs: take the most resident warps (the FP64 pipe is
     // shared by all of them and needs several warps per scheduler to stay busy).
     int best = maxActive;
-    if (ctaPerSM > 0) best = std::min(ctaPerSM, maxActive);
+    if (cta > 0) best = std::min(cta, maxActive);
+    else if (ctaPerSM > 0) best = std::min(ctaPerSM, maxActive);
     long long grid = std::min<long long>(groups, (long long)sms * best);
-    Schedule s{(int)std::max<long long>(1, grid), block, ipc, smem};
+    Schedule s{(int)std::max<long long>(1, grid), block, ipc, smem, maxActive, best};
     return s;
+  }
+
+  // ---- autotuner -----------------------------------------------------------------------------
+  // For a batched launch it times every registered kernel variant of the path (points per thread R),
+  // ipc multiplier {1, 2} and resident CTAs per SM on the real arguments with the z march cut to a
+  // few steps, and keeps the fastest per (kernel kind, key, grid, propagation count) for the process.
+  struct TuneChoice {
+    int R = 0, cta = 0, ipcMul = 1;
+    float ms = 0;
+  };
+  static std::mutex& tuneMutex() {
+    static std::mutex mu;
+    return mu;
+  }
+  static std::map<std::vector<unsigned char>, TuneChoice>& tuneTable() {
+    static std::map<std::vector<unsigned char>, TuneChoice> t;
+    return t;
+  }
+  static bool autotuneEnabled() {
+    const char* e = std::getenv("NLM_AUTOTUNE");
+    return !(e && e[0] == '0');
+  }
+  DevBuf<unsigned long long> tuneCounter;
+  Schedule lastSchedule{};
+  int lastR = 0, lastTuned = 0;
+  long tuneTrials = 0;
+
+  bool tuneWanted(const PropArgs& a, long long nInst) const {
+    if (ctaPerSM != 0 || !autotuneEnabled()) return false;
+    if (a.gridF || a.gridT || a.ckpt) return false;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (stream == nullptr || cudaStreamIsCapturing(stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone)
+      return false;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return nInst >= 2LL * sms;
+  }
+
+  void launchKernel(const KernelEntry* k, const Schedule& s, const PropArgs& a, const FFTables* ffT) {
+    if (ffT) {
+      void* args[] = {(void*)&a, (void*)ffT};
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    } else {
+      void* args[] = {(void*)&a};
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    }
+  }
+
+  TuneChoice autotune(int kind, int key, const PropArgs& a0, long long nInst, const FFTables* ffT) {
+    GraphKey tk;
+    tk.add(kind).add(key).add(N).add(nInst).add(nSignal).add(a0.inKind).add(a0.inTime).add(a0.nOut);
+    {
+      std::lock_guard<std::mutex> g(tuneMutex());
+      auto it = tuneTable().find(tk.bytes);
+      if (it != tuneTable().end()) return it->second;
+    }
+    int count = 0;
+    const KernelEntry* t = kernel_table(&count);
+    TuneChoice best;
+    best.ms = 1e30f;
+    tuneCounter.reserve(1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    try {
+      for (int i = 0; i < count; i++) {
+        const KernelEntry* kc = &t[i];
+        if (kc->kind != kind || kc->key != key) continue;
+        const int R = kc->R;
+        if (!is_pow2((int)N) || (int)N < R || N / R > 512 || N > (uint)kMaxFFT) continue;
+        for (int ipcMul = 1; ipcMul <= 2; ipcMul++) {
+          Schedule base;
+          try {
+            base = schedule(kc, nInst, R, 0, ipcMul);
+          } catch (const Unsupported&) {
+            continue;
+          }
+          for (int c = 1; c <= base.maxActive; c++) {
+            const Schedule sc = schedule(kc, nInst, R, c, ipcMul);
+            PropArgs ta = a0;
+            ta.plan = make_plan((int)N, R);
+            ta.R = R;
+            ta.nZ = std::min<int>(a0.nZ, 17);
+            ta.nInst = nInst;
+            ta.ipc = sc.ipc;
+            const bool counter = (long long)sc.grid < (nInst + sc.ipc - 1) / sc.ipc;
+            ta.work = counter ? tuneCounter.p : nullptr;
+            float ms = 0;
+            for (int rep = 0; rep < 2; rep++) {
+              if (counter) ck(cudaMemsetAsync(tuneCounter.p, 0, sizeof(unsigned long long), stream), "tune counter");
+              ck(cudaEventRecord(e0, stream), "event");
+              launchKernel(kc, sc, ta, ffT);
+              ck(cudaEventRecord(e1, stream), "event");
+              ck(cudaEventSynchronize(e1), "tune");
+              ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+            }
+            launches += 2;
+            tuneTrials++;
+            if (ms < best.ms) best = TuneChoice{R, c, ipcMul, ms};
+          }
+        }
+      }
+    } catch (...) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best.R == 0) return best;
+    std::lock_guard<std::mutex> g(tuneMutex());
+    tuneTable()[tk.bytes] = best;
+    return best;
   }
 
   PropArgs baseArgs(int R) const {
@@ -1198,7 +1412,10 @@ struct Medium {
   }
 
   // Launch one propagation kernel over `nInst` instances (inputs/outputs prepared in `a`).
-  void propagate(PropArgs a, long long nInst, bool allowPropagator, bool plainOne = false) {
+  // `tail` (optional): launches that follow the propagation in the same graph (e.g. the Green's
+  // function epilogue); `tailKey` holds the host values they read.
+  void propagate(PropArgs a, long long nInst, bool allowPropagator, bool plainOne = false,
+                 const std::function<void()>& tail = {}, const GraphKey* tailKey = nullptr) {
     const int R = chooseR();
     checkGrid(R);
     a.nInst = nInst;
@@ -1221,32 +1438,65 @@ struct Medium {
       k = findKernel(kKindDirect, solver, R);
     }
     if (!k) throw Unsupported("no fused kernel for this solver and grid");
-    Schedule s = schedule(k, nInst, R);
+    Schedule s{};
+    lastTuned = 0;
+    if (!plainOne && !gnlse && tuneWanted(a, nInst)) {
+      const TuneChoice c = autotune(k->kind, k->key, a, nInst, ff ? &ffT : nullptr);
+      if (c.R != 0) {
+        k = findKernel(k->kind, k->key, c.R);
+        a.plan = make_plan((int)N, c.R);
+        a.R = c.R;
+        s = schedule(k, nInst, c.R, c.cta, c.ipcMul);
+        lastTuned = 1;
+      }
+    }
+    if (!lastTuned) s = schedule(k, nInst, R, ctaPerSM < 0 ? 0 : ctaPerSM);
     if (plainOne) s.grid = 1;
+    lastSchedule = s;
+    lastR = a.R;
     a.ipc = s.ipc;
     a.work = nullptr;
-    if (!plainOne && (long long)s.grid < (nInst + s.ipc - 1) / s.ipc) {
+    const bool counter = !plainOne && (long long)s.grid < (nInst + s.ipc - 1) / s.ipc;
+    if (counter) {
       workCounter.reserve(1);
-      ck(cudaMemsetAsync(workCounter.p, 0, sizeof(unsigned long long), stream), "work counter");
       a.work = workCounter.p;
     }
+    double2* sp = nullptr;
+    if (gnlse) {
+      scratch.reserve((size_t)s.grid * s.ipc * 2 * N);
+      sp = scratch.p;
+    }
+    // with kernel timing on, the tail runs after the timed region, outside the graph
+    const bool tailInside = tail && !timeKernels;
+    auto record = [&] {
+      if (counter) ck(cudaMemsetAsync(workCounter.p, 0, sizeof(unsigned long long), stream), "work counter");
+      if (gnlse) {
+        void* args[] = {(void*)&a, (void*)&sp};
+        ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+      } else if (ff) {
+        void* args[] = {(void*)&a, (void*)&ffT};
+        ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+      } else {
+        void* args[] = {(void*)&a};
+        ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+      }
+      if (tailInside) tail();
+    };
     if (timeKernels) {
       if (!ev0) ck(cudaEventCreate(&ev0), "event");
       if (!ev1) ck(cudaEventCreate(&ev1), "event");
       ck(cudaEventRecord(ev0, stream), "event");
     }
-    if (gnlse) {
-      const size_t need = (size_t)s.grid * s.ipc * 2 * N;
-      scratch.reserve(need);
-      double2* sp = scratch.p;
-      void* args[] = {(void*)&a, (void*)&sp};
-      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
-    } else if (ff) {
-      void* args[] = {(void*)&a, (void*)&ffT};
-      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+    if (useGraph && !plainOne) {
+      GraphKey key;
+      add_prop_key(key, a);
+      key.add(s.grid).add(s.block).add(s.smem).add(k->fn).add(sp).add(ff);
+      key.add(ffT.tw).add(ffT.dstep).add(ffT.dlast).add(ffT.half).add(ffT.back).add(ffT.prop);
+      key.add(tailInside);
+      if (tailInside && tailKey) key.bytes.insert(key.bytes.end(), tailKey->bytes.begin(), tailKey->bytes.end());
+      graphs.run(key, stream, record);
     } else {
-      void* args[] = {(void*)&a};
-      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+      record();
     }
     launches++;
     if (timeKernels) {
@@ -1257,6 +1507,7 @@ struct Medium {
       kernelMs += ms;
       kernelCount++;
     }
+    if (tail && !tailInside) tail();
   }
 
   // ---- adjoint (no counterpart in the reference) -------------------------------------------------
@@ -1453,18 +1704,6 @@ struct Medium {
     for (int i = 0; i < nOut; i++) a.outModes[i] = outputs[i];
     a.out = raw.p;
     a.outStride = outStride;
-    if (maxInstances >= 0) {
-      // one propagation per launch (timing helper)
-      ck(cudaMemsetAsync(raw.p, 0, (size_t)nInst * outStride * sizeof(double2), stream), "memset");
-      const long long todo = std::min(nInst, maxInstances == 0 ? nInst : maxInstances);
-      for (long long i = 0; i < todo; i++) {
-        PropArgs b = a;
-        b.instBase = i;
-        propagate(b, 1, false, true);
-      }
-    } else {
-      propagate(a, nInst, true);
-    }
     // epilogue flags per (om, im) block, src/_NonlinearMedium.cpp:360-372
     std::vector<uint8_t> flags((size_t)nOut * nIn, 0);
     std::vector<double2> scales((size_t)nOut * nIn, make_double2(1, 0));
@@ -1491,7 +1730,26 @@ struct Medium {
       C = cs.p;
       S = cs.p + mat;
     }
-    ck(launch_green_epilogue(raw.p, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, C, S, stream), "epilogue");
+    // the epilogue reads the flags and scales through device pointers: they are uploaded above, on
+    // the same stream and before the graph runs, so a replay reads this call's values
+    auto epilogue = [&] {
+      ck(launch_green_epilogue(raw.p, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, C, S, stream), "epilogue");
+    };
+    if (maxInstances >= 0) {
+      // one propagation per launch (timing helper)
+      ck(cudaMemsetAsync(raw.p, 0, (size_t)nInst * outStride * sizeof(double2), stream), "memset");
+      const long long todo = std::min(nInst, maxInstances == 0 ? nInst : maxInstances);
+      for (long long i = 0; i < todo; i++) {
+        PropArgs b = a;
+        b.instBase = i;
+        propagate(b, 1, false, true);
+      }
+      epilogue();
+    } else {
+      GraphKey ek;
+      ek.add(raw.p).add(outStride).add(N).add(nIn).add(nOut).add(scaleD.p).add(flagsD.p).add(C).add(S);
+      propagate(a, nInst, true, false, epilogue, &ek);
+    }
     launches++;
     if (!deviceDst) {
       ck(cudaMemcpyAsync(Cdst, C, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "C download");
@@ -2441,6 +2699,32 @@ nlm_status nlm_set_precision(nlm_medium* h, int precision) {
     Medium* m = M(h);
     m->precision = precision;
     for (Medium* c : m->media) c->precision = precision;
+  });
+}
+
+nlm_status nlm_last_schedule(const nlm_medium* h, int* values) {
+  return guarded([&] {
+    const Medium* m = CM(h);
+    values[0] = m->lastR;
+    values[1] = m->lastSchedule.ipc;
+    values[2] = m->lastSchedule.grid;
+    values[3] = m->lastSchedule.block;
+    values[4] = m->lastSchedule.ctas;
+    values[5] = m->lastTuned;
+    values[6] = (int)m->tuneTrials;
+  });
+}
+
+nlm_status nlm_graph_stats(const nlm_medium* h, long* captures, long* replays) {
+  return guarded([&] {
+    const Medium* m = CM(h);
+    long c = m->graphs.captures, r = m->graphs.replays;
+    for (const Medium* x : m->media) {
+      c += x->graphs.captures;
+      r += x->graphs.replays;
+    }
+    if (captures) *captures = c;
+    if (replays) *replays = r;
   });
 }
 

@@ -72,6 +72,8 @@ def _load():
         "nlm_device_available": (i, []),
         "nlm_set_schedule": (i, [vp, i, i, i]),
         "nlm_set_precision": (i, [vp, i]),
+        "nlm_graph_stats": (i, [vp, P(ctypes.c_long), P(ctypes.c_long)]),
+        "nlm_last_schedule": (i, [vp, P(i)]),
         "nlm_last_launch_count": (i, [vp, P(ctypes.c_long)]),
         "nlm_kernel_timing": (i, [vp, i, P(d), P(ctypes.c_long)]),
         "nlm_set_poling_profile": (i, [vp, P(d), sz]),
@@ -336,6 +338,18 @@ class _NonlinearMedium:
 
     def _set_stream(self, stream_handle):
         _check(_lib.nlm_set_stream(self._h(), ctypes.c_void_p(stream_handle)))
+
+    def _last_schedule(self):
+        """Launch shape of the last propagation (R, ipc, grid, block, CTAs per SM, tuned, trials)."""
+        v = (ctypes.c_int * 7)()
+        _check(_lib.nlm_last_schedule(self._h(), v))
+        return dict(zip(("R", "ipc", "grid", "block", "cta_per_sm", "tuned", "trials"), list(v)))
+
+    def _graph_stats(self):
+        """(captures, replays) of the CUDA graphs of this medium's batched propagations."""
+        c, r = ctypes.c_long(), ctypes.c_long()
+        _check(_lib.nlm_graph_stats(self._h(), ctypes.byref(c), ctypes.byref(r)))
+        return c.value, r.value
 
     def _launch_count(self):
         v = ctypes.c_long()
