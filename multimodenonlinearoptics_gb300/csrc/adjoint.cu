@@ -228,6 +228,7 @@ cudaError_t launch_adj_coef_reduce(const double2* ga, const double2* pump, int n
 }
 
 void add_kernels_adjoint(std::vector<KernelEntry>& t) {
+  t.push_back({kKindAdjoint, kChi2PDC, 4, (const void*)k_adjoint_pdc<4>});
   t.push_back({kKindAdjoint, kChi2PDC, 8, (const void*)k_adjoint_pdc<8>});
   t.push_back({kKindAdjoint, kChi2PDC, 16, (const void*)k_adjoint_pdc<16>});
 }

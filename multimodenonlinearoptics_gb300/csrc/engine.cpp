@@ -1081,7 +1081,8 @@ struct Medium {
   // solvers/Chi3.cpp:41-70
   void runPumpChi3() {
     if (!(is_pow2((int)N) && N >= 8 && N <= (uint)kMaxFFT)) throw Unsupported("Chi3 pump march needs a power-of-two grid of 8..8192 points");
-    FFTPlanH plan = make_plan((int)N, N <= 4096 ? 8 : 16);
+    // one CTA marches the pump: N/4 threads up to N=512 so that all four schedulers of the SM issue
+    FFTPlanH plan = make_plan((int)N, N <= 512 ? 4 : (N <= 4096 ? 8 : 16));
     std::vector<double2> e(N), hP(N), dP(N), bP(N);
     for (uint k = 0; k < N; k++) {
       e[k] = make_double2(envelope[0][k].real(), envelope[0][k].imag());
@@ -1164,6 +1165,13 @@ struct Medium {
   }
 
   bool linearSolver() const { return kSolvers[solver].linear; }
+
+  static int smCount() {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+  }
 
   void checkGrid(int R) const {
     if (!is_pow2((int)N) || (int)N < R || N > (uint)kMaxFFT || N / R > 512)
@@ -1378,6 +1386,13 @@ struct Medium {
     return precision == 1 && nSignal == 1 && R == 8 && !a.gridF && !a.gridT && !a.ckpt;
   }
 
+  // radix of the plan's one non-radix-8 pass (1 when all passes are radix 8)
+  static int shortRadix(const FFTPlanH& p) {
+    for (int i = 0; i < p.nPass; i++)
+      if (p.radix[i] != 8) return p.radix[i];
+    return 1;
+  }
+
   FFTables prepareFF() {
     std::vector<SplitSeg> segs;
     if (!ffTables) {
@@ -1430,12 +1445,22 @@ struct Medium {
       if (wantFF(R, a)) {
         ff = true;
         ffT = prepareFF();
-        k = findKernel(kKindLinearFF, 1, R);
+        k = findKernel(kKindLinearFF, 1 + 10 * shortRadix(a.plan), R);
       } else {
         k = findKernel(kKindLinear, (int)nSignal, R);
       }
     } else {
       k = findKernel(kKindDirect, solver, R);
+      // Launches with fewer propagations than SMs are latency-bound: one SM's FP64 units run each
+      // propagation, and N/R threads below 128 leave some of its four schedulers idle.  Use the
+      // four-points-per-thread variant when there is one.
+      if (nInst < smCount() && (int)N / R < 128 && (int)N / 4 <= 512) {
+        if (const KernelEntry* k4 = findKernel(kKindDirect, solver, 4)) {
+          k = k4;
+          a.plan = make_plan((int)N, 4);
+          a.R = 4;
+        }
+      }
     }
     if (!k) throw Unsupported("no fused kernel for this solver and grid");
     Schedule s{};
@@ -1450,7 +1475,7 @@ struct Medium {
         lastTuned = 1;
       }
     }
-    if (!lastTuned) s = schedule(k, nInst, R, ctaPerSM < 0 ? 0 : ctaPerSM);
+    if (!lastTuned) s = schedule(k, nInst, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
     if (plainOne) s.grid = 1;
     lastSchedule = s;
     lastR = a.R;
@@ -1565,8 +1590,15 @@ struct Medium {
   void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {
     if (adjRows == 0 || adjPumpVersion != pumpVersion)
       throw std::runtime_error("no adjoint forward pass to differentiate: run nlm_adjoint_forward first");
-    const int R = chooseR();
+    int R = chooseR();
     const KernelEntry* k = findKernel(kKindAdjoint, solver, R);
+    // few rows: four points per thread, as for the forward (Medium::propagate)
+    if (adjRows < (long long)smCount() && (int)N / R < 128 && (int)N / 4 <= 512) {
+      if (const KernelEntry* k4 = findKernel(kKindAdjoint, solver, 4)) {
+        k = k4;
+        R = 4;
+      }
+    }
     if (!k) throw Unsupported("no adjoint kernel for this grid");
     const size_t steps = nZ - 1;
     adjGa.reserve(steps * 3 * N);

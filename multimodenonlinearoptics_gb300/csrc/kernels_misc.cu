@@ -17,6 +17,7 @@ void add_kernels_adjoint(std::vector<KernelEntry>& t);
 void add_kernels_ragged(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_ff(std::vector<KernelEntry>& t);
+void add_kernels_direct_c(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -30,6 +31,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_ragged(table);
     add_kernels_adjoint_gnlse(table);
     add_kernels_ff(table);
+    add_kernels_direct_c(table);
   });
   *count = (int)table.size();
   return table.data();
@@ -278,6 +280,10 @@ cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2
     cudaError_t e = smem_optin((const void*)k_pump_chi3<8>);
     if (e != cudaSuccess) return e;
     k_pump_chi3<8><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
+  } else if (R == 4) {
+    cudaError_t e = smem_optin((const void*)k_pump_chi3<4>);
+    if (e != cudaSuccess) return e;
+    k_pump_chi3<4><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
   } else if (R == 16) {
     cudaError_t e = smem_optin((const void*)k_pump_chi3<16>);
     if (e != cudaSuccess) return e;

@@ -34,14 +34,19 @@ __device__ __forceinline__ ff ff_renorm(float s, float e) {
   return ff{hi, __fsub_rn(e, __fsub_rn(hi, s))};
 }
 
-// a + b (error-free sum of the high parts, low parts added in)
+// a + b: error-free sum of the high parts (TwoSum), low parts and the rounding error added into
+// the low part, without renormalisation.  The result's low part may reach a few ulp of its high
+// part after chained additions; every multiplication below renormalises, and the FFT passes
+// renormalise their outputs, so chains stay a few additions long.  Errors stay ~2^-47 of the
+// operands' magnitudes (what the FFT's norm-wise error bound needs).
 __device__ __forceinline__ ff ff_add(ff a, ff b) {
   const float s = __fadd_rn(a.hi, b.hi);
   const float bb = __fsub_rn(s, a.hi);
   float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
   e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  return ff_renorm(s, e);
+  return ff{s, e};
 }
+__device__ __forceinline__ ff ff_norm(ff a) { return ff_renorm(a.hi, a.lo); }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
@@ -100,6 +105,7 @@ __device__ __forceinline__ double2 ffc_to(ffc a) {
   return make_double2((double)a.re.hi + (double)a.re.lo, (double)a.im.hi + (double)a.im.lo);
 }
 
+__device__ __forceinline__ ffc fnorm(ffc a) { return ffc{ff_norm(a.re), ff_norm(a.im)}; }
 __device__ __forceinline__ ffc fadd(ffc a, ffc b) { return ffc{ff_add(a.re, b.re), ff_add(a.im, b.im)}; }
 __device__ __forceinline__ ffc fsub(ffc a, ffc b) { return ffc{ff_sub(a.re, b.re), ff_sub(a.im, b.im)}; }
 // a * b
@@ -193,6 +199,8 @@ __device__ __forceinline__ void fstockham_pass(ffc (&x)[R], float4* __restrict__
   }
 #pragma unroll
   for (int u = 0; u < B; u++) fdft_r<r, INV>(x, u, B);
+#pragma unroll
+  for (int v = 0; v < R; v++) x[v] = fnorm(x[v]);
   if (to_smem) {
     __syncthreads();
 #pragma unroll
@@ -206,23 +214,25 @@ __device__ __forceinline__ void fstockham_pass(ffc (&x)[R], float4* __restrict__
   }
 }
 
-template <int R, bool INV>
+// Transform with the plan of make_plan: radix-8 passes with one pass of radix SMALL (2 or 4; 1 =
+// none) in position 1 (position 0 when it is the only pass).  SMALL is a template parameter so that
+// each call site holds two pass bodies only.
+template <int R, int SMALL, bool INV>
 __device__ __forceinline__ void ffft_regs(ffc (&x)[R], float4* __restrict__ buf, const float4* __restrict__ tw,
                                           const FFTPlanH& plan, int j) {
   int L = 1;
+  const int smallAt = plan.nPass > 1 ? 1 : 0;
   for (int p = 0; p < plan.nPass; p++) {
     const bool from = p > 0, to = p < plan.nPass - 1;
-    const int r = plan.radix[p];
-    if (r == 8) {
-      fstockham_pass<R, 8, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
-      L *= 8;
-    } else if (r == 4) {
-      fstockham_pass<R, 4, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
-      L *= 4;
-    } else {
-      fstockham_pass<R, 2, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
-      L *= 2;
+    if constexpr (SMALL > 1) {
+      if (p == smallAt) {
+        fstockham_pass<R, SMALL, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
+        L *= SMALL;
+        continue;
+      }
     }
+    fstockham_pass<R, 8, INV>(x, buf, tw, plan.N, plan.T, j, L, from, to);
+    L *= 8;
   }
 }
 

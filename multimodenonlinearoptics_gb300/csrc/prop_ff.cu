@@ -13,7 +13,15 @@
 
 namespace nlm {
 
-template <int R>
+// SMALL: radix of the one non-radix-8 pass of the plan (1 = none).  The z march is written as a
+// loop over stages s = 0..last, each [inverse FFT][RK4 propagator][forward FFT][table], so that the
+// kernel holds one forward and one inverse transform (the code of a float-float transform is large
+// enough for instruction fetch to matter):
+//   s = 0:          [forward FFT if the input is in the time domain] x exp(+i dz/2 D)/N
+//   s = 1..nZ-1:    inverse FFT, propagator of step s, forward FFT, dispStep/N (dispStep exp(-i dz/2 D)/N last)
+//   nZ = 1:         s = 1 is inverse FFT, forward FFT, exp(-i dz/2 D)/N (no propagator)
+//   time-domain output: one more inverse FFT.
+template <int R, int SMALL>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropArgs a, const FFTables f) {
   extern __shared__ float4 fsm[];
   __shared__ long long s_group;
@@ -33,6 +41,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropA
   }
   float4* buf = bufs + (long long)g * N;
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
+  const int last = a.nZ > 1 ? a.nZ - 1 : 1;
   for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
     const long long local = cg * a.ipc + g;
     const bool active = local < a.nInst;
@@ -53,32 +62,25 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropA
 #pragma unroll
       for (int v = 0; v < R; v++) x[v] = (active && has) ? ffc_from(row[j + v * T]) : ffc_zero();
     }
-    if (a.inTime) ffft_regs<R, false>(x, buf, tw, plan, j);
+    for (int s = 0;; s++) {
+      if (s > 0) ffft_regs<R, SMALL, true>(x, buf, tw, plan, j);
+      if (s > last) break;
+      if (s > 0 && a.nZ > 1) {
+        const float4* mat = f.prop + (long long)(s - 1) * 2 * N;
 #pragma unroll
-    for (int v = 0; v < R; v++) x[v] = fmul(x[v], ffc_ldg(f.half + j + v * T));
-    ffft_regs<R, true>(x, buf, tw, plan, j);
-    for (int i = 1; i < a.nZ; i++) {
-      const float4* mat = f.prop + (long long)(i - 1) * 2 * N;
-#pragma unroll
-      for (int v = 0; v < R; v++) {
-        const int t = j + v * T;
-        const float4 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
-        const ff re = ff_dot2(ff{e0.x, e0.y}, x[v].re, ff{e0.z, e0.w}, x[v].im);
-        const ff im = ff_dot2(ff{e1.x, e1.y}, x[v].re, ff{e1.z, e1.w}, x[v].im);
-        x[v] = ffc{re, im};
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          const float4 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
+          const ff re = ff_dot2(ff{e0.x, e0.y}, x[v].re, ff{e0.z, e0.w}, x[v].im);
+          const ff im = ff_dot2(ff{e1.x, e1.y}, x[v].re, ff{e1.z, e1.w}, x[v].im);
+          x[v] = ffc{re, im};
+        }
       }
-      const bool last = i == a.nZ - 1;
-      ffft_regs<R, false>(x, buf, tw, plan, j);
-      const float4* d = last ? f.dlast : f.dstep;
+      if (s > 0 || a.inTime) ffft_regs<R, SMALL, false>(x, buf, tw, plan, j);
+      const float4* tab = s == 0 ? f.half : (a.nZ == 1 ? f.back : (s == last ? f.dlast : f.dstep));
 #pragma unroll
-      for (int v = 0; v < R; v++) x[v] = fmul(x[v], ffc_ldg(d + j + v * T));
-      if (!last || a.inTime) ffft_regs<R, true>(x, buf, tw, plan, j);
-    }
-    if (a.nZ == 1) {
-      ffft_regs<R, false>(x, buf, tw, plan, j);
-#pragma unroll
-      for (int v = 0; v < R; v++) x[v] = fmul(x[v], ffc_ldg(f.back + j + v * T));
-      if (a.inTime) ffft_regs<R, true>(x, buf, tw, plan, j);
+      for (int v = 0; v < R; v++) x[v] = fmul(x[v], ffc_ldg(tab + j + v * T));
+      if (s == last && !a.inTime) break;
     }
     if (active && a.out != nullptr) {
       const double scale = a.inTime ? 1.0 : (double)N;
@@ -131,8 +133,11 @@ cudaError_t launch_split_ff(const SplitSeg* segs, int nSegs, cudaStream_t s) {
   return cudaSuccess;
 }
 
+// key = M + 10 * SMALL (single mode; SMALL the radix of the plan's short pass)
 void add_kernels_ff(std::vector<KernelEntry>& t) {
-  t.push_back({kKindLinearFF, 1, 8, (const void*)k_propagate_linear_ff<8>});
+  t.push_back({kKindLinearFF, 1 + 10 * 1, 8, (const void*)k_propagate_linear_ff<8, 1>});
+  t.push_back({kKindLinearFF, 1 + 10 * 2, 8, (const void*)k_propagate_linear_ff<8, 2>});
+  t.push_back({kKindLinearFF, 1 + 10 * 4, 8, (const void*)k_propagate_linear_ff<8, 4>});
 }
 
 }  // namespace nlm

@@ -220,3 +220,25 @@ def test_chi3_soliton_config(nlm, oracle):
     ref.run_signal_simulation(a)
     assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
     assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
+def test_wide_and_narrow_direct_kernels(nlm, oracle, name):
+    """The direct-DiffEq kernels in both launch forms: a batch with at least as many rows as SMs runs
+    N/8 threads per propagation (N/4 for three and four modes), a batch of a few rows runs N/4."""
+    med, ref = make(nlm, name), getattr(oracle, name)(**cases.oracle_kwargs(name))
+    fnl = name in cases.FULLY_NONLINEAR
+    if not fnl:
+        med._set_schedule(use_propagator=0)
+        med.runPumpSimulation()
+        ref.run_pump_simulation()
+    n = med._dims["nFreqs"]
+    modes = med._dims["nSignalModes"]
+    rng = np.random.default_rng(31)
+    for rows, want_r in ((160, 8 if modes <= 2 else 4), (3, 4)):
+        x = cases.noise(rng, rows * n, 0.5).reshape(rows, n)
+        out = med.batchSignalSimulation(x, inTimeDomain=False) if fnl else \
+            med.batchSignalSimulation(x, False, False)
+        assert med._last_schedule()["R"] == want_r
+        assert cases.rel_l2(out, ref.batch_signal_simulation(x, False) if fnl else
+                            ref.batch_signal_simulation(x, False, False)) < TOL
