@@ -196,17 +196,22 @@ def dist_info():
     return rank, world, local
 
 
-def read_profile_traffic():
+def read_profile_value(key):
+    """A figure of the committed ncu summary of the benchmark kernel (a line `key: value ...`)."""
     path = os.path.join(ROOT, "profiles", "k_propagate_linear_green_n1024.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch_full:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def read_profile_traffic():
+    return read_profile_value("dram_bytes_per_launch_full")
 
 
 def run_reference(args):
@@ -610,6 +615,7 @@ def run_ours(args):
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "kernel": "k_propagate_linear<1,8>", "kernel_ms": 1e3 * avg_kernel_s,
                          "algorithmic_flops_per_launch": flops,
+                         "ncu_fp64_pipe_active_pct": read_profile_value("fp64_pipe_active_pct"),
                          "peak_source": "FP64 FMA chains measured in this run (MEASURED_PEAKS.json has no FP64 entry)"},
             "cpu_baseline": cpu,
             "plain": {"value": plain, "unit": UNIT, "sample": args.plain_sample,
