@@ -1,10 +1,13 @@
-"""computeGreensFunction split over several GPUs, one process per GPU.
+"""computeGreensFunction, batchSignalSimulation and ragged batches split over several GPUs, one
+process per GPU.
 
 The 2·N·nModes impulse propagations of a Green's function are independent.  The reference splits
 them over std::threads in contiguous ranges (src/_NonlinearMedium.cpp:350-353); here each rank
 propagates one contiguous range on its own GPU (nlm_green_rows: every rank regenerates the pump
 locally, nothing is exchanged during the propagation), the raw rows are gathered once to rank 0 and
-rank 0 builds C and S (nlm_green_finish: transpose, block fftshift, normalisation).
+rank 0 builds C and S (nlm_green_finish: transpose, block fftshift, normalisation).  The rows of a
+batch are split the same way.  The media of a ragged set are assigned to ranks by cost (longest
+processing time first), each rank running its media in one ragged launch.
 
 Failure handling: before the only collective, every rank publishes its status in the process
 group's store; a rank whose propagation raised, or that never reports within `timeout` seconds, makes
@@ -58,15 +61,42 @@ def engine_finish(medium, normalize):
 _CALLS = itertools.count()
 
 
-def green_sharded(medium, n_units, row_width, compute_rows, finish, group=None, timeout=60.0):
-    """Run the row blocks of one Green's function over the ranks of `group`.
-
-    compute_rows(lo, hi) -> (hi - lo, row_width) complex rows of this rank; finish(raw) -> (C, S) on
-    rank 0.  Returns (C, S) on rank 0 and None elsewhere.
-    """
+def _publish_and_check(store, call, rank, world, status, timeout):
+    """Every rank writes its status, then reads all others; raises RankFailure on a failed or silent rank."""
     import datetime
+    store.set("nlm-shard/%d/%d" % (call, rank), status)
+    store.set_timeout(datetime.timedelta(seconds=timeout))
+    for r in range(world):
+        try:
+            other = store.get("nlm-shard/%d/%d" % (call, r)).decode()
+        except Exception as exc:
+            raise RankFailure("rank %d did not report within %.0f s (%s)" % (r, timeout, exc)) from exc
+        if other != "ok":
+            raise RankFailure("rank %d failed: %s" % (r, other))
 
+
+def _gather_flat(flat, counts, group):
+    """All-gather of complex vectors of per-rank lengths `counts` (padded to the longest);
+    returns the list of per-rank vectors."""
     import torch
+    import torch.distributed as dist
+    width = max(max(counts), 1)
+    use_cuda = dist.get_backend(group) == "nccl"
+    dev = torch.device("cuda", torch.cuda.current_device()) if use_cuda else torch.device("cpu")
+    block = torch.zeros((width, 2), dtype=torch.float64, device=dev)
+    if flat.size:
+        block[: flat.size] = torch.view_as_real(torch.from_numpy(np.ascontiguousarray(flat))).to(dev)
+    parts = [torch.empty_like(block) for _ in range(len(counts))]
+    dist.all_gather(parts, block, group=group)
+    return [torch.view_as_complex(p[:c].cpu()).numpy() for p, c in zip(parts, counts)]
+
+
+def sharded_rows(n_units, row_width, compute_rows, group=None, timeout=60.0):
+    """Rows [lo, hi) of n_units independent units per rank (contiguous ranges), gathered.
+
+    compute_rows(lo, hi) -> (hi - lo, row_width) complex rows of this rank.  Returns the
+    (n_units, row_width) rows on rank 0 and None elsewhere.
+    """
     import torch.distributed as dist
 
     rank, world = dist.get_rank(group), dist.get_world_size(group)
@@ -78,28 +108,101 @@ def green_sharded(medium, n_units, row_width, compute_rows, finish, group=None, 
         rows = np.asarray(compute_rows(lo, hi), dtype=np.complex128).reshape(hi - lo, row_width)
     except Exception as exc:  # reported to every rank below
         status = "error: %s: %s" % (type(exc).__name__, exc)
-    store.set("nlm-green/%d/%d" % (call, rank), status)
-    store.set_timeout(datetime.timedelta(seconds=timeout))
-    for r in range(world):
-        try:
-            other = store.get("nlm-green/%d/%d" % (call, r)).decode()
-        except Exception as exc:
-            raise RankFailure("rank %d did not report within %.0f s (%s)" % (r, timeout, exc)) from exc
-        if other != "ok":
-            raise RankFailure("rank %d failed: %s" % (r, other))
-    # one gather of the row blocks (padded to the largest block)
-    counts = [b - a for a, b in partition(n_units, world)]
-    width = max(counts)
-    use_cuda = dist.get_backend(group) == "nccl"
-    dev = torch.device("cuda", torch.cuda.current_device()) if use_cuda else torch.device("cpu")
-    block = torch.zeros((width, row_width, 2), dtype=torch.float64, device=dev)
-    block[: hi - lo] = torch.view_as_real(torch.from_numpy(rows)).to(dev)
-    parts = [torch.empty_like(block) for _ in range(world)]
-    dist.all_gather(parts, block, group=group)
+    _publish_and_check(store, call, rank, world, status, timeout)
+    counts = [(b - a) * row_width for a, b in partition(n_units, world)]
+    parts = _gather_flat(rows.ravel(), counts, group)
     if rank != 0:
         return None
-    raw = np.concatenate([torch.view_as_complex(p[:c].cpu()).numpy() for p, c in zip(parts, counts)], axis=0)
-    return finish(raw)
+    return np.concatenate(parts).reshape(n_units, row_width)
+
+
+def green_sharded(medium, n_units, row_width, compute_rows, finish, group=None, timeout=60.0):
+    """Run the row blocks of one Green's function over the ranks of `group`.
+
+    compute_rows(lo, hi) -> (hi - lo, row_width) complex rows of this rank; finish(raw) -> (C, S) on
+    rank 0.  Returns (C, S) on rank 0 and None elsewhere.
+    """
+    raw = sharded_rows(n_units, row_width, compute_rows, group, timeout)
+    return None if raw is None else finish(raw)
+
+
+def batch_sharded(medium, inputProfs, group=None, timeout=60.0, **kwargs):
+    """batchSignalSimulation of `medium` with its rows split over the ranks (contiguous ranges), each
+    rank propagating its rows on its own GPU.  Returns the output rows on rank 0, None elsewhere."""
+    x = np.asarray(inputProfs, dtype=np.complex128)
+    if x.ndim == 1:
+        x = x.reshape(1, -1)
+    d = medium._dims
+    out_modes = kwargs.get("useOutput") or [1] * d["nSignalModes"]
+    width = sum(1 for u in out_modes if u) * d["nFreqs"]
+
+    def rows(lo, hi):
+        if hi == lo:
+            return np.zeros((0, width), dtype=np.complex128)
+        return medium.batchSignalSimulation(x[lo:hi], **kwargs)
+    return sharded_rows(x.shape[0], width, rows, group, timeout)
+
+
+def assign_media(costs, world):
+    """Longest-processing-time assignment of media (by cost) to ranks: each medium in decreasing cost
+    goes to the least loaded rank (ties to the lowest rank).  Returns one index list per rank."""
+    load = [0.0] * world
+    owned = [[] for _ in range(world)]
+    for k in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owned[r].append(k)
+        load[r] += costs[k]
+    return [sorted(o) for o in owned]
+
+
+def media_cost(medium):
+    """Propagation cost of one medium: nZSteps x modes x N log2 N."""
+    d = medium._dims
+    n = d["nFreqs"]
+    return float(d["nZSteps"] * d["nSignalModes"] * n * max(1.0, np.log2(n)))
+
+
+def ragged_sharded(media, inputs, inTimeDomain=False, group=None, timeout=60.0, run=None, costs=None,
+                   out_shapes=None):
+    """nlm_ragged_batch over the ranks: media assigned by cost (assign_media), each rank running its
+    media in one ragged launch on its own GPU, outputs gathered.  Returns the list of outputs (one
+    (modes, N) array per medium, in input order) on rank 0, None elsewhere.  `run(media, inputs)`,
+    `costs` and `out_shapes` replace the engine call and the engine's cost and shape queries (tests)."""
+    import torch.distributed as dist
+    from . import nonlinearmedium as nlm_mod
+
+    media = list(media)
+    inputs = list(inputs)
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    store = dist.distributed_c10d._get_default_store()
+    call = next(_CALLS)
+    if costs is None:
+        costs = [media_cost(m) for m in media]
+    owned = assign_media(costs, world)
+    if out_shapes is None:
+        out_shapes = [(m._dims["nSignalModes"], m._dims["nFreqs"]) for m in media]
+    shapes = [tuple(sh) for sh in out_shapes]
+    run = run or (lambda ms, xs: nlm_mod.ragged_batch(ms, xs, inTimeDomain))
+    status, flat = "ok", np.zeros(0, dtype=np.complex128)
+    try:
+        mine = owned[rank]
+        outs = run([media[k] for k in mine], [inputs[k] for k in mine]) if mine else []
+        flat = np.concatenate([np.asarray(o, dtype=np.complex128).ravel() for o in outs]) if outs else flat
+    except Exception as exc:
+        status = "error: %s: %s" % (type(exc).__name__, exc)
+    _publish_and_check(store, call, rank, world, status, timeout)
+    counts = [sum(int(np.prod(shapes[k])) for k in owned[r]) for r in range(world)]
+    parts = _gather_flat(flat, counts, group)
+    if rank != 0:
+        return None
+    result = [None] * len(media)
+    for r in range(world):
+        off = 0
+        for k in owned[r]:
+            size = int(np.prod(shapes[k]))
+            result[k] = parts[r][off: off + size].reshape(shapes[k])
+            off += size
+    return result
 
 
 def compute_greens_function_sharded(medium, inTimeDomain=False, runPump=True, normalize=False, group=None,

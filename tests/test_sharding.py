@@ -101,3 +101,79 @@ def test_silent_rank_times_out(tmp_path):
     _run(tmp_path, silent_rank=1)
     msg = open(os.path.join(tmp_path, "fail0")).read()
     assert "did not report" in msg
+
+
+def test_media_assignment_is_balanced_and_deterministic():
+    costs = [5.0, 1.0, 9.0, 3.0, 3.0, 7.0, 2.0]
+    owned = sharding.assign_media(costs, 3)
+    assert sorted(k for o in owned for k in o) == list(range(len(costs)))
+    loads = [sum(costs[k] for k in o) for o in owned]
+    assert max(loads) - min(loads) <= max(costs)
+    assert owned == sharding.assign_media(costs, 3)
+    assert sharding.assign_media(costs, 1) == [list(range(len(costs)))]
+    assert sharding.assign_media([], 2) == [[], []]
+
+
+class _OracleBatchMedium:
+    """The engine medium's batch interface on the oracle (for CPU ranks)."""
+
+    def __init__(self, med):
+        self.med = med
+        self._dims = {"nSignalModes": med.n_signal_modes, "nFreqs": med.n_freqs}
+
+    def batchSignalSimulation(self, x, **kw):
+        return self.med.batch_signal_simulation(x, kw.get("inTimeDomain", False), False)
+
+
+SFG = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=0.3, beta2s=-0.2, beta2o=0, beta1s=1.1, beta3s=0.05,
+           tMax=10, zPrecision=6)
+
+
+def _ragged_media(O):
+    media, inputs = [], []
+    rng = np.random.default_rng(7)
+    for n, doms in ((32, [1, 2, 1]), (64, [2, 1]), (16, [1, 1, 1, 1]), (32, [3, 1]), (64, [1, 2, 2])):
+        m = O.Chi2SFG(tPrecision=n, poling=doms, **SFG)
+        m.run_pump_simulation()
+        media.append(m)
+        inputs.append((rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3)
+    return media, inputs
+
+
+def _oracle_ragged_run(ms, xs):
+    return [m.propagate(np.asarray(x)[None, :], False, 0)[0][0] for m, x in zip(ms, xs)]
+
+
+def _worker_rows(rank, world, port, outdir):
+    import torch.distributed as dist
+    from oracle import nlm_oracle as O
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    med = O.Chi2PDC(**CFG)
+    med.run_pump_simulation()
+    x = (np.random.default_rng(3).standard_normal((7, med.n_freqs)) + 0j)
+    out = sharding.batch_sharded(_OracleBatchMedium(med), x, timeout=5.0, inTimeDomain=False)
+    media, inputs = _ragged_media(O)
+    costs = [m.n_z_steps * m.n_freqs * np.log2(m.n_freqs) * m.n_signal_modes for m in media]
+    shapes = [(m.n_signal_modes, m.n_freqs) for m in media]
+    rag = sharding.ragged_sharded(media, inputs, group=None, timeout=5.0, run=_oracle_ragged_run, costs=costs,
+                                  out_shapes=shapes)
+    if rank == 0:
+        np.savez(os.path.join(outdir, "rows.npz"), batch=out, *rag)
+    dist.destroy_process_group()
+
+
+def test_batch_and_ragged_sharding_equal_single_rank(tmp_path):
+    from oracle import nlm_oracle as O
+    port = _free_port()
+    mp.spawn(_worker_rows, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    res = np.load(os.path.join(tmp_path, "rows.npz"))
+    med = O.Chi2PDC(**CFG)
+    med.run_pump_simulation()
+    x = (np.random.default_rng(3).standard_normal((7, med.n_freqs)) + 0j)
+    assert np.array_equal(res["batch"], med.batch_signal_simulation(x, False, False))
+    media, inputs = _ragged_media(O)
+    ref = _oracle_ragged_run(media, inputs)
+    for k, r in enumerate(ref):
+        assert np.array_equal(res["arr_%d" % k], r)
