@@ -6,7 +6,8 @@
 //     g <- conj(table_i) * FFT(g),  g <- IFFT(g),  g <- RK4_i^T(g; s_{i-1})
 // where RK4_i^T is the transposed RK4 step at each point, evaluated with the forward state s_{i-1}.
 // s_{i-1} comes from checkpoints stored by the forward kernel every K steps; inside a segment the
-// states are recomputed from its checkpoint (K = 1 stores every state and recomputes nothing).
+// states are recomputed from its checkpoint (K = 1 stores every state and recomputes nothing), with
+// the per-point RK4 propagator matrices when the engine provides them (PropArgs::prop).
 // Per step the sweep also accumulates the gradients of the RK4 stage factors a_s = c_s P_s
 // (c_s: poling sign x nonlinear step x phase mismatch of stage s, P_s: pump row 2i-2, 2i-1, 2i),
 // from which the pump-spectrum and poling-profile gradients are reduced afterwards.
@@ -57,15 +58,27 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc(const PropArgs a, c
           segp[j + v * T] = x[0][v];
         }
         for (int i = s0 + 1; i < segEnd; i++) {
-          const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+          if (a.prop) {
+            // the RK4 step as its per-point real 2x2 matrix (pairs (M00, M01), (M10, M11))
+            const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * 2 * N;
 #pragma unroll
-          for (int v = 0; v < R; v++) {
-            const int t = j + v * T;
-            const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
-            double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
-            double2 xm[1] = {x[0][v]};
-            rk4_point<FChi2PDC>(xm, p, c);
-            x[0][v] = xm[0];
+            for (int v = 0; v < R; v++) {
+              const int t = j + v * T;
+              const double2 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
+              const double re = x[0][v].x, im = x[0][v].y;
+              x[0][v] = make_double2(fma(e0.y, im, e0.x * re), fma(e1.y, im, e1.x * re));
+            }
+          } else {
+            const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+#pragma unroll
+            for (int v = 0; v < R; v++) {
+              const int t = j + v * T;
+              const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
+              double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
+              double2 xm[1] = {x[0][v]};
+              rk4_point<FChi2PDC>(xm, p, c);
+              x[0][v] = xm[0];
+            }
           }
           fft_regs<R, false>(x[0], buf, tw, plan, j);
 #pragma unroll
@@ -120,7 +133,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc(const PropArgs a, c
           const double2 ga0 = cmul(x, gk1);
           gx = cadd(gx, cmulc(a0, gk1));
           gv[v] = gx;
-          if (active) {
+          if (active && d.single) {   // the only instance: each element is written once
+            gacc[t] = ga0;
+            gacc[N + t] = ga1;
+            gacc[2 * N + t] = ga2;
+          } else if (active) {
             atomic_add2(gacc + t, ga0);
             atomic_add2(gacc + N + t, ga1);
             atomic_add2(gacc + 2 * N + t, ga2);
@@ -166,17 +183,30 @@ __global__ void k_adj_pump_rows(const double2* __restrict__ ga, const double2* _
 }
 
 // gF0[t] = (1/N) sum_r exp(-i r dzp D[t]) FFT(gP)[r][t]: the pump rows are IFFT(F0 exp(i r dzp D)).
+// Grid: x over the bins, y over chunks of kPumpChunk rows.  Each chunk starts from an exact
+// sincos and advances the phase by multiplying with exp(i dzp D) (error ~kPumpChunk ulp), and adds
+// its partial sum into gF0 (zeroed by the launcher).
+constexpr int kPumpChunk = 32;
+
 __global__ void k_adj_pump_reduce(const double2* __restrict__ fgP, const double* __restrict__ disp, double dzp,
                                   int nRowsP, int N, double2* __restrict__ gF0) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N) return;
+  const int r0 = blockIdx.y * kPumpChunk;
+  const int r1 = min(nRowsP, r0 + kPumpChunk);
+  double sn, cs, sn1, cs1;
+  sincos(((double)r0 * dzp) * disp[t], &sn, &cs);
+  sincos(dzp * disp[t], &sn1, &cs1);
+  double2 w = make_double2(cs, sn);
+  const double2 step = make_double2(cs1, sn1);
   double2 acc = czero();
-  for (int r = 0; r < nRowsP; r++) {
-    double sn = 0, cs = 1;
-    if (r > 0) sincos(((double)r * dzp) * disp[t], &sn, &cs);
-    acc = cadd(acc, cmulc(fgP[(long long)r * N + t], make_double2(cs, sn)));
+  for (int r = r0; r < r1; r++) {
+    acc = cadd(acc, cmulc(fgP[(long long)r * N + t], w));
+    w = cmul(w, step);
   }
-  gF0[t] = cscale(acc, 1.0 / N);
+  acc = cscale(acc, 1.0 / N);
+  atomicAdd(&gF0[t].x, acc.x);
+  atomicAdd(&gF0[t].y, acc.y);
 }
 
 // gc[i][s] = sum_t conj(P_row(i,s)[t]) ga[i][s][t]: gradient of the stage coefficient c_s of step i+1.
@@ -216,7 +246,10 @@ cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const d
 
 cudaError_t launch_adj_pump_reduce(const double2* fgP, const double* disp, double dzp, int nRowsP, int N,
                                    double2* gF0, cudaStream_t s) {
-  k_adj_pump_reduce<<<(N + 127) / 128, 128, 0, s>>>(fgP, disp, dzp, nRowsP, N, gF0);
+  cudaError_t e = cudaMemsetAsync(gF0, 0, (size_t)N * sizeof(double2), s);
+  if (e != cudaSuccess) return e;
+  const dim3 grid((unsigned)((N + 127) / 128), (unsigned)((nRowsP + kPumpChunk - 1) / kPumpChunk));
+  k_adj_pump_reduce<<<grid, 128, 0, s>>>(fgP, disp, dzp, nRowsP, N, gF0);
   return cudaGetLastError();
 }
 

@@ -1417,11 +1417,12 @@ struct Medium {
     return FFTables{twF.p, dstepF.p, dlastF.p, halfF.p, backF.p, propF.p};
   }
 
+  double propagatorBytes() const { return (double)(nZ > 1 ? nZ - 1 : 0) * 4.0 * nSignal * nSignal * N * 8.0; }
+
   bool wantPropagator(long long nInst) const {
     if (!linearSolver()) return false;
     if (usePropagator == 0) return false;
-    const double bytes = (double)(nZ > 1 ? nZ - 1 : 0) * 4.0 * nSignal * nSignal * N * 8.0;
-    if (bytes > 16e9) return false;
+    if (propagatorBytes() > 16e9) return false;
     if (usePropagator == 1) return true;
     return nInst >= 4LL * nSignal;
   }
@@ -1612,6 +1613,12 @@ struct Medium {
     a.nInst = adjRows;
     a.ipc = s.ipc;
     a.work = nullptr;
+    // segments between checkpoints are recomputed with the RK4 propagator matrices (built in parallel
+    // over all steps and points) instead of the four stage evaluations per step
+    if (!gn && adjK > 1 && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+      buildPropagator(R);
+      a.prop = prop.p;
+    }
     AdjArgs d{};
     d.gout = gout;
     d.ckpt = ckpt.p;
@@ -1620,6 +1627,7 @@ struct Medium {
     d.seg = (gn || adjK > 1) ? adjSeg.p : nullptr;
     d.ga = adjGa.p;
     d.gin = gin;
+    d.single = adjRows == 1 ? 1 : 0;
     void* args[] = {(void*)&a, (void*)&d};
     ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
     launches++;

@@ -72,6 +72,7 @@ struct AdjArgs {
   double2* seg;          // scratch [slot][K][N] for the recomputed states of one segment (K > 1)
   double2* ga;           // [(nZ-1)][3][N] accumulated gradients of the stage factors a_s = c_s P_s
   double2* gin;          // [nInst][N]: gradient with respect to the input spectrum
+  int single;            // 1: a single instance, whose stage-factor gradients are stored without atomics
 };
 
 // Registry of the propagation kernels.  The host engine launches them generically with
