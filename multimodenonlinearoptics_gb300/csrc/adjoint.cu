@@ -13,13 +13,148 @@
 // from which the pump-spectrum and poling-profile gradients are reduced afterwards.
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "nlm_propagate.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace nlm {
 
 __device__ __forceinline__ void atomic_add2(double2* p, double2 v) {
   atomicAdd(&p->x, v.x);
   atomicAdd(&p->y, v.y);
+}
+
+// States s_{s0} .. s_{segEnd-1} of one segment, recomputed from its checkpoint into seg[0 ..].
+template <int R>
+__device__ __forceinline__ void pdc_recompute_segment(const PropArgs& a, const double2* ck, int jseg, int s0,
+                                                      int segEnd, double2* seg, double2* buf, const double2* tw,
+                                                      int j) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  double2 x[R];
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    x[v] = ck[(long long)jseg * N + j + v * T];
+    seg[j + v * T] = x[v];
+  }
+  for (int i = s0 + 1; i < segEnd; i++) {
+    if (a.prop) {
+      // the RK4 step as its per-point real 2x2 matrix (pairs (M00, M01), (M10, M11))
+      const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * 2 * N;
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        const double2 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
+        const double re = x[v].x, im = x[v].y;
+        x[v] = make_double2(fma(e0.y, im, e0.x * re), fma(e1.y, im, e1.x * re));
+      }
+    } else {
+      const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
+        double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
+        double2 xm[1] = {x[v]};
+        rk4_point<FChi2PDC>(xm, p, c);
+        x[v] = xm[0];
+      }
+    }
+    fft_regs<R, false>(x, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+    fft_regs<R, true>(x, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) seg[(long long)(i - s0) * N + j + v * T] = x[v];
+  }
+}
+
+// Reverse steps i = segEnd .. s0+1; states[(i-1-s0) N ..] holds s_{i-1}.
+template <int R>
+__device__ __forceinline__ void pdc_reverse_segment(const PropArgs& a, const AdjArgs& d, const double2* states,
+                                                    int s0, int segEnd, double2 (&gv)[R], bool active, double2* buf,
+                                                    const double2* tw, int j) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  for (int i = segEnd; i > s0; i--) {
+    const double2* prev = states + (long long)(i - 1 - s0) * N;
+    if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
+    const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+#pragma unroll
+    for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
+    fft_regs<R, true>(gv, buf, tw, plan, j);
+    const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+    const double2 c0 = c[0], c1 = c[1], c2 = c[2];
+    double2* gacc = d.ga + (long long)(i - 1) * 3 * N;
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      const int t = j + v * T;
+      const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
+      const double2 a0 = cmul(c0, __ldg(pr)), a1 = cmul(c1, __ldg(pr + N)), a2 = cmul(c2, __ldg(pr + 2 * N));
+      const double2 x = prev[t];
+      // forward stages (solvers/Chi2PDC.cpp:40-43)
+      const double2 k1 = cmulc(a0, x);
+      const double2 y1 = caxpy(x, 0.5, k1);
+      const double2 k2 = cmulc(a1, y1);
+      const double2 y2 = caxpy(x, 0.5, k2);
+      const double2 k3 = cmulc(a1, y2);
+      const double2 y3 = cadd(x, k3);
+      // reverse: x' = x + (k1 + 2 k2 + 2 k3 + k4) / 6 with k = a conj(y)
+      const double2 gp = gv[v];
+      double2 gx = gp;
+      double2 gk1 = cscale(gp, 1.0 / 6.0);
+      double2 gk2 = cscale(gp, 1.0 / 3.0);
+      double2 gk3 = gk2;
+      const double2 gk4 = gk1;
+      const double2 ga2 = cmul(y3, gk4);
+      const double2 gy3 = cmulc(a2, gk4);
+      gx = cadd(gx, gy3);
+      gk3 = cadd(gk3, gy3);
+      double2 ga1 = cmul(y2, gk3);
+      const double2 gy2 = cmulc(a1, gk3);
+      gx = cadd(gx, gy2);
+      gk2 = caxpy(gk2, 0.5, gy2);
+      ga1 = cadd(ga1, cmul(y1, gk2));
+      const double2 gy1 = cmulc(a1, gk2);
+      gx = cadd(gx, gy1);
+      gk1 = caxpy(gk1, 0.5, gy1);
+      const double2 ga0 = cmul(x, gk1);
+      gx = cadd(gx, cmulc(a0, gk1));
+      gv[v] = gx;
+      if (active && d.single) {   // the only instance: each element is written once
+        gacc[t] = ga0;
+        gacc[N + t] = ga1;
+        gacc[2 * N + t] = ga2;
+      } else if (active) {
+        atomic_add2(gacc + t, ga0);
+        atomic_add2(gacc + N + t, ga1);
+        atomic_add2(gacc + 2 * N + t, ga2);
+      }
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void pdc_load_gout(const PropArgs& a, const AdjArgs& d, long long inst, bool active,
+                                              double2 (&gv)[R], int j) {
+  const int N = a.plan.N, T = a.plan.T;
+  const double2* go = d.gout + (active ? inst : 0) * (long long)N;
+#pragma unroll
+  for (int v = 0; v < R; v++) gv[v] = active ? cscale(go[j + v * T], (double)N) : czero();
+}
+
+// gradient of the input spectrum: s_0 = IFFT(half X_in)
+template <int R>
+__device__ __forceinline__ void pdc_store_gin(const PropArgs& a, const AdjArgs& d, long long inst, bool active,
+                                              double2 (&gv)[R], double2* buf, const double2* tw, int j) {
+  const int N = a.plan.N, T = a.plan.T;
+  fft_regs<R, false>(gv, buf, tw, a.plan, j);
+  if (active) {
+#pragma unroll
+    for (int v = 0; v < R; v++) d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+  }
 }
 
 template <int R>
@@ -40,119 +175,57 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc(const PropArgs a, c
     const long long inst = a.instBase + local;
     const double2* ck = d.ckpt + (active ? inst : 0) * (long long)d.nCk * N;
     double2 gv[R];
-    {
-      const double2* go = d.gout + (active ? inst : 0) * (long long)N;
-#pragma unroll
-      for (int v = 0; v < R; v++) gv[v] = active ? cscale(go[j + v * T], (double)N) : czero();
-    }
+    pdc_load_gout<R>(a, d, inst, active, gv, j);
     int segEnd = a.nZ - 1;
     while (segEnd >= 1) {
       const int jseg = (segEnd - 1) / d.K;
       const int s0 = jseg * d.K;
-      if (d.K > 1) {
-        // recompute the states s_{s0} .. s_{segEnd-1} of this segment from its checkpoint
-        double2 x[1][R];
-#pragma unroll
-        for (int v = 0; v < R; v++) {
-          x[0][v] = ck[(long long)jseg * N + j + v * T];
-          segp[j + v * T] = x[0][v];
-        }
-        for (int i = s0 + 1; i < segEnd; i++) {
-          if (a.prop) {
-            // the RK4 step as its per-point real 2x2 matrix (pairs (M00, M01), (M10, M11))
-            const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * 2 * N;
-#pragma unroll
-            for (int v = 0; v < R; v++) {
-              const int t = j + v * T;
-              const double2 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
-              const double re = x[0][v].x, im = x[0][v].y;
-              x[0][v] = make_double2(fma(e0.y, im, e0.x * re), fma(e1.y, im, e1.x * re));
-            }
-          } else {
-            const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-#pragma unroll
-            for (int v = 0; v < R; v++) {
-              const int t = j + v * T;
-              const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
-              double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
-              double2 xm[1] = {x[0][v]};
-              rk4_point<FChi2PDC>(xm, p, c);
-              x[0][v] = xm[0];
-            }
-          }
-          fft_regs<R, false>(x[0], buf, tw, plan, j);
-#pragma unroll
-          for (int v = 0; v < R; v++) x[0][v] = cmul(x[0][v], __ldg(a.dstep + j + v * T));
-          fft_regs<R, true>(x[0], buf, tw, plan, j);
-#pragma unroll
-          for (int v = 0; v < R; v++) segp[(long long)(i - s0) * N + j + v * T] = x[0][v];
-        }
-      }
-      for (int i = segEnd; i > s0; i--) {
-        const double2* prev = d.K > 1 ? segp + (long long)(i - 1 - s0) * N : ck + (long long)(i - 1) * N;
-        if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
-        const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
-#pragma unroll
-        for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
-        fft_regs<R, true>(gv, buf, tw, plan, j);
-        const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-        const double2 c0 = c[0], c1 = c[1], c2 = c[2];
-        double2* gacc = d.ga + (long long)(i - 1) * 3 * N;
-#pragma unroll
-        for (int v = 0; v < R; v++) {
-          const int t = j + v * T;
-          const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
-          const double2 a0 = cmul(c0, __ldg(pr)), a1 = cmul(c1, __ldg(pr + N)), a2 = cmul(c2, __ldg(pr + 2 * N));
-          const double2 x = prev[t];
-          // forward stages (solvers/Chi2PDC.cpp:40-43)
-          const double2 k1 = cmulc(a0, x);
-          const double2 y1 = caxpy(x, 0.5, k1);
-          const double2 k2 = cmulc(a1, y1);
-          const double2 y2 = caxpy(x, 0.5, k2);
-          const double2 k3 = cmulc(a1, y2);
-          const double2 y3 = cadd(x, k3);
-          // reverse: x' = x + (k1 + 2 k2 + 2 k3 + k4) / 6 with k = a conj(y)
-          const double2 gp = gv[v];
-          double2 gx = gp;
-          double2 gk1 = cscale(gp, 1.0 / 6.0);
-          double2 gk2 = cscale(gp, 1.0 / 3.0);
-          double2 gk3 = gk2;
-          const double2 gk4 = gk1;
-          const double2 ga2 = cmul(y3, gk4);
-          const double2 gy3 = cmulc(a2, gk4);
-          gx = cadd(gx, gy3);
-          gk3 = cadd(gk3, gy3);
-          double2 ga1 = cmul(y2, gk3);
-          const double2 gy2 = cmulc(a1, gk3);
-          gx = cadd(gx, gy2);
-          gk2 = caxpy(gk2, 0.5, gy2);
-          ga1 = cadd(ga1, cmul(y1, gk2));
-          const double2 gy1 = cmulc(a1, gk2);
-          gx = cadd(gx, gy1);
-          gk1 = caxpy(gk1, 0.5, gy1);
-          const double2 ga0 = cmul(x, gk1);
-          gx = cadd(gx, cmulc(a0, gk1));
-          gv[v] = gx;
-          if (active && d.single) {   // the only instance: each element is written once
-            gacc[t] = ga0;
-            gacc[N + t] = ga1;
-            gacc[2 * N + t] = ga2;
-          } else if (active) {
-            atomic_add2(gacc + t, ga0);
-            atomic_add2(gacc + N + t, ga1);
-            atomic_add2(gacc + 2 * N + t, ga2);
-          }
-        }
-      }
+      if (d.K > 1) pdc_recompute_segment<R>(a, ck, jseg, s0, segEnd, segp, buf, tw, j);
+      pdc_reverse_segment<R>(a, d, d.K > 1 ? segp : ck + (long long)s0 * N, s0, segEnd, gv, active, buf, tw, j);
       segEnd = s0;
     }
-    // gradient of the input spectrum: s_0 = IFFT(half X_in)
-    fft_regs<R, false>(gv, buf, tw, plan, j);
-    if (active) {
-#pragma unroll
-      for (int v = 0; v < R; v++)
-        d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+    pdc_store_gin<R>(a, d, inst, active, gv, buf, tw, j);
+    __syncthreads();
+  }
+}
+
+// Pipelined reverse sweep for checkpoint intervals K > 1, launched as clusters of two CTAs, one
+// propagation per cluster at a time (ipc = 1).  CTA 1 of the cluster recomputes segment j-1 from
+// its checkpoint while CTA 0 runs the reverse steps of segment j, so the recomputation that
+// checkpointing adds runs on a second SM instead of lengthening the sweep.  The two alternate
+// between two state buffers per cluster (d.seg: [cluster][2][K][N]); a cluster barrier (hardware,
+// release/acquire at cluster scope) separates the iterations.  Both CTAs execute the same number of
+// barriers: nSeg + 1 per propagation.
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_pipe(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N;
+  const int j = threadIdx.x;
+  const int role = (int)cluster.block_rank();
+  const long long clusterId = blockIdx.x / 2, nClusters = gridDim.x / 2;
+  double2* buf;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &buf);
+  double2* states = d.seg + clusterId * 2LL * d.K * N;
+  const int nSeg = (a.nZ - 2) / d.K + 1;
+  for (long long local = clusterId; local < a.nInst; local += nClusters) {
+    const long long inst = a.instBase + local;
+    const double2* ck = d.ckpt + inst * (long long)d.nCk * N;
+    double2 gv[R];
+    if (role == 0) pdc_load_gout<R>(a, d, inst, true, gv, j);
+    for (int it = 0; it <= nSeg; it++) {
+      if (role == 1 && it < nSeg) {
+        const int jseg = nSeg - 1 - it, s0 = jseg * d.K, segEnd = min(s0 + d.K, a.nZ - 1);
+        pdc_recompute_segment<R>(a, ck, jseg, s0, segEnd, states + (long long)(it & 1) * d.K * N, buf, tw, j);
+      }
+      if (role == 0 && it >= 1) {
+        const int jseg = nSeg - it, s0 = jseg * d.K, segEnd = min(s0 + d.K, a.nZ - 1);
+        pdc_reverse_segment<R>(a, d, states + (long long)((it - 1) & 1) * d.K * N, s0, segEnd, gv, true, buf, tw, j);
+      }
+      cluster.sync();
     }
+    if (role == 0) pdc_store_gin<R>(a, d, inst, true, gv, buf, tw, j);
     __syncthreads();
   }
 }
@@ -260,7 +333,11 @@ cudaError_t launch_adj_coef_reduce(const double2* ga, const double2* pump, int n
   return cudaGetLastError();
 }
 
+// key = solver id + 100: the pipelined two-CTA-cluster variant (checkpoint interval > 1)
 void add_kernels_adjoint(std::vector<KernelEntry>& t) {
+  t.push_back({kKindAdjoint, kChi2PDC + 100, 4, (const void*)k_adjoint_pdc_pipe<4>});
+  t.push_back({kKindAdjoint, kChi2PDC + 100, 8, (const void*)k_adjoint_pdc_pipe<8>});
+  t.push_back({kKindAdjoint, kChi2PDC + 100, 16, (const void*)k_adjoint_pdc_pipe<16>});
   t.push_back({kKindAdjoint, kChi2PDC, 4, (const void*)k_adjoint_pdc<4>});
   t.push_back({kKindAdjoint, kChi2PDC, 8, (const void*)k_adjoint_pdc<8>});
   t.push_back({kKindAdjoint, kChi2PDC, 16, (const void*)k_adjoint_pdc<16>});

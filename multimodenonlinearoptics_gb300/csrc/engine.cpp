@@ -1604,9 +1604,20 @@ struct Medium {
     const size_t steps = nZ - 1;
     adjGa.reserve(steps * 3 * N);
     ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
-    Schedule s = schedule(k, adjRows, R);
     const bool gn = solver == kChi3GNLSE;
     if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
+    // Few rows with checkpoint segments: the pipelined variant, one two-CTA cluster per propagation
+    // (one CTA recomputes the next segment while the other reverses the current one).
+    const KernelEntry* kp = (!gn && adjK > 1 && adjRows <= (long long)smCount() / 2)
+                                ? findKernel(kKindAdjoint, solver + 100, R) : nullptr;
+    if (kp) k = kp;
+    Schedule s = schedule(k, adjRows, R);
+    if (kp) {
+      s.ipc = 1;
+      s.block = (int)N / R;
+      s.smem = (size_t)(1 + (R != 16 ? 1 : 0)) * N * sizeof(double2);
+      s.grid = 2 * (int)adjRows;
+    }
     const size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
     if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
     PropArgs a = baseArgs(R);
@@ -1629,7 +1640,23 @@ struct Medium {
     d.gin = gin;
     d.single = adjRows == 1 ? 1 : 0;
     void* args[] = {(void*)&a, (void*)&d};
-    ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
+    if (kp) {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3(s.grid);
+      cfg.blockDim = dim3(s.block);
+      cfg.dynamicSmemBytes = s.smem;
+      cfg.stream = stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 2;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster)");
+    } else {
+      ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
+    }
     launches++;
     if (gpump) {
       const size_t rowsP = nZP;

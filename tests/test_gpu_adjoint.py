@@ -240,3 +240,33 @@ def test_gnlse_checkpointed_sweep(nlm):
         torch.sum(torch.abs(out) ** 2 * torch.arange(64, device="cuda")).backward()
         grads.append(xt.grad.cpu().numpy())
     assert cases.rel_l2(grads[1], grads[0]) < 1e-12
+
+
+@pytest.mark.parametrize("rows", [1, 80])
+def test_checkpoint_paths_agree(nlm, rows):
+    """Checkpoint interval > 1 with few rows runs the two-CTA pipelined sweep, with more rows than half
+    the SMs the one-CTA sweep; both must give the stored-state (interval 1) gradients."""
+    kw = dict(KW, zPrecision=60)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    x, f0, d, target = _problem(64, nz, rows=rows, seed=12)
+    a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
+    b = _engine_grads(nlm, kw, x, f0, d, target, interval=11)
+    for ga, gb in zip(a[1:4], b[1:4]):
+        assert cases.rel_l2(gb, ga) < 1e-12
+
+
+def test_sqrt_checkpoints_at_config_size(nlm):
+    """The gradient configuration with sqrt(nZSteps) checkpoints against all states stored."""
+    kw = dict(KW, tMax=40, tPrecision=512, zPrecision=1000, diffBeta0=0)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    rng = np.random.default_rng(4)
+    x = cases.noise(rng, 512, 1e-3).reshape(1, 512)
+    t = np.fft.fftshift(np.linspace(-40, 40, 512, endpoint=False))
+    f0 = np.fft.fft(np.exp(-t ** 2 / 2))
+    d = rng.uniform(-1, 1, nz)
+    target = cases.noise(rng, 512, 1.0).reshape(1, 512)
+    target /= np.linalg.norm(target)
+    a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
+    b = _engine_grads(nlm, kw, x, f0, d, target, interval=int(np.ceil(np.sqrt(nz - 1))))
+    for ga, gb in zip(a[1:4], b[1:4]):
+        assert cases.rel_l2(gb, ga) < 1e-11
