@@ -11,7 +11,11 @@
 // Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and SEG[K][N] when K > 1.
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "nlm_propagate.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace nlm {
 
@@ -59,6 +63,66 @@ __device__ __forceinline__ void gnlse_stages(const PropArgs& a, int i, int j, do
       }
     }
   }
+}
+
+// One reverse step i: gv (this thread's points of g, time domain after the step) becomes the gradient
+// with respect to the state before the step.  Y/U2: the stage inputs y_s and convolutions u2_s of
+// step i; GX/GXP: per-propagation global scratch of N points each.
+template <int R>
+__device__ __forceinline__ void gnlse_reverse_step(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
+                                                   const double2* Y, const double2* U2, double2* GX, double2* GXP,
+                                                   double2 (&gv)[R]) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  // dispersion half: g_x' = F^H(conj(table) F g)
+  if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
+  const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+#pragma unroll
+  for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
+  fft_regs<R, true>(gv, buf, tw, plan, j);
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    GX[j + v * T] = gv[v];
+    GXP[j + v * T] = gv[v];
+  }
+  const double* rel = a.relInt + (long long)(i - 1) * 3;
+  double2 gke[R];
+#pragma unroll
+  for (int v = 0; v < R; v++) gke[v] = czero();
+  for (int s = 3; s >= 0; s--) {
+    const double w = (s == 1 || s == 2) ? 2.0 / 6.0 : 1.0 / 6.0;
+    const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+    const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+    double2 u[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = caxpy(gke[v], w, GXP[j + v * T]);   // g_k_s
+    fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
+    fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u3
+    double2 gy[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      const int t = j + v * T;
+      const double2 y = Y[(long long)s * N + t], u2 = U2[(long long)s * N + t];
+      gy[v] = cmulc(u[v], u2);     // conj(u2) g_u3
+      u[v] = cmulc(u[v], y);       // g_u2 = conj(y) g_u3
+    }
+    fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.raman + j + v * T));
+    fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u1 (real part)
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      const int t = j + v * T;
+      const double2 y = Y[(long long)s * N + t];
+      gy[v] = caxpy(gy[v], 2.0 * ri * u[v].x, y);
+      GX[t] = cadd(GX[t], gy[v]);
+      gke[v] = cscale(gy[v], fac);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < R; v++) gv[v] = GX[j + v * T];
 }
 
 template <int R>
@@ -114,55 +178,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a,
       for (int i = segEnd; i > s0; i--) {
         const double2* prev = d.K > 1 ? SEG + (long long)(i - 1 - s0) * N : ck + (long long)(i - 1) * N;
         gnlse_stages<R>(a, i, j, buf, tw, prev, Y, U2, nullptr);
-        // dispersion half: g_x' = F^H(conj(table) F g)
-        if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
-        const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
-#pragma unroll
-        for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
-        fft_regs<R, true>(gv, buf, tw, plan, j);
-#pragma unroll
-        for (int v = 0; v < R; v++) {
-          GX[j + v * T] = gv[v];
-          GXP[j + v * T] = gv[v];
-        }
-        const double* rel = a.relInt + (long long)(i - 1) * 3;
-        double2 gke[R];
-#pragma unroll
-        for (int v = 0; v < R; v++) gke[v] = czero();
-        for (int s = 3; s >= 0; s--) {
-          const double w = (s == 1 || s == 2) ? 2.0 / 6.0 : 1.0 / 6.0;
-          const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
-          const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
-          double2 u[R];
-#pragma unroll
-          for (int v = 0; v < R; v++) u[v] = caxpy(gke[v], w, GXP[j + v * T]);   // g_k_s
-          fft_regs<R, false>(u, buf, tw, plan, j);
-#pragma unroll
-          for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
-          fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u3
-          double2 gy[R];
-#pragma unroll
-          for (int v = 0; v < R; v++) {
-            const int t = j + v * T;
-            const double2 y = Y[(long long)s * N + t], u2 = U2[(long long)s * N + t];
-            gy[v] = cmulc(u[v], u2);     // conj(u2) g_u3
-            u[v] = cmulc(u[v], y);       // g_u2 = conj(y) g_u3
-          }
-          fft_regs<R, false>(u, buf, tw, plan, j);
-#pragma unroll
-          for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.raman + j + v * T));
-          fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u1 (real part)
-#pragma unroll
-          for (int v = 0; v < R; v++) {
-            const int t = j + v * T;
-            const double2 y = Y[(long long)s * N + t];
-            gy[v] = caxpy(gy[v], 2.0 * ri * u[v].x, y);
-            GX[t] = cadd(GX[t], gy[v]);
-            gke[v] = cscale(gy[v], fac);
-          }
-        }
-#pragma unroll
-        for (int v = 0; v < R; v++) gv[v] = GX[j + v * T];
+        gnlse_reverse_step<R>(a, i, j, buf, tw, Y, U2, GX, GXP, gv);
       }
       segEnd = s0;
     }
@@ -176,8 +192,86 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a,
   }
 }
 
+// Pipelined reverse sweep, launched as clusters of two CTAs, one propagation per cluster at a time.
+// CTA 1 marches segment j-1 forward from its checkpoint and stores the stage inputs y_s and the
+// convolutions u2_s of every step; CTA 0 runs the reverse steps of segment j from the stored stages.
+// Both do about one forward step of work per step (18 transforms), so the stage recomputation that
+// the one-CTA sweep adds to every reverse step runs on a second SM.  Scratch per cluster:
+// STG[2][K][8][N] (double-buffered stages), XS[N], ACC[N] (CTA 1), GX[N], GXP[N] (CTA 0).  A cluster
+// barrier separates the iterations; both CTAs execute nSeg + 1 barriers per propagation.
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pipe(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const int j = threadIdx.x;
+  const int role = (int)cluster.block_rank();
+  const long long clusterId = blockIdx.x / 2, nClusters = gridDim.x / 2;
+  double2* buf;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &buf);
+  const long long stepStride = 8LL * N, bufStride = (long long)d.K * stepStride;
+  double2* STG = d.seg + clusterId * (2 * bufStride + 4LL * N);
+  double2* XS = STG + 2 * bufStride;
+  double2* ACC = XS + N;
+  double2* GX = ACC + N;
+  double2* GXP = GX + N;
+  const int nSeg = (a.nZ - 2) / d.K + 1;
+  for (long long local = clusterId; local < a.nInst; local += nClusters) {
+    const long long inst = a.instBase + local;
+    const double2* ck = d.ckpt + inst * (long long)d.nCk * N;
+    double2 gv[R];
+    if (role == 0) {
+      const double2* go = d.gout + inst * (long long)N;
+#pragma unroll
+      for (int v = 0; v < R; v++) gv[v] = cscale(go[j + v * T], (double)N);
+    }
+    for (int it = 0; it <= nSeg; it++) {
+      if (role == 1 && it < nSeg) {
+        const int jseg = nSeg - 1 - it, s0 = jseg * d.K, segEnd = min(s0 + d.K, a.nZ - 1);
+        double2* stg = STG + (long long)(it & 1) * bufStride;
+#pragma unroll
+        for (int v = 0; v < R; v++) XS[j + v * T] = ck[(long long)jseg * N + j + v * T];
+        for (int i = s0 + 1; i <= segEnd; i++) {
+          double2* Yi = stg + (long long)(i - 1 - s0) * stepStride;
+          const bool more = i < segEnd;   // the state after step i starts the next step of the segment
+          gnlse_stages<R>(a, i, j, buf, tw, XS, Yi, Yi + 4LL * N, more ? ACC : nullptr);
+          if (more) {
+            double2 x[R];
+#pragma unroll
+            for (int v = 0; v < R; v++) x[v] = caxpy(XS[j + v * T], 1.0 / 6.0, ACC[j + v * T]);
+            fft_regs<R, false>(x, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+            fft_regs<R, true>(x, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) XS[j + v * T] = x[v];
+          }
+        }
+      }
+      if (role == 0 && it >= 1) {
+        const int jseg = nSeg - it, s0 = jseg * d.K, segEnd = min(s0 + d.K, a.nZ - 1);
+        const double2* stg = STG + (long long)((it - 1) & 1) * bufStride;
+        for (int i = segEnd; i > s0; i--) {
+          const double2* Yi = stg + (long long)(i - 1 - s0) * stepStride;
+          gnlse_reverse_step<R>(a, i, j, buf, tw, Yi, Yi + 4LL * N, GX, GXP, gv);
+        }
+      }
+      cluster.sync();
+    }
+    if (role == 0) {
+      fft_regs<R, false>(gv, buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+    }
+    __syncthreads();
+  }
+}
+
 void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t) {
   t.push_back({kKindAdjoint, kChi3GNLSE, 8, (const void*)k_adjoint_gnlse<8>});
+  // key + 100: the pipelined two-CTA-cluster variant
+  t.push_back({kKindAdjoint, kChi3GNLSE + 100, 8, (const void*)k_adjoint_gnlse_pipe<8>});
 }
 
 }  // namespace nlm

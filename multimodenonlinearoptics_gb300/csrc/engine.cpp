@@ -1608,7 +1608,9 @@ struct Medium {
     if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
     // Few rows with checkpoint segments: the pipelined variant, one two-CTA cluster per propagation
     // (one CTA recomputes the next segment while the other reverses the current one).
-    const KernelEntry* kp = (!gn && adjK > 1 && adjRows <= (long long)smCount() / 2)
+    // (Chi3GNLSE: one CTA marches each segment forward storing the stage values of every step, the
+    // other reverses the previous segment from them.)
+    const KernelEntry* kp = ((gn || adjK > 1) && adjRows <= (long long)smCount() / 2)
                                 ? findKernel(kKindAdjoint, solver + 100, R) : nullptr;
     if (kp) k = kp;
     Schedule s = schedule(k, adjRows, R);
@@ -1618,8 +1620,12 @@ struct Medium {
       s.smem = (size_t)(1 + (R != 16 ? 1 : 0)) * N * sizeof(double2);
       s.grid = 2 * (int)adjRows;
     }
-    const size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
-    if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
+    if (kp && gn) {
+      adjSeg.reserve((size_t)adjRows * (2 * (size_t)adjK * 8 + 4) * N);   // per cluster: STG[2][K][8][N], 4 N
+    } else {
+      const size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
+      if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
+    }
     PropArgs a = baseArgs(R);
     a.nInst = adjRows;
     a.ipc = s.ipc;

@@ -270,3 +270,23 @@ def test_sqrt_checkpoints_at_config_size(nlm):
     b = _engine_grads(nlm, kw, x, f0, d, target, interval=int(np.ceil(np.sqrt(nz - 1))))
     for ga, gb in zip(a[1:4], b[1:4]):
         assert cases.rel_l2(gb, ga) < 1e-11
+
+
+def test_gnlse_pipelined_and_one_cta_sweeps_agree(nlm):
+    """3 rows run the two-CTA pipelined sweep, 80 rows (more than half the SMs) the one-CTA sweep;
+    the loss is a sum over rows, so the first 3 rows' gradients must agree between the two."""
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    rng = np.random.default_rng(13)
+    x80 = np.fft.fft(cases.noise(rng, 80 * 64, 0.5).reshape(80, 64), axis=1)
+    weights = torch.arange(64, device="cuda", dtype=torch.float64)
+    grads = {}
+    for rows in (3, 80):
+        for k in (1, 5):
+            med = nlm.Chi3GNLSE(**GN)
+            xt = torch.tensor(x80[:rows], device="cuda", requires_grad=True)
+            torch.sum(torch.abs(propagate_gnlse(med, xt, k)) ** 2 * weights).backward()
+            grads[rows, k] = xt.grad.cpu().numpy()
+    for key in ((3, 5), (80, 1), (80, 5)):
+        assert cases.rel_l2(grads[key][:3], grads[3, 1]) < 1e-12
+    assert cases.rel_l2(grads[80, 5], grads[80, 1]) < 1e-12
