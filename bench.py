@@ -31,38 +31,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Green's-fn propagations/s at 1e-9 rel err: batched vs plain GPU; grad/fwd cost"
 UNIT = "propagations/s"
-CONFIG = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0, beta1s=2, beta3=0,
-              beta3s=0.1, diffBeta0=0, tMax=40, tPrecision=1024, zPrecision=500)
-N_DOMAINS = 100
+from multimodenonlinearoptics_gb300.workloads import (GNLSE_CONFIG, GREEN_CONFIG as CONFIG,  # noqa: E402
+                                                     GREEN_DOMAINS as N_DOMAINS, ragged_media_params)
+
 C_SOLVER = 80          # point-wise flops per mode per step of Chi2PDC's DiffEq (fixed, not tuned)
-
-
-def ragged_media_params(seed=3, count=64):
-    """The ragged workload: Chi2SFG media with N in {128..2048}, beta1s ~ U[-3,3], beta2, beta2s ~ U[-1,1],
-    beta3s ~ U[-0.2,0.2], Gaussian pump of width U[0.5,3], poling domains of U{5..50} z steps with
-    alternating sign, nZSteps ~ U[200,2000] (realised through zPrecision), relativeLength=1,
-    nlLength=nlLengthOrig=1, beta2o=beta1o=beta3o=0, diffBeta0=0, tMax=10."""
-    rng = np.random.default_rng(seed)
-    out = []
-    for _ in range(count):
-        n = int(rng.choice([128, 256, 512, 1024, 2048]))
-        b1s, b2, b2s, b3s = rng.uniform(-3, 3), rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-0.2, 0.2)
-        w = rng.uniform(0.5, 3)
-        target = int(rng.integers(200, 2001))
-        min_len = min(1.0, 1.0 / max(abs(b1s), abs(b2), abs(b2s), abs(b3s)))
-        zp = int(math.ceil(target * min_len))
-        kw = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=b2, beta2s=b2s, beta2o=0, beta1=0, beta1s=b1s,
-                  beta1o=0, beta3=0, beta3s=b3s, beta3o=0, diffBeta0=0, tMax=10, tPrecision=n, zPrecision=zp)
-        doms, total = [], 0
-        while total < target:
-            d = int(rng.integers(5, 51))
-            doms.append(d)
-            total += d
-        t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
-        pump = np.exp(-t ** 2 / (2 * w * w))
-        sig = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3 / np.sqrt(2)
-        out.append((kw, np.array(doms, dtype=float), pump, sig))
-    return out
 
 
 def algorithmic_flops(n_inst, n_z, n, modes=1, c_solver=C_SOLVER):
@@ -306,10 +278,6 @@ def measure_adjoint(nlm, torch, reps=3):
             "grad_fwd_cost_sqrt_checkpoints": t_grad_sqrt / t_fwd, "sqrt_checkpoint_interval": k_sqrt,
             "workload": "Chi2PDC N=512 nZSteps=%d, gradients wrt input spectrum, pump spectrum (512 bins) and "
                         "poling profile (%d values)" % (nz, nz)}
-
-
-GNLSE_CONFIG = dict(relativeLength=1, nlLength=1.0 / 9, selfSteepLength=6.5, fr=0.18, fb=0.21, tau1=0.244, tau2=0.64,
-                    tau3=1.92, beta2=-1, beta3=0.05, tMax=50, tPrecision=4096, zPrecision=1111)
 
 
 def measure_configs(nlm, torch, cpu=True):
