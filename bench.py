@@ -434,13 +434,16 @@ def measure_ff(nlm, torch, args, stream, flush, C64, S64, f64_value, f64_kernel_
         e1.synchronize()
         elapsed += e0.elapsed_time(e1) / 1e3
     kernel_ms, kernel_count = med._kernel_timing(0)
+    sched = med._last_schedule()
     value = 2 * n * args.steps / elapsed
     err = max(float(torch.linalg.norm(C - C64) / torch.linalg.norm(C64)),
               float(torch.linalg.norm(S - S64) / torch.linalg.norm(S64)))
     return {"value": value, "unit": UNIT, "kernel": "k_propagate_linear_ff<8>",
             "kernel_ms": kernel_ms / max(kernel_count, 1), "speedup_vs_f64": value / f64_value,
             "kernel_speedup_vs_f64": f64_kernel_ms / max(kernel_ms / max(kernel_count, 1), 1e-12),
-            "rel_err_vs_f64": err, "dtype": "f32x2 (double-float, ~48-bit significand)"}
+            "rel_err_vs_f64": err, "dtype": "f32x2 (double-float, ~48-bit significand)",
+            "schedule": {"cta_per_sm": sched["cta_per_sm"], "registers_per_thread": sched["registers"],
+                         "chosen_by": "autotuner" if sched["tuned"] else "occupancy"}}
 
 
 def run_ours(args):
@@ -592,6 +595,7 @@ def run_ours(args):
             "parity_sample_rel_err": parity,
             "schedule": {"points_per_thread": sched["R"], "propagations_per_cta": sched["ipc"], "grid": sched["grid"],
                          "block": sched["block"], "cta_per_sm": sched["cta_per_sm"],
+                         "registers_per_thread": sched["registers"],
                          "chosen_by": "autotuner" if sched["tuned"] else "occupancy"},
             "cuda_graphs": dict(zip(("captures", "replays"), med._graph_stats())),
             "variant_ff": ff,

@@ -221,9 +221,10 @@ int nlm_device_available(void);
  * -1 = automatic; use_graph: 1 = batched launches captured into CUDA graphs and replayed
  * (default), 0 = direct launches.  No counterpart in the reference. */
 nlm_status nlm_set_schedule(nlm_medium* m, int cta_per_sm, int use_propagator, int use_graph);
-/* Launch shape of the last propagation of this handle: values[0..6] = points per thread R,
- * propagations per CTA, grid, block, resident CTAs per SM, 1 if chosen by the autotuner, and the
- * autotuner trials this handle ran.  No counterpart in the reference. */
+/* Launch shape of the last propagation of this handle: values[0..7] = points per thread R,
+ * propagations per CTA, grid, block, resident CTAs per SM, 1 if chosen by the autotuner, the
+ * autotuner trials this handle ran, and the registers per thread of the kernel variant.  No
+ * counterpart in the reference. */
 nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float

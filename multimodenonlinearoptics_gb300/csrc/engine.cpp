@@ -1156,6 +1156,14 @@ struct Medium {
     return 8;
   }
 
+  static const KernelEntry* findKernelFn(const void* fn) {
+    int count = 0;
+    const KernelEntry* t = kernel_table(&count);
+    for (int i = 0; i < count; i++)
+      if (t[i].fn == fn) return &t[i];
+    return nullptr;
+  }
+
   const KernelEntry* findKernel(int kind, int key, int R) const {
     int count = 0;
     const KernelEntry* t = kernel_table(&count);
@@ -1228,6 +1236,7 @@ struct Medium {
   struct TuneChoice {
     int R = 0, cta = 0, ipcMul = 1;
     float ms = 0;
+    const void* fn = nullptr;   // the kernel variant (several may share kind, key and R)
   };
   static std::mutex& tuneMutex() {
     static std::mutex mu;
@@ -1243,7 +1252,7 @@ struct Medium {
   }
   DevBuf<unsigned long long> tuneCounter;
   Schedule lastSchedule{};
-  int lastR = 0, lastTuned = 0;
+  int lastR = 0, lastTuned = 0, lastRegs = 0;
   long tuneTrials = 0;
 
   bool tuneWanted(const PropArgs& a, long long nInst) const {
@@ -1318,7 +1327,7 @@ struct Medium {
             }
             launches += 2;
             tuneTrials++;
-            if (ms < best.ms) best = TuneChoice{R, c, ipcMul, ms};
+            if (ms < best.ms) best = TuneChoice{R, c, ipcMul, ms, kc->fn};
           }
         }
       }
@@ -1469,7 +1478,7 @@ struct Medium {
     if (!plainOne && !gnlse && tuneWanted(a, nInst)) {
       const TuneChoice c = autotune(k->kind, k->key, a, nInst, ff ? &ffT : nullptr);
       if (c.R != 0) {
-        k = findKernel(k->kind, k->key, c.R);
+        k = findKernelFn(c.fn);
         a.plan = make_plan((int)N, c.R);
         a.R = c.R;
         s = schedule(k, nInst, c.R, c.cta, c.ipcMul);
@@ -1480,6 +1489,10 @@ struct Medium {
     if (plainOne) s.grid = 1;
     lastSchedule = s;
     lastR = a.R;
+    {
+      cudaFuncAttributes fa;
+      lastRegs = cudaFuncGetAttributes(&fa, k->fn) == cudaSuccess ? fa.numRegs : 0;
+    }
     a.ipc = s.ipc;
     a.work = nullptr;
     const bool counter = !plainOne && (long long)s.grid < (nInst + s.ipc - 1) / s.ipc;
@@ -2785,6 +2798,7 @@ nlm_status nlm_last_schedule(const nlm_medium* h, int* values) {
     values[4] = m->lastSchedule.ctas;
     values[5] = m->lastTuned;
     values[6] = (int)m->tuneTrials;
+    values[7] = m->lastRegs;
   });
 }
 

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
 // of the (2M)x(2M) real matrix over (Re a0, Im a0, Re a1, ...).
 // --------------------------------------------------------------------------------------------
 template <int M, int R>
-__global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs a) {
+__device__ __forceinline__ void linear_body(const PropArgs& a) {
   constexpr int D = 2 * M, E = D * D;
   extern __shared__ double2 smem[];
   const FFTPlanH& plan = a.plan;
@@ -319,6 +319,19 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs
     store_output<M, R>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
     __syncthreads();
   }
+}
+
+template <int M, int R>
+__global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs a) {
+  linear_body<M, R>(a);
+}
+
+// The same kernel compiled for 128-thread CTAs with at least MINB of them resident per SM: fewer
+// registers per thread, more warps to hide the shared-memory phases of the transforms.  The
+// autotuner times it against k_propagate_linear where a CTA has 128 threads.
+template <int M, int R, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_propagate_linear_occ(const PropArgs a) {
+  linear_body<M, R>(a);
 }
 
 // --------------------------------------------------------------------------------------------

@@ -22,7 +22,7 @@ namespace nlm {
 //   nZ = 1:         s = 1 is inverse FFT, forward FFT, exp(-i dz/2 D)/N (no propagator)
 //   time-domain output: one more inverse FFT.
 template <int R, int SMALL>
-__global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropArgs a, const FFTables f) {
+__device__ __forceinline__ void linear_ff_body(const PropArgs& a, const FFTables& f) {
   extern __shared__ float4 fsm[];
   __shared__ long long s_group;
   const FFTPlanH& plan = a.plan;
@@ -95,6 +95,18 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropA
   }
 }
 
+template <int R, int SMALL>
+__global__ void __launch_bounds__(kMaxThreads) k_propagate_linear_ff(const PropArgs a, const FFTables f) {
+  linear_ff_body<R, SMALL>(a, f);
+}
+
+// 128-thread CTAs with at least MINB resident per SM (fewer registers, more warps); an autotuner
+// candidate where a CTA has 128 threads.
+template <int R, int SMALL, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_propagate_linear_ff_occ(const PropArgs a, const FFTables f) {
+  linear_ff_body<R, SMALL>(a, f);
+}
+
 constexpr int kMaxSplitSegs = 8;
 struct SplitBatch {
   SplitSeg seg[kMaxSplitSegs];
@@ -138,6 +150,13 @@ void add_kernels_ff(std::vector<KernelEntry>& t) {
   t.push_back({kKindLinearFF, 1 + 10 * 1, 8, (const void*)k_propagate_linear_ff<8, 1>});
   t.push_back({kKindLinearFF, 1 + 10 * 2, 8, (const void*)k_propagate_linear_ff<8, 2>});
   t.push_back({kKindLinearFF, 1 + 10 * 4, 8, (const void*)k_propagate_linear_ff<8, 4>});
+  // autotuner candidates: 128-thread CTAs with 5 or 6 resident per SM (96 / 80 registers)
+  t.push_back({kKindLinearFF, 1 + 10 * 1, 8, (const void*)k_propagate_linear_ff_occ<8, 1, 5>});
+  t.push_back({kKindLinearFF, 1 + 10 * 2, 8, (const void*)k_propagate_linear_ff_occ<8, 2, 5>});
+  t.push_back({kKindLinearFF, 1 + 10 * 4, 8, (const void*)k_propagate_linear_ff_occ<8, 4, 5>});
+  t.push_back({kKindLinearFF, 1 + 10 * 1, 8, (const void*)k_propagate_linear_ff_occ<8, 1, 6>});
+  t.push_back({kKindLinearFF, 1 + 10 * 2, 8, (const void*)k_propagate_linear_ff_occ<8, 2, 6>});
+  t.push_back({kKindLinearFF, 1 + 10 * 4, 8, (const void*)k_propagate_linear_ff_occ<8, 4, 6>});
 }
 
 }  // namespace nlm

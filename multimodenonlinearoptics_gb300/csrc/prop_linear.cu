@@ -8,6 +8,9 @@ namespace nlm {
 void add_kernels_linear(std::vector<KernelEntry>& t) {
   t.push_back({kKindLinear, 1, 8, (const void*)k_propagate_linear<1, 8>});
   t.push_back({kKindLinear, 1, 16, (const void*)k_propagate_linear<1, 16>});
+  // autotuner candidates: 128-thread CTAs with 5 or 6 resident per SM (96 / 80 registers)
+  t.push_back({kKindLinear, 1, 8, (const void*)k_propagate_linear_occ<1, 8, 5>});
+  t.push_back({kKindLinear, 1, 8, (const void*)k_propagate_linear_occ<1, 8, 6>});
   t.push_back({kKindLinear, 2, 8, (const void*)k_propagate_linear<2, 8>});
   t.push_back({kKindLinear, 4, 4, (const void*)k_propagate_linear<4, 4>});
   // linear (pump-driven) solvers: their RK4 step is real-linear in the signal

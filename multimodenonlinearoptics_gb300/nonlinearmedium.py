@@ -340,10 +340,11 @@ class _NonlinearMedium:
         _check(_lib.nlm_set_stream(self._h(), ctypes.c_void_p(stream_handle)))
 
     def _last_schedule(self):
-        """Launch shape of the last propagation (R, ipc, grid, block, CTAs per SM, tuned, trials)."""
-        v = (ctypes.c_int * 7)()
+        """Launch shape of the last propagation (R, ipc, grid, block, CTAs per SM, tuned, trials,
+        registers per thread of the kernel variant)."""
+        v = (ctypes.c_int * 8)()
         _check(_lib.nlm_last_schedule(self._h(), v))
-        return dict(zip(("R", "ipc", "grid", "block", "cta_per_sm", "tuned", "trials"), list(v)))
+        return dict(zip(("R", "ipc", "grid", "block", "cta_per_sm", "tuned", "trials", "registers"), list(v)))
 
     def _graph_stats(self):
         """(captures, replays) of the CUDA graphs of this medium's batched propagations."""
