@@ -2499,10 +2499,18 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (size_t k : fused) bySolver[ms[k]->solver].push_back(k);
     for (auto& kv : bySolver) {
       std::vector<size_t>& ks = kv.second;
+      // pump-driven solvers: each medium's per-point RK4 matrices, built on its own stream (the builds
+      // of the media overlap, each one parallel over all steps and points)
+      std::vector<bool> withProp(n_media, false);
       for (size_t k : ks) {
-        ms[k]->ensureDevice();
-        ck(cudaStreamSynchronize(ms[k]->stream), "medium stream");
+        Medium* m = ms[k];
+        m->ensureDevice();
+        if (m->linearSolver() && m->usePropagator != 0 && m->nZ > 1 && m->propagatorBytes() <= 16e9) {
+          m->buildPropagator(8);
+          withProp[k] = true;
+        }
       }
+      for (size_t k : ks) ck(cudaStreamSynchronize(ms[k]->stream), "medium stream");
       // largest first (cost ~ nZSteps * modes * N log N)
       std::sort(ks.begin(), ks.end(), [&](size_t x, size_t y) {
         auto cost = [&](Medium* m) { return (double)m->nZ * m->nSignal * m->N * std::log2((double)m->N); };
@@ -2540,6 +2548,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
         a.out = g_ragged.out.p + oo;
         a.outStride = (long long)m->nSignal * m->N;
+        a.prop = withProp[ks[q]] ? m->prop.p : nullptr;
         items[q] = a;
         outOff[q] = oo;
         io += m->N;

@@ -6,7 +6,10 @@
 // work counter.  A CTA is sized for the largest grid of the set; for a smaller grid the threads past
 // N/R take part in the barriers only.  The RK4 step is the solver's DiffEq evaluated per point
 // (src/_NonlinearMedium.hpp:204-218 with solvers/*.cpp DiffEq), the dispersion half of the step is the
-// register/shared-memory Stockham transform pair.
+// register/shared-memory Stockham transform pair.  For pump-driven (linear) solvers the engine passes
+// each medium's precomputed per-point RK4 matrices (PropArgs::prop, built in parallel over all steps
+// and points before the launch), so the sequential march does a small matrix-vector product per point
+// instead of the four stage evaluations.
 #include <vector>
 
 #include "nlm_propagate.cuh"
@@ -58,7 +61,35 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_ragged(const PropArgs
     }
     for (int i = 1; i < a.nZ; i++) {
       const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-      if (act) {
+      if (act && a.prop) {
+        // pump-driven solvers: the RK4 step as its per-point real (2M)x(2M) matrix, stored as pairs
+        // (row r, columns 2c and 2c+1) at [step][r * M + c][N]
+        constexpr int D = 2 * M;
+        const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (D * D / 2) * N;
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          double in[D], outv[D];
+#pragma unroll
+          for (int m = 0; m < M; m++) {
+            in[2 * m] = x[m][v].x;
+            in[2 * m + 1] = x[m][v].y;
+          }
+#pragma unroll
+          for (int r = 0; r < D; r++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int cc = 0; cc < D / 2; cc++) {
+              const double2 e = __ldg(mat + (long long)(r * (D / 2) + cc) * N + t);
+              acc = fma(e.x, in[2 * cc], acc);
+              acc = fma(e.y, in[2 * cc + 1], acc);
+            }
+            outv[r] = acc;
+          }
+#pragma unroll
+          for (int m = 0; m < M; m++) x[m][v] = make_double2(outv[2 * m], outv[2 * m + 1]);
+        }
+      } else if (act) {
 #pragma unroll
         for (int v = 0; v < R; v++) {
           const int t = j + v * T;

@@ -8,9 +8,12 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-9
 
 
-def test_ragged_launch_matches_oracle(nlm, oracle):
-    import bench
-    params = bench.ragged_media_params(seed=11, count=6)
+@pytest.mark.parametrize("use_prop", [1, 0])
+def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
+    """With use_prop, every (pump-driven) medium's RK4 matrices are built before the one launch (one
+    build launch per medium); without, the launch evaluates the DiffEq."""
+    from multimodenonlinearoptics_gb300.workloads import ragged_media_params
+    params = ragged_media_params(seed=11, count=6)
     media, refs, ins = [], [], []
     for kw, doms, pump, sig in params:
         kw = dict(kw, zPrecision=max(10, kw["zPrecision"] // 20))   # fewer steps for the oracle
@@ -29,8 +32,11 @@ def test_ragged_launch_matches_oracle(nlm, oracle):
     media[-1].runPumpSimulation()
     refs[-1].run_pump_simulation()
     ins.append(cases.signal_input("Chi2PDC", 64, 1, seed=3))
+    for m in media:
+        m._set_schedule(use_propagator=-1 if use_prop else 0)
     outs = nlm.ragged_batch(media, ins)
-    assert sum(m._launch_count() for m in media) == 2     # one launch per solver in the set
+    # one launch per solver in the set (plus the propagator builds)
+    assert sum(m._launch_count() for m in media) == 2 + (len(media) if use_prop else 0)
     for m, r, x, o in zip(media, refs, ins, outs):
         f, _ = r.propagate(x[None, :], False, 0)
         assert cases.rel_l2(o, f[0]) < TOL
