@@ -226,6 +226,10 @@ nlm_status nlm_set_schedule(nlm_medium* m, int cta_per_sm, int use_propagator, i
  * autotuner trials this handle ran, and the registers per thread of the kernel variant.  No
  * counterpart in the reference. */
 nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
+/* 1 (default): a launch of at most SMs/4 propagations on a grid of 1024 to 8192 points spreads
+ * each propagation over a cluster of 4 CTAs (one per SM, four-step FFT through distributed
+ * shared memory); 0: one CTA per propagation.  No counterpart in the reference. */
+nlm_status nlm_set_cluster(nlm_medium* m, int enable);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float
  * (pairs of FP32 values, ~48-bit significand, on the FP32 units).  Other paths stay FP64.

@@ -1389,6 +1389,80 @@ struct Medium {
     propBuilds++;
   }
 
+  // ---- cluster-distributed propagation (prop_cluster.cu) -------------------------------------
+  static constexpr int kClusterSize = 4;   // CTAs per propagation; also the points per thread
+  int useCluster = 1;
+
+  const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
+    if (!useCluster || plainOne || a.ckpt || a.inKind != 1 || solver == kChi3GNLSE) return nullptr;
+    if (!is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return nullptr;
+    if (nInst * kClusterSize > smCount()) return nullptr;
+    return findKernel(kKindCluster, solver, kClusterSize);
+  }
+
+  void launchCluster(const KernelEntry* k, PropArgs a, long long nInst) {
+    constexpr int C = kClusterSize;
+    const int M = (int)N / C;
+    a.plan = make_plan(M, C);
+    a.R = C;
+    a.nInst = nInst;
+    a.ipc = 1;
+    a.work = nullptr;
+    const int T = a.plan.T;
+    const size_t smem = (size_t)5 * M * sizeof(double2);   // M-point twiddles x2, exchange buffer, 2 x C x T receive
+    int dev = 0, optin = 0;
+    ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    if ((int)smem > optin - (int)fa.sharedSizeBytes) throw Unsupported("grid too large for the cluster kernel");
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
+       "smem attribute");
+    const long long clusters = std::min<long long>(nInst, smCount() / C);
+    lastSchedule = Schedule{(int)(C * clusters), T, 1, smem, 1, 1};
+    lastR = C;
+    lastTuned = 0;
+    lastRegs = fa.numRegs;
+    auto record = [&] {
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)(C * clusters));
+      cfg.blockDim = dim3((unsigned)T);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = C;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      void* args[] = {(void*)&a};
+      ck(cudaLaunchKernelExC(&cfg, k->fn, args), "propagate (cluster)");
+    };
+    if (timeKernels) {
+      if (!ev0) ck(cudaEventCreate(&ev0), "event");
+      if (!ev1) ck(cudaEventCreate(&ev1), "event");
+      ck(cudaEventRecord(ev0, stream), "event");
+    }
+    if (useGraph) {
+      GraphKey key;
+      add_prop_key(key, a);
+      key.add(k->fn).add(clusters).add(smem);
+      graphs.run(key, stream, record);
+    } else {
+      record();
+    }
+    launches++;
+    if (timeKernels) {
+      ck(cudaEventRecord(ev1, stream), "event");
+      ck(cudaEventSynchronize(ev1), "event");
+      float ms = 0;
+      ck(cudaEventElapsedTime(&ms, ev0, ev1), "event");
+      kernelMs += ms;
+      kernelCount++;
+    }
+  }
+
   // Double-float path: the FP64 tables and propagator are split into float-float copies once
   // (and again after every rebuild of the propagator).
   bool wantFF(int R, const PropArgs& a) const {
@@ -1447,6 +1521,16 @@ struct Medium {
     const KernelEntry* k = nullptr;
     bool gnlse = solver == kChi3GNLSE, ff = false;
     FFTables ffT{};
+    // A few propagations on a large grid: each one spread over a cluster of kClusterSize CTAs
+    if (const KernelEntry* kc = clusterKernel(a, nInst, plainOne)) {
+      if (linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+        buildPropagator(R);
+        a.prop = prop.p;
+      }
+      launchCluster(kc, a, nInst);
+      if (tail) tail();
+      return;
+    }
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
     } else if (allowPropagator && wantPropagator(nInst)) {
@@ -2785,6 +2869,14 @@ nlm_status nlm_set_schedule(nlm_medium* h, int cta_per_sm, int use_propagator, i
     m->ctaPerSM = cta_per_sm;
     m->usePropagator = use_propagator;
     m->useGraph = use_graph;
+  });
+}
+
+nlm_status nlm_set_cluster(nlm_medium* h, int enable) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->useCluster = enable ? 1 : 0;
+    for (Medium* c : m->media) c->useCluster = m->useCluster;
   });
 }
 

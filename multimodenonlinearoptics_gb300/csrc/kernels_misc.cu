@@ -18,6 +18,7 @@ void add_kernels_ragged(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_ff(std::vector<KernelEntry>& t);
 void add_kernels_direct_c(std::vector<KernelEntry>& t);
+void add_kernels_cluster(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -32,6 +33,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_adjoint_gnlse(table);
     add_kernels_ff(table);
     add_kernels_direct_c(table);
+    add_kernels_cluster(table);
   });
   *count = (int)table.size();
   return table.data();

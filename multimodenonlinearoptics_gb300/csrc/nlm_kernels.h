@@ -84,7 +84,8 @@ enum KernelKind : int {
   kKindBuildProp = 3,  // k_build_propagator<Solver>         key = solver id, R = 0
   kKindAdjoint = 4,    // k_adjoint_pdc<R>                   key = solver id; args (PropArgs, AdjArgs)
   kKindRagged = 5,     // k_propagate_ragged<Solver, R>      key = solver id; args (items, nItems, work)
-  kKindLinearFF = 6    // k_propagate_linear_ff<R, SMALL>    key = M + 10 SMALL; args (PropArgs, FFTables)
+  kKindLinearFF = 6,   // k_propagate_linear_ff<R, SMALL>    key = M + 10 SMALL; args (PropArgs, FFTables)
+  kKindCluster = 7     // k_propagate_cluster<Solver, C>     key = solver id, R = C; cluster launch
 };
 
 // Float-float copies (float4 {re.hi, re.lo, im.hi, im.lo} per complex value) of the tables of a

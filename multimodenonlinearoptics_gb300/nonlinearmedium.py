@@ -72,6 +72,7 @@ def _load():
         "nlm_device_available": (i, []),
         "nlm_set_schedule": (i, [vp, i, i, i]),
         "nlm_set_precision": (i, [vp, i]),
+        "nlm_set_cluster": (i, [vp, i]),
         "nlm_graph_stats": (i, [vp, P(ctypes.c_long), P(ctypes.c_long)]),
         "nlm_last_schedule": (i, [vp, P(i)]),
         "nlm_last_launch_count": (i, [vp, P(ctypes.c_long)]),
@@ -317,6 +318,10 @@ class _NonlinearMedium:
     # -- engine controls (no counterpart in the reference) ------------------------------------
     def _set_schedule(self, cta_per_sm=0, use_propagator=-1, use_graph=1):
         _check(_lib.nlm_set_schedule(self._h(), int(cta_per_sm), int(use_propagator), int(use_graph)))
+
+    def _set_cluster(self, enable):
+        """Spread each propagation of small launches on large grids over a 4-CTA cluster (default on)."""
+        _check(_lib.nlm_set_cluster(self._h(), int(bool(enable))))
 
     def _set_precision(self, precision):
         """"f64" (default) or "ff": double-float arithmetic (FP32 pairs, ~48-bit significand) for the

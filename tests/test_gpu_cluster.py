@@ -1,0 +1,74 @@
+"""Propagations spread over a 4-CTA cluster (four-step FFT through distributed shared memory): the
+full grids of runSignalSimulation and small batches on grids of 1024 to 8192 points, against the
+oracle and against the one-CTA kernels."""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+PDC = dict(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, pulseType=0, beta1=0.2, beta1s=2, beta3=0.05,
+           beta3s=0.1, diffBeta0=0.4, tMax=40, zPrecision=8, poling=[1, 2, 1])
+SFG = dict(relativeLength=1, nlLength=0.8, nlLengthOrig=1.2, beta2=0.5, beta2s=-0.3, beta2o=0.2, pulseType=0,
+           beta1=0.1, beta1s=1, beta1o=-0.5, beta3=0, beta3s=0.05, beta3o=0.02, diffBeta0=1.3, tMax=20,
+           zPrecision=8, poling=[2, 1, 3, 1])
+CHI3 = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0.02, tMax=40, zPrecision=12)
+SHG = dict(relativeLength=1, nlLengthH=0.9, nlLengthP=1.1, beta2h=0.3, beta2p=-0.2, beta1h=0.5, beta1p=-0.1,
+           diffBeta0=0.4, tMax=20, zPrecision=8, poling=[1, 1, 2])
+MEDIA = {"Chi2PDC": PDC, "Chi2SFG": SFG, "Chi3": CHI3, "Chi2SHG": SHG}
+
+
+@pytest.mark.parametrize("n", [1024, 2048, 4096, 8192])
+@pytest.mark.parametrize("name", ["Chi2PDC", "Chi3"])
+def test_cluster_signal_grids_match_oracle(nlm, oracle, name, n):
+    kw = dict(MEDIA[name], tPrecision=n)
+    med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    a = cases.noise(np.random.default_rng(n), n, 0.2)
+    for in_time in (True, False):
+        med.runSignalSimulation(a, in_time)
+        ref.run_signal_simulation(a, in_time)
+        sched = med._last_schedule()
+        assert sched["R"] == 4 and sched["grid"] == 4 and sched["block"] == n // 16
+        assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
+        assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
+
+
+@pytest.mark.parametrize("name", ["Chi2SFG", "Chi2SHG"])
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_cluster_two_modes_match_oracle(nlm, oracle, name, n):
+    kw = dict(MEDIA[name], tPrecision=n)
+    med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw)
+    fnl = name in cases.FULLY_NONLINEAR
+    if not fnl:
+        med.runPumpSimulation()
+        ref.run_pump_simulation()
+    a = cases.noise(np.random.default_rng(3), n, 0.2)
+    med.runSignalSimulation(a)
+    ref.run_signal_simulation(a)
+    assert med._last_schedule()["grid"] == 4
+    for m in range(2):
+        assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
+        assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL
+    x = cases.noise(np.random.default_rng(4), 3 * n, 0.2).reshape(3, n)
+    out = med.batchSignalSimulation(x, inTimeDomain=True) if fnl else med.batchSignalSimulation(x, True, False)
+    want = ref.batch_signal_simulation(x, True) if fnl else ref.batch_signal_simulation(x, True, False)
+    assert med._last_schedule()["grid"] == 12
+    assert cases.rel_l2(out, want) < TOL
+
+
+def test_cluster_equals_one_cta_kernels(nlm):
+    kw = dict(PDC, tPrecision=2048, zPrecision=40)
+    a = cases.noise(np.random.default_rng(9), 2048, 0.3)
+    res = []
+    for use in (1, 0):
+        med = nlm.Chi2PDC(**kw)
+        med._set_cluster(use)
+        med.runPumpSimulation()
+        med.runSignalSimulation(a)
+        assert (med._last_schedule()["grid"] == 4) == bool(use)
+        res.append((med.signalFreq.copy(), med.signalTime.copy()))
+    assert cases.rel_l2(res[0][0], res[1][0]) < 1e-12 and cases.rel_l2(res[0][1], res[1][1]) < 1e-12

@@ -21,8 +21,11 @@ def _batch_pair(med, ref, rows, seed, fnl=False):
 
 
 def test_largest_single_mode_grid(nlm, oracle):
+    """The one-CTA kernels with sixteen points per thread (few propagations on this grid otherwise
+    run on 4-CTA clusters, covered by test_gpu_cluster.py)."""
     kw = dict(PDC, tPrecision=8192)
     med, ref = nlm.Chi2PDC(**kw), oracle.Chi2PDC(**kw)
+    med._set_cluster(0)
     med.runPumpSimulation()
     ref.run_pump_simulation()
     assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
