@@ -306,6 +306,34 @@ def measure_configs(nlm, torch, cpu=True):
         o1.run_pump_simulation()
         o1.run_signal_simulation(sig)
         res["chi3_pump_signal_n512"]["cpu_oracle_latency_ms"] = 1e3 * (time.perf_counter() - t0)
+    # single propagations on large grids (runSignalSimulation, full grids): one CTA against a
+    # 4-CTA cluster per propagation
+    single = {}
+    for n in (2048, 8192):
+        kw = dict(CONFIG, tPrecision=n, zPrecision=500)
+        a = (np.random.default_rng(n).standard_normal(n) + 0j) * 0.1
+        row = {"n_freqs": n}
+        for use, label in ((0, "one_cta_ms"), (1, "cluster_ms")):
+            m = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kw)
+            m._set_cluster(use)
+            m.runPumpSimulation()
+            m.runSignalSimulation(a)
+            best = float("inf")
+            for _ in range(3):
+                t0 = time.perf_counter()
+                m.runSignalSimulation(a)
+                best = min(best, time.perf_counter() - t0)
+            row[label] = 1e3 * best
+            row["z_steps"] = m._dims["nZSteps"]
+        if cpu and n == 2048:
+            from oracle import nlm_oracle as O
+            o = O.Chi2PDC(poling=np.ones(N_DOMAINS), **kw)
+            o.run_pump_simulation()
+            t0 = time.perf_counter()
+            o.run_signal_simulation(a)
+            row["cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t0)
+        single["chi2pdc_run_signal_n%d" % n] = row
+    res["single_propagation"] = single
     # 3. 64 ragged Chi2SFG media in one launch
     params = ragged_media_params()
     media = []
