@@ -351,6 +351,14 @@ def measure_configs(nlm, torch, cpu=True):
         t0 = time.perf_counter()
         nlm.ragged_batch(media, ins)
         wall.append(time.perf_counter() - t0)
+    wall_one = []
+    for m in media:
+        m._set_cluster(0)
+    nlm.ragged_batch(media, ins)
+    for _ in range(2):
+        t0 = time.perf_counter()
+        nlm.ragged_batch(media, ins)
+        wall_one.append(time.perf_counter() - t0)
     for m in media:
         m._set_schedule(use_propagator=0)
     nlm.ragged_batch(media, ins)
@@ -362,7 +370,10 @@ def measure_configs(nlm, torch, cpu=True):
     res["ragged_chi2sfg_64_media"] = {"gpu_wall_ms": 1e3 * min(wall), "media": len(media), "total_z_steps": steps,
                                       "n_freqs": sorted({m._dims["nFreqs"] for m in media}),
                                       "includes": "the per-medium RK4 matrix builds (pumps rerun before each call)",
-                                      "gpu_wall_ms_diffeq_form": 1e3 * min(wall_direct)}
+                                      "form": "the costliest media on grids of 1024+ points as 4-CTA cluster "
+                                              "propagations beside one ragged launch of the others",
+                                      "gpu_wall_ms_one_cta_per_medium": 1e3 * min(wall_one),
+                                      "gpu_wall_ms_one_cta_diffeq_form": 1e3 * min(wall_direct)}
     if cpu:
         from oracle import nlm_oracle as O
         t0 = time.perf_counter()

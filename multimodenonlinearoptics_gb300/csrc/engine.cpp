@@ -2547,6 +2547,7 @@ nlm_status nlm_batch_device(nlm_medium* h, const void* inputs_dev, size_t rows, 
 struct RaggedWorkspace {
   std::mutex mu;
   nlm::DevBuf<double2> in, out;
+  nlm::DevBuf<double2> cin, cout;   // inputs and outputs of the media run as cluster propagations
   nlm::DevBuf<nlm::PropArgs> items;
   nlm::DevBuf<unsigned long long> counter;
 };
@@ -2578,6 +2579,18 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     }
     if (fused.empty()) return;
     std::lock_guard<std::mutex> lock(g_ragged.mu);
+    std::vector<cudaStream_t> clusterSync;   // streams holding the read-back of cluster propagations
+    {
+      // room for every medium, so cluster propagations of different solver groups never share it
+      size_t inAll = 0, outAll = 0;
+      for (size_t k : fused) {
+        inAll += ms[k]->N;
+        outAll += (size_t)ms[k]->nSignal * ms[k]->N;
+      }
+      g_ragged.cin.reserve(inAll);
+      g_ragged.cout.reserve(outAll);
+    }
+    size_t cio = 0, coo = 0;
     // one launch per solver present in the set
     std::map<int, std::vector<size_t>> bySolver;
     for (size_t k : fused) bySolver[ms[k]->solver].push_back(k);
@@ -2600,6 +2613,80 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         auto cost = [&](Medium* m) { return (double)m->nZ * m->nSignal * m->N * std::log2((double)m->N); };
         return cost(ms[x]) > cost(ms[y]);
       });
+      // The costliest media on grids of 1024+ points run as cluster-distributed propagations (4 SMs
+      // each, on their own streams, concurrently with the ragged launch of the others), as long as
+      // clusters and the remaining media (one SM each) fit on the GPU.
+      std::vector<size_t> clustered;
+      {
+        const int sms = Medium::smCount();
+        size_t q = 0;
+        while (q < ks.size()) {
+          Medium* m = ms[ks[q]];
+          const size_t rest = ks.size() - q - 1;
+          const bool eligible = m->useCluster && is_pow2((int)m->N) && m->N >= 1024 && m->N <= (uint)kMaxFFT &&
+                                m->findKernel(kKindCluster, m->solver, Medium::kClusterSize) != nullptr;
+          if (!eligible || (clustered.size() + 1) * Medium::kClusterSize + rest > (size_t)sms) break;
+          clustered.push_back(ks[q]);
+          q++;
+        }
+        ks.erase(ks.begin(), ks.begin() + q);
+      }
+      if (!clustered.empty()) {
+        Medium* lead0 = ms[clustered[0]];
+        cudaStream_t st0 = lead0->stream;
+        size_t io = cio;
+        for (size_t k : clustered) {
+          ck(cudaMemcpyAsync(g_ragged.cin.p + io, inputs[k], ms[k]->N * sizeof(double2), cudaMemcpyHostToDevice, st0),
+             "ragged input");
+          io += ms[k]->N;
+        }
+        cudaEvent_t evIn = nullptr;
+        ck(cudaEventCreateWithFlags(&evIn, cudaEventDisableTiming), "event");
+        ck(cudaEventRecord(evIn, st0), "event");
+        std::vector<cudaEvent_t> done;
+        size_t oo = coo;
+        io = cio;
+        for (size_t k : clustered) {
+          Medium* m = ms[k];
+          ck(cudaStreamWaitEvent(m->stream, evIn, 0), "stream wait");
+          PropArgs a = m->baseArgs(m->chooseR());
+          a.inKind = 1;
+          a.inTime = in_time_domain ? 1 : 0;
+          a.in = g_ragged.cin.p + io;
+          a.inStride = (long long)m->N;
+          a.inChannels = 1;
+          a.inputMode = 0;
+          a.nOut = (int)m->nSignal;
+          for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
+          a.out = g_ragged.cout.p + oo;
+          a.outStride = (long long)m->nSignal * m->N;
+          m->propagate(a, 1, true);
+          cudaEvent_t ev = nullptr;
+          ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+          ck(cudaEventRecord(ev, m->stream), "event");
+          done.push_back(ev);
+          io += m->N;
+          oo += (size_t)m->nSignal * m->N;
+        }
+        // the outputs are read back on st0 after every cluster propagation (and, below, while the
+        // ragged launch of the other media runs)
+        cio = io;
+        const size_t cooEnd = oo;
+        for (cudaEvent_t ev : done) ck(cudaStreamWaitEvent(st0, ev, 0), "stream wait");
+        oo = coo;
+        for (size_t k : clustered) {
+          Medium* m = ms[k];
+          ck(cudaMemcpyAsync(outputs[k], g_ragged.cout.p + oo, (size_t)m->nSignal * m->N * sizeof(double2),
+                             cudaMemcpyDeviceToHost, st0),
+             "ragged output");
+          oo += (size_t)m->nSignal * m->N;
+        }
+        coo = cooEnd;
+        clusterSync.push_back(st0);
+        for (cudaEvent_t ev : done) cudaEventDestroy(ev);
+        cudaEventDestroy(evIn);
+      }
+      if (ks.empty()) continue;
       size_t inTot = 0, outTot = 0, maxN = 0;
       for (size_t k : ks) {
         inTot += ms[k]->N;
@@ -2685,6 +2772,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       ck(cudaStreamSynchronize(st), "ragged batch");
     }
+    for (cudaStream_t st : clusterSync) ck(cudaStreamSynchronize(st), "ragged batch (clusters)");
   });
 }
 

@@ -34,6 +34,7 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
     ins.append(cases.signal_input("Chi2PDC", 64, 1, seed=3))
     for m in media:
         m._set_schedule(use_propagator=-1 if use_prop else 0)
+        m._set_cluster(0)                                   # every medium in the ragged launch
     outs = nlm.ragged_batch(media, ins)
     # one launch per solver in the set (plus the propagator builds)
     assert sum(m._launch_count() for m in media) == 2 + (len(media) if use_prop else 0)
@@ -46,3 +47,30 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
     for m, r, x, o in zip(media[:3], refs[:3], ins[:3], outs_t):
         _, t = r.propagate(x[None, :], True, 0)
         assert cases.rel_l2(o, t[0]) < TOL
+
+
+def test_ragged_set_with_cluster_propagations(nlm, oracle):
+    """The costliest media on grids of 1024+ points run as 4-CTA cluster propagations beside the ragged
+    launch of the others; every output matches the oracle."""
+    kw0 = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=0.4, beta2s=-0.3, beta2o=0, beta1=0, beta1s=1.2,
+               beta1o=0, beta3=0, beta3s=0.05, beta3o=0, diffBeta0=0, tMax=10)
+    rng = np.random.default_rng(21)
+    media, refs, ins = [], [], []
+    for n, zp in ((2048, 14), (1024, 12), (256, 10), (128, 8), (1024, 6)):
+        kw = dict(kw0, tPrecision=n, zPrecision=zp)
+        t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
+        pump = np.exp(-t ** 2 / 2)
+        m = nlm.Chi2SFG(customPump=pump, poling=[3, 4, 3], **kw)
+        r = oracle.Chi2SFG(customPump=pump, poling=[3, 4, 3], **kw)
+        m.runPumpSimulation()
+        r.run_pump_simulation()
+        media.append(m)
+        refs.append(r)
+        ins.append(cases.noise(rng, n, 1e-2))
+    outs = nlm.ragged_batch(media, ins)
+    for m in media:
+        on_cluster = m._last_schedule()["grid"] == 4 and m._last_schedule()["R"] == 4
+        assert on_cluster == (m._dims["nFreqs"] >= 1024)
+    for r, x, o in zip(refs, ins, outs):
+        f, _ = r.propagate(x[None, :], False, 0)
+        assert cases.rel_l2(o, f[0]) < TOL
