@@ -1409,13 +1409,17 @@ struct Medium {
     a.ipc = 1;
     a.work = nullptr;
     const int T = a.plan.T;
-    const size_t smem = (size_t)5 * M * sizeof(double2);   // M-point twiddles x2, exchange buffer, 2 x C x T receive
+    const size_t need = (size_t)5 * M * sizeof(double2);   // M-point twiddles x2, exchange buffer, 2 x C x T receive
     int dev = 0, optin = 0;
     ck(cudaGetDevice(&dev), "device");
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
     ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
-    if ((int)smem > optin - (int)fa.sharedSizeBytes) throw Unsupported("grid too large for the cluster kernel");
+    const int dynMax = optin - (int)fa.sharedSizeBytes;
+    if ((int)need > dynMax) throw Unsupported("grid too large for the cluster kernel");
+    // each CTA alone on its SM (more than half the shared memory): a latency-bound march shares its
+    // SM's FP64 units with nothing else, e.g. with the CTAs of a ragged launch running beside it
+    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);
     ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
        "smem attribute");
     const long long clusters = std::min<long long>(nInst, smCount() / C);
@@ -2695,6 +2699,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       Medium* lead = ms[ks[0]];
       cudaStream_t st = lead->stream;
+      // N/4 threads per medium when the largest grid allows it (four warps from N = 512), else N/8
+      const KernelEntry* k4 = maxN / 4 <= 512 ? lead->findKernel(kKindRagged, kv.first, 4) : nullptr;
+      const KernelEntry* ke = k4 ? k4 : lead->findKernel(kKindRagged, kv.first, 8);
+      const int Rg = ke->R;
       g_ragged.in.reserve(inTot);
       g_ragged.out.reserve(outTot);
       g_ragged.items.reserve(ks.size());
@@ -2706,7 +2714,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         Medium* m = ms[ks[q]];
         ck(cudaMemcpyAsync(g_ragged.in.p + io, inputs[ks[q]], m->N * sizeof(double2), cudaMemcpyHostToDevice, st),
            "ragged input");
-        PropArgs a = m->baseArgs(8);
+        PropArgs a = m->baseArgs(Rg);
         a.nInst = 1;
         a.ipc = 1;
         a.inKind = 1;
@@ -2728,17 +2736,19 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       ck(cudaMemcpyAsync(g_ragged.items.p, items.data(), items.size() * sizeof(PropArgs), cudaMemcpyHostToDevice, st),
          "ragged items");
       ck(cudaMemsetAsync(g_ragged.counter.p, 0, sizeof(unsigned long long), st), "ragged counter");
-      const KernelEntry* ke = lead->findKernel(kKindRagged, kv.first, 8);
-      int block = (int)((maxN / 8 + 31) / 32 * 32);
-      const size_t smem = maxN * sizeof(double2);
+      int block = (int)((maxN / Rg + 31) / 32 * 32);
       int dev = 0, sms = 1, optin = 0;
       ck(cudaGetDevice(&dev), "device");
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
       cudaFuncAttributes fa;
       ck(cudaFuncGetAttributes(&fa, ke->fn), "kernel attributes");
-      ck(cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
-         "smem attribute");
+      const int dynMax = optin - (int)fa.sharedSizeBytes;
+      // One CTA per SM: every medium is a sequential march bound by its SM's FP64 units, so a second
+      // resident CTA (of this launch or of a cluster propagation running beside it) would only halve
+      // both.  Asking for more than half of the SM's shared memory keeps the others off.
+      const size_t smem = std::max<size_t>(maxN * sizeof(double2), (size_t)dynMax / 2 + 1024);
+      ck(cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
       if (block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
       int active = 0;
       ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, ke->fn, block, smem), "occupancy");

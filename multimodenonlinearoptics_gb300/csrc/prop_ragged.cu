@@ -158,6 +158,10 @@ void add_kernels_ragged(std::vector<KernelEntry>& t) {
   t.push_back({kKindRagged, kChi3, 8, (const void*)k_propagate_ragged<FChi3, 8>});
   t.push_back({kKindRagged, kChi2PDC, 8, (const void*)k_propagate_ragged<FChi2PDC, 8>});
   t.push_back({kKindRagged, kChi2SFG, 8, (const void*)k_propagate_ragged<FChi2SFG, 8>});
+  // four points per thread: N/4 threads per medium (all four schedulers of an SM from N = 512)
+  t.push_back({kKindRagged, kChi3, 4, (const void*)k_propagate_ragged<FChi3, 4>});
+  t.push_back({kKindRagged, kChi2PDC, 4, (const void*)k_propagate_ragged<FChi2PDC, 4>});
+  t.push_back({kKindRagged, kChi2SFG, 4, (const void*)k_propagate_ragged<FChi2SFG, 4>});
 }
 
 }  // namespace nlm
