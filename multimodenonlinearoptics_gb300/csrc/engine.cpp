@@ -2584,6 +2584,18 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     if (fused.empty()) return;
     std::lock_guard<std::mutex> lock(g_ragged.mu);
     std::vector<cudaStream_t> clusterSync;   // streams holding the read-back of cluster propagations
+    struct PendingCopy {
+      double* dst;
+      const double2* src;
+      size_t bytes;
+      cudaStream_t st;
+    };
+    std::vector<PendingCopy> pendingD2H;
+    auto flushD2H = [&] {
+      for (const PendingCopy& c : pendingD2H)
+        ck(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, c.st), "ragged output");
+      pendingD2H.clear();
+    };
     {
       // room for every medium, so cluster propagations of different solver groups never share it
       size_t inAll = 0, outAll = 0;
@@ -2677,12 +2689,13 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         cio = io;
         const size_t cooEnd = oo;
         for (cudaEvent_t ev : done) ck(cudaStreamWaitEvent(st0, ev, 0), "stream wait");
+        // The read-back into (pageable) host memory blocks the calling thread until the copy has run,
+        // i.e. until every cluster propagation has finished: it is issued after the ragged launch of
+        // the other media (below), so that launch runs beside the clusters.
         oo = coo;
         for (size_t k : clustered) {
           Medium* m = ms[k];
-          ck(cudaMemcpyAsync(outputs[k], g_ragged.cout.p + oo, (size_t)m->nSignal * m->N * sizeof(double2),
-                             cudaMemcpyDeviceToHost, st0),
-             "ragged output");
+          pendingD2H.push_back({outputs[k], g_ragged.cout.p + oo, (size_t)m->nSignal * m->N * sizeof(double2), st0});
           oo += (size_t)m->nSignal * m->N;
         }
         coo = cooEnd;
@@ -2690,7 +2703,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         for (cudaEvent_t ev : done) cudaEventDestroy(ev);
         cudaEventDestroy(evIn);
       }
-      if (ks.empty()) continue;
+      if (ks.empty()) {
+        flushD2H();
+        continue;
+      }
       size_t inTot = 0, outTot = 0, maxN = 0;
       for (size_t k : ks) {
         inTot += ms[k]->N;
@@ -2774,6 +2790,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         lead->kernelMs += ms_;
         lead->kernelCount++;
       }
+      flushD2H();   // the cluster propagations' outputs (the ragged launch is queued by now)
       for (size_t q = 0; q < ks.size(); q++) {
         Medium* m = ms[ks[q]];
         ck(cudaMemcpyAsync(outputs[ks[q]], g_ragged.out.p + outOff[q], (size_t)m->nSignal * m->N * sizeof(double2),
