@@ -2630,8 +2630,9 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         return cost(ms[x]) > cost(ms[y]);
       });
       // The costliest media on grids of 1024+ points run as cluster-distributed propagations (4 SMs
-      // each, on their own streams, concurrently with the ragged launch of the others), as long as
-      // clusters and the remaining media (one SM each) fit on the GPU.
+      // each, on their own streams, concurrently with the ragged launch of the others) while the
+      // clusters leave the ragged launch about one SM per two remaining media: it claims its media
+      // largest first from a work counter, so the smallest ones queue behind the others.
       std::vector<size_t> clustered;
       {
         const int sms = Medium::smCount();
@@ -2641,7 +2642,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
           const size_t rest = ks.size() - q - 1;
           const bool eligible = m->useCluster && is_pow2((int)m->N) && m->N >= 1024 && m->N <= (uint)kMaxFFT &&
                                 m->findKernel(kKindCluster, m->solver, Medium::kClusterSize) != nullptr;
-          if (!eligible || (clustered.size() + 1) * Medium::kClusterSize + rest > (size_t)sms) break;
+          if (!eligible || (clustered.size() + 1) * Medium::kClusterSize + (rest + 1) / 2 > (size_t)sms) break;
           clustered.push_back(ks[q]);
           q++;
         }
