@@ -144,6 +144,29 @@ struct DevBuf {
 
 static double2* d2(void* p) { return reinterpret_cast<double2*>(p); }
 
+// Page-locked host staging: copies from and to it are asynchronous (a copy from pageable memory
+// waits for earlier work before it starts, one to pageable memory blocks the caller until it ran).
+template <class T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void reserve(size_t count) {
+    if (count <= n && p) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return;
+    ck(cudaHostAlloc(reinterpret_cast<void**>(&p), count * sizeof(T), cudaHostAllocDefault), "cudaHostAlloc");
+    n = count;
+  }
+};
+
 // Launch sequences captured into CUDA graphs and replayed.  The key holds the bytes of every
 // host-side value the captured launches read (kernel arguments, grid shape, pointers), so a replay
 // is exactly the launch sequence it stands for; any change of a key byte captures a new graph.
@@ -2553,6 +2576,8 @@ struct RaggedWorkspace {
   nlm::DevBuf<double2> in, out;
   nlm::DevBuf<double2> cin, cout;   // inputs and outputs of the media run as cluster propagations
   nlm::DevBuf<nlm::PropArgs> items;
+  nlm::PinnedBuf<double2> hin, hout;   // host staging of every medium's input and output
+  nlm::PinnedBuf<nlm::PropArgs> hitems;
   nlm::DevBuf<unsigned long long> counter;
 };
 static RaggedWorkspace g_ragged;
@@ -2585,7 +2610,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     std::lock_guard<std::mutex> lock(g_ragged.mu);
     std::vector<cudaStream_t> clusterSync;   // streams holding the read-back of cluster propagations
     struct PendingCopy {
-      double* dst;
+      double2* dst;
       const double2* src;
       size_t bytes;
       cudaStream_t st;
@@ -2605,6 +2630,20 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       g_ragged.cin.reserve(inAll);
       g_ragged.cout.reserve(outAll);
+      g_ragged.hin.reserve(inAll);
+      g_ragged.hout.reserve(outAll);
+    }
+    // every input is staged in page-locked memory first, so no copy below waits on earlier work
+    std::vector<size_t> hinOff(n_media, 0), houtOff(n_media, 0);
+    {
+      size_t io = 0, oo = 0;
+      for (size_t k : fused) {
+        hinOff[k] = io;
+        houtOff[k] = oo;
+        std::memcpy(g_ragged.hin.p + io, inputs[k], ms[k]->N * sizeof(double2));
+        io += ms[k]->N;
+        oo += (size_t)ms[k]->nSignal * ms[k]->N;
+      }
     }
     size_t cio = 0, coo = 0;
     // one launch per solver present in the set
@@ -2653,7 +2692,8 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         cudaStream_t st0 = lead0->stream;
         size_t io = cio;
         for (size_t k : clustered) {
-          ck(cudaMemcpyAsync(g_ragged.cin.p + io, inputs[k], ms[k]->N * sizeof(double2), cudaMemcpyHostToDevice, st0),
+          ck(cudaMemcpyAsync(g_ragged.cin.p + io, g_ragged.hin.p + hinOff[k], ms[k]->N * sizeof(double2),
+                             cudaMemcpyHostToDevice, st0),
              "ragged input");
           io += ms[k]->N;
         }
@@ -2690,13 +2730,12 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         cio = io;
         const size_t cooEnd = oo;
         for (cudaEvent_t ev : done) ck(cudaStreamWaitEvent(st0, ev, 0), "stream wait");
-        // The read-back into (pageable) host memory blocks the calling thread until the copy has run,
-        // i.e. until every cluster propagation has finished: it is issued after the ragged launch of
-        // the other media (below), so that launch runs beside the clusters.
+        // read back after the ragged launch of the other media is queued (below)
         oo = coo;
         for (size_t k : clustered) {
           Medium* m = ms[k];
-          pendingD2H.push_back({outputs[k], g_ragged.cout.p + oo, (size_t)m->nSignal * m->N * sizeof(double2), st0});
+          pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
+                                (size_t)m->nSignal * m->N * sizeof(double2), st0});
           oo += (size_t)m->nSignal * m->N;
         }
         coo = cooEnd;
@@ -2729,7 +2768,8 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       size_t io = 0, oo = 0;
       for (size_t q = 0; q < ks.size(); q++) {
         Medium* m = ms[ks[q]];
-        ck(cudaMemcpyAsync(g_ragged.in.p + io, inputs[ks[q]], m->N * sizeof(double2), cudaMemcpyHostToDevice, st),
+        ck(cudaMemcpyAsync(g_ragged.in.p + io, g_ragged.hin.p + hinOff[ks[q]], m->N * sizeof(double2),
+                           cudaMemcpyHostToDevice, st),
            "ragged input");
         PropArgs a = m->baseArgs(Rg);
         a.nInst = 1;
@@ -2750,7 +2790,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         io += m->N;
         oo += (size_t)m->nSignal * m->N;
       }
-      ck(cudaMemcpyAsync(g_ragged.items.p, items.data(), items.size() * sizeof(PropArgs), cudaMemcpyHostToDevice, st),
+      g_ragged.hitems.reserve(items.size());
+      std::memcpy(g_ragged.hitems.p, items.data(), items.size() * sizeof(PropArgs));
+      ck(cudaMemcpyAsync(g_ragged.items.p, g_ragged.hitems.p, items.size() * sizeof(PropArgs), cudaMemcpyHostToDevice,
+                         st),
          "ragged items");
       ck(cudaMemsetAsync(g_ragged.counter.p, 0, sizeof(unsigned long long), st), "ragged counter");
       int block = (int)((maxN / Rg + 31) / 32 * 32);
@@ -2794,13 +2837,15 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       flushD2H();   // the cluster propagations' outputs (the ragged launch is queued by now)
       for (size_t q = 0; q < ks.size(); q++) {
         Medium* m = ms[ks[q]];
-        ck(cudaMemcpyAsync(outputs[ks[q]], g_ragged.out.p + outOff[q], (size_t)m->nSignal * m->N * sizeof(double2),
-                           cudaMemcpyDeviceToHost, st),
+        ck(cudaMemcpyAsync(g_ragged.hout.p + houtOff[ks[q]], g_ragged.out.p + outOff[q],
+                           (size_t)m->nSignal * m->N * sizeof(double2), cudaMemcpyDeviceToHost, st),
            "ragged output");
       }
       ck(cudaStreamSynchronize(st), "ragged batch");
     }
     for (cudaStream_t st : clusterSync) ck(cudaStreamSynchronize(st), "ragged batch (clusters)");
+    for (size_t k : fused)
+      std::memcpy(outputs[k], g_ragged.hout.p + houtOff[k], (size_t)ms[k]->nSignal * ms[k]->N * sizeof(double2));
   });
 }
 
