@@ -2688,24 +2688,16 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         ks.erase(ks.begin(), ks.begin() + q);
       }
       if (!clustered.empty()) {
-        Medium* lead0 = ms[clustered[0]];
-        cudaStream_t st0 = lead0->stream;
-        size_t io = cio;
-        for (size_t k : clustered) {
-          ck(cudaMemcpyAsync(g_ragged.cin.p + io, g_ragged.hin.p + hinOff[k], ms[k]->N * sizeof(double2),
-                             cudaMemcpyHostToDevice, st0),
-             "ragged input");
-          io += ms[k]->N;
-        }
-        cudaEvent_t evIn = nullptr;
-        ck(cudaEventCreateWithFlags(&evIn, cudaEventDisableTiming), "event");
-        ck(cudaEventRecord(evIn, st0), "event");
-        std::vector<cudaEvent_t> done;
-        size_t oo = coo;
-        io = cio;
+        // Each cluster propagation runs on its medium's own stream: input copy (page-locked source),
+        // propagation, and -- after the ragged launch of the other media is queued, below -- the
+        // read-back.  No stream waits on another: CUDA maps the streams onto a few hardware queues,
+        // and a cross-stream wait at the head of one would hold back whatever shares its queue.
+        size_t io = cio, oo = coo;
         for (size_t k : clustered) {
           Medium* m = ms[k];
-          ck(cudaStreamWaitEvent(m->stream, evIn, 0), "stream wait");
+          ck(cudaMemcpyAsync(g_ragged.cin.p + io, g_ragged.hin.p + hinOff[k], m->N * sizeof(double2),
+                             cudaMemcpyHostToDevice, m->stream),
+             "ragged input");
           PropArgs a = m->baseArgs(m->chooseR());
           a.inKind = 1;
           a.inTime = in_time_domain ? 1 : 0;
@@ -2718,30 +2710,14 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
           a.out = g_ragged.cout.p + oo;
           a.outStride = (long long)m->nSignal * m->N;
           m->propagate(a, 1, true);
-          cudaEvent_t ev = nullptr;
-          ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-          ck(cudaEventRecord(ev, m->stream), "event");
-          done.push_back(ev);
+          pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
+                                (size_t)m->nSignal * m->N * sizeof(double2), m->stream});
+          clusterSync.push_back(m->stream);
           io += m->N;
           oo += (size_t)m->nSignal * m->N;
         }
-        // the outputs are read back on st0 after every cluster propagation (and, below, while the
-        // ragged launch of the other media runs)
         cio = io;
-        const size_t cooEnd = oo;
-        for (cudaEvent_t ev : done) ck(cudaStreamWaitEvent(st0, ev, 0), "stream wait");
-        // read back after the ragged launch of the other media is queued (below)
-        oo = coo;
-        for (size_t k : clustered) {
-          Medium* m = ms[k];
-          pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
-                                (size_t)m->nSignal * m->N * sizeof(double2), st0});
-          oo += (size_t)m->nSignal * m->N;
-        }
-        coo = cooEnd;
-        clusterSync.push_back(st0);
-        for (cudaEvent_t ev : done) cudaEventDestroy(ev);
-        cudaEventDestroy(evIn);
+        coo = oo;
       }
       if (ks.empty()) {
         flushD2H();
