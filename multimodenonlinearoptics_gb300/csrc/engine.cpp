@@ -2675,17 +2675,18 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       std::vector<size_t> clustered;
       {
         const int sms = Medium::smCount();
-        size_t q = 0;
-        while (q < ks.size()) {
-          Medium* m = ms[ks[q]];
-          const size_t rest = ks.size() - q - 1;
+        std::vector<size_t> others;
+        for (size_t k : ks) {
+          Medium* m = ms[k];
           const bool eligible = m->useCluster && is_pow2((int)m->N) && m->N >= 1024 && m->N <= (uint)kMaxFFT &&
                                 m->findKernel(kKindCluster, m->solver, Medium::kClusterSize) != nullptr;
-          if (!eligible || (clustered.size() + 1) * Medium::kClusterSize + (rest + 1) / 2 > (size_t)sms) break;
-          clustered.push_back(ks[q]);
-          q++;
+          const size_t rest = ks.size() - clustered.size() - 1;   // the ragged launch's media if this one joins
+          if (eligible && (clustered.size() + 1) * Medium::kClusterSize + (rest + 1) / 2 <= (size_t)sms)
+            clustered.push_back(k);
+          else
+            others.push_back(k);   // still largest first
         }
-        ks.erase(ks.begin(), ks.begin() + q);
+        ks.swap(others);
       }
       if (!clustered.empty()) {
         // Each cluster propagation runs on its medium's own stream: input copy (page-locked source),
@@ -2790,7 +2791,11 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, ke->fn, block, smem), "occupancy");
       if (active < 1) throw Unsupported("ragged kernel does not fit on an SM");
       const int nItems = (int)ks.size();
-      const int grid = std::min(nItems, sms * active);
+      // launched as clusters of four CTAs (each CTA still runs its own media): the hardware places a
+      // cluster on four SMs of one GPC, so the ragged CTAs take whole groups of four SMs and do not
+      // break up the groups that the cluster propagations launched beside them need
+      const int grid = (std::min(nItems, sms * active) + Medium::kClusterSize - 1) / Medium::kClusterSize *
+                       Medium::kClusterSize;
       PropArgs* itemsD = g_ragged.items.p;
       unsigned long long* ctr = g_ragged.counter.p;
       int nIt = nItems;
@@ -2800,7 +2805,21 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         if (!lead->ev1) ck(cudaEventCreate(&lead->ev1), "event");
         ck(cudaEventRecord(lead->ev0, st), "event");
       }
-      ck(cudaLaunchKernel(ke->fn, dim3(grid), dim3(block), args, smem, st), "ragged launch");
+      {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)block);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = Medium::kClusterSize;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        ck(cudaLaunchKernelExC(&cfg, ke->fn, args), "ragged launch");
+      }
       lead->launches++;
       if (lead->timeKernels) {
         ck(cudaEventRecord(lead->ev1, st), "event");
