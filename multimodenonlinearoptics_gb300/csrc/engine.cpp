@@ -1389,7 +1389,8 @@ struct Medium {
     return a;
   }
 
-  void buildPropagator(int R) {
+  // on: the stream of the build (default: the medium's own)
+  void buildPropagator(int R, cudaStream_t on = nullptr) {
     if (propVersion == pumpVersion && prop.p) return;
     const int M = (int)nSignal, E = 4 * M * M;
     const size_t count = (size_t)(nZ > 1 ? nZ - 1 : 0) * E * N;
@@ -1406,7 +1407,7 @@ struct Medium {
     long long grid = (total + 127) / 128;
     grid = std::min<long long>(grid, (long long)sms * 16);
     void* args[] = {(void*)&a};
-    ck(cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(128), args, 0, stream), "propagator build");
+    ck(cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(128), args, 0, on ? on : stream), "propagator build");
     launches++;
     propVersion = pumpVersion;
     propBuilds++;
@@ -2651,18 +2652,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (size_t k : fused) bySolver[ms[k]->solver].push_back(k);
     for (auto& kv : bySolver) {
       std::vector<size_t>& ks = kv.second;
-      // pump-driven solvers: each medium's per-point RK4 matrices, built on its own stream (the builds
-      // of the media overlap, each one parallel over all steps and points)
-      std::vector<bool> withProp(n_media, false);
-      for (size_t k : ks) {
-        Medium* m = ms[k];
-        m->ensureDevice();
-        if (m->linearSolver() && m->usePropagator != 0 && m->nZ > 1 && m->propagatorBytes() <= 16e9) {
-          m->buildPropagator(8);
-          withProp[k] = true;
-        }
-      }
-      for (size_t k : ks) ck(cudaStreamSynchronize(ms[k]->stream), "medium stream");
+      for (size_t k : ks) ms[k]->ensureDevice();
       // largest first (cost ~ nZSteps * modes * N log N)
       std::sort(ks.begin(), ks.end(), [&](size_t x, size_t y) {
         auto cost = [&](Medium* m) { return (double)m->nZ * m->nSignal * m->N * std::log2((double)m->N); };
@@ -2732,6 +2722,17 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       Medium* lead = ms[ks[0]];
       cudaStream_t st = lead->stream;
+      // pump-driven solvers: each medium's per-point RK4 matrices, built on the launch's stream just
+      // before it (each build is parallel over all steps and points of its medium); the media run as
+      // cluster propagations build theirs on their own streams
+      std::vector<bool> withProp(n_media, false);
+      for (size_t k : ks) {
+        Medium* m = ms[k];
+        if (m->linearSolver() && m->usePropagator != 0 && m->nZ > 1 && m->propagatorBytes() <= 16e9) {
+          m->buildPropagator(8, st);
+          withProp[k] = true;
+        }
+      }
       // N/4 threads per medium when the largest grid allows it (four warps from N = 512), else N/8
       const KernelEntry* k4 = maxN / 4 <= 512 ? lead->findKernel(kKindRagged, kv.first, 4) : nullptr;
       const KernelEntry* ke = k4 ? k4 : lead->findKernel(kKindRagged, kv.first, 8);
