@@ -72,3 +72,21 @@ def test_cluster_equals_one_cta_kernels(nlm):
         assert (med._last_schedule()["grid"] == 4) == bool(use)
         res.append((med.signalFreq.copy(), med.signalTime.copy()))
     assert cases.rel_l2(res[0][0], res[1][0]) < 1e-12 and cases.rel_l2(res[0][1], res[1][1]) < 1e-12
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
+def test_cluster_every_solver_matches_oracle(nlm, oracle, name):
+    """runSignalSimulation of each DiffEq solver on a 1024-point grid runs on a 4-CTA cluster and
+    matches the oracle's full grids."""
+    kw = dict(cases.CASES[name], tPrecision=1024)
+    med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**cases.oracle_kwargs(name) | {"tPrecision": 1024})
+    if name not in cases.FULLY_NONLINEAR:
+        med.runPumpSimulation()
+        ref.run_pump_simulation()
+    a = cases.noise(np.random.default_rng(5), 1024, 0.3)
+    med.runSignalSimulation(a, True, 0)
+    ref.run_signal_simulation(a, True, 0)
+    assert med._last_schedule()["grid"] == 4 and med._last_schedule()["R"] == 4
+    for m in range(med._dims["nSignalModes"]):
+        assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
+        assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
