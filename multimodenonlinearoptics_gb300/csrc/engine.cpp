@@ -1418,7 +1418,7 @@ struct Medium {
   int useCluster = 1;
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
-    if (!useCluster || plainOne || a.ckpt || a.inKind != 1 || solver == kChi3GNLSE) return nullptr;
+    if (!useCluster || plainOne || a.ckpt || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return nullptr;
     if (nInst * kClusterSize > smCount()) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);

@@ -90,3 +90,25 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name):
     for m in range(med._dims["nSignalModes"]):
         assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
+
+
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_cluster_gnlse_matches_oracle(nlm, oracle, n):
+    """Chi3GNLSE on a 4-CTA cluster (all 16 stage transforms and the dispersion pair as cluster
+    FFTs): full grids of one propagation and a small batch, against the oracle and the one-CTA kernel."""
+    kw = dict(cases.CASES["Chi3GNLSE"], tPrecision=n, tMax=20)
+    med, ref = nlm.Chi3GNLSE(**kw), oracle.Chi3GNLSE(**kw)
+    t = np.fft.fftshift(np.linspace(-20, 20, n, endpoint=False))
+    a = 2.0 / np.cosh(t) + cases.noise(np.random.default_rng(n), n, 1e-3)
+    med.runSignalSimulation(a)
+    ref.run_signal_simulation(a)
+    assert med._last_schedule()["grid"] == 4 and med._last_schedule()["R"] == 4
+    assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
+    assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
+    x = np.fft.fft(a)[None, :] * np.exp(1j * np.arange(3))[:, None]
+    out = med.batchSignalSimulation(x, inTimeDomain=False)
+    assert med._last_schedule()["grid"] == 12
+    assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
+    one = nlm.Chi3GNLSE(**kw)
+    one._set_cluster(0)
+    assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-12
