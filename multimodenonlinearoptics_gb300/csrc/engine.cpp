@@ -1544,12 +1544,12 @@ struct Medium {
   void propagate(PropArgs a, long long nInst, bool allowPropagator, bool plainOne = false,
                  const std::function<void()>& tail = {}, const GraphKey* tailKey = nullptr) {
     const int R = chooseR();
-    checkGrid(R);
     a.nInst = nInst;
     const KernelEntry* k = nullptr;
     bool gnlse = solver == kChi3GNLSE, ff = false;
     FFTables ffT{};
-    // A few propagations on a large grid: each one spread over a cluster of kClusterSize CTAs
+    // A few propagations on a large grid: each one spread over a cluster of kClusterSize CTAs (also on
+    // grids that the one-CTA kernels do not take, e.g. Chi3GNLSE at N=8192)
     if (const KernelEntry* kc = clusterKernel(a, nInst, plainOne)) {
       if (linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
         buildPropagator(R);
@@ -1559,6 +1559,7 @@ struct Medium {
       if (tail) tail();
       return;
     }
+    checkGrid(R);
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
     } else if (allowPropagator && wantPropagator(nInst)) {

@@ -92,14 +92,18 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name):
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
 
 
-@pytest.mark.parametrize("n", [1024, 4096])
-def test_cluster_gnlse_matches_oracle(nlm, oracle, n):
+@pytest.mark.parametrize("n,t_max", [(1024, 50), (4096, 50), (8192, 100)])
+def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     """Chi3GNLSE on a 4-CTA cluster (all 16 stage transforms and the dispersion pair as cluster
-    FFTs): full grids of one propagation and a small batch, against the oracle and the one-CTA kernel."""
-    kw = dict(cases.CASES["Chi3GNLSE"], tPrecision=n, tMax=20)
+    FFTs): full grids of one propagation and a small batch, against the oracle and the one-CTA kernel
+    (N=8192 has no one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
+    self-steepening) over 0.2 of its length with its z step (199 steps); at N=8192 the time window
+    doubles so that the RK4 step stays stable for the self-steepening term at the highest frequency."""
+    from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG
+    kw = dict(GNLSE_CONFIG, tPrecision=n, relativeLength=0.2, tMax=t_max)
     med, ref = nlm.Chi3GNLSE(**kw), oracle.Chi3GNLSE(**kw)
-    t = np.fft.fftshift(np.linspace(-20, 20, n, endpoint=False))
-    a = 2.0 / np.cosh(t) + cases.noise(np.random.default_rng(n), n, 1e-3)
+    t = np.fft.fftshift(np.linspace(-t_max, t_max, n, endpoint=False))
+    a = 3.0 / np.cosh(t) + cases.noise(np.random.default_rng(n), n, 1e-4)
     med.runSignalSimulation(a)
     ref.run_signal_simulation(a)
     assert med._last_schedule()["grid"] == 4 and med._last_schedule()["R"] == 4
@@ -109,6 +113,7 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n):
     out = med.batchSignalSimulation(x, inTimeDomain=False)
     assert med._last_schedule()["grid"] == 12
     assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
-    one = nlm.Chi3GNLSE(**kw)
-    one._set_cluster(0)
-    assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-12
+    if n <= 4096:
+        one = nlm.Chi3GNLSE(**kw)
+        one._set_cluster(0)
+        assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-12
