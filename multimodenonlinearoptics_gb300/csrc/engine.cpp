@@ -1204,7 +1204,19 @@ struct Medium {
     return sms;
   }
 
+  // A grid that a cluster propagation can take (1024 to 8192 points); whether a launch runs on
+  // clusters is decided in propagate(), which checks the one-CTA kernels' limits otherwise.
+  bool clusterGrid() const {
+    return useCluster && is_pow2((int)N) && N >= 1024 && N <= (uint)kMaxFFT &&
+           findKernel(kKindCluster, solver, kClusterSize) != nullptr;
+  }
+
   void checkGrid(int R) const {
+    if (clusterGrid()) return;
+    checkGridStrict(R);
+  }
+
+  void checkGridStrict(int R) const {
     if (!is_pow2((int)N) || (int)N < R || N > (uint)kMaxFFT || N / R > 512)
       throw Unsupported("grid of " + std::to_string(N) + " points is not supported by the fused split-step kernels "
                         "(power of two, R=" + std::to_string(R) + " to 8192 points)");
@@ -1559,7 +1571,7 @@ struct Medium {
       if (tail) tail();
       return;
     }
-    checkGrid(R);
+    checkGridStrict(R);
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
     } else if (allowPropagator && wantPropagator(nInst)) {

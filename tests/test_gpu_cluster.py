@@ -116,4 +116,5 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     if n <= 4096:
         one = nlm.Chi3GNLSE(**kw)
         one._set_cluster(0)
-        assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-12
+        # soliton fission amplifies rounding differences between the two transform orders
+        assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-10
