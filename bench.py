@@ -333,6 +333,26 @@ def measure_configs(nlm, torch, cpu=True):
             o.run_signal_simulation(a)
             row["cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t0)
         single["chi2pdc_run_signal_n%d" % n] = row
+    # one Chi3GNLSE propagation (the GNLSE medium, N=4096, 999 steps): 18 transforms per step
+    kw = dict(GNLSE_CONFIG, zPrecision=111)
+    t = np.fft.fftshift(np.linspace(-50, 50, 4096, endpoint=False))
+    a = 3 / np.cosh(t) + 0j
+    row = {"n_freqs": 4096}
+    for use, label in ((0, "one_cta_ms"), (1, "cluster_ms")):
+        m = nlm.Chi3GNLSE(**kw)
+        m._set_cluster(use)
+        m.runSignalSimulation(a)
+        t0 = time.perf_counter()
+        m.runSignalSimulation(a)
+        row[label] = 1e3 * (time.perf_counter() - t0)
+        row["z_steps"] = m._dims["nZSteps"]
+    if cpu:
+        from oracle import nlm_oracle as O
+        o = O.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=12))
+        t0 = time.perf_counter()
+        o.run_signal_simulation(a)
+        row["cpu_oracle_ms_estimate"] = 1e3 * (time.perf_counter() - t0) * (row["z_steps"] - 1) / (o.n_z_steps - 1)
+    single["gnlse_run_signal_n4096"] = row
     res["single_propagation"] = single
     # 3. 64 ragged Chi2SFG media in one launch
     params = ragged_media_params()
