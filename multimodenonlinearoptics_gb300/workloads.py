@@ -12,6 +12,7 @@ self-contained command for ncu.
 * gnlse       Chi3GNLSE batch of 3 sech(t) + noise rows, N=4096
 * gnlse_grad  gradient of the band energy (omega in [2, 4]) with respect to the input spectral phase
 * signal      one Chi2PDC runSignalSimulation (full grids) on the Green's medium at N=2048
+* gnlse_signal  one Chi3GNLSE runSignalSimulation (full grids) on the GNLSE medium at N=4096
 """
 
 import argparse
@@ -143,6 +144,9 @@ def _run(name, z_precision, rows, reps):
                             **dict(GREEN_CONFIG, tPrecision=2048, zPrecision=z_precision or 500))
             m.runPumpSimulation()
             m.runSignalSimulation((np.random.default_rng(2048).standard_normal(2048) + 0j) * 0.1)
+        elif name == "gnlse_signal":
+            m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
+            m.runSignalSimulation(gnlse_rows(1)[0])
         elif name == "gnlse":
             m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
             m.batchSignalSimulation(gnlse_rows(rows or 304), inTimeDomain=True)
@@ -161,7 +165,8 @@ def _run(name, z_precision, rows, reps):
 
 def main():
     ap = argparse.ArgumentParser(description="run one benchmark workload on cuda:0")
-    ap.add_argument("name", choices=["green", "chi3", "ragged", "adjoint", "gnlse", "gnlse_grad", "signal"])
+    ap.add_argument("name", choices=["green", "chi3", "ragged", "adjoint", "gnlse", "gnlse_grad", "signal",
+                                         "gnlse_signal"])
     ap.add_argument("--zprecision", type=int, default=0, help="zPrecision override (0: the workload's own)")
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")
     ap.add_argument("--reps", type=int, default=1)
