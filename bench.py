@@ -353,6 +353,22 @@ def measure_configs(nlm, torch, cpu=True):
         o.run_signal_simulation(a)
         row["cpu_oracle_ms_estimate"] = 1e3 * (time.perf_counter() - t0) * (row["z_steps"] - 1) / (o.n_z_steps - 1)
     single["gnlse_run_signal_n4096"] = row
+    # the Chi3 self-phase-modulation pump march (runPumpSimulation) on 8192 points, 1000 rows
+    kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0.02, tMax=40, tPrecision=8192,
+              zPrecision=500)
+    row = {"n_freqs": 8192}
+    for use, label in ((0, "one_cta_ms"), (1, "cluster_ms")):
+        m = nlm.Chi3(**kw)
+        m._set_cluster(use)
+        m.runPumpSimulation()
+        best = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            m.runPumpSimulation()
+            best = min(best, time.perf_counter() - t0)
+        row[label] = 1e3 * best
+        row["z_steps"] = m._dims["nZSteps"]
+    single["chi3_run_pump_n8192"] = row
     res["single_propagation"] = single
     # 3. 64 ragged Chi2SFG media in one launch
     params = ragged_media_params()

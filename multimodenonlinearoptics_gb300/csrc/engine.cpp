@@ -1136,7 +1136,15 @@ struct Medium {
     upload(dd, dP);
     upload(db, bP);
     upload(dr, rel);
-    ck(launch_pump_chi3(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, plan, tw, stream), "chi3 pump");
+    if (useCluster && N >= 1024) {
+      // 1024..8192 points: the march on four SMs (prop_cluster_pump.cu), four points per thread
+      const FFTPlanH local = make_plan((int)N / kClusterSize, kClusterSize);
+      ck(launch_pump_chi3_cluster(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, local, tw, stream),
+         "chi3 pump (cluster)");
+    } else {
+      ck(launch_pump_chi3(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, plan, tw, stream),
+         "chi3 pump");
+    }
     launches++;
     ck(cudaStreamSynchronize(stream), "chi3 pump");
   }

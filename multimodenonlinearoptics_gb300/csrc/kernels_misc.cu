@@ -216,37 +216,6 @@ cudaError_t launch_scale_rows(double2* a, const double* scale, int nRows, int N,
 // ------------------------------------------------------------------------------------------
 // Chi3 pump: sequential self-phase-modulation march on one CTA (solvers/Chi3.cpp:41-70)
 // ------------------------------------------------------------------------------------------
-// exp(re + i im), the self-phase factor of one pump row.  im is the nonlinear phase of half a z step,
-// small in practice: for |im| <= 1/4 sine and cosine come from their Taylor series (terms to x^13 and
-// x^14; the first omitted term is below 1e-21 of the result), otherwise from sincos.  re is zero
-// for a real nonlinear length, and exp(0) = 1 exactly.
-__device__ __forceinline__ double2 spm_factor(double re, double im) {
-  double sn, cs;
-  if (fabs(im) <= 0.25) {
-    const double x2 = im * im;
-    sn = 1.0 / 6227020800.0;                      // 1/13!
-    sn = fma(sn, -x2, 1.0 / 39916800.0);          // 1/11!
-    sn = fma(sn, -x2, 1.0 / 362880.0);            // 1/9!
-    sn = fma(sn, -x2, 1.0 / 5040.0);              // 1/7!
-    sn = fma(sn, -x2, 1.0 / 120.0);               // 1/5!
-    sn = fma(sn, -x2, 1.0 / 6.0);                 // 1/3!
-    sn = fma(sn, -x2, 1.0);
-    sn *= im;
-    cs = 1.0 / 87178291200.0;                     // 1/14!
-    cs = fma(cs, -x2, 1.0 / 479001600.0);         // 1/12!
-    cs = fma(cs, -x2, 1.0 / 3628800.0);           // 1/10!
-    cs = fma(cs, -x2, 1.0 / 40320.0);             // 1/8!
-    cs = fma(cs, -x2, 1.0 / 720.0);               // 1/6!
-    cs = fma(cs, -x2, 1.0 / 24.0);                // 1/4!
-    cs = fma(cs, -x2, 0.5);                       // 1/2!
-    cs = fma(cs, -x2, 1.0);
-  } else {
-    sincos(im, &sn, &cs);
-  }
-  const double e = re == 0.0 ? 1.0 : exp(re);
-  return make_double2(e * cs, e * sn);
-}
-
 template <int R>
 __global__ void __launch_bounds__(512) k_pump_chi3(double2* __restrict__ pf, double2* __restrict__ pt,
                                                    const double2* __restrict__ env, const double2* __restrict__ halfP,

@@ -115,6 +115,10 @@ cudaError_t launch_scale_rows(double2* a, const double* scale, int nRows, int N,
 cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                              const double2* dstepP, const double2* backP, const double2* rel, int nRows,
                              const FFTPlanH& plan, const double2* tw, cudaStream_t s);
+// the same march over a 4-CTA cluster; localPlan is the (N/4)-point plan with four points per thread
+cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
+                                     const double2* dstepP, const double2* backP, const double2* rel, int nRows,
+                                     const FFTPlanH& localPlan, const double2* tw, cudaStream_t s);
 cudaError_t launch_green_epilogue(const double2* raw, long long rawStride, int N, int nIn, int nOut,
                                   const double2* blockScale, const uint8_t* blockShift, double2* C,
                                   double2* S, cudaStream_t s);

@@ -118,3 +118,19 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
         one._set_cluster(0)
         # soliton fission amplifies rounding differences between the two transform orders
         assert cases.rel_l2(one.batchSignalSimulation(x, inTimeDomain=False), out) < 1e-10
+
+
+@pytest.mark.parametrize("n", [1024, 2048, 8192])
+def test_cluster_chi3_pump_march(nlm, oracle, n):
+    """The self-phase-modulation pump march on four SMs: both pump grids against the oracle, and
+    against the one-CTA march (same arithmetic, other transform order)."""
+    kw = dict(CHI3, tPrecision=n, zPrecision=15)
+    med, ref, one = nlm.Chi3(**kw), oracle.Chi3(**kw), nlm.Chi3(**kw)
+    one._set_cluster(0)
+    for m in (med, one):
+        m.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(med.pumpFreq, ref.pump_freq[0]) < TOL
+    assert cases.rel_l2(med.pumpTime, one.pumpTime) < 1e-12
+    assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12

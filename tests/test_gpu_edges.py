@@ -42,8 +42,10 @@ def test_largest_single_mode_grid(nlm, oracle):
 
 
 def test_largest_grid_chi3_pump_march(nlm, oracle):
+    """The one-CTA march with sixteen points per thread (the cluster march is in test_gpu_cluster.py)."""
     kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0.02, tMax=40, tPrecision=8192, zPrecision=15)
     med, ref = nlm.Chi3(**kw), oracle.Chi3(**kw)
+    med._set_cluster(0)
     med.runPumpSimulation()
     ref.run_pump_simulation()
     assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
