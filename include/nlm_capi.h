@@ -158,6 +158,9 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
  * nlm_adjoint_forward: propagate rows x N input spectra (device) to rows x N output spectra (device),
  *   storing the states every checkpoint_interval steps (<= 0: every step when that fits in 1 GB,
  *   else every ceil(sqrt(nZSteps-1)) steps, the segments being recomputed in the reverse sweep).
+ *   Chi3GNLSE with checkpoint_interval <= 0 on a grid of 1024..8192 points, with rows x 4 <= SMs and
+ *   the stage values of every step within a quarter of the free device memory (and 64 GB): the
+ *   forward stores those stage values instead and *used_interval is 0 (nothing is recomputed).
  *   The pump must have been run.
  * nlm_adjoint_backward: given dL/dX (device, rows x N) returns dL/dX_in (device, rows x N), dL/dF0
  *   (device, N; may be NULL) and dL/dd (host, nZSteps doubles; may be NULL). */

@@ -191,7 +191,7 @@ static void add_prop_key(GraphKey& k, const PropArgs& a) {
   for (int i = 0; i < kMaxModes; i++) k.add(a.outModes[i]);
   k.add(a.out).add(a.outStride).add(a.tw).add(a.dstep).add(a.dlast).add(a.half).add(a.back).add(a.prop);
   k.add(a.pump).add(a.pumpStride).add(a.nPumps).add(a.coef).add(a.nCoef).add(a.gridF).add(a.gridT);
-  k.add(a.ckpt).add(a.ckK).add(a.ckN).add(a.raman).add(a.steep).add(a.relInt);
+  k.add(a.ckpt).add(a.ckK).add(a.ckN).add(a.stages).add(a.raman).add(a.steep).add(a.relInt);
 }
 
 struct GraphCache {
@@ -599,7 +599,8 @@ struct Medium {
   DevBuf<uint8_t> flagsD;
   DevBuf<unsigned long long> workCounter;
   // adjoint state: forward checkpoints of the last nlm_adjoint_forward
-  DevBuf<double2> ckpt, adjSeg, adjGa, adjGP, adjFGP, adjGc;
+  DevBuf<double2> ckpt, adjSeg, adjGa, adjGP, adjFGP, adjGc, adjStages;
+  bool adjStored = false;   // the last adjoint forward stored the Chi3GNLSE stage values of every step
   DevBuf<double> profD;
   long long adjRows = 0;
   int adjK = 0, adjNCk = 0;
@@ -1438,7 +1439,9 @@ struct Medium {
   int useCluster = 1;
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
-    if (!useCluster || plainOne || a.ckpt || a.inKind != 1) return nullptr;
+    // checkpointed forwards (the adjoint's) on clusters only for Chi3GNLSE, whose reverse sweep has
+    // a cluster form too
+    if (!useCluster || plainOne || (a.ckpt && solver != kChi3GNLSE) || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return nullptr;
     if (nInst * kClusterSize > smCount()) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);
@@ -1579,6 +1582,7 @@ struct Medium {
       if (tail) tail();
       return;
     }
+    if (a.stages) throw std::logic_error("stage values are stored by the cluster kernels only");
     checkGridStrict(R);
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
@@ -1705,6 +1709,32 @@ struct Medium {
     const int R = chooseR();
     checkGrid(R);
     const size_t steps = nZ - 1;
+    adjStored = false;
+    if (interval <= 0 && storeStages(rows)) {
+      // Chi3GNLSE with few rows on a cluster grid: the forward on 4-CTA clusters stores the stage values
+      // of every step, and the reverse sweep reads them (nothing recomputed)
+      adjStages.reserve((size_t)rows * steps * 8 * N);
+      PropArgs a = baseArgs(R);
+      a.inKind = 1;
+      a.inTime = 0;
+      a.in = in;
+      a.inStride = (long long)N;
+      a.inChannels = 1;
+      a.inputMode = 0;
+      a.nOut = 1;
+      a.outModes[0] = 0;
+      a.out = out;
+      a.outStride = (long long)N;
+      a.stages = adjStages.p;
+      propagate(a, (long long)rows, false);
+      ck(cudaStreamSynchronize(stream), "adjoint forward");
+      adjStored = true;
+      adjRows = (long long)rows;
+      adjK = 0;
+      adjNCk = 0;
+      adjPumpVersion = pumpVersion;
+      return;
+    }
     int K = interval;
     if (K <= 0) {
       const double bytes = (double)rows * steps * N * sizeof(double2);
@@ -1734,9 +1764,150 @@ struct Medium {
     adjPumpVersion = pumpVersion;
   }
 
+  // Stage values of every Chi3GNLSE step fit (at most a quarter of the free device memory and 64 GB),
+  // and the forward of `rows` propagations runs on 4-CTA clusters (Medium::clusterKernel).
+  bool storeStages(size_t rows) const {
+    if (solver != kChi3GNLSE || !useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
+    if ((long long)rows * kClusterSize > smCount()) return false;
+    if (!findKernel(kKindCluster, solver, kClusterSize) || !findKernel(kKindAdjoint, solver + 300, kClusterSize))
+      return false;
+    size_t freeB = 0, totalB = 0;
+    if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const double bytes = (double)rows * (nZ - 1) * 8.0 * N * sizeof(double2);
+    return bytes <= std::min(0.25 * (double)freeB, 64e9);
+  }
+
+  // Reverse sweep over the stored stage values: one propagation per 4-CTA cluster.
+  void adjointStored(const double2* gout, double2* gin) {
+    constexpr int C = kClusterSize;
+    const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
+    if (!k) throw Unsupported("no stored-stage adjoint kernel");
+    const int M = (int)N / C;
+    const size_t need = (size_t)5 * M * sizeof(double2);
+    int dev = 0, optin = 0;
+    ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    const int dynMax = optin - (int)fa.sharedSizeBytes;
+    if ((int)need > dynMax) throw Unsupported("grid too large for the cluster adjoint");
+    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    PropArgs a = baseArgs(C);
+    a.plan = make_plan(M, C);
+    a.R = C;
+    a.nInst = adjRows;
+    a.ipc = 1;
+    a.work = nullptr;
+    a.stages = adjStages.p;
+    AdjArgs d{};
+    d.gout = gout;
+    d.gin = gin;
+    const long long clusters = std::min<long long>(adjRows, smCount() / C);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(C * clusters));
+    cfg.blockDim = dim3((unsigned)a.plan.T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {(void*)&a, (void*)&d};
+    lastSchedule = Schedule{(int)(C * clusters), a.plan.T, 1, smem, 1, 1};
+    lastR = C;
+    lastTuned = 0;
+    lastRegs = fa.numRegs;
+    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (stored stages)");
+    launches++;
+    ck(cudaStreamSynchronize(stream), "adjoint");
+  }
+
+  // Chi3GNLSE on grids of 1024 to 8192 points with few rows: the pipelined sweep on clusters of eight
+  // CTAs (adjoint_gnlse_cluster.cu), one cluster per row; false when it does not apply (more rows than
+  // such clusters fit on the device at once, or a grid outside its range).
+  bool adjointCluster(const double2* gout, double2* gin) {
+    constexpr int C = kClusterSize;
+    if (!useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
+    const KernelEntry* k = findKernel(kKindAdjoint, solver + 200, C);
+    if (!k) return false;
+    const int M = (int)N / C;
+    const size_t need = (size_t)5 * M * sizeof(double2);
+    int dev = 0, optin = 0;
+    ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    const int dynMax = optin - (int)fa.sharedSizeBytes;
+    if ((int)need > dynMax) return false;
+    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    PropArgs a = baseArgs(C);
+    a.plan = make_plan(M, C);
+    a.R = C;
+    a.nInst = adjRows;
+    a.ipc = 1;
+    a.work = nullptr;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(2 * C);
+    cfg.blockDim = dim3((unsigned)a.plan.T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2 * C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int fit = 0;
+    if (cudaOccupancyMaxActiveClusters(&fit, k->fn, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    // up to three waves of clusters (the two-CTA pipelined sweep is about 3.5 times slower per row)
+    if (fit < 1 || adjRows > 3LL * fit) return false;
+    const long long waves = (adjRows + fit - 1) / fit;
+    const long long clusters = (adjRows + waves - 1) / waves;
+    adjSeg.reserve((size_t)clusters * 2 * (size_t)adjK * 8 * N);   // per cluster: STG[2][K][8][N]
+    AdjArgs d{};
+    d.gout = gout;
+    d.ckpt = ckpt.p;
+    d.K = adjK;
+    d.nCk = adjNCk;
+    d.seg = adjSeg.p;
+    d.ga = adjGa.p;
+    d.gin = gin;
+    d.single = adjRows == 1 ? 1 : 0;
+    cfg.gridDim = dim3((unsigned)(2 * C * clusters));
+    void* args[] = {(void*)&a, (void*)&d};
+    lastSchedule = Schedule{(int)(2 * C * clusters), a.plan.T, 1, smem, 1, 1};
+    lastR = C;
+    lastTuned = 0;
+    lastRegs = fa.numRegs;
+    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster of eight)");
+    launches++;
+    ck(cudaStreamSynchronize(stream), "adjoint");
+    return true;
+  }
+
   void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {
     if (adjRows == 0 || adjPumpVersion != pumpVersion)
       throw std::runtime_error("no adjoint forward pass to differentiate: run nlm_adjoint_forward first");
+    const bool gn = solver == kChi3GNLSE;
+    if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
+    // Chi3GNLSE on cluster grids: over the stored stage values, or pipelined on clusters of eight CTAs
+    if (gn && adjStored) {
+      adjointStored(gout, gin);
+      return;
+    }
+    if (gn && adjointCluster(gout, gin)) return;
     int R = chooseR();
     const KernelEntry* k = findKernel(kKindAdjoint, solver, R);
     // few rows: four points per thread, as for the forward (Medium::propagate)
@@ -1750,8 +1921,6 @@ struct Medium {
     const size_t steps = nZ - 1;
     adjGa.reserve(steps * 3 * N);
     ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
-    const bool gn = solver == kChi3GNLSE;
-    if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
     // Few rows with checkpoint segments: the pipelined variant, one two-CTA cluster per propagation
     // (one CTA recomputes the next segment while the other reverses the current one).
     // (Chi3GNLSE: one CTA marches each segment forward storing the stage values of every step, the

@@ -33,6 +33,7 @@ struct ClusterFFT {
   double2* recv;        // [2][C][T] transpose receive buffers
   const FFTPlanH* plan; // the local M-point plan (R = C): the kernel parameter's, indexed in place
   int rank, j, phase;
+  int base = 0;         // cluster rank of the group's first CTA (clusters holding several groups)
 };
 
 template <int C>
@@ -41,7 +42,7 @@ __device__ __forceinline__ void cluster_transpose(ClusterFFT<C>& f, double2 (&x)
   double2* half = f.recv + (long long)f.phase * C * T;
 #pragma unroll
   for (int v = 0; v < C; v++) {
-    double2* dst = cl.map_shared_rank(half + f.rank * T + f.j, v);
+    double2* dst = cl.map_shared_rank(half + f.rank * T + f.j, f.base + v);
     *dst = x[v];
   }
   cl.sync();

@@ -58,6 +58,9 @@ struct PropArgs {
   // at ckpt[((inst * ckN) + i / ckK) * nModes + m][N] when i % ckK == 0 and i < nZ - 1
   double2* ckpt;
   int ckK, ckN;
+  // Chi3GNLSE adjoint forward on clusters: the stage inputs y_s and convolutions u2_s of every step
+  // (time domain) at stages[((inst * (nZ - 1) + i - 1) * 8 + {s, 4 + s})][N]; null otherwise
+  double2* stages;
   // Chi3GNLSE tables
   const double2* raman;   // ramanResponse / N
   const double2* steep;   // (nlStep0 + nlStep1 * omega) / N

@@ -58,8 +58,15 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
 #pragma unroll
       for (int v = 0; v < R; v++) a.gridT[tn(v)] = x[v];
     }
+    // checkpoints for the reverse sweep: the time-domain state before steps 1, K + 1, 2 K + 1, ...
+    double2* ckRow = a.ckpt ? a.ckpt + inst * a.ckN * (long long)N : nullptr;
+    if (ckRow && a.nZ > 1) {
+#pragma unroll
+      for (int v = 0; v < R; v++) ckRow[tn(v)] = x[v];
+    }
     for (int i = 1; i < a.nZ; i++) {
       const double* rel = a.relInt + (long long)(i - 1) * 3;
+      double2* stg = a.stages ? a.stages + ((inst * (a.nZ - 1) + i - 1) * 8LL) * N : nullptr;
       double2 k[R], acc[R];
 #pragma unroll
       for (int v = 0; v < R; v++) k[v] = czero();
@@ -72,12 +79,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
         for (int v = 0; v < R; v++) {
           y[v] = caxpy(x[v], fac, k[v]);
           u[v] = make_double2(ri * cabs2(y[v]), 0.0);
+          if (stg) stg[(long long)s * N + tn(v)] = y[v];
         }
         // Raman convolution R~ * (rel |y|^2)
         cluster_fft_fwd<C>(f, u, cl);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + fk(v)));
         cluster_fft_inv<C>(f, u, cl);
+        if (stg) {
+#pragma unroll
+          for (int v = 0; v < R; v++) stg[(long long)(4 + s) * N + tn(v)] = u[v];
+        }
         // times the field, then the self-steepening operator (g0 + g1 w)
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], y[v]);
@@ -107,6 +119,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
         if (a.gridT) {
 #pragma unroll
           for (int v = 0; v < R; v++) a.gridT[(long long)i * N + tn(v)] = x[v];
+        }
+        if (ckRow && !last && i % a.ckK == 0) {
+#pragma unroll
+          for (int v = 0; v < R; v++) ckRow[(long long)(i / a.ckK) * N + tn(v)] = x[v];
         }
       }
     }

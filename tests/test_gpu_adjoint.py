@@ -290,3 +290,53 @@ def test_gnlse_pipelined_and_one_cta_sweeps_agree(nlm):
     for key in ((3, 5), (80, 1), (80, 5)):
         assert cases.rel_l2(grads[key][:3], grads[3, 1]) < 1e-12
     assert cases.rel_l2(grads[80, 5], grads[80, 1]) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_gnlse_cluster_sweep(nlm, n):
+    """Few rows on grids of 1024+ points: the forward runs on 4-CTA clusters.  With the interval chosen
+    by the engine (0) it stores the stage values of every step and the reverse sweep reads them on
+    4-CTA clusters; with an explicit checkpoint interval the reverse sweep runs on clusters of eight CTAs
+    (four reverse the current segment while four recompute the next).  Gradients agree with the one-CTA
+    sweeps for intervals 1 and one that leaves a short last segment, and match a directional central
+    difference of the engine's forward."""
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG
+    kw = dict(GNLSE_CONFIG, tPrecision=n, relativeLength=0.05, tMax=50)
+    rows = 3
+    rng = np.random.default_rng(n)
+    t = np.fft.fftshift(np.linspace(-50, 50, n, endpoint=False))
+    x = np.fft.fft(3.0 / np.cosh(t) + cases.noise(rng, rows * n, 1e-3).reshape(rows, n), axis=1)
+    weights = torch.linspace(0, 1, n, device="cuda", dtype=torch.float64)
+    nz = nlm.Chi3GNLSE(**kw)._dims["nZSteps"]
+    k_short = 7 if (nz - 1) % 7 else 6
+
+    def grad(cluster, k):
+        med = nlm.Chi3GNLSE(**kw)
+        med._set_cluster(cluster)
+        xt = torch.tensor(x, device="cuda", requires_grad=True)
+        torch.sum(torch.abs(propagate_gnlse(med, xt, k)) ** 2 * weights).backward()
+        return xt.grad.cpu().numpy(), med._last_schedule()
+
+    g = {}
+    g[1, 0], sched = grad(1, 0)
+    assert sched["grid"] == 4 * rows and sched["R"] == 4
+    for k in (1, k_short):
+        g[1, k], sched = grad(1, k)
+        assert sched["grid"] == 8 * rows and sched["R"] == 4
+        g[0, k], sched = grad(0, k)
+        assert sched["grid"] not in (4 * rows, 8 * rows)
+    for key in ((1, 1), (1, k_short), (0, 1), (0, k_short)):
+        assert cases.rel_l2(g[key], g[1, 0]) < 1e-10
+    med = nlm.Chi3GNLSE(**kw)
+    w = weights.cpu().numpy()
+
+    def loss(y):
+        return float(np.sum(np.abs(med.batchSignalSimulation(y, inTimeDomain=False)) ** 2 * w))
+
+    d = cases.noise(np.random.default_rng(1), rows * n, 1.0).reshape(rows, n)
+    adj = float(np.sum(np.real(np.conj(g[1, 0]) * d)))
+    # the loss is ~1e7 at N=4096: a larger step keeps the difference's round-off (~1e-16 L / h) small
+    fd = _dir_fd(loss, x, d, 1e-4)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
