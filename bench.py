@@ -565,6 +565,7 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     med._set_stream(stream.cuda_stream)
     peak = nlm.fp64_peak_tflops()
+    peak_mma = nlm.fp64_mma_peak_tflops()
     C = torch.empty((n, n), dtype=torch.complex128, device="cuda")
     S = torch.empty_like(C)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
@@ -674,7 +675,10 @@ def run_ours(args):
                          "kernel": "k_propagate_linear<1,8>", "kernel_ms": 1e3 * avg_kernel_s,
                          "algorithmic_flops_per_launch": flops,
                          "ncu_fp64_pipe_active_pct": read_profile_value("fp64_pipe_active_pct"),
-                         "peak_source": "FP64 FMA chains measured in this run (MEASURED_PEAKS.json has no FP64 entry)"},
+                         "peak_source": "FP64 FMA chains measured in this run (MEASURED_PEAKS.json has no FP64 entry)",
+                         "fp64_tensor_peak": peak_mma,
+                         "fp64_tensor_peak_source": "m16n8k16 f64 MMAs (DMMA) measured in this run: the rate a "
+                                                    "DFT-as-GEMM schedule could draw on"},
             "cpu_baseline": cpu,
             "plain": {"value": plain, "unit": UNIT, "sample": args.plain_sample,
                       "form": "one propagation per kernel launch"},

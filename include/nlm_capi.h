@@ -258,6 +258,9 @@ nlm_status nlm_kernel_timing(nlm_medium* m, int enable, double* total_ms, long* 
  * flops): the roofline denominator of the propagation kernels.  No counterpart in the
  * reference (measurement support). */
 nlm_status nlm_fp64_peak(double* tflops);
+/* Measured FP64 tensor-core (DMMA, m16n8k16) throughput of the current device in TFLOP/s: what a
+ * DFT-as-GEMM schedule could draw on in FP64.  No counterpart in the reference (measurement support). */
+nlm_status nlm_fp64_mma_peak(double* tflops);
 
 #ifdef __cplusplus
 }

@@ -15,16 +15,11 @@
 
 #include <cooperative_groups.h>
 
-#include "nlm_propagate.cuh"
+#include "nlm_adjoint_pdc.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace nlm {
-
-__device__ __forceinline__ void atomic_add2(double2* p, double2 v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
 
 // States s_{s0} .. s_{segEnd-1} of one segment, recomputed from its checkpoint into seg[0 ..].
 template <int R>
@@ -40,28 +35,8 @@ __device__ __forceinline__ void pdc_recompute_segment(const PropArgs& a, const d
     seg[j + v * T] = x[v];
   }
   for (int i = s0 + 1; i < segEnd; i++) {
-    if (a.prop) {
-      // the RK4 step as its per-point real 2x2 matrix (pairs (M00, M01), (M10, M11))
-      const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * 2 * N;
 #pragma unroll
-      for (int v = 0; v < R; v++) {
-        const int t = j + v * T;
-        const double2 e0 = __ldg(mat + t), e1 = __ldg(mat + N + t);
-        const double re = x[v].x, im = x[v].y;
-        x[v] = make_double2(fma(e0.y, im, e0.x * re), fma(e1.y, im, e1.x * re));
-      }
-    } else {
-      const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-#pragma unroll
-      for (int v = 0; v < R; v++) {
-        const int t = j + v * T;
-        const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
-        double2 p[3][1] = {{__ldg(pr)}, {__ldg(pr + N)}, {__ldg(pr + 2 * N)}};
-        double2 xm[1] = {x[v]};
-        rk4_point<FChi2PDC>(xm, p, c);
-        x[v] = xm[0];
-      }
-    }
+    for (int v = 0; v < R; v++) x[v] = pdc_step_point(a, N, i, j + v * T, x[v]);
     fft_regs<R, false>(x, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
@@ -87,51 +62,10 @@ __device__ __forceinline__ void pdc_reverse_segment(const PropArgs& a, const Adj
     fft_regs<R, true>(gv, buf, tw, plan, j);
     const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
     const double2 c0 = c[0], c1 = c[1], c2 = c[2];
-    double2* gacc = d.ga + (long long)(i - 1) * 3 * N;
 #pragma unroll
     for (int v = 0; v < R; v++) {
       const int t = j + v * T;
-      const double2* pr = a.pump + (long long)(2 * i - 2) * N + t;
-      const double2 a0 = cmul(c0, __ldg(pr)), a1 = cmul(c1, __ldg(pr + N)), a2 = cmul(c2, __ldg(pr + 2 * N));
-      const double2 x = prev[t];
-      // forward stages (solvers/Chi2PDC.cpp:40-43)
-      const double2 k1 = cmulc(a0, x);
-      const double2 y1 = caxpy(x, 0.5, k1);
-      const double2 k2 = cmulc(a1, y1);
-      const double2 y2 = caxpy(x, 0.5, k2);
-      const double2 k3 = cmulc(a1, y2);
-      const double2 y3 = cadd(x, k3);
-      // reverse: x' = x + (k1 + 2 k2 + 2 k3 + k4) / 6 with k = a conj(y)
-      const double2 gp = gv[v];
-      double2 gx = gp;
-      double2 gk1 = cscale(gp, 1.0 / 6.0);
-      double2 gk2 = cscale(gp, 1.0 / 3.0);
-      double2 gk3 = gk2;
-      const double2 gk4 = gk1;
-      const double2 ga2 = cmul(y3, gk4);
-      const double2 gy3 = cmulc(a2, gk4);
-      gx = cadd(gx, gy3);
-      gk3 = cadd(gk3, gy3);
-      double2 ga1 = cmul(y2, gk3);
-      const double2 gy2 = cmulc(a1, gk3);
-      gx = cadd(gx, gy2);
-      gk2 = caxpy(gk2, 0.5, gy2);
-      ga1 = cadd(ga1, cmul(y1, gk2));
-      const double2 gy1 = cmulc(a1, gk2);
-      gx = cadd(gx, gy1);
-      gk1 = caxpy(gk1, 0.5, gy1);
-      const double2 ga0 = cmul(x, gk1);
-      gx = cadd(gx, cmulc(a0, gk1));
-      gv[v] = gx;
-      if (active && d.single) {   // the only instance: each element is written once
-        gacc[t] = ga0;
-        gacc[N + t] = ga1;
-        gacc[2 * N + t] = ga2;
-      } else if (active) {
-        atomic_add2(gacc + t, ga0);
-        atomic_add2(gacc + N + t, ga1);
-        atomic_add2(gacc + 2 * N + t, ga2);
-      }
+      gv[v] = pdc_reverse_point(a, d, N, i, t, c0, c1, c2, prev[t], gv[v], active);
     }
   }
 }

@@ -1439,9 +1439,9 @@ struct Medium {
   int useCluster = 1;
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
-    // checkpointed forwards (the adjoint's) on clusters only for Chi3GNLSE, whose reverse sweep has
-    // a cluster form too
-    if (!useCluster || plainOne || (a.ckpt && solver != kChi3GNLSE) || a.inKind != 1) return nullptr;
+    // checkpointed forwards (the adjoint's, Chi2PDC and Chi3GNLSE) run on clusters too: their reverse
+    // sweeps have cluster forms that read the same checkpoints
+    if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return nullptr;
     if (nInst * kClusterSize > smCount()) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);
@@ -1897,17 +1897,72 @@ struct Medium {
     return true;
   }
 
-  void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {
-    if (adjRows == 0 || adjPumpVersion != pumpVersion)
-      throw std::runtime_error("no adjoint forward pass to differentiate: run nlm_adjoint_forward first");
-    const bool gn = solver == kChi3GNLSE;
-    if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
-    // Chi3GNLSE on cluster grids: over the stored stage values, or pipelined on clusters of eight CTAs
-    if (gn && adjStored) {
-      adjointStored(gout, gin);
-      return;
+  // Chi2PDC with few rows on a cluster grid (the forward ran on 4-CTA clusters): the reverse sweep
+  // over 4-CTA clusters too (adjoint_cluster.cu); false when it does not apply.
+  bool adjointClusterPdc(const double2* gout, double2* gin) {
+    constexpr int C = kClusterSize;
+    if (solver != kChi2PDC || !useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
+    if (adjRows * C > smCount()) return false;
+    const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
+    if (!k) return false;
+    const int M = (int)N / C;
+    const size_t need = (size_t)5 * M * sizeof(double2);
+    int dev = 0, optin = 0;
+    ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
+    const int dynMax = optin - (int)fa.sharedSizeBytes;
+    if ((int)need > dynMax) return false;
+    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
+    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    PropArgs a = baseArgs(C);
+    a.plan = make_plan(M, C);
+    a.R = C;
+    a.nInst = adjRows;
+    a.ipc = 1;
+    a.work = nullptr;
+    // segments are recomputed with the RK4 propagator matrices when they fit
+    if (adjK > 1 && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+      buildPropagator(C);
+      a.prop = prop.p;
     }
-    if (gn && adjointCluster(gout, gin)) return;
+    const long long clusters = adjRows;
+    if (adjK > 1) adjSeg.reserve((size_t)clusters * adjK * N);
+    AdjArgs d{};
+    d.gout = gout;
+    d.ckpt = ckpt.p;
+    d.K = adjK;
+    d.nCk = adjNCk;
+    d.seg = adjK > 1 ? adjSeg.p : nullptr;
+    d.ga = adjGa.p;
+    d.gin = gin;
+    d.single = adjRows == 1 ? 1 : 0;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(C * clusters));
+    cfg.blockDim = dim3((unsigned)a.plan.T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {(void*)&a, (void*)&d};
+    lastSchedule = Schedule{(int)(C * clusters), a.plan.T, 1, smem, 1, 1};
+    lastR = C;
+    lastTuned = 0;
+    lastRegs = fa.numRegs;
+    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster)");
+    launches++;
+    return true;
+  }
+
+  // The one-CTA and two-CTA-cluster reverse sweeps (the stage-factor gradients go to adjGa).
+  void adjointLaunch(const double2* gout, double2* gin) {
+    const bool gn = solver == kChi3GNLSE;
     int R = chooseR();
     const KernelEntry* k = findKernel(kKindAdjoint, solver, R);
     // few rows: four points per thread, as for the forward (Medium::propagate)
@@ -1918,9 +1973,6 @@ struct Medium {
       }
     }
     if (!k) throw Unsupported("no adjoint kernel for this grid");
-    const size_t steps = nZ - 1;
-    adjGa.reserve(steps * 3 * N);
-    ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
     // Few rows with checkpoint segments: the pipelined variant, one two-CTA cluster per propagation
     // (one CTA recomputes the next segment while the other reverses the current one).
     // (Chi3GNLSE: one CTA marches each segment forward storing the stage values of every step, the
@@ -1979,6 +2031,23 @@ struct Medium {
       ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
     }
     launches++;
+  }
+
+  void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {
+    if (adjRows == 0 || adjPumpVersion != pumpVersion)
+      throw std::runtime_error("no adjoint forward pass to differentiate: run nlm_adjoint_forward first");
+    const bool gn = solver == kChi3GNLSE;
+    if (gn && (gpump || gpol)) throw std::invalid_argument("Chi3GNLSE has no pump or poling to differentiate");
+    // Chi3GNLSE on cluster grids: over the stored stage values, or pipelined on clusters of eight CTAs
+    if (gn && adjStored) {
+      adjointStored(gout, gin);
+      return;
+    }
+    if (gn && adjointCluster(gout, gin)) return;
+    const size_t steps = nZ - 1;
+    adjGa.reserve(steps * 3 * N);
+    ck(cudaMemsetAsync(adjGa.p, 0, steps * 3 * N * sizeof(double2), stream), "memset");
+    if (gn || !adjointClusterPdc(gout, gin)) adjointLaunch(gout, gin);
     if (gpump) {
       const size_t rowsP = nZP;
       adjGP.reserve(rowsP * N);
@@ -3280,32 +3349,50 @@ nlm_status nlm_kernel_timing(nlm_medium* h, int enable, double* total_ms, long* 
   });
 }
 
+namespace {
+// Best of three timed launches (after one warm-up) of a peak kernel; flops per launch given.
+double time_peak(const std::function<cudaError_t(double*, int, int, int)>& launch, int iters, double flopsPerThreadIter) {
+  int dev = 0, sms = 1;
+  nlm::ck(cudaGetDevice(&dev), "device");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 4, threads = 256;
+  nlm::DevBuf<double> out;
+  out.alloc((size_t)blocks * threads);
+  cudaEvent_t a, b;
+  nlm::ck(cudaEventCreate(&a), "event");
+  nlm::ck(cudaEventCreate(&b), "event");
+  double best = 0;
+  for (int rep = 0; rep < 4; rep++) {
+    nlm::ck(cudaEventRecord(a, 0), "event");
+    nlm::ck(launch(out.p, iters, blocks, threads), "peak kernel");
+    nlm::ck(cudaEventRecord(b, 0), "event");
+    nlm::ck(cudaEventSynchronize(b), "event");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double flops = flopsPerThreadIter * iters * (double)blocks * threads;
+    if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+}  // namespace
+
 nlm_status nlm_fp64_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();
-    int dev = 0, sms = 1;
-    nlm::ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = sms * 4, threads = 256, iters = 2000;
-    nlm::DevBuf<double> out;
-    out.alloc((size_t)blocks * threads);
-    cudaEvent_t a, b;
-    nlm::ck(cudaEventCreate(&a), "event");
-    nlm::ck(cudaEventCreate(&b), "event");
-    double best = 0;
-    for (int rep = 0; rep < 4; rep++) {
-      nlm::ck(cudaEventRecord(a, 0), "event");
-      nlm::ck(nlm::launch_fp64_peak(out.p, iters, blocks, threads, 0), "fp64 peak");
-      nlm::ck(cudaEventRecord(b, 0), "event");
-      nlm::ck(cudaEventSynchronize(b), "event");
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      const double flops = 2.0 * 32.0 * iters * (double)blocks * threads;
-      if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
-    }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    *tflops = best;
+    // 32 FMAs (64 flops) per thread and iteration
+    *tflops = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
+                        2000, 64.0);
+  });
+}
+
+nlm_status nlm_fp64_mma_peak(double* tflops) {
+  return guarded([&] {
+    nlm::require_device();
+    // 4 m16n8k16 MMAs per warp and iteration: 4 x 2 x 16 x 8 x 16 flops over 32 threads
+    *tflops = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_mma_peak(o, it, bl, th, 0); },
+                        200, 4.0 * 2 * 16 * 8 * 16 / 32);
   });
 }
 

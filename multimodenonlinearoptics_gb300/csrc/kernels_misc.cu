@@ -22,6 +22,7 @@ void add_kernels_cluster(std::vector<KernelEntry>& t);
 void add_kernels_cluster_b(std::vector<KernelEntry>& t);
 void add_kernels_cluster_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse_cluster(std::vector<KernelEntry>& t);
+void add_kernels_adjoint_cluster(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -40,6 +41,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_cluster_b(table);
     add_kernels_cluster_gnlse(table);
     add_kernels_adjoint_gnlse_cluster(table);
+    add_kernels_adjoint_cluster(table);
   });
   *count = (int)table.size();
   return table.data();
@@ -463,6 +465,42 @@ __global__ void k_fp64_peak(double* out, int iters, double a, double b) {
 
 cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s) {
   k_fp64_peak<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);
+  return cudaGetLastError();
+}
+
+// FP64 tensor-core (DMMA) peak: independent m16n8k16 f64 MMAs per warp (4096 FMAs each).  Measures
+// what a DFT-as-GEMM schedule could get from the tensor cores in FP64 on this device.
+__global__ void k_fp64_mma_peak(double* out, int iters, double a0, double b0) {
+  double a[8], b[4], c[4][4];
+#pragma unroll
+  for (int q = 0; q < 8; q++) a[q] = a0 + 1e-9 * (threadIdx.x + q);
+#pragma unroll
+  for (int q = 0; q < 4; q++) b[q] = b0 - 1e-9 * q;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) c[u][q] = 0.0;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7,%8,%9,%10,%11}, "
+          "{%12,%13,%14,%15}, {%0,%1,%2,%3};"
+          : "+d"(c[u][0]), "+d"(c[u][1]), "+d"(c[u][2]), "+d"(c[u][3])
+          : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]), "d"(a[7]), "d"(b[0]),
+            "d"(b[1]), "d"(b[2]), "d"(b[3]));
+    }
+  }
+  double acc = 0.0;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc += c[u][q];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+cudaError_t launch_fp64_mma_peak(double* out, int iters, int blocks, int threads, cudaStream_t s) {
+  k_fp64_mma_peak<<<blocks, threads, 0, s>>>(out, iters, 1e-3, 1e-3);
   return cudaGetLastError();
 }
 

@@ -131,6 +131,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_cluster(const PropArg
 #pragma unroll
         for (int v = 0; v < R; v++) a.gridT[m * ms + tn(v)] = x[m][v];
     }
+    // checkpoints for the reverse sweep: the time-domain state before steps 1, K + 1, 2 K + 1, ...
+    double2* ckRow = a.ckpt ? a.ckpt + inst * a.ckN * MD * (long long)N : nullptr;
+    if (ckRow && a.nZ > 1) {
+#pragma unroll
+      for (int m = 0; m < MD; m++)
+#pragma unroll
+        for (int v = 0; v < R; v++) ckRow[(long long)m * N + tn(v)] = x[m][v];
+    }
     for (int i = 1; i < a.nZ; i++) {
       if (a.prop) {
         // pump-driven solvers: the RK4 step as its per-point real (2M)x(2M) matrix, stored as pairs
@@ -203,6 +211,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_cluster(const PropArg
 #pragma unroll
             for (int v = 0; v < R; v++) a.gridT[m * ms + (long long)i * N + tn(v)] = x[m][v];
           }
+        }
+        if (ckRow && !last && i % a.ckK == 0) {
+#pragma unroll
+          for (int v = 0; v < R; v++) ckRow[((long long)(i / a.ckK) * MD + m) * N + tn(v)] = x[m][v];
         }
       }
     }

@@ -139,6 +139,7 @@ struct SplitSeg {
 };
 cudaError_t launch_split_ff(const SplitSeg* segs, int nSegs, cudaStream_t s);
 cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
+cudaError_t launch_fp64_mma_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
 // Post-processing of the adjoint of Chi2PDC (adjoint.cu)
 cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const double* prof, int nZ, int N,
                                  double2* gP, cudaStream_t s);

@@ -83,6 +83,7 @@ def _load():
         "nlm_adjoint_forward": (i, [vp, vp, sz, vp, i, P(i)]),
         "nlm_adjoint_backward": (i, [vp, vp, vp, vp, P(d)]),
         "nlm_fp64_peak": (i, [P(d)]),
+        "nlm_fp64_mma_peak": (i, [P(d)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -152,6 +153,13 @@ def fp64_peak_tflops():
     """Measured FP64 FMA throughput of the current device (TFLOP/s, FMA = 2 flops)."""
     v = ctypes.c_double()
     _check(_lib.nlm_fp64_peak(ctypes.byref(v)))
+    return v.value
+
+
+def fp64_mma_peak_tflops():
+    """Measured FP64 tensor-core (DMMA) throughput of the current device (TFLOP/s)."""
+    v = ctypes.c_double()
+    _check(_lib.nlm_fp64_mma_peak(ctypes.byref(v)))
     return v.value
 
 

@@ -39,10 +39,11 @@ def _loss(out, target):
     return float(np.sum(np.abs(out) ** 2) - 2 * np.real(np.vdot(target, out)))
 
 
-def _engine_grads(nlm, kw, x, f0, d, target, interval=0):
+def _engine_grads(nlm, kw, x, f0, d, target, interval=0, cluster=1):
     torch = pytest.importorskip("torch")
     from multimodenonlinearoptics_gb300.autograd import propagate_pdc
     med = nlm.Chi2PDC(**kw)
+    med._set_cluster(cluster)
     xt = torch.tensor(x, dtype=torch.complex128, device="cuda", requires_grad=True)
     ft = torch.tensor(f0, dtype=torch.complex128, device="cuda", requires_grad=True)
     dt = torch.tensor(d, dtype=torch.float64, requires_grad=True)
@@ -339,4 +340,36 @@ def test_gnlse_cluster_sweep(nlm, n):
     adj = float(np.sum(np.real(np.conj(g[1, 0]) * d)))
     # the loss is ~1e7 at N=4096: a larger step keeps the difference's round-off (~1e-16 L / h) small
     fd = _dir_fd(loss, x, d, 1e-4)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
+
+
+@pytest.mark.parametrize("n", [1024, 4096])
+def test_pdc_cluster_sweep(nlm, oracle, n):
+    """Few rows on grids of 1024+ points: the checkpointed forward and the reverse sweep both run on
+    4-CTA clusters.  The input, pump and poling gradients agree with the one-CTA sweeps for checkpoint
+    intervals 1 and 7 (segments recomputed with the cluster transforms), and match directional central
+    differences of the oracle's forward."""
+    kw = dict(KW, tPrecision=n, zPrecision=30)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    x, f0, d, target = _problem(n, nz, rows=2, seed=n)
+    res = {}
+    for cluster in (1, 0):
+        for k in (1, 7):
+            res[cluster, k] = _engine_grads(nlm, kw, x, f0, d, target, interval=k, cluster=cluster)
+            if cluster:
+                sched = res[cluster, k][4]._last_schedule()
+                assert sched["grid"] == 8 and sched["R"] == 4
+    for key in ((1, 7), (0, 1), (0, 7)):
+        for ga, gb in zip(res[1, 1][1:4], res[key][1:4]):
+            assert cases.rel_l2(gb, ga) < 1e-11
+    out, gx, gf, gd, _ = res[1, 1]
+    assert cases.rel_l2(out, _oracle_out(oracle, kw, x, f0, d)) < 1e-9
+    r2 = np.random.default_rng(5)
+    v = f0 * np.exp(2j * np.pi * r2.uniform(size=n)) * r2.uniform(0.5, 1.5, n)
+    adj = float(np.sum(gf.real * v.real + gf.imag * v.imag))
+    fd = _dir_fd(lambda f: _loss(_oracle_out(oracle, kw, x, f, d), target), f0, v, 5e-4)
+    assert abs(adj - fd) < 1e-6 * abs(fd)
+    u = r2.uniform(-1, 1, nz)
+    adj = float(np.dot(gd, u))
+    fd = _dir_fd(lambda p: _loss(_oracle_out(oracle, kw, x, f0, p), target), d, u, 5e-4)
     assert abs(adj - fd) < 1e-6 * abs(fd)
