@@ -492,6 +492,66 @@ def measure_configs(nlm, torch, cpu=True):
     return res
 
 
+def measure_consumers(nlm, torch, green_device, C, S, cpu=True):
+    """Green's-function consumers on the benchmark's C and S (N=1024, left in HBM by the engine):
+    the quadrature matrix Z (engine kernel), the covariance Z Z^T with its determinant check
+    (cuBLAS, cuSOLVER) and the Bloch-Messiah principal values (cuSOLVER SVD); against the oracle
+    (numpy / scipy, the reference's own method) on the host."""
+    from multimodenonlinearoptics_gb300 import multimode as mm
+    green_device()
+    torch.cuda.synchronize()
+    n = C.shape[0]
+    Z = mm.calcQuadratureGreens(C, S)
+    mm.calcCovarianceMtx(Z, tol=1e-6)
+    mm.blochMessiahEigs(Z)            # warm-up: library handles and workspaces
+    torch.cuda.synchronize()
+    res = {"n_modes": n, "z_shape": list(Z.shape)}
+    # the element-wise kernel, CUDA events on the current stream.  The L2 is flushed by reading a
+    # 256 MB buffer: a written flush would leave ~129 MB of dirty lines to be written back during
+    # the timed kernel.
+    flush = torch.ones(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    best = float("inf")
+    for _ in range(5):
+        flush.sum()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mm.calcQuadratureGreens(C, S)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    bytes_moved = 2 * n * n * 16 + 4 * n * n * 8          # C and S read, Z written
+    res["quadrature_z_ms"] = best
+    res["quadrature_z_gbs"] = bytes_moved / (best * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    res["hbm_peak_gbs"] = peaks.get("hbm_gbs")
+    if res["hbm_peak_gbs"]:
+        res["quadrature_z_frac_of_measured_hbm"] = res["quadrature_z_gbs"] / res["hbm_peak_gbs"]
+    for name, fn in (("covariance_ms", lambda: mm.calcCovarianceMtx(Z, tol=1e-6)),
+                     ("bloch_messiah_eigs_ms", lambda: mm.blochMessiahEigs(Z)),
+                     ("bloch_messiah_vecs_ms", lambda: mm.blochMessiahVecs(Z))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        res[name] = 1e3 * (time.perf_counter() - t0)
+    if cpu:
+        from oracle import multimode_oracle as M
+        Ch, Sh = C.cpu().numpy(), S.cpu().numpy()
+        t0 = time.perf_counter()
+        Zh = M.quadrature_greens(Ch, Sh)
+        M.covariance(Zh, 1e-6)
+        res["cpu_oracle_z_and_covariance_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        M.bloch_messiah_eigs(Zh)
+        res["cpu_oracle_bloch_messiah_eigs_ms"] = 1e3 * (time.perf_counter() - t0)
+        res["cpu_threads"] = os.cpu_count()
+    return res
+
+
 def measure_ff(nlm, torch, args, stream, flush, C64, S64, f64_value, f64_kernel_ms):
     """The same Green's function with the double-float kernel (FP32 pairs on the FP32 units): device
     throughput over the same steps, kernel time, and its distance from the FP64 result."""
@@ -635,6 +695,10 @@ def run_ours(args):
     ff = measure_ff(nlm, torch, args, stream, flush, C, S, value, kernel_ms / max(kernel_count, 1)) if args.ff else None
     adjoint = measure_adjoint(nlm, torch) if args.adjoint else None
     configs = measure_configs(nlm, torch, cpu=args.cpu_bins > 0) if args.configs else None
+    if configs is not None:
+        with torch.cuda.stream(stream):
+            configs["green_consumers_n1024"] = measure_consumers(nlm, torch, green_device, C, S,
+                                                                 cpu=args.cpu_bins > 0)
 
     line = None
     if rank == 0:

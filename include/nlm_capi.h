@@ -262,6 +262,19 @@ nlm_status nlm_fp64_peak(double* tflops);
  * DFT-as-GEMM schedule could draw on in FP64.  No counterpart in the reference (measurement support). */
 nlm_status nlm_fp64_mma_peak(double* tflops);
 
+/* --- Green's-function consumers (multimode.py:15-47) -------------------------------------------
+ * Device pointers, row-major, on the given CUDA stream (NULL: the legacy default stream); the call
+ * returns after the launch.  green_c / green_s: rows x cols complex128 (the (C, S) pair of
+ * nlm_green*).
+ * nlm_quadrature_greens: z = [[Re(C+S), -Im(C-S)], [Im(C+S), Re(C-S)]], 2 rows x 2 cols float64
+ *   (calcQuadratureGreens, multimode.py:15-26).
+ * nlm_abasis_greens: z = sqrt(1/2) [[C, S], [conj(S), conj(C)]], 2 rows x 2 cols complex128 (the
+ *   matrix of calcCovarianceMtxABasis, multimode.py:40-47). */
+nlm_status nlm_quadrature_greens(const void* green_c_dev, const void* green_s_dev, size_t rows, size_t cols,
+                                 void* z_dev, void* cuda_stream);
+nlm_status nlm_abasis_greens(const void* green_c_dev, const void* green_s_dev, size_t rows, size_t cols, void* z_dev,
+                             void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

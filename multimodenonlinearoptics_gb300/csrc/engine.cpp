@@ -3387,6 +3387,30 @@ nlm_status nlm_fp64_peak(double* tflops) {
   });
 }
 
+nlm_status nlm_quadrature_greens(const void* green_c_dev, const void* green_s_dev, size_t rows, size_t cols,
+                                 void* z_dev, void* cuda_stream) {
+  return guarded([&] {
+    nlm::require_device();
+    if (!green_c_dev || !green_s_dev || !z_dev) throw std::invalid_argument("null device pointer");
+    nlm::ck(nlm::launch_quadrature_z(reinterpret_cast<const double2*>(green_c_dev),
+                                     reinterpret_cast<const double2*>(green_s_dev), (long long)rows, (long long)cols,
+                                     static_cast<double*>(z_dev), static_cast<cudaStream_t>(cuda_stream)),
+            "quadrature Z");
+  });
+}
+
+nlm_status nlm_abasis_greens(const void* green_c_dev, const void* green_s_dev, size_t rows, size_t cols, void* z_dev,
+                             void* cuda_stream) {
+  return guarded([&] {
+    nlm::require_device();
+    if (!green_c_dev || !green_s_dev || !z_dev) throw std::invalid_argument("null device pointer");
+    nlm::ck(nlm::launch_abasis_z(reinterpret_cast<const double2*>(green_c_dev),
+                                 reinterpret_cast<const double2*>(green_s_dev), (long long)rows, (long long)cols,
+                                 nlm::d2(z_dev), static_cast<cudaStream_t>(cuda_stream)),
+            "a-basis Z");
+  });
+}
+
 nlm_status nlm_fp64_mma_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();

@@ -140,6 +140,11 @@ struct SplitSeg {
 cudaError_t launch_split_ff(const SplitSeg* segs, int nSegs, cudaStream_t s);
 cudaError_t launch_fp64_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
 cudaError_t launch_fp64_mma_peak(double* out, int iters, int blocks, int threads, cudaStream_t s);
+// Green's-function consumers (greens_quadrature.cu): quadrature-basis Z and the a-basis block matrix
+cudaError_t launch_quadrature_z(const double2* C, const double2* S, long long rows, long long cols, double* Z,
+                                cudaStream_t s);
+cudaError_t launch_abasis_z(const double2* C, const double2* S, long long rows, long long cols, double2* Za,
+                            cudaStream_t s);
 // Post-processing of the adjoint of Chi2PDC (adjoint.cu)
 cudaError_t launch_adj_pump_rows(const double2* ga, const double2* coef, const double* prof, int nZ, int N,
                                  double2* gP, cudaStream_t s);

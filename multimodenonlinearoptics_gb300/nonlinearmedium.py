@@ -84,6 +84,8 @@ def _load():
         "nlm_adjoint_backward": (i, [vp, vp, vp, vp, P(d)]),
         "nlm_fp64_peak": (i, [P(d)]),
         "nlm_fp64_mma_peak": (i, [P(d)]),
+        "nlm_quadrature_greens": (i, [vp, vp, sz, sz, vp, vp]),
+        "nlm_abasis_greens": (i, [vp, vp, sz, sz, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -4,7 +4,10 @@
    ``setPoling`` (poling.py:439-471, ``domainsToSpace``) is imported from a checkout of the
    reference and run on seeded domain-length arrays.  Run with REFERENCE_ROOT pointing at the
    reference checkout (default: /root/reference).
-2. ``oracle_golden.npz`` -- outputs of the numpy oracle (oracle/nlm_oracle.py) for the small
+2. ``multimode_golden.npz`` -- pinned to the reference itself: outputs of the reference's
+   ``multimode.py`` and ``decompositions.py`` (imported from the checkout) on a Green's pair of the
+   oracle and seeded matrices.
+3. ``oracle_golden.npz`` -- outputs of the numpy oracle (oracle/nlm_oracle.py) for the small
    configurations of tests/cases.py: pump grids, signal grids, Green's matrices and batch rows
    of every solver.  They pin the oracle over time and give the GPU tests fixed expectations.
 
@@ -57,6 +60,66 @@ def make_poling(ref_root):
     np.savez_compressed(os.path.join(HERE, "poling_golden.npz"), **data)
 
 
+def multimode_inputs():
+    """A symplectic Green's pair (the Chi2PDC test medium, from the oracle), its pump profile, and
+    seeded matrices for the decompositions."""
+    kw = cases.oracle_kwargs("Chi2PDC")
+    med = O.SOLVERS["Chi2PDC"](**kw)
+    med.run_pump_simulation()
+    C, S = med.compute_greens_function(False, False)
+    rng = np.random.default_rng(21)
+    n = C.shape[0]
+    a = rng.standard_normal((6, 6)) + 1j * rng.standard_normal((6, 6))
+    return {"C": C, "S": S, "omega": med.omega, "pump": med.pump_time[0][0],
+            "sym_complex": a + a.T, "sym_real": (a + a.T).real, "polar_in": a,
+            "modes": rng.standard_normal((n, n)), "diag": np.exp(rng.uniform(-1, 1, n)),
+            "transmission": rng.uniform(0.2, 0.9, n)}
+
+
+def make_multimode(ref_root):
+    """Outputs of the reference's multimode.py and decompositions.py on multimode_inputs()."""
+    sys.path.insert(0, ref_root)
+    if not hasattr(np, "float_"):
+        np.float_ = np.float64  # the reference predates numpy 2
+    if not hasattr(np, "int"):
+        np.int = int
+    import multimode as mm  # the reference's modules
+    import decompositions as dc
+    x = multimode_inputs()
+    C, S = x["C"], x["S"]
+    out = dict(("in_" + k, v) for k, v in x.items())
+    Z = mm.calcQuadratureGreens(C, S)
+    out["Z"] = Z
+    cov = mm.calcCovarianceMtx(Z)
+    out["cov"] = cov
+    out["cov_a"] = mm.calcCovarianceMtxABasis(C, S)
+    out["normalized_cov"] = mm.normalizedCov(cov)
+    out["lo_squeezing"] = mm.calcLOSqueezing(cov, x["pump"], tol=1.0)   # C_xx = 0.93 here
+    out["downsampled_cov"] = mm.downSampledCov(Z, 12, x["omega"], 2.0)
+    out["downsampled_cov_a"] = mm.downSampledCovABasis(C, S, 12, x["omega"], 2.0)
+    out["bm_eigs"] = mm.blochMessiahEigs(Z)
+    d, lv, rv = mm.blochMessiahVecs(Z)
+    out["bm_diag"], out["bm_left"], out["bm_right"] = d, lv, rv
+    out["ft_c_time"], out["ft_s_time"] = mm.ftGreens(C, S, True)
+    out["ft_c_freq"], out["ft_s_freq"] = mm.ftGreens(C, S, False)
+    out["to_xp"], out["from_xp"] = mm.basisTransforms(5)
+    out["combined_c"], out["combined_s"] = mm.combineGreens(C, S, C.T, S.conj())
+    out["incoherent"] = mm.incoherentPowerGreens(Z)
+    out["photon_mean"] = mm.photonMean(cov)
+    out["photon_mean_a"] = mm.photonMeanA(out["cov_a"])
+    out["photon_cov"] = mm.photonCov(cov)
+    out["fluorescence"] = mm.parametricFluorescence(x["modes"], x["diag"])
+    out["adjacency"] = mm.effectiveAdjacencyMatrix(x["modes"], x["diag"])
+    out["full_adjacency"] = mm.fullEffectiveAdjacencyMatrix(cov)
+    out["lump_scalar"] = mm.covLumpLoss(cov, 0.7)
+    out["lump_vector_a"] = mm.covLumpLoss(out["cov_a"], x["transmission"], abasis=True)
+    out["polar_u"], out["polar_p"] = dc.leftPolar(x["polar_in"])
+    out["takagi_c_l"], out["takagi_c_u"] = dc.takagi(x["sym_complex"])
+    out["takagi_r_l"], out["takagi_r_u"] = dc.takagi(x["sym_real"])
+    out["bm_ut"], out["bm_st"], out["bm_v"] = dc.bloch_messiah(Z, tol=1e-6)   # RK4: symplectic to 2.4e-7
+    np.savez_compressed(os.path.join(HERE, "multimode_golden.npz"), **out)
+
+
 def oracle_case(name):
     kw = cases.oracle_kwargs(name)
     med = O.SOLVERS[name](**kw)
@@ -102,6 +165,7 @@ if __name__ == "__main__":
     ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
     if os.path.exists(os.path.join(ref_root, "poling.py")):
         make_poling(ref_root)
+        make_multimode(ref_root)
     else:
-        print("reference checkout not found; poling fixtures left unchanged", file=sys.stderr)
+        print("reference checkout not found; poling and multimode fixtures left unchanged", file=sys.stderr)
     make_oracle()

@@ -74,3 +74,55 @@ def test_weak_gain_pdc_matches_pump_spectrum(oracle):
     C, S = m.compute_greens_function()
     s_diag = np.abs(np.fliplr(S).diagonal())
     assert np.argmax(s_diag) in (31, 32, 33)
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_multimode_oracle_matches_reference():
+    """The restatement of the Green's-function consumers (multimode.py, decompositions.py) against
+    the reference modules' own outputs (tests/golden/make_golden.py)."""
+    from oracle import multimode_oracle as M
+    g = np.load(os.path.join(HERE, "golden", "multimode_golden.npz"))
+    C, S = g["in_C"], g["in_S"]
+    Z = M.quadrature_greens(C, S)
+    assert np.array_equal(Z, g["Z"])
+    cov = M.covariance(Z)
+    assert _rel(cov, g["cov"]) < 1e-14
+    assert _rel(M.covariance_abasis(C, S), g["cov_a"]) < 1e-14
+    assert _rel(M.normalized_cov(cov), g["normalized_cov"]) < 1e-14
+    assert _rel(M.lo_squeezing(cov, g["in_pump"], tol=1.0), g["lo_squeezing"]) < 1e-13
+    with pytest.raises(AssertionError, match="C_xx"):
+        M.lo_squeezing(cov, g["in_pump"])
+    assert _rel(M.downsampled_cov(Z, 12, g["in_omega"], 2.0), g["downsampled_cov"]) < 1e-14
+    assert _rel(M.downsampled_cov_abasis(C, S, 12, g["in_omega"], 2.0), g["downsampled_cov_a"]) < 1e-14
+    assert _rel(M.bloch_messiah_eigs(Z), g["bm_eigs"]) < 1e-13
+    d, lv, rv = M.bloch_messiah_vecs(Z)
+    assert _rel(d, g["bm_diag"]) < 1e-13 and _rel(lv, g["bm_left"]) < 1e-12 and _rel(rv, g["bm_right"]) < 1e-12
+    for to_time, suffix in ((True, "time"), (False, "freq")):
+        c, s = M.ft_greens(C, S, to_time)
+        assert _rel(c, g["ft_c_" + suffix]) < 1e-14 and _rel(s, g["ft_s_" + suffix]) < 1e-14
+    to_xp, from_xp = M.basis_transforms(5)
+    assert np.array_equal(to_xp, g["to_xp"]) and np.array_equal(from_xp, g["from_xp"])
+    cc, cs = M.combine_greens(C, S, C.T, S.conj())
+    assert _rel(cc, g["combined_c"]) < 1e-14 and _rel(cs, g["combined_s"]) < 1e-14
+    assert _rel(M.incoherent_power_greens(Z), g["incoherent"]) < 1e-15
+    assert _rel(M.photon_mean(cov), g["photon_mean"]) < 1e-13
+    assert _rel(M.photon_mean_a(g["cov_a"]), g["photon_mean_a"]) < 1e-13
+    assert _rel(M.photon_cov(cov), g["photon_cov"]) < 1e-14
+    assert _rel(M.parametric_fluorescence(g["in_modes"], g["in_diag"]), g["fluorescence"]) < 1e-14
+    assert _rel(M.effective_adjacency(g["in_modes"], g["in_diag"]), g["adjacency"]) < 1e-14
+    assert _rel(M.full_effective_adjacency(cov), g["full_adjacency"]) < 1e-13
+    assert _rel(M.cov_lump_loss(cov, 0.7), g["lump_scalar"]) < 1e-15
+    assert _rel(M.cov_lump_loss(g["cov_a"], g["in_transmission"], abasis=True), g["lump_vector_a"]) < 1e-15
+    u, p = M.left_polar(g["in_polar_in"])
+    assert _rel(u, g["polar_u"]) < 1e-13 and _rel(p, g["polar_p"]) < 1e-13
+    for kind in ("c", "r"):
+        src = g["in_sym_complex"] if kind == "c" else g["in_sym_real"]
+        lam, U = M.takagi(src)
+        assert _rel(lam, g["takagi_%s_l" % kind]) < 1e-13 and _rel(U, g["takagi_%s_u" % kind]) < 1e-12
+    ut, st, v = M.bloch_messiah(Z, tol=1e-6)
+    assert _rel(st, g["bm_st"]) < 1e-12
+    assert _rel(ut, g["bm_ut"]) < 1e-10 and _rel(v, g["bm_v"]) < 1e-10
