@@ -216,14 +216,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_adjoint(nlm, torch, reps=3):
-    """grad/fwd cost on the gradient configuration: Chi2PDC N=512, nZSteps=2000, one seeded noise signal
-    (sigma 1e-3), continuous poling d(z) ~ U[-1, 1] (seed 4), loss ||X(L) - target||^2.  fwd = one forward
-    propagation with the pump run (batchSignalSimulation); grad = forward with checkpoints + reverse sweep
-    with the pump-spectrum and poling-profile reductions."""
+def _adjoint_costs(nlm, torch, n, cluster=1, reps=3):
+    """fwd / grad times (ms) of the gradient configuration at n frequency bins: Chi2PDC with
+    nZSteps=2000, one seeded noise signal (sigma 1e-3), continuous poling d(z) ~ U[-1, 1] (seed 4),
+    loss ||X(L) - target||^2.  fwd = one forward propagation with the pump run
+    (batchSignalSimulation); grad = forward with checkpoints + reverse sweep with the pump-spectrum
+    and poling-profile reductions; with the engine's checkpoint interval and with sqrt(nZSteps)."""
     import ctypes
-    kw = dict(CONFIG, tPrecision=512, zPrecision=1000)
+    kw = dict(CONFIG, tPrecision=n, zPrecision=1000)
     med = nlm.Chi2PDC(**kw)
+    med._set_cluster(cluster)
     n, nz = med._dims["nFreqs"], med._dims["nZSteps"]
     rng = np.random.default_rng(4)
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3 / np.sqrt(2)
@@ -275,9 +277,24 @@ def measure_adjoint(nlm, torch, reps=3):
     k_sqrt = int(math.ceil(math.sqrt(nz - 1)))
     t_grad_sqrt = timed(lambda: grad(k_sqrt))
     return {"grad_fwd_cost": t_grad / t_fwd, "fwd_ms": t_fwd, "grad_ms": t_grad, "checkpoint_interval": k_auto,
-            "grad_fwd_cost_sqrt_checkpoints": t_grad_sqrt / t_fwd, "sqrt_checkpoint_interval": k_sqrt,
-            "workload": "Chi2PDC N=512 nZSteps=%d, gradients wrt input spectrum, pump spectrum (512 bins) and "
-                        "poling profile (%d values)" % (nz, nz)}
+            "grad_fwd_cost_sqrt_checkpoints": t_grad_sqrt / t_fwd, "sqrt_checkpoint_interval": k_sqrt, "nz": nz}
+
+
+def measure_adjoint(nlm, torch, reps=3):
+    """grad/fwd cost on the gradient configuration (Chi2PDC N=512, nZSteps=2000), and the same
+    problem on a 2048-point grid, where one propagation runs on a 4-CTA cluster, with the reverse
+    sweep on clusters and on one CTA."""
+    res = _adjoint_costs(nlm, torch, 512, 1, reps)
+    nz = res.pop("nz")
+    res["workload"] = ("Chi2PDC N=512 nZSteps=%d, gradients wrt input spectrum, pump spectrum (512 bins) and "
+                       "poling profile (%d values)" % (nz, nz))
+    big = {"n_freqs": 2048}
+    for cluster, label in ((1, "cluster"), (0, "one_cta")):
+        r = _adjoint_costs(nlm, torch, 2048, cluster, reps)
+        r.pop("nz")
+        big[label] = r
+    res["n2048"] = big
+    return res
 
 
 def measure_configs(nlm, torch, cpu=True):

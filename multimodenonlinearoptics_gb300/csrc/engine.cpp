@@ -25,6 +25,7 @@
 
 #include "../../include/nlm_capi.h"
 #include "nlm_kernels.h"
+#include "nlm_launch.h"
 
 namespace nlm {
 
@@ -1456,39 +1457,20 @@ struct Medium {
     a.ipc = 1;
     a.work = nullptr;
     const int T = a.plan.T;
-    const size_t need = (size_t)5 * M * sizeof(double2);   // M-point twiddles x2, exchange buffer, 2 x C x T receive
-    int dev = 0, optin = 0;
-    ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // M-point twiddles x2, exchange buffer, 2 x C x T receive; each CTA alone on its SM, e.g. beside
+    // the CTAs of a ragged launch
+    size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
-    const int dynMax = optin - (int)fa.sharedSizeBytes;
-    if ((int)need > dynMax) throw Unsupported("grid too large for the cluster kernel");
-    // each CTA alone on its SM (more than half the shared memory): a latency-bound march shares its
-    // SM's FP64 units with nothing else, e.g. with the CTAs of a ragged launch running beside it
-    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);
-    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes),
-       "smem attribute");
+    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    if (smem == 0) throw Unsupported("grid too large for the cluster kernel");
     const long long clusters = std::min<long long>(nInst, smCount() / C);
     lastSchedule = Schedule{(int)(C * clusters), T, 1, smem, 1, 1};
     lastR = C;
     lastTuned = 0;
     lastRegs = fa.numRegs;
     auto record = [&] {
-      cudaLaunchConfig_t cfg{};
-      cfg.gridDim = dim3((unsigned)(C * clusters));
-      cfg.blockDim = dim3((unsigned)T);
-      cfg.dynamicSmemBytes = smem;
-      cfg.stream = stream;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = C;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
       void* args[] = {(void*)&a};
-      ck(cudaLaunchKernelExC(&cfg, k->fn, args), "propagate (cluster)");
+      ck(launch_clustered(k->fn, (int)(C * clusters), T, smem, stream, C, args), "propagate (cluster)");
     };
     if (timeKernels) {
       if (!ev0) ck(cudaEventCreate(&ev0), "event");
@@ -1786,16 +1768,10 @@ struct Medium {
     const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
     if (!k) throw Unsupported("no stored-stage adjoint kernel");
     const int M = (int)N / C;
-    const size_t need = (size_t)5 * M * sizeof(double2);
-    int dev = 0, optin = 0;
-    ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
-    const int dynMax = optin - (int)fa.sharedSizeBytes;
-    if ((int)need > dynMax) throw Unsupported("grid too large for the cluster adjoint");
-    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
-    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    if (smem == 0) throw Unsupported("grid too large for the cluster adjoint");
     PropArgs a = baseArgs(C);
     a.plan = make_plan(M, C);
     a.R = C;
@@ -1807,24 +1783,12 @@ struct Medium {
     d.gout = gout;
     d.gin = gin;
     const long long clusters = std::min<long long>(adjRows, smCount() / C);
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)(C * clusters));
-    cfg.blockDim = dim3((unsigned)a.plan.T);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     void* args[] = {(void*)&a, (void*)&d};
     lastSchedule = Schedule{(int)(C * clusters), a.plan.T, 1, smem, 1, 1};
     lastR = C;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (stored stages)");
+    ck(launch_clustered(k->fn, (int)(C * clusters), a.plan.T, smem, stream, C, args), "adjoint (stored stages)");
     launches++;
     ck(cudaStreamSynchronize(stream), "adjoint");
   }
@@ -1838,34 +1802,18 @@ struct Medium {
     const KernelEntry* k = findKernel(kKindAdjoint, solver + 200, C);
     if (!k) return false;
     const int M = (int)N / C;
-    const size_t need = (size_t)5 * M * sizeof(double2);
-    int dev = 0, optin = 0;
-    ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
-    const int dynMax = optin - (int)fa.sharedSizeBytes;
-    if ((int)need > dynMax) return false;
-    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
-    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    if (smem == 0) return false;
     PropArgs a = baseArgs(C);
     a.plan = make_plan(M, C);
     a.R = C;
     a.nInst = adjRows;
     a.ipc = 1;
     a.work = nullptr;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(2 * C);
-    cfg.blockDim = dim3((unsigned)a.plan.T);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2 * C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cudaLaunchAttribute attr;
+    cudaLaunchConfig_t cfg = cluster_config(2 * C, a.plan.T, smem, stream, 2 * C, &attr);
     int fit = 0;
     if (cudaOccupancyMaxActiveClusters(&fit, k->fn, &cfg) != cudaSuccess) {
       cudaGetLastError();
@@ -1906,16 +1854,10 @@ struct Medium {
     const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
     if (!k) return false;
     const int M = (int)N / C;
-    const size_t need = (size_t)5 * M * sizeof(double2);
-    int dev = 0, optin = 0;
-    ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(cudaFuncGetAttributes(&fa, k->fn), "kernel attributes");
-    const int dynMax = optin - (int)fa.sharedSizeBytes;
-    if ((int)need > dynMax) return false;
-    const size_t smem = std::max<size_t>(need, (size_t)dynMax / 2 + 1024);   // one CTA per SM
-    ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    if (smem == 0) return false;
     PropArgs a = baseArgs(C);
     a.plan = make_plan(M, C);
     a.R = C;
@@ -1938,24 +1880,12 @@ struct Medium {
     d.ga = adjGa.p;
     d.gin = gin;
     d.single = adjRows == 1 ? 1 : 0;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)(C * clusters));
-    cfg.blockDim = dim3((unsigned)a.plan.T);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = C;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     void* args[] = {(void*)&a, (void*)&d};
     lastSchedule = Schedule{(int)(C * clusters), a.plan.T, 1, smem, 1, 1};
     lastR = C;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster)");
+    ck(launch_clustered(k->fn, (int)(C * clusters), a.plan.T, smem, stream, C, args), "adjoint (cluster)");
     launches++;
     return true;
   }
@@ -2014,19 +1944,7 @@ struct Medium {
     d.single = adjRows == 1 ? 1 : 0;
     void* args[] = {(void*)&a, (void*)&d};
     if (kp) {
-      cudaLaunchConfig_t cfg{};
-      cfg.gridDim = dim3(s.grid);
-      cfg.blockDim = dim3(s.block);
-      cfg.dynamicSmemBytes = s.smem;
-      cfg.stream = stream;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = 2;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster)");
+      ck(launch_clustered(k->fn, s.grid, s.block, s.smem, stream, 2, args), "adjoint (cluster)");
     } else {
       ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
     }
@@ -3034,18 +2952,16 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
          "ragged items");
       ck(cudaMemsetAsync(g_ragged.counter.p, 0, sizeof(unsigned long long), st), "ragged counter");
       int block = (int)((maxN / Rg + 31) / 32 * 32);
-      int dev = 0, sms = 1, optin = 0;
+      int dev = 0, sms = 1;
       ck(cudaGetDevice(&dev), "device");
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-      cudaFuncAttributes fa;
-      ck(cudaFuncGetAttributes(&fa, ke->fn), "kernel attributes");
-      const int dynMax = optin - (int)fa.sharedSizeBytes;
       // One CTA per SM: every medium is a sequential march bound by its SM's FP64 units, so a second
       // resident CTA (of this launch or of a cluster propagation running beside it) would only halve
       // both.  Asking for more than half of the SM's shared memory keeps the others off.
-      const size_t smem = std::max<size_t>(maxN * sizeof(double2), (size_t)dynMax / 2 + 1024);
-      ck(cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax), "smem attribute");
+      size_t smem = 0;
+      cudaFuncAttributes fa;
+      ck(exclusive_smem(ke->fn, maxN * sizeof(double2), &smem, &fa), "smem attribute");
+      if (smem == 0) throw Unsupported("ragged kernel does not fit on an SM");
       if (block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
       int active = 0;
       ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, ke->fn, block, smem), "occupancy");
@@ -3065,21 +2981,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         if (!lead->ev1) ck(cudaEventCreate(&lead->ev1), "event");
         ck(cudaEventRecord(lead->ev0, st), "event");
       }
-      {
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3((unsigned)grid);
-        cfg.blockDim = dim3((unsigned)block);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = Medium::kClusterSize;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        ck(cudaLaunchKernelExC(&cfg, ke->fn, args), "ragged launch");
-      }
+      ck(launch_clustered(ke->fn, grid, block, smem, st, Medium::kClusterSize, args), "ragged launch");
       lead->launches++;
       if (lead->timeKernels) {
         ck(cudaEventRecord(lead->ev1, st), "event");

@@ -6,6 +6,7 @@
 // domain (stored as the frequency row), and the inverse transform / N (the time row); the last
 // frequency row then undoes half of the last dispersion step.  The tables are not divided by N here.
 #include "nlm_cluster.cuh"
+#include "nlm_launch.h"
 
 namespace nlm {
 
@@ -94,36 +95,15 @@ cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const
                                      const FFTPlanH& localPlan, const double2* tw, cudaStream_t s) {
   constexpr int C = 4;
   const int M = localPlan.N;
-  const size_t need = (size_t)5 * M * sizeof(double2);   // M-point twiddles x2, exchange buffer, 2 x C x T receive
-  cudaFuncAttributes fa;
-  cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)k_pump_chi3_cluster);
+  // M-point twiddles x2, exchange buffer, 2 x C x T receive; each CTA alone on its SM
+  size_t smem = 0;
+  cudaError_t e = exclusive_smem((const void*)k_pump_chi3_cluster, (size_t)5 * M * sizeof(double2), &smem);
   if (e != cudaSuccess) return e;
-  int dev = 0, optin = 0;
-  e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int dynMax = optin - (int)fa.sharedSizeBytes;
-  if ((int)need > dynMax) return cudaErrorInvalidValue;
-  // each CTA alone on its SM (more than half the shared memory): the march is latency-bound
-  const size_t smem = need > (size_t)dynMax / 2 + 1024 ? need : (size_t)dynMax / 2 + 1024;
-  e = cudaFuncSetAttribute((const void*)k_pump_chi3_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax);
-  if (e != cudaSuccess) return e;
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(C);
-  cfg.blockDim = dim3((unsigned)localPlan.T);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  if (smem == 0) return cudaErrorInvalidValue;
   FFTPlanH plan = localPlan;
   void* args[] = {(void*)&pumpFreq, (void*)&pumpTime, (void*)&env, (void*)&halfP, (void*)&dstepP, (void*)&backP,
                   (void*)&rel, (void*)&nRows, (void*)&plan, (void*)&tw};
-  return cudaLaunchKernelExC(&cfg, (const void*)k_pump_chi3_cluster, args);
+  return launch_clustered((const void*)k_pump_chi3_cluster, C, localPlan.T, smem, s, C, args);
 }
 
 }  // namespace nlm
