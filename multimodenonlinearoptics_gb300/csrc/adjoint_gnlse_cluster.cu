@@ -27,10 +27,6 @@ namespace {
 
 constexpr int kStepSyncs = 18;   // cluster barriers of one forward or reverse step
 
-__device__ __forceinline__ void idle_syncs(cg::cluster_group& cl, int n) {
-  for (int q = 0; q < n; q++) cl.sync();
-}
-
 // Forward step i from the state x (time domain): stores y_s at Yi[s][N] and u2_s at Yi[4 + s][N] and
 // advances x by the step (RK4, then the dispersion step).  18 transposes.
 template <int C>
@@ -190,10 +186,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_cluster(const Pro
           for (int q = 0; q < K; q++) {
             const int i = s0 + 1 + q;
             if (i <= segEnd) forward_step<C>(a, i, N, f, cl, tn, fk, x, stg + (long long)q * stepStride);
-            else idle_syncs(cl, kStepSyncs);
+            else cluster_idle(cl, kStepSyncs);
           }
         } else {
-          idle_syncs(cl, kStepSyncs * K);
+          cluster_idle(cl, kStepSyncs * K);
         }
       } else {
         if (it >= 1) {
@@ -202,10 +198,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_cluster(const Pro
           for (int q = 0; q < K; q++) {
             const int i = segEnd - q;
             if (i > s0) reverse_step<C>(a, i, N, f, cl, tn, fk, g, stg + (long long)(i - 1 - s0) * stepStride);
-            else idle_syncs(cl, kStepSyncs);
+            else cluster_idle(cl, kStepSyncs);
           }
         } else {
-          idle_syncs(cl, kStepSyncs * K);
+          cluster_idle(cl, kStepSyncs * K);
         }
       }
       cl.sync();

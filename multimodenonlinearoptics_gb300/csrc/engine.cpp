@@ -1798,7 +1798,7 @@ struct Medium {
   // such clusters fit on the device at once, or a grid outside its range).
   bool adjointCluster(const double2* gout, double2* gin) {
     constexpr int C = kClusterSize;
-    if (!useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
+    if (solver != kChi3GNLSE || !useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
     const KernelEntry* k = findKernel(kKindAdjoint, solver + 200, C);
     if (!k) return false;
     const int M = (int)N / C;
@@ -1812,13 +1812,7 @@ struct Medium {
     a.nInst = adjRows;
     a.ipc = 1;
     a.work = nullptr;
-    cudaLaunchAttribute attr;
-    cudaLaunchConfig_t cfg = cluster_config(2 * C, a.plan.T, smem, stream, 2 * C, &attr);
-    int fit = 0;
-    if (cudaOccupancyMaxActiveClusters(&fit, k->fn, &cfg) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
+    const int fit = maxActiveClusters(k->fn, 2 * C, a.plan.T, smem);
     // up to three waves of clusters (the two-CTA pipelined sweep is about 3.5 times slower per row)
     if (fit < 1 || adjRows > 3LL * fit) return false;
     const long long waves = (adjRows + fit - 1) / fit;
@@ -1833,13 +1827,13 @@ struct Medium {
     d.ga = adjGa.p;
     d.gin = gin;
     d.single = adjRows == 1 ? 1 : 0;
-    cfg.gridDim = dim3((unsigned)(2 * C * clusters));
     void* args[] = {(void*)&a, (void*)&d};
     lastSchedule = Schedule{(int)(2 * C * clusters), a.plan.T, 1, smem, 1, 1};
     lastR = C;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(cudaLaunchKernelExC(&cfg, k->fn, args), "adjoint (cluster of eight)");
+    ck(launch_clustered(k->fn, (int)(2 * C * clusters), a.plan.T, smem, stream, 2 * C, args),
+       "adjoint (cluster of eight)");
     launches++;
     ck(cudaStreamSynchronize(stream), "adjoint");
     return true;
@@ -1869,8 +1863,27 @@ struct Medium {
       buildPropagator(C);
       a.prop = prop.p;
     }
-    const long long clusters = adjRows;
-    if (adjK > 1) adjSeg.reserve((size_t)clusters * adjK * N);
+    // K > 1: the pipelined form on clusters of eight CTAs (segment recomputation beside the reverse
+    // steps), in at most three waves of clusters
+    int group = C;
+    long long clusters = adjRows;
+    if (adjK > 1) {
+      if (const KernelEntry* kp = findKernel(kKindAdjoint, solver + 200, C)) {
+        size_t smemP = 0;
+        cudaFuncAttributes faP;
+        ck(exclusive_smem(kp->fn, (size_t)5 * M * sizeof(double2), &smemP, &faP), "smem attribute");
+        const int fit = smemP ? maxActiveClusters(kp->fn, 2 * C, a.plan.T, smemP) : 0;
+        if (fit >= 1 && adjRows <= 3LL * fit) {
+          const long long waves = (adjRows + fit - 1) / fit;
+          clusters = (adjRows + waves - 1) / waves;
+          group = 2 * C;
+          k = kp;
+          smem = smemP;
+          fa = faP;
+        }
+      }
+    }
+    if (adjK > 1) adjSeg.reserve((size_t)clusters * (group / C) * adjK * N);   // [cluster][1 or 2][K][N]
     AdjArgs d{};
     d.gout = gout;
     d.ckpt = ckpt.p;
@@ -1881,13 +1894,25 @@ struct Medium {
     d.gin = gin;
     d.single = adjRows == 1 ? 1 : 0;
     void* args[] = {(void*)&a, (void*)&d};
-    lastSchedule = Schedule{(int)(C * clusters), a.plan.T, 1, smem, 1, 1};
+    lastSchedule = Schedule{(int)(group * clusters), a.plan.T, 1, smem, 1, 1};
     lastR = C;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(launch_clustered(k->fn, (int)(C * clusters), a.plan.T, smem, stream, C, args), "adjoint (cluster)");
+    ck(launch_clustered(k->fn, (int)(group * clusters), a.plan.T, smem, stream, group, args), "adjoint (cluster)");
     launches++;
     return true;
+  }
+
+  // Clusters of clusterSize CTAs of `fn` that fit on the device at once (0 when the query fails).
+  int maxActiveClusters(const void* fn, int clusterSize, int block, size_t smem) {
+    cudaLaunchAttribute attr;
+    cudaLaunchConfig_t cfg = cluster_config(clusterSize, block, smem, stream, clusterSize, &attr);
+    int fit = 0;
+    if (cudaOccupancyMaxActiveClusters(&fit, fn, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return fit;
   }
 
   // The one-CTA and two-CTA-cluster reverse sweeps (the stage-factor gradients go to adjGa).

@@ -51,6 +51,12 @@ __device__ __forceinline__ void cluster_transpose(ClusterFFT<C>& f, double2 (&x)
   f.phase ^= 1;
 }
 
+// n bare cluster barriers: the slots of a group that has no transform to do while the other group of
+// the same cluster does (every transpose ends with a barrier of the whole cluster)
+__device__ __forceinline__ void cluster_idle(cg::cluster_group& cl, int n) {
+  for (int q = 0; q < n; q++) cl.sync();
+}
+
 // time-domain ownership -> frequency-domain ownership
 template <int C>
 __device__ __forceinline__ void cluster_fft_fwd(ClusterFFT<C>& f, double2 (&x)[C], cg::cluster_group& cl) {

@@ -345,10 +345,10 @@ def test_gnlse_cluster_sweep(nlm, n):
 
 @pytest.mark.parametrize("n", [1024, 4096])
 def test_pdc_cluster_sweep(nlm, oracle, n):
-    """Few rows on grids of 1024+ points: the checkpointed forward and the reverse sweep both run on
-    4-CTA clusters.  The input, pump and poling gradients agree with the one-CTA sweeps for checkpoint
-    intervals 1 and 7 (segments recomputed with the cluster transforms), and match directional central
-    differences of the oracle's forward."""
+    """Few rows on grids of 1024+ points: the checkpointed forward runs on 4-CTA clusters, and so does
+    the reverse sweep for checkpoint interval 1; interval 7 (segments recomputed with the cluster
+    transforms) runs pipelined on clusters of eight CTAs.  The input, pump and poling gradients agree
+    with the one-CTA sweeps, and match directional central differences of the oracle's forward."""
     kw = dict(KW, tPrecision=n, zPrecision=30)
     nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
     x, f0, d, target = _problem(n, nz, rows=2, seed=n)
@@ -358,7 +358,7 @@ def test_pdc_cluster_sweep(nlm, oracle, n):
             res[cluster, k] = _engine_grads(nlm, kw, x, f0, d, target, interval=k, cluster=cluster)
             if cluster:
                 sched = res[cluster, k][4]._last_schedule()
-                assert sched["grid"] == 8 and sched["R"] == 4
+                assert sched["grid"] == (8 if k == 1 else 16) and sched["R"] == 4
     for key in ((1, 7), (0, 1), (0, 7)):
         for ga, gb in zip(res[1, 1][1:4], res[key][1:4]):
             assert cases.rel_l2(gb, ga) < 1e-11
