@@ -1535,12 +1535,17 @@ struct Medium {
 
   double propagatorBytes() const { return (double)(nZ > 1 ? nZ - 1 : 0) * 4.0 * nSignal * nSignal * N * 8.0; }
 
+  // The RK4 propagator matrices replace the four stage evaluations of every step and point by one
+  // (2M x 2M) matrix product.  Their build evaluates the 2M unit vectors' RK4 steps for all steps and
+  // points in one parallel launch: 2M propagations' worth of point-wise work, which a batch of 4M or
+  // more propagations amortises, and which costs little wall time beside a latency-bound launch of
+  // fewer propagations than SMs (the build runs on the idle SMs).
   bool wantPropagator(long long nInst) const {
     if (!linearSolver()) return false;
     if (usePropagator == 0) return false;
     if (propagatorBytes() > 16e9) return false;
     if (usePropagator == 1) return true;
-    return nInst >= 4LL * nSignal;
+    return nInst >= 4LL * nSignal || nInst < smCount();
   }
 
   // Launch one propagation kernel over `nInst` instances (inputs/outputs prepared in `a`).
@@ -1577,6 +1582,14 @@ struct Medium {
         k = findKernel(kKindLinearFF, 1 + 10 * shortRadix(a.plan), R);
       } else {
         k = findKernel(kKindLinear, (int)nSignal, R);
+        // latency-bound launches: four points per thread, as for the direct kernels below
+        if (nInst < smCount() && (int)N / R < 128 && (int)N / 4 <= 512) {
+          if (const KernelEntry* k4 = findKernel(kKindLinear, (int)nSignal, 4)) {
+            k = k4;
+            a.plan = make_plan((int)N, 4);
+            a.R = 4;
+          }
+        }
       }
     } else {
       k = findKernel(kKindDirect, solver, R);
@@ -2052,7 +2065,7 @@ struct Medium {
     a.inputMode = (a.inChannels > 1 || nSignal <= 1) ? 0 : (int)inputMode;
     a.gridF = sigFreq.p;
     a.gridT = sigTime.p;
-    propagate(a, 1, false);
+    propagate(a, 1, true);
     ck(cudaStreamSynchronize(stream), "signal simulation");
     signalVersion++;
   }

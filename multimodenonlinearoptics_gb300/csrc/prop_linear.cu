@@ -13,6 +13,9 @@ void add_kernels_linear(std::vector<KernelEntry>& t) {
   t.push_back({kKindLinear, 1, 8, (const void*)k_propagate_linear_occ<1, 8, 6>});
   t.push_back({kKindLinear, 2, 8, (const void*)k_propagate_linear<2, 8>});
   t.push_back({kKindLinear, 4, 4, (const void*)k_propagate_linear<4, 4>});
+  // latency-bound launches (fewer propagations than SMs): N/4 threads, all four schedulers of the SM
+  t.push_back({kKindLinear, 1, 4, (const void*)k_propagate_linear<1, 4>});
+  t.push_back({kKindLinear, 2, 4, (const void*)k_propagate_linear<2, 4>});
   // linear (pump-driven) solvers: their RK4 step is real-linear in the signal
   t.push_back({kKindBuildProp, kChi3, 0, (const void*)k_build_propagator<FChi3>});
   t.push_back({kKindBuildProp, kChi2PDC, 0, (const void*)k_build_propagator<FChi2PDC>});
