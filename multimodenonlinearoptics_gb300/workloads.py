@@ -85,11 +85,11 @@ def ragged_media(nlm, seed=3, count=64):
     return media, [p[3] for p in params]
 
 
-def adjoint_problem(nlm, z_precision=1000):
-    """The gradient configuration: Chi2PDC as the Green's workload but N=512, nZSteps=2 zPrecision (2000),
-    one seeded noise signal (sigma 1e-3), continuous poling d(z) ~ U[-1, 1] (seed 4), a unit-energy
-    seeded target spectrum."""
-    med = nlm.Chi2PDC(**dict(GREEN_CONFIG, tPrecision=512, zPrecision=z_precision))
+def adjoint_problem(nlm, z_precision=1000, n=512):
+    """The gradient configuration: Chi2PDC as the Green's workload but N=512 (or n), nZSteps=2 zPrecision
+    (2000), one seeded noise signal (sigma 1e-3), continuous poling d(z) ~ U[-1, 1] (seed 4), a
+    unit-energy seeded target spectrum."""
+    med = nlm.Chi2PDC(**dict(GREEN_CONFIG, tPrecision=n, zPrecision=z_precision))
     n, nz = med._dims["nFreqs"], med._dims["nZSteps"]
     rng = np.random.default_rng(4)
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * 1e-3 / np.sqrt(2)
@@ -139,6 +139,26 @@ def _run(name, z_precision, rows, reps):
             nlm._check(nlm._lib.nlm_adjoint_backward(med._h(), ctypes.c_void_p(g.data_ptr()),
                                                      ctypes.c_void_p(gin.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
                                                      nlm._dptr(gpol)))
+        elif name == "chi3_pump":
+            m = nlm.Chi3(**dict(CHI3_CONFIG, tPrecision=8192, tMax=40, beta3=0.02, zPrecision=z_precision or 500))
+            m.runPumpSimulation()
+        elif name == "adjoint_cluster":
+            med, x, d, target = adjoint_problem(nlm, z_precision or 1000, n=2048)
+            nz = med._dims["nZSteps"]
+            med._set_poling_profile(d)
+            xin = torch.tensor(x.reshape(1, -1), dtype=torch.complex128, device="cuda")
+            out = torch.empty_like(xin)
+            used = ctypes.c_int()
+            nlm._check(nlm._lib.nlm_run_pump(med._h()))
+            nlm._check(nlm._lib.nlm_adjoint_forward(med._h(), ctypes.c_void_p(xin.data_ptr()), 1,
+                                                    ctypes.c_void_p(out.data_ptr()), 0, ctypes.byref(used)))
+            g = (2 * (out - torch.tensor(target.reshape(1, -1), device="cuda"))).contiguous()
+            gin = torch.empty_like(xin)
+            gp = torch.empty(x.size, dtype=torch.complex128, device="cuda")
+            gpol = np.zeros(nz)
+            nlm._check(nlm._lib.nlm_adjoint_backward(med._h(), ctypes.c_void_p(g.data_ptr()),
+                                                     ctypes.c_void_p(gin.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
+                                                     nlm._dptr(gpol)))
         elif name == "signal":
             m = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS),
                             **dict(GREEN_CONFIG, tPrecision=2048, zPrecision=z_precision or 500))
@@ -165,8 +185,8 @@ def _run(name, z_precision, rows, reps):
 
 def main():
     ap = argparse.ArgumentParser(description="run one benchmark workload on cuda:0")
-    ap.add_argument("name", choices=["green", "chi3", "ragged", "adjoint", "gnlse", "gnlse_grad", "signal",
-                                         "gnlse_signal"])
+    ap.add_argument("name", choices=["green", "chi3", "chi3_pump", "ragged", "adjoint", "adjoint_cluster", "gnlse",
+                                     "gnlse_grad", "signal", "gnlse_signal"])
     ap.add_argument("--zprecision", type=int, default=0, help="zPrecision override (0: the workload's own)")
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")
     ap.add_argument("--reps", type=int, default=1)
