@@ -1571,8 +1571,17 @@ struct Medium {
     }
     if (a.stages) throw std::logic_error("stage values are stored by the cluster kernels only");
     checkGridStrict(R);
+    bool paired = false;
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
+      // at least two rows per SM: two rows per thread group, sharing their Raman transforms
+      // (k_propagate_gnlse_pair: 14 transforms per row and step instead of 18)
+      if (!plainOne && nInst >= 2LL * smCount() && !a.gridF && !a.gridT) {
+        if (const KernelEntry* kp = findKernel(kKindGnlse, solver + 400, R)) {
+          k = kp;
+          paired = true;
+        }
+      }
     } else if (allowPropagator && wantPropagator(nInst)) {
       buildPropagator(R);
       a.prop = prop.p;
@@ -1617,7 +1626,8 @@ struct Medium {
         lastTuned = 1;
       }
     }
-    if (!lastTuned) s = schedule(k, nInst, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
+    const long long units = paired ? (nInst + 1) / 2 : nInst;   // thread groups' work items
+    if (!lastTuned) s = schedule(k, units, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
     if (plainOne) s.grid = 1;
     lastSchedule = s;
     lastR = a.R;
@@ -1627,14 +1637,14 @@ struct Medium {
     }
     a.ipc = s.ipc;
     a.work = nullptr;
-    const bool counter = !plainOne && (long long)s.grid < (nInst + s.ipc - 1) / s.ipc;
+    const bool counter = !plainOne && (long long)s.grid < (units + s.ipc - 1) / s.ipc;
     if (counter) {
       workCounter.reserve(1);
       a.work = workCounter.p;
     }
     double2* sp = nullptr;
     if (gnlse) {
-      scratch.reserve((size_t)s.grid * s.ipc * 2 * N);
+      scratch.reserve((size_t)s.grid * s.ipc * (paired ? 7 : 2) * N);
       sp = scratch.p;
     }
     // with kernel timing on, the tail runs after the timed region, outside the graph

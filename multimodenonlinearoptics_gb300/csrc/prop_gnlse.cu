@@ -98,8 +98,132 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
   }
 }
 
+// Two rows per thread group (rows 2q and 2q+1 of the launch).  The Raman convolution acts on the real
+// intensity rel |y|^2 with the transform of a real response, R~ (Hermitian), so the two rows'
+// convolutions run as one complex convolution: IFFT[R~ FFT[uA + i uB]] = conv(uA) + i conv(uB).  A row
+// then costs 14 transforms per step instead of 18 (4 stages x (1 shared Raman pair / 2 + steepening
+// pair) + the dispersion pair); the Raman result is taken real, as it is in exact arithmetic.  A
+// second row past the end of the launch propagates zeros and is not stored.
+// Scratch per slot: the two rows' states X, RK4 sums A and stage results K, and their real Raman
+// results (7 N complex values).
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const PropArgs a, double2* __restrict__ scratch) {
+  extern __shared__ double2 smem[];
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const int g = threadIdx.x / T, j = threadIdx.x - g * T;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
+  // slot: X of row 0 and 1, then A of row 0 and 1, then K of row 0 and 1 (N values each), then the
+  // two rows' real Raman results (N reals each, in the space of N complex values)
+  double2* slot = scratch + ((long long)blockIdx.x * a.ipc + g) * 7 * N;
+  auto U = [&](int r) { return reinterpret_cast<double*>(slot + 6 * N) + (long long)r * N; };
+  auto X = [&](int r) { return slot + (long long)r * N; };
+  auto A = [&](int r) { return slot + (long long)(2 + r) * N; };
+  auto K = [&](int r) { return slot + (long long)(4 + r) * N; };
+  const long long nPairs = (a.nInst + 1) / 2;
+  const long long nGroups = (nPairs + a.ipc - 1) / a.ipc;
+  __shared__ long long s_group;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
+    const long long pair = cg * a.ipc + g;
+    auto active = [&](int r) { return pair < nPairs && 2 * pair + r < a.nInst; };
+    auto inst = [&](int r) { return a.instBase + 2 * pair + r; };
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      double2 x[1][R];
+      load_input<1, R>(a, inst(r), active(r), j, x, buf, plan, tw);
+      fft_regs<R, true>(x[0], buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) X(r)[j + v * T] = x[0][v];
+      if (a.ckpt && a.nZ > 1) store_rows<1, R>(a.ckpt + inst(r) * a.ckN * (long long)N, N, 0, N, T, j, x, 1.0, active(r));
+    }
+    for (int i = 1; i < a.nZ; i++) {
+      const double* rel = a.relInt + (long long)(i - 1) * 3;
+      for (int s = 0; s < 4; s++) {
+        const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+        const double wgt = (s == 1 || s == 2) ? 2.0 : 1.0;
+        const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+        // both rows' Raman convolutions in one complex transform pair
+        double2 u[R];
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          const double2 yA = s == 0 ? X(0)[t] : caxpy(X(0)[t], fac, K(0)[t]);
+          const double2 yB = s == 0 ? X(1)[t] : caxpy(X(1)[t], fac, K(1)[t]);
+          u[v] = make_double2(ri * cabs2(yA), ri * cabs2(yB));
+        }
+        fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+        for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + j + v * T));
+        fft_regs<R, true>(u, buf, tw, plan, j);
+        // the two real results wait in scratch (each thread reads back its own points)
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          U(0)[j + v * T] = u[v].x;
+          U(1)[j + v * T] = u[v].y;
+        }
+        // per row: times the field, then the self-steepening operator (g0 + g1 w)
+#pragma unroll 1
+        for (int r = 0; r < 2; r++) {
+          double2 w[R];
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            const double2 y = s == 0 ? X(r)[t] : caxpy(X(r)[t], fac, K(r)[t]);
+            const double c = U(r)[t];
+            w[v] = make_double2(c * y.x, c * y.y);
+          }
+          fft_regs<R, false>(w, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) w[v] = cmul(w[v], __ldg(a.steep + j + v * T));
+          fft_regs<R, true>(w, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            K(r)[t] = w[v];
+            A(r)[t] = s == 0 ? w[v] : caxpy(A(r)[t], wgt, w[v]);
+          }
+        }
+      }
+      const bool last = i == a.nZ - 1;
+#pragma unroll 1
+      for (int r = 0; r < 2; r++) {
+        double2 x[1][R];
+#pragma unroll
+        for (int v = 0; v < R; v++) x[0][v] = caxpy(X(r)[j + v * T], 1.0 / 6.0, A(r)[j + v * T]);
+        dispersion_step<1, R>(a, i, last, j, x, buf, plan, active(r), last ? a.dlast : a.dstep, tw);
+        if (!last) {
+#pragma unroll
+          for (int v = 0; v < R; v++) X(r)[j + v * T] = x[0][v];
+          if (a.ckpt && i % a.ckK == 0)
+            store_rows<1, R>(a.ckpt + (inst(r) * a.ckN + i / a.ckK) * (long long)N, N, 0, N, T, j, x, 1.0, active(r));
+        } else {
+          store_output<1, R>(a, inst(r), active(r), j, x, a.inTime ? 1.0 : (double)N);
+        }
+      }
+    }
+    if (a.nZ == 1) {
+#pragma unroll 1
+      for (int r = 0; r < 2; r++) {
+        double2 x[1][R];
+#pragma unroll
+        for (int v = 0; v < R; v++) x[0][v] = X(r)[j + v * T];
+        fft_regs<R, false>(x[0], buf, tw, plan, j);
+#pragma unroll
+        for (int v = 0; v < R; v++) x[0][v] = cmul(x[0][v], __ldg(a.back + j + v * T));
+        if (a.inTime) fft_regs<R, true>(x[0], buf, tw, plan, j);
+        store_output<1, R>(a, inst(r), active(r), j, x, a.inTime ? 1.0 : (double)N);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 void add_kernels_gnlse(std::vector<KernelEntry>& t) {
   t.push_back({kKindGnlse, kChi3GNLSE, 8, (const void*)k_propagate_gnlse<8>});
+  // key + 400: two rows per thread group, shared Raman transforms
+  t.push_back({kKindGnlse, kChi3GNLSE + 400, 8, (const void*)k_propagate_gnlse_pair<8>});
 }
 
 }  // namespace nlm

@@ -1,0 +1,58 @@
+"""Chi3GNLSE batches of at least two rows per SM run two rows per thread group, with the two rows'
+Raman convolutions as one complex convolution (k_propagate_gnlse_pair).  Against the oracle, against
+the one-row kernel on the same rows, with an odd row count, and under the adjoint's checkpointed
+forward."""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+
+def _rows(n, rows, seed):
+    t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
+    rng = np.random.default_rng(seed)
+    base = 2.0 / np.cosh(t)
+    return np.fft.fft(base[None, :] + cases.noise(rng, rows * n, 0.05).reshape(rows, n), axis=1)
+
+
+@pytest.mark.parametrize("rows", [320, 321])
+def test_paired_rows_match_oracle_and_one_row_kernel(nlm, oracle, rows):
+    kw = dict(cases.CASES["Chi3GNLSE"])
+    med, ref = nlm.Chi3GNLSE(**kw), oracle.Chi3GNLSE(**kw)
+    n = med._dims["nFreqs"]
+    x = _rows(n, rows, rows)
+    out = med.batchSignalSimulation(x, inTimeDomain=False)
+    sched = med._last_schedule()
+    assert sched["grid"] <= (rows + 1) // 2      # thread groups hold pairs of rows
+    assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
+    # the same rows through the one-row kernel (fewer than two rows per SM per launch)
+    single = np.concatenate([med.batchSignalSimulation(x[k:k + 100], inTimeDomain=False)
+                             for k in range(0, rows, 100)])
+    assert cases.rel_l2(out, single) < 1e-12
+    assert not np.array_equal(out, single)        # two kernels (the Raman result is taken real)
+    # each row on its own: the unpaired last row of an odd count is computed like the others
+    assert cases.rel_l2(out[-1], single[-1]) < 1e-12
+
+
+def test_paired_forward_under_the_adjoint(nlm):
+    """320 rows: the adjoint's checkpointed forward runs paired; the gradients of the first rows equal
+    those of a 3-row problem (the loss is a sum over rows)."""
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    kw = dict(cases.CASES["Chi3GNLSE"])
+    n = nlm.Chi3GNLSE(**kw)._dims["nFreqs"]
+    x = _rows(n, 320, 5)
+    weights = torch.linspace(0, 1, n, device="cuda", dtype=torch.float64)
+    grads = {}
+    for rows in (3, 320):
+        for k in (1, 4):
+            med = nlm.Chi3GNLSE(**kw)
+            xt = torch.tensor(x[:rows], device="cuda", requires_grad=True)
+            out = propagate_gnlse(med, xt, k)
+            torch.sum(torch.abs(out) ** 2 * weights).backward()
+            grads[rows, k] = xt.grad.cpu().numpy()
+    for key in ((3, 4), (320, 1), (320, 4)):
+        assert cases.rel_l2(grads[key][:3], grads[3, 1]) < 1e-11
