@@ -1535,6 +1535,19 @@ struct Medium {
 
   double propagatorBytes() const { return (double)(nZ > 1 ? nZ - 1 : 0) * 4.0 * nSignal * nSignal * N * 8.0; }
 
+  // Ragged batches run each medium once per call, and fill the GPU: a medium's RK4 matrices (2M stage
+  // evaluations per point and step, built beside the propagations) pay off only when they are used
+  // again.  Use them while fresh, build them when the medium runs again with the same pump, and
+  // propagate with the DiffEq otherwise.
+  bool raggedPropagator() {
+    if (!linearSolver() || usePropagator == 0 || nZ <= 1 || propagatorBytes() > 16e9) return false;
+    if (usePropagator == 1 || (propVersion == pumpVersion && prop.p)) return true;
+    const bool again = raggedPumpVersion == pumpVersion;
+    raggedPumpVersion = pumpVersion;
+    return again;
+  }
+  long long raggedPumpVersion = -1;
+
   // The RK4 propagator matrices replace the four stage evaluations of every step and point by one
   // (2M x 2M) matrix product.  Their build evaluates the 2M unit vectors' RK4 steps for all steps and
   // points in one parallel launch: 2M propagations' worth of point-wise work, which a batch of 4M or
@@ -1561,7 +1574,7 @@ struct Medium {
     // A few propagations on a large grid: each one spread over a cluster of kClusterSize CTAs (also on
     // grids that the one-CTA kernels do not take, e.g. Chi3GNLSE at N=8192)
     if (const KernelEntry* kc = clusterKernel(a, nInst, plainOne)) {
-      if (linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+      if (allowPropagator && wantPropagator(nInst)) {
         buildPropagator(R);
         a.prop = prop.p;
       }
@@ -1761,7 +1774,7 @@ struct Medium {
     a.ckpt = ckpt.p;
     a.ckK = K;
     a.ckN = nCk;
-    propagate(a, (long long)rows, false);
+    propagate(a, (long long)rows, true);
     ck(cudaStreamSynchronize(stream), "adjoint forward");
     adjRows = (long long)rows;
     adjK = K;
@@ -2925,7 +2938,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
           for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
           a.out = g_ragged.cout.p + oo;
           a.outStride = (long long)m->nSignal * m->N;
-          m->propagate(a, 1, true);
+          m->propagate(a, 1, m->raggedPropagator());
           pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
                                 (size_t)m->nSignal * m->N * sizeof(double2), m->stream});
           clusterSync.push_back(m->stream);
@@ -2947,13 +2960,13 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       Medium* lead = ms[ks[0]];
       cudaStream_t st = lead->stream;
-      // pump-driven solvers: each medium's per-point RK4 matrices, built on the launch's stream just
-      // before it (each build is parallel over all steps and points of its medium); the media run as
-      // cluster propagations build theirs on their own streams
+      // pump-driven solvers: each medium's per-point RK4 matrices when Medium::raggedPropagator wants
+      // them, built on the launch's stream just before it (each build is parallel over all steps and
+      // points of its medium); the media run as cluster propagations build theirs on their own streams
       std::vector<bool> withProp(n_media, false);
       for (size_t k : ks) {
         Medium* m = ms[k];
-        if (m->linearSolver() && m->usePropagator != 0 && m->nZ > 1 && m->propagatorBytes() <= 16e9) {
+        if (m->raggedPropagator()) {
           m->buildPropagator(8, st);
           withProp[k] = true;
         }

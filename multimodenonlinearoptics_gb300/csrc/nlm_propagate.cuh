@@ -274,6 +274,7 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
 #pragma unroll
     for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
     if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+    if (a.ckpt && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       // entries stored as pairs (row r, columns 2c and 2c+1) so a point loads D*D/2 16-byte words
       const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (E / 2) * N;
@@ -303,6 +304,8 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
       }
       const bool last = i == a.nZ - 1;
       dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      if (a.ckpt && !last && i % a.ckK == 0)
+        store_rows<M, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     }
     if (a.nZ == 1) {
 #pragma unroll

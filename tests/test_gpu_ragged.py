@@ -8,10 +8,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-9
 
 
-@pytest.mark.parametrize("use_prop", [1, 0])
+@pytest.mark.parametrize("use_prop", [1, -1, 0])
 def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
-    """With use_prop, every (pump-driven) medium's RK4 matrices are built before the one launch (one
-    build launch per medium); without, the launch evaluates the DiffEq."""
+    """use_prop 1: every (pump-driven) medium's RK4 matrices are built before the one launch (one
+    build launch per medium); 0: the launch evaluates the DiffEq; -1 (the default): the DiffEq on the
+    first call after a pump change, the matrices built on the second and reused from the third."""
     from multimodenonlinearoptics_gb300.workloads import ragged_media_params
     params = ragged_media_params(seed=11, count=6)
     media, refs, ins = [], [], []
@@ -33,11 +34,18 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
     refs[-1].run_pump_simulation()
     ins.append(cases.signal_input("Chi2PDC", 64, 1, seed=3))
     for m in media:
-        m._set_schedule(use_propagator=-1 if use_prop else 0)
+        m._set_schedule(use_propagator=use_prop)
         m._set_cluster(0)                                   # every medium in the ragged launch
     outs = nlm.ragged_batch(media, ins)
     # one launch per solver in the set (plus the propagator builds)
-    assert sum(m._launch_count() for m in media) == 2 + (len(media) if use_prop else 0)
+    assert sum(m._launch_count() for m in media) == 2 + (len(media) if use_prop == 1 else 0)
+    if use_prop == -1:
+        again = nlm.ragged_batch(media, ins)
+        assert sum(m._launch_count() for m in media) == 2 + len(media)
+        third = nlm.ragged_batch(media, ins)
+        assert sum(m._launch_count() for m in media) == 2
+        for o, o2, o3 in zip(outs, again, third):
+            assert cases.rel_l2(o2, o) < 1e-13 and np.array_equal(o3, o2)
     for m, r, x, o in zip(media, refs, ins, outs):
         f, _ = r.propagate(x[None, :], False, 0)
         assert cases.rel_l2(o, f[0]) < TOL
