@@ -46,11 +46,11 @@ __device__ __forceinline__ void pdc_recompute_segment(const PropArgs& a, const d
   }
 }
 
-// Reverse steps i = segEnd .. s0+1; states[(i-1-s0) N ..] holds s_{i-1}.
+// Reverse steps i = segEnd .. s0+1; states[(i-1-s0) N ..] holds s_{i-1} (unused in the marching form).
 template <int R>
 __device__ __forceinline__ void pdc_reverse_segment(const PropArgs& a, const AdjArgs& d, const double2* states,
                                                     int s0, int segEnd, double2 (&gv)[R], bool active, double2* buf,
-                                                    const double2* tw, int j) {
+                                                    const double2* tw, int j, long long inst) {
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
   for (int i = segEnd; i > s0; i--) {
@@ -60,6 +60,11 @@ __device__ __forceinline__ void pdc_reverse_segment(const PropArgs& a, const Adj
 #pragma unroll
     for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
     fft_regs<R, true>(gv, buf, tw, plan, j);
+    if (d.gp) {
+#pragma unroll
+      for (int v = 0; v < R; v++) gv[v] = pdc_march_point(a, d, N, i, j + v * T, inst, gv[v], active);
+      continue;
+    }
     const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
     const double2 c0 = c[0], c1 = c[1], c2 = c[2];
 #pragma unroll
@@ -115,7 +120,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc(const PropArgs a, c
       const int jseg = (segEnd - 1) / d.K;
       const int s0 = jseg * d.K;
       if (d.K > 1) pdc_recompute_segment<R>(a, ck, jseg, s0, segEnd, segp, buf, tw, j);
-      pdc_reverse_segment<R>(a, d, d.K > 1 ? segp : ck + (long long)s0 * N, s0, segEnd, gv, active, buf, tw, j);
+      pdc_reverse_segment<R>(a, d, d.K > 1 ? segp : ck + (long long)s0 * N, s0, segEnd, gv, active, buf, tw, j, inst);
       segEnd = s0;
     }
     pdc_store_gin<R>(a, d, inst, active, gv, buf, tw, j);
@@ -155,13 +160,52 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_pipe(const PropArgs
       }
       if (role == 0 && it >= 1) {
         const int jseg = nSeg - it, s0 = jseg * d.K, segEnd = min(s0 + d.K, a.nZ - 1);
-        pdc_reverse_segment<R>(a, d, states + (long long)((it - 1) & 1) * d.K * N, s0, segEnd, gv, true, buf, tw, j);
+        pdc_reverse_segment<R>(a, d, states + (long long)((it - 1) & 1) * d.K * N, s0, segEnd, gv, true, buf, tw, j,
+                               inst);
       }
       cluster.sync();
     }
     if (role == 0) pdc_store_gin<R>(a, d, inst, true, gv, buf, tw, j);
     __syncthreads();
   }
+}
+
+// The stage-factor gradients of the marching form: for every step i and point t, the stage chain at
+// the state before the step (checkpoint interval 1: d.ckpt row i-1) and the gradient after it (d.gp),
+// summed over the rows.  Parallel over all steps and points, after the sequential march.
+__global__ void k_adj_stage_grads(const PropArgs a, const AdjArgs d, int N, long long rows) {
+  const long long total = (long long)(a.nZ - 1) * N;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / N) + 1, t = (int)(idx - (long long)(i - 1) * N);
+    const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+    const double2 c0 = c[0], c1 = c[1], c2 = c[2];
+    double2 s0 = czero(), s1 = czero(), s2 = czero();
+    for (long long r = 0; r < rows; r++) {
+      const double2 x = d.ckpt[(r * d.nCk + (i - 1)) * (long long)N + t];
+      const double2 gp = d.gp[(r * (a.nZ - 1) + (i - 1)) * (long long)N + t];
+      double2 g0, g1, g2;
+      pdc_stage_chain(a, N, i, t, c0, c1, c2, x, gp, g0, g1, g2);
+      s0 = cadd(s0, g0);
+      s1 = cadd(s1, g1);
+      s2 = cadd(s2, g2);
+    }
+    double2* gacc = d.ga + (long long)(i - 1) * 3 * N;
+    gacc[t] = s0;
+    gacc[N + t] = s1;
+    gacc[2 * N + t] = s2;
+  }
+}
+
+static int sm_count_adj();
+
+cudaError_t launch_adj_stage_grads(const PropArgs& a, const AdjArgs& d, int N, long long rows, cudaStream_t s) {
+  const long long total = (long long)(a.nZ - 1) * N;
+  if (total <= 0) return cudaSuccess;
+  long long grid = (total + 255) / 256;
+  if (grid > 8LL * sm_count_adj()) grid = 8LL * sm_count_adj();
+  k_adj_stage_grads<<<(unsigned)grid, 256, 0, s>>>(a, d, N, rows);
+  return cudaGetLastError();
 }
 
 // Pump-row gradients: gP[r] = sum over the stages reading pump row r of conj(c_s) ga_s, times the

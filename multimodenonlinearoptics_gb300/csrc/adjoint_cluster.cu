@@ -84,6 +84,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_cluster(const PropA
 #pragma unroll
         for (int v = 0; v < C; v++) g[v] = cmulc(g[v], __ldg(tab + fk[v]));
         cluster_fft_inv<C>(f, g, cl);
+        if (d.gp) {   // marching form: P^T per point, the stage-factor gradients afterwards in parallel
+#pragma unroll
+          for (int v = 0; v < C; v++) g[v] = pdc_march_point(a, d, N, i, tn[v], inst, g[v], true);
+          continue;
+        }
         const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
         const double2 c0 = c[0], c1 = c[1], c2 = c[2];
 #pragma unroll

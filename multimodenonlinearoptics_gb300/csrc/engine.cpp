@@ -600,7 +600,7 @@ struct Medium {
   DevBuf<uint8_t> flagsD;
   DevBuf<unsigned long long> workCounter;
   // adjoint state: forward checkpoints of the last nlm_adjoint_forward
-  DevBuf<double2> ckpt, adjSeg, adjGa, adjGP, adjFGP, adjGc, adjStages;
+  DevBuf<double2> ckpt, adjSeg, adjGa, adjGP, adjFGP, adjGc, adjStages, adjGPS;
   bool adjStored = false;   // the last adjoint forward stored the Chi3GNLSE stage values of every step
   DevBuf<double> profD;
   long long adjRows = 0;
@@ -1875,6 +1875,15 @@ struct Medium {
     return true;
   }
 
+  // The marching form of the Chi2PDC reverse sweep (AdjArgs::gp): every state stored (interval 1) and
+  // the RK4 propagator matrices available, the stored gradients (rows x (nZSteps-1) x N) within 8 GB.
+  // The sequential sweep then applies P^T per point (4 FMAs) and the stage-factor gradients follow in
+  // one parallel launch over all steps and points.
+  bool marchForm() const {
+    return solver == kChi2PDC && adjK == 1 && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9 &&
+           (double)adjRows * (nZ - 1) * N * sizeof(double2) <= 8e9;
+  }
+
   // Chi2PDC with few rows on a cluster grid (the forward ran on 4-CTA clusters): the reverse sweep
   // over 4-CTA clusters too (adjoint_cluster.cu); false when it does not apply.
   bool adjointClusterPdc(const double2* gout, double2* gin) {
@@ -1894,8 +1903,10 @@ struct Medium {
     a.nInst = adjRows;
     a.ipc = 1;
     a.work = nullptr;
-    // segments are recomputed with the RK4 propagator matrices when they fit
-    if (adjK > 1 && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+    // segments are recomputed with the RK4 propagator matrices when they fit; with every state stored,
+    // the matrices give the marching form
+    const bool march = marchForm();
+    if ((adjK > 1 || march) && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
       buildPropagator(C);
       a.prop = prop.p;
     }
@@ -1929,6 +1940,10 @@ struct Medium {
     d.ga = adjGa.p;
     d.gin = gin;
     d.single = adjRows == 1 ? 1 : 0;
+    if (march) {
+      adjGPS.reserve((size_t)adjRows * (nZ - 1) * N);
+      d.gp = adjGPS.p;
+    }
     void* args[] = {(void*)&a, (void*)&d};
     lastSchedule = Schedule{(int)(group * clusters), a.plan.T, 1, smem, 1, 1};
     lastR = C;
@@ -1936,6 +1951,10 @@ struct Medium {
     lastRegs = fa.numRegs;
     ck(launch_clustered(k->fn, (int)(group * clusters), a.plan.T, smem, stream, group, args), "adjoint (cluster)");
     launches++;
+    if (march) {
+      ck(launch_adj_stage_grads(a, d, (int)N, adjRows, stream), "stage gradients");
+      launches++;
+    }
     return true;
   }
 
@@ -1989,12 +2008,18 @@ struct Medium {
     a.ipc = s.ipc;
     a.work = nullptr;
     // segments between checkpoints are recomputed with the RK4 propagator matrices (built in parallel
-    // over all steps and points) instead of the four stage evaluations per step
-    if (!gn && adjK > 1 && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
+    // over all steps and points) instead of the four stage evaluations per step; with every state
+    // stored, the matrices give the marching form
+    const bool march = marchForm();
+    if (!gn && (adjK > 1 || march) && linearSolver() && usePropagator != 0 && propagatorBytes() <= 16e9) {
       buildPropagator(R);
       a.prop = prop.p;
     }
     AdjArgs d{};
+    if (march) {
+      adjGPS.reserve((size_t)adjRows * (nZ - 1) * N);
+      d.gp = adjGPS.p;
+    }
     d.gout = gout;
     d.ckpt = ckpt.p;
     d.K = adjK;
@@ -2010,6 +2035,10 @@ struct Medium {
       ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
     }
     launches++;
+    if (march) {
+      ck(launch_adj_stage_grads(a, d, (int)N, adjRows, stream), "stage gradients");
+      launches++;
+    }
   }
 
   void adjointBackward(const double2* gout, double2* gin, double2* gpump, double* gpol) {

@@ -76,6 +76,9 @@ struct AdjArgs {
   double2* ga;           // [(nZ-1)][3][N] accumulated gradients of the stage factors a_s = c_s P_s
   double2* gin;          // [nInst][N]: gradient with respect to the input spectrum
   int single;            // 1: a single instance, whose stage-factor gradients are stored without atomics
+  // marching form (checkpoint interval 1 with the propagator matrices): the gradient after every
+  // step's RK4, [nInst][nZ-1][N], for k_adj_stage_grads; null otherwise
+  double2* gp;
 };
 
 // Registry of the propagation kernels.  The host engine launches them generically with
@@ -115,6 +118,9 @@ cudaError_t launch_fft_rows(const double2* in, double2* out, long long rows, con
 cudaError_t launch_pump_linear(const double2* freq0, const double* disp, double dzp, int nRows, int N,
                                double2* pumpFreq, cudaStream_t s);
 cudaError_t launch_scale_rows(double2* a, const double* scale, int nRows, int N, cudaStream_t s);
+// stage-factor gradients of every step and point from the marching form's stored gradients (rows
+// summed): d.ga = sum over rows of the stage chain at (state before the step, gradient after it)
+cudaError_t launch_adj_stage_grads(const PropArgs& a, const AdjArgs& d, int N, long long rows, cudaStream_t s);
 cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                              const double2* dstepP, const double2* backP, const double2* rel, int nRows,
                              const FFTPlanH& plan, const double2* tw, cudaStream_t s);
