@@ -20,7 +20,8 @@ namespace cg = cooperative_groups;
 namespace nlm {
 
 // Forward stages of step i from the state in `xs` (global, this thread's points): stores y_s and
-// u2_s, and (when acc != nullptr) the next state x + (k0 + 2 k1 + 2 k2 + k3)/6 into acc.
+// u2_s, and (when acc != nullptr) the stage sum k0 + 2 k1 + 2 k2 + k3 into acc.  Without acc the
+// last stage's self-steepening pair is skipped (14 transforms instead of 16).
 template <int R>
 __device__ __forceinline__ void gnlse_stages(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
                                              const double2* xs, double2* Y, double2* U2, double2* acc) {
@@ -50,6 +51,7 @@ __device__ __forceinline__ void gnlse_stages(const PropArgs& a, int i, int j, do
       U2[(long long)s * N + j + v * T] = u[v];
       u[v] = cmul(u[v], y[v]);
     }
+    if (!acc && s == 3) break;   // the last stage's k only enters the next state: not needed here
     fft_regs<R, false>(u, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + j + v * T));

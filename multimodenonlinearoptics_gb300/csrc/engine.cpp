@@ -1755,8 +1755,15 @@ struct Medium {
     }
     int K = interval;
     if (K <= 0) {
+      // every state while the states fit in a quarter of the free device memory (at most 64 GB),
+      // else every ceil(sqrt(steps)) steps
       const double bytes = (double)rows * steps * N * sizeof(double2);
-      K = bytes <= 1e9 ? 1 : (int)std::ceil(std::sqrt((double)steps));
+      size_t freeB = 0, totalB = 0;
+      if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess) {
+        cudaGetLastError();
+        freeB = 0;
+      }
+      K = bytes <= std::max(1e9, std::min(0.25 * (double)freeB, 64e9)) ? 1 : (int)std::ceil(std::sqrt((double)steps));
     }
     const int nCk = (int)((steps + K - 1) / K);
     ckpt.reserve((size_t)rows * nCk * N);
