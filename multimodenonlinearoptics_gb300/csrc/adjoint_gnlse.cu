@@ -270,10 +270,261 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pipe(const PropAr
   }
 }
 
+// ---- two rows per thread group ---------------------------------------------------------------
+// The Raman operator L(z) = IFFT[H FFT[z]] with H = R~ or conj(R~) (the transform of a real response,
+// Hermitian) maps real fields to real fields.  The forward's Raman input rel |y|^2 is real, and the
+// reverse step only uses Re L(g_u2) = L(Re g_u2): so two rows' Raman transforms run as one complex
+// pair, L(a + i b) = L(a) + i L(b).  Per row and step: 10 transforms to recompute the stages (4
+// shared Raman pairs, 3 self-steepening pairs) and 14 to reverse the step (the dispersion pair, 4 x
+// the self-steepening pair and 4 shared Raman pairs), against 14 + 18.  Per-row scratch (each thread
+// touches only its own points): Y[4], U2[4] (real, stored as complex), K, GX, GXP, G, GY, GKE, ZR
+// (real, stored as complex), ACC: 16 N, and SEG[K] for checkpoint intervals K > 1.
+namespace {
+
+constexpr int kPairRowSlot = 16;   // per-row scratch values in units of N
+
+struct PairRow {
+  double2 *Y, *U2, *K, *GX, *GXP, *G, *GY, *GKE, *ZR, *ACC, *SEG;
+};
+
+__device__ __forceinline__ PairRow pair_row(double2* base, int N, int K) {
+  PairRow r;
+  r.Y = base;
+  r.U2 = base + 4LL * N;
+  r.K = base + 8LL * N;
+  r.GX = base + 9LL * N;
+  r.GXP = base + 10LL * N;
+  r.G = base + 11LL * N;
+  r.GY = base + 12LL * N;
+  r.GKE = base + 13LL * N;
+  r.ZR = base + 14LL * N;
+  r.ACC = base + 15LL * N;
+  r.SEG = K > 1 ? base + (long long)kPairRowSlot * N : nullptr;
+  return r;
+}
+
+// Stages of step i for both rows from their states xs[0], xs[1]: stores y_s and the real u2_s; with
+// acc, also k_3 and the stage sums into ACC (a forward step), else the last self-steepening pair is
+// skipped.
+template <int R>
+__device__ __forceinline__ void pair_stages(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
+                                            const double2* xs0, const double2* xs1, PairRow (&row)[2], bool acc) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const double* rel = a.relInt + (long long)(i - 1) * 3;
+  for (int s = 0; s < 4; s++) {
+    const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+    const double wgt = (s == 1 || s == 2) ? 2.0 : 1.0;
+    const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+    double2 u[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      const int t = j + v * T;
+      const double2 y0 = s == 0 ? xs0[t] : caxpy(xs0[t], fac, row[0].K[t]);
+      const double2 y1 = s == 0 ? xs1[t] : caxpy(xs1[t], fac, row[1].K[t]);
+      row[0].Y[(long long)s * N + t] = y0;
+      row[1].Y[(long long)s * N + t] = y1;
+      u[v] = make_double2(ri * cabs2(y0), ri * cabs2(y1));
+    }
+    fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + j + v * T));
+    fft_regs<R, true>(u, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      row[0].U2[(long long)s * N + j + v * T] = make_double2(u[v].x, 0.0);
+      row[1].U2[(long long)s * N + j + v * T] = make_double2(u[v].y, 0.0);
+    }
+    if (!acc && s == 3) break;
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      double2 w[R];
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        const double c = row[r].U2[(long long)s * N + t].x;
+        const double2 y = row[r].Y[(long long)s * N + t];
+        w[v] = make_double2(c * y.x, c * y.y);
+      }
+      fft_regs<R, false>(w, buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) w[v] = cmul(w[v], __ldg(a.steep + j + v * T));
+      fft_regs<R, true>(w, buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        row[r].K[t] = w[v];
+        if (acc) row[r].ACC[t] = s == 0 ? w[v] : caxpy(row[r].ACC[t], wgt, w[v]);
+      }
+    }
+  }
+}
+
+// One reverse step i for both rows: G (time domain after the step; frequency domain for the last
+// step) becomes the gradient with respect to the state before the step.
+template <int R>
+__device__ __forceinline__ void pair_reverse_step(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
+                                                  PairRow (&row)[2]) {
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+#pragma unroll 1
+  for (int r = 0; r < 2; r++) {
+    double2 g[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) g[v] = row[r].G[j + v * T];
+    if (i < a.nZ - 1) fft_regs<R, false>(g, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) g[v] = cmulc(g[v], __ldg(tab + j + v * T));
+    fft_regs<R, true>(g, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) {
+      const int t = j + v * T;
+      row[r].GX[t] = g[v];
+      row[r].GXP[t] = g[v];
+      row[r].GKE[t] = czero();
+    }
+  }
+  const double* rel = a.relInt + (long long)(i - 1) * 3;
+  for (int s = 3; s >= 0; s--) {
+    const double w = (s == 1 || s == 2) ? 2.0 / 6.0 : 1.0 / 6.0;
+    const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+    const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      double2 u[R];
+#pragma unroll
+      for (int v = 0; v < R; v++) u[v] = caxpy(row[r].GKE[j + v * T], w, row[r].GXP[j + v * T]);   // g_k_s
+      fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
+      fft_regs<R, true>(u, buf, tw, plan, j);                                                 // g_u3
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        const double2 y = row[r].Y[(long long)s * N + t];
+        const double u2 = row[r].U2[(long long)s * N + t].x;
+        row[r].GY[t] = make_double2(u[v].x * u2, u[v].y * u2);   // conj(u2) g_u3, u2 real
+        row[r].ZR[t] = make_double2(y.x * u[v].x + y.y * u[v].y, 0.0);   // Re(conj(y) g_u3)
+      }
+    }
+    // both rows' Raman adjoints: Re L(conj(y) g_u3) = L(Re(conj(y) g_u3))
+    double2 p[R];
+#pragma unroll
+    for (int v = 0; v < R; v++) p[v] = make_double2(row[0].ZR[j + v * T].x, row[1].ZR[j + v * T].x);
+    fft_regs<R, false>(p, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) p[v] = cmulc(p[v], __ldg(a.raman + j + v * T));
+    fft_regs<R, true>(p, buf, tw, plan, j);                                                   // g_u1 of both rows
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+#pragma unroll
+      for (int v = 0; v < R; v++) {
+        const int t = j + v * T;
+        const double g1 = r == 0 ? p[v].x : p[v].y;
+        const double2 y = row[r].Y[(long long)s * N + t];
+        const double2 gy = caxpy(row[r].GY[t], 2.0 * ri * g1, y);
+        row[r].GX[t] = cadd(row[r].GX[t], gy);
+        row[r].GKE[t] = cscale(gy, fac);
+      }
+    }
+  }
+#pragma unroll 1
+  for (int r = 0; r < 2; r++) {
+#pragma unroll
+    for (int v = 0; v < R; v++) row[r].G[j + v * T] = row[r].GX[j + v * T];
+  }
+}
+
+}  // namespace
+
+// a.nInst rows, two per thread group (a second row past the end propagates zeros and is not stored).
+template <int R>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pair(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  __shared__ long long s_group;
+  const FFTPlanH& plan = a.plan;
+  const int N = plan.N, T = plan.T;
+  const int g = threadIdx.x / T, j = threadIdx.x - g * T;
+  double2* bufs;
+  const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
+  double2* buf = bufs + (long long)g * N;
+  const int K = d.K;
+  const long long perRow = (long long)(kPairRowSlot + (K > 1 ? K : 0)) * N;
+  double2* slot = d.seg + ((long long)blockIdx.x * a.ipc + g) * 2 * perRow;
+  PairRow row[2] = {pair_row(slot, N, K), pair_row(slot + perRow, N, K)};
+  const long long nPairs = (a.nInst + 1) / 2;
+  const long long nGroups = (nPairs + a.ipc - 1) / a.ipc;
+  for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
+    const long long pair = cg * a.ipc + g;
+    const bool act[2] = {pair < nPairs && 2 * pair < a.nInst, pair < nPairs && 2 * pair + 1 < a.nInst};
+    const long long inst0 = a.instBase + 2 * pair;
+    const double2* ck[2] = {d.ckpt + (act[0] ? inst0 : 0) * (long long)d.nCk * N,
+                            d.ckpt + (act[1] ? inst0 + 1 : 0) * (long long)d.nCk * N};
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      const double2* go = d.gout + (act[r] ? inst0 + r : 0) * (long long)N;
+#pragma unroll
+      for (int v = 0; v < R; v++) row[r].G[j + v * T] = act[r] ? cscale(go[j + v * T], (double)N) : czero();
+    }
+    int segEnd = a.nZ - 1;
+    while (segEnd >= 1) {
+      const int jseg = (segEnd - 1) / K;
+      const int s0 = jseg * K;
+      if (K > 1) {
+        // recompute both rows' states of the segment: SEG[q] = s_{s0 + q}
+#pragma unroll 1
+        for (int r = 0; r < 2; r++) {
+#pragma unroll
+          for (int v = 0; v < R; v++) row[r].SEG[j + v * T] = ck[r][(long long)jseg * N + j + v * T];
+        }
+        for (int i = s0 + 1; i < segEnd; i++) {
+          const long long q = i - 1 - s0;
+          pair_stages<R>(a, i, j, buf, tw, row[0].SEG + q * N, row[1].SEG + q * N, row, true);
+#pragma unroll 1
+          for (int r = 0; r < 2; r++) {
+            double2 x[R];
+#pragma unroll
+            for (int v = 0; v < R; v++) x[v] = caxpy(row[r].SEG[q * N + j + v * T], 1.0 / 6.0, row[r].ACC[j + v * T]);
+            fft_regs<R, false>(x, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+            fft_regs<R, true>(x, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) row[r].SEG[(q + 1) * N + j + v * T] = x[v];
+          }
+        }
+      }
+      for (int i = segEnd; i > s0; i--) {
+        const double2* p0 = K > 1 ? row[0].SEG + (long long)(i - 1 - s0) * N : ck[0] + (long long)(i - 1) * N;
+        const double2* p1 = K > 1 ? row[1].SEG + (long long)(i - 1 - s0) * N : ck[1] + (long long)(i - 1) * N;
+        pair_stages<R>(a, i, j, buf, tw, p0, p1, row, false);
+        pair_reverse_step<R>(a, i, j, buf, tw, row);
+      }
+      segEnd = s0;
+    }
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      double2 gv[R];
+#pragma unroll
+      for (int v = 0; v < R; v++) gv[v] = row[r].G[j + v * T];
+      fft_regs<R, false>(gv, buf, tw, plan, j);
+      if (act[r]) {
+#pragma unroll
+        for (int v = 0; v < R; v++)
+          d.gin[(inst0 + r) * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+      }
+    }
+    __syncthreads();
+  }
+}
+
 void add_kernels_adjoint_gnlse(std::vector<KernelEntry>& t) {
   t.push_back({kKindAdjoint, kChi3GNLSE, 8, (const void*)k_adjoint_gnlse<8>});
   // key + 100: the pipelined two-CTA-cluster variant
   t.push_back({kKindAdjoint, kChi3GNLSE + 100, 8, (const void*)k_adjoint_gnlse_pipe<8>});
+  // key + 400: two rows per thread group, shared Raman transforms
+  t.push_back({kKindAdjoint, kChi3GNLSE + 400, 8, (const void*)k_adjoint_gnlse_pair<8>});
 }
 
 }  // namespace nlm

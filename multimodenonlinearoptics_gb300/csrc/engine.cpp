@@ -1587,9 +1587,10 @@ struct Medium {
     bool paired = false;
     if (gnlse) {
       k = findKernel(kKindGnlse, solver, R);
-      // at least two rows per SM: two rows per thread group, sharing their Raman transforms
-      // (k_propagate_gnlse_pair: 14 transforms per row and step instead of 18)
-      if (!plainOne && nInst >= 2LL * smCount() && !a.gridF && !a.gridT) {
+      // more rows than SMs (one row per thread group would take a second wave): two rows per thread
+      // group, sharing their Raman transforms (k_propagate_gnlse_pair: 14 transforms per row and step
+      // instead of 18, so a pair takes 1.56 rows' time)
+      if (!plainOne && nInst > smCount() && !a.gridF && !a.gridT) {
         if (const KernelEntry* kp = findKernel(kKindGnlse, solver + 400, R)) {
           k = kp;
           paired = true;
@@ -1997,7 +1998,12 @@ struct Medium {
     const KernelEntry* kp = ((gn || adjK > 1) && adjRows <= (long long)smCount() / 2)
                                 ? findKernel(kKindAdjoint, solver + 100, R) : nullptr;
     if (kp) k = kp;
-    Schedule s = schedule(k, adjRows, R);
+    // Chi3GNLSE with more rows than SMs (where the forward pairs rows as well): two rows per thread
+    // group, sharing their Raman transforms (k_adjoint_gnlse_pair)
+    const KernelEntry* kq =
+        (gn && !kp && adjRows > smCount()) ? findKernel(kKindAdjoint, solver + 400, R) : nullptr;
+    if (kq) k = kq;
+    Schedule s = schedule(k, kq ? (adjRows + 1) / 2 : adjRows, R);
     if (kp) {
       s.ipc = 1;
       s.block = (int)N / R;
@@ -2007,7 +2013,8 @@ struct Medium {
     if (kp && gn) {
       adjSeg.reserve((size_t)adjRows * (2 * (size_t)adjK * 8 + 4) * N);   // per cluster: STG[2][K][8][N], 4 N
     } else {
-      const size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
+      size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
+      if (kq) perSlot = 2 * (size_t)(16 + (adjK > 1 ? adjK : 0)) * N;   // two rows of the pair kernel's scratch
       if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
     }
     PropArgs a = baseArgs(R);

@@ -1,7 +1,7 @@
-"""Chi3GNLSE batches of at least two rows per SM run two rows per thread group, with the two rows'
-Raman convolutions as one complex convolution (k_propagate_gnlse_pair).  Against the oracle, against
-the one-row kernel on the same rows, with an odd row count, and under the adjoint's checkpointed
-forward."""
+"""Chi3GNLSE batches of more rows than SMs run two rows per thread group, with the two rows' Raman
+convolutions as one complex convolution (k_propagate_gnlse_pair, k_adjoint_gnlse_pair).  Against
+the oracle, against the one-row kernels on the same rows, with an odd row count, and under the
+adjoint."""
 import numpy as np
 import pytest
 
@@ -28,7 +28,7 @@ def test_paired_rows_match_oracle_and_one_row_kernel(nlm, oracle, rows):
     sched = med._last_schedule()
     assert sched["grid"] <= (rows + 1) // 2      # thread groups hold pairs of rows
     assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
-    # the same rows through the one-row kernel (fewer than two rows per SM per launch)
+    # the same rows through the one-row kernel (fewer rows than SMs per launch)
     single = np.concatenate([med.batchSignalSimulation(x[k:k + 100], inTimeDomain=False)
                              for k in range(0, rows, 100)])
     assert cases.rel_l2(out, single) < 1e-12
@@ -56,3 +56,27 @@ def test_paired_forward_under_the_adjoint(nlm):
             grads[rows, k] = xt.grad.cpu().numpy()
     for key in ((3, 4), (320, 1), (320, 4)):
         assert cases.rel_l2(grads[key][:3], grads[3, 1]) < 1e-11
+
+
+@pytest.mark.parametrize("k", [1, 4])
+def test_paired_reverse_sweep(nlm, k):
+    """320 rows: the reverse sweep also runs two rows per thread group (shared Raman transforms in the
+    stage recomputation and in the Raman adjoint); its gradients equal those of 100-row sweeps (one row
+    per thread group) on the same rows, to rounding."""
+    torch = pytest.importorskip("torch")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    kw = dict(cases.CASES["Chi3GNLSE"])
+    n = nlm.Chi3GNLSE(**kw)._dims["nFreqs"]
+    x = _rows(n, 320, 9)
+    weights = torch.linspace(0, 1, n, device="cuda", dtype=torch.float64)
+
+    def grad(rows_x):
+        med = nlm.Chi3GNLSE(**kw)
+        xt = torch.tensor(rows_x, device="cuda", requires_grad=True)
+        torch.sum(torch.abs(propagate_gnlse(med, xt, k)) ** 2 * weights).backward()
+        return xt.grad.cpu().numpy()
+
+    paired = grad(x)
+    single = np.concatenate([grad(x[q:q + 100]) for q in range(0, 320, 100)])
+    assert cases.rel_l2(paired, single) < 1e-11
+    assert not np.array_equal(paired, single)
