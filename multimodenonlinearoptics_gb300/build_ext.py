@@ -22,7 +22,7 @@ CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_
                 "nlm_noalloc.cu", "adjoint.cu", "prop_ragged.cu", "adjoint_gnlse.cu", "prop_ff.cu", "prop_direct_c.cu", "prop_cluster.cu", "prop_cluster_b.cu", "prop_cluster_gnlse.cu", "prop_cluster_pump.cu",
                 "adjoint_gnlse_cluster.cu", "adjoint_cluster.cu",
                 "greens_quadrature.cu"]
-CXX_SOURCES = ["engine.cpp"]
+CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]
 
 
 def _cuda_home():

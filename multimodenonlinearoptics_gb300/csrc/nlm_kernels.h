@@ -1,4 +1,4 @@
-// nlm_kernels.h -- launch interface between the host engine (engine.cpp) and the kernels.
+// nlm_kernels.h -- launch interface between the host engine (engine.h) and the kernels.
 // Plain C++ (no device code): included by both nvcc and g++ translation units.
 #pragma once
 #include <cuda_runtime.h>
