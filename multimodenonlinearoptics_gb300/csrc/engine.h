@@ -1348,6 +1348,9 @@ struct Medium {
         if (kc->kind != kind || kc->key != key) continue;
         const int R = kc->R;
         if (!is_pow2((int)N) || (int)N < R || N / R > 512 || N > (uint)kMaxFFT) continue;
+        // the four-points-per-thread variants of one- and two-mode propagators serve latency-bound
+        // launches (fewer propagations than SMs), which are not tuned
+        if (kind == kKindLinear && key <= 2 && R == 4) continue;
         for (int ipcMul = 1; ipcMul <= 2; ipcMul++) {
           Schedule base;
           try {
@@ -1608,10 +1611,12 @@ struct Medium {
         ffT = prepareFF();
         k = findKernel(kKindLinearFF, 1 + 10 * shortRadix(a.plan), R);
       } else {
-        k = findKernel(kKindLinear, (int)nSignal, R);
+        // the adjoint's checkpointed forwards: the checkpoint-writing instantiations (key + 100)
+        const int lkey = (int)nSignal + (a.ckpt ? 100 : 0);
+        k = findKernel(kKindLinear, lkey, R);
         // latency-bound launches: four points per thread, as for the direct kernels below
         if (nInst < smCount() && (int)N / R < 128 && (int)N / 4 <= 512) {
-          if (const KernelEntry* k4 = findKernel(kKindLinear, (int)nSignal, 4)) {
+          if (const KernelEntry* k4 = findKernel(kKindLinear, lkey, 4)) {
             k = k4;
             a.plan = make_plan((int)N, 4);
             a.R = 4;

@@ -251,7 +251,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
 // prop layout: [step][E/2][N] double2, word w = row * M + c holding the entries (row, 2c), (row, 2c+1)
 // of the (2M)x(2M) real matrix over (Re a0, Im a0, Re a1, ...).
 // --------------------------------------------------------------------------------------------
-template <int M, int R>
+// CK: the forward checkpoints of the adjoint (PropArgs::ckpt) are written; a separate instantiation,
+// so that the other launches carry no per-step test.
+template <int M, int R, bool CK = false>
 __device__ __forceinline__ void linear_body(const PropArgs& a) {
   constexpr int D = 2 * M, E = D * D;
   extern __shared__ double2 smem[];
@@ -274,7 +276,7 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
 #pragma unroll
     for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
     if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
-    if (a.ckpt && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
+    if (CK && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       // entries stored as pairs (row r, columns 2c and 2c+1) so a point loads D*D/2 16-byte words
       const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (E / 2) * N;
@@ -304,7 +306,7 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
       }
       const bool last = i == a.nZ - 1;
       dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
-      if (a.ckpt && !last && i % a.ckK == 0)
+      if (CK && !last && i % a.ckK == 0)
         store_rows<M, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     }
     if (a.nZ == 1) {
@@ -324,9 +326,9 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
   }
 }
 
-template <int M, int R>
+template <int M, int R, bool CK = false>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs a) {
-  linear_body<M, R>(a);
+  linear_body<M, R, CK>(a);
 }
 
 // The same kernel compiled for 128-thread CTAs with at least MINB of them resident per SM: fewer

@@ -16,6 +16,10 @@ void add_kernels_linear(std::vector<KernelEntry>& t) {
   // latency-bound launches (fewer propagations than SMs): N/4 threads, all four schedulers of the SM
   t.push_back({kKindLinear, 1, 4, (const void*)k_propagate_linear<1, 4>});
   t.push_back({kKindLinear, 2, 4, (const void*)k_propagate_linear<2, 4>});
+  // key + 100: the adjoint's checkpointed forwards
+  t.push_back({kKindLinear, 101, 4, (const void*)k_propagate_linear<1, 4, true>});
+  t.push_back({kKindLinear, 101, 8, (const void*)k_propagate_linear<1, 8, true>});
+  t.push_back({kKindLinear, 101, 16, (const void*)k_propagate_linear<1, 16, true>});
   // linear (pump-driven) solvers: their RK4 step is real-linear in the signal
   t.push_back({kKindBuildProp, kChi3, 0, (const void*)k_build_propagator<FChi3>});
   t.push_back({kKindBuildProp, kChi2PDC, 0, (const void*)k_build_propagator<FChi2PDC>});
