@@ -182,6 +182,14 @@ def read_profile_value(key):
     return None
 
 
+def measured_hbm_gbs():
+    """The measured HBM copy bandwidth of this machine's GPUs (MEASURED_PEAKS.json), when present."""
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+    except (OSError, ValueError):
+        return None
+
+
 def read_profile_traffic():
     return read_profile_value("dram_bytes_per_launch_full")
 
@@ -765,6 +773,14 @@ def run_ours(args):
                          "algorithmic_flops_per_launch": flops,
                          "ncu_fp64_pipe_active_pct": read_profile_value("fp64_pipe_active_pct"),
                          "peak_source": "FP64 FMA chains measured in this run (MEASURED_PEAKS.json has no FP64 entry)",
+                         "secondary": {
+                             "l2_gbs": (read_profile_value("l2_bytes_per_launch_full") or 0) / avg_kernel_s / 1e9
+                             if avg_kernel_s and read_profile_value("l2_bytes_per_launch_full") else None,
+                             "dram_gbs": traffic / avg_kernel_s / 1e9 if (traffic and avg_kernel_s) else None,
+                             "hbm_peak_gbs": measured_hbm_gbs(),
+                             "source": "L2 and DRAM bytes per launch from the committed ncu summary "
+                                       "(small-case capture scaled to the full step count) over the "
+                                       "kernel's CUDA-event time"},
                          "fp64_tensor_peak": peak_mma,
                          "fp64_tensor_peak_source": "m16n8k16 f64 MMAs (DMMA) measured in this run: the rate a "
                                                     "DFT-as-GEMM schedule could draw on"},
