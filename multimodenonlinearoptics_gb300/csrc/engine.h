@@ -1348,9 +1348,10 @@ struct Medium {
         if (kc->kind != kind || kc->key != key) continue;
         const int R = kc->R;
         if (!is_pow2((int)N) || (int)N < R || N / R > 512 || N > (uint)kMaxFFT) continue;
-        // the four-points-per-thread variants of one- and two-mode propagators serve latency-bound
-        // launches (fewer propagations than SMs), which are not tuned
-        if (kind == kKindLinear && key <= 2 && R == 4) continue;
+        // the four-points-per-thread variant of the single-mode propagator serves latency-bound launches
+        // (fewer propagations than SMs), which are not tuned; for two modes it is a candidate (the
+        // eight-point variant spills)
+        if (kind == kKindLinear && key == 1 && R == 4) continue;
         for (int ipcMul = 1; ipcMul <= 2; ipcMul++) {
           Schedule base;
           try {
