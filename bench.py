@@ -395,6 +395,42 @@ def measure_configs(nlm, torch, cpu=True):
         row["z_steps"] = m._dims["nZSteps"]
     single["chi3_run_pump_n8192"] = row
     res["single_propagation"] = single
+    # Cascade of two Chi2PDC media (N=1024, 200 steps each): the two Green's functions and their
+    # composition C2 C1 + S2 conj(S1), C2 S1 + S2 conj(C1) on the FP64 pipe (k_cgemm_compose), against
+    # cuBLAS ZGEMMs of the same composition (measurement only)
+    kwa = dict(CONFIG, zPrecision=100)
+    kwb = dict(kwa, beta1s=-1, diffBeta0=0.2)
+    ma, mb = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kwa), nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kwb)
+    casc = nlm.Cascade([ma, mb], [{0: 0}], False)
+    casc.computeGreensFunction()
+    ma.computeGreensFunction()
+    mb.computeGreensFunction()
+
+    def best_of(fn, reps=3):
+        b = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            b = min(b, time.perf_counter() - t0)
+        return b, out
+    t_c, (Cc, Sc) = best_of(lambda: casc.computeGreensFunction())
+    t_a, (Ca, Sa) = best_of(lambda: ma.computeGreensFunction())
+    t_b, (Cb, Sb) = best_of(lambda: mb.computeGreensFunction())
+    g = [torch.tensor(x, device="cuda") for x in (Ca, Sa, Cb, Sb)]
+
+    def zgemm():
+        return g[2] @ g[0] + g[3] @ g[1].conj(), g[2] @ g[1] + g[3] @ g[0].conj()
+    zgemm()
+    t_z, (Cz, Sz) = best_of(zgemm)
+    res["cascade_green_n1024"] = {"media": 2, "n_freqs": 1024, "z_steps_each": ma._dims["nZSteps"],
+                                  "cascade_ms": 1e3 * t_c, "media_green_ms": 1e3 * (t_a + t_b),
+                                  "composition_ms_estimate": 1e3 * max(t_c - t_a - t_b, 0.0),
+                                  "cublas_zgemm_composition_ms": 1e3 * t_z,
+                                  "composition_flops": 32 * 1024 ** 3,
+                                  "rel_diff_vs_cublas": float(np.linalg.norm(Cc - Cz.cpu().numpy()) /
+                                                              np.linalg.norm(Cc))}
     # 3. 64 ragged Chi2SFG media in one launch
     params = ragged_media_params()
     media = []

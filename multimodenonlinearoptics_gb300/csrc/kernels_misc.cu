@@ -412,38 +412,77 @@ cudaError_t launch_pump_from(const double2* otherSignalFreq, int otherRows, doub
 // Cascade composition (src/Cascade.cpp:128-129):
 //   Cout = Ci C + Si conj(S),  Sout = Ci S + Si conj(C)     (row-major, FP64 complex)
 // ------------------------------------------------------------------------------------------
+// 32 x 32 output tile per CTA of 16 x 16 threads, each thread a 2 x 2 register tile of both outputs
+// (rows ty, ty + 16; columns tx, tx + 16): per k, 8 shared-memory loads feed 64 FMAs, and the 16
+// accumulator chains of a thread are independent.
 __global__ void __launch_bounds__(256) k_cgemm_compose(const double2* __restrict__ Ci, const double2* __restrict__ Si,
                                                        const double2* __restrict__ C, const double2* __restrict__ S,
                                                        int rows, int inner, int cols, double2* __restrict__ Co,
                                                        double2* __restrict__ So) {
-  __shared__ double2 aC[16][17], aS[16][17], bC[16][17], bS[16][17];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int r = blockIdx.y * 16 + ty, c = blockIdx.x * 16 + tx;
-  double2 accC = czero(), accS = czero();
-  for (int k0 = 0; k0 < inner; k0 += 16) {
-    const int ka = k0 + tx, kb = k0 + ty;
-    aC[ty][tx] = (r < rows && ka < inner) ? Ci[(long long)r * inner + ka] : czero();
-    aS[ty][tx] = (r < rows && ka < inner) ? Si[(long long)r * inner + ka] : czero();
-    bC[ty][tx] = (kb < inner && c < cols) ? C[(long long)kb * cols + c] : czero();
-    bS[ty][tx] = (kb < inner && c < cols) ? S[(long long)kb * cols + c] : czero();
+  constexpr int TM = 32, TK = 16;
+  __shared__ double2 aC[TM][TK + 1], aS[TM][TK + 1], bC[TK][TM + 1], bS[TK][TM + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 16 + tx;
+  const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TM;
+  double2 accC[2][2], accS[2][2];
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++) accC[a][b] = accS[a][b] = czero();
+  for (int k0 = 0; k0 < inner; k0 += TK) {
+    // A tiles: 32 rows x 16 k; B tiles: 16 k x 32 columns (two elements of each per thread)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int q = tid + e * 256;
+      const int ar = q / TK, ak = q - ar * TK;
+      const int r = r0 + ar, ka = k0 + ak;
+      const bool inA = r < rows && ka < inner;
+      aC[ar][ak] = inA ? Ci[(long long)r * inner + ka] : czero();
+      aS[ar][ak] = inA ? Si[(long long)r * inner + ka] : czero();
+      const int bk = q / TM, bc = q - bk * TM;
+      const int kb = k0 + bk, c = c0 + bc;
+      const bool inB = kb < inner && c < cols;
+      bC[bk][bc] = inB ? C[(long long)kb * cols + c] : czero();
+      bS[bk][bc] = inB ? S[(long long)kb * cols + c] : czero();
+    }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const double2 ci = aC[ty][k], si = aS[ty][k], cc = bC[k][tx], ss = bS[k][tx];
-      accC = cadd(accC, cadd(cmul(ci, cc), cmulc(si, ss)));
-      accS = cadd(accS, cadd(cmul(ci, ss), cmulc(si, cc)));
+    for (int k = 0; k < TK; k++) {
+      double2 ci[2], si[2], cc[2], ss[2];
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        ci[a] = aC[ty + 16 * a][k];
+        si[a] = aS[ty + 16 * a][k];
+        cc[a] = bC[k][tx + 16 * a];
+        ss[a] = bS[k][tx + 16 * a];
+      }
+#pragma unroll
+      for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+          // Co += Ci C + Si conj(S), So += Ci S + Si conj(C)
+          accC[a][b].x = fma(ci[a].x, cc[b].x, fma(-ci[a].y, cc[b].y, fma(si[a].x, ss[b].x, fma(si[a].y, ss[b].y, accC[a][b].x))));
+          accC[a][b].y = fma(ci[a].x, cc[b].y, fma(ci[a].y, cc[b].x, fma(si[a].y, ss[b].x, fma(-si[a].x, ss[b].y, accC[a][b].y))));
+          accS[a][b].x = fma(ci[a].x, ss[b].x, fma(-ci[a].y, ss[b].y, fma(si[a].x, cc[b].x, fma(si[a].y, cc[b].y, accS[a][b].x))));
+          accS[a][b].y = fma(ci[a].x, ss[b].y, fma(ci[a].y, ss[b].x, fma(si[a].y, cc[b].x, fma(-si[a].x, cc[b].y, accS[a][b].y))));
+        }
     }
     __syncthreads();
   }
-  if (r < rows && c < cols) {
-    Co[(long long)r * cols + c] = accC;
-    So[(long long)r * cols + c] = accS;
-  }
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      const int r = r0 + ty + 16 * a, c = c0 + tx + 16 * b;
+      if (r < rows && c < cols) {
+        Co[(long long)r * cols + c] = accC[a][b];
+        So[(long long)r * cols + c] = accS[a][b];
+      }
+    }
 }
 
 cudaError_t launch_cgemm_compose(const double2* Ci, const double2* Si, const double2* C, const double2* S, int rows,
                                  int inner, int cols, double2* Cout, double2* Sout, cudaStream_t s) {
-  dim3 grid((cols + 15) / 16, (rows + 15) / 16);
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
   k_cgemm_compose<<<grid, dim3(16, 16), 0, s>>>(Ci, Si, C, S, rows, inner, cols, Cout, Sout);
   return cudaGetLastError();
 }

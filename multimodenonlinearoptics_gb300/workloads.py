@@ -139,6 +139,12 @@ def _run(name, z_precision, rows, reps):
             nlm._check(nlm._lib.nlm_adjoint_backward(med._h(), ctypes.c_void_p(g.data_ptr()),
                                                      ctypes.c_void_p(gin.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
                                                      nlm._dptr(gpol)))
+        elif name == "cascade":
+            kwa = dict(GREEN_CONFIG, zPrecision=z_precision or 100)
+            kwb = dict(kwa, beta1s=-1, diffBeta0=0.2)
+            ma = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwa)
+            mb = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwb)
+            nlm.Cascade([ma, mb], [{0: 0}], False).computeGreensFunction()
         elif name == "chi3_pump":
             m = nlm.Chi3(**dict(CHI3_CONFIG, tPrecision=8192, tMax=40, beta3=0.02, zPrecision=z_precision or 500))
             m.runPumpSimulation()
@@ -185,7 +191,7 @@ def _run(name, z_precision, rows, reps):
 
 def main():
     ap = argparse.ArgumentParser(description="run one benchmark workload on cuda:0")
-    ap.add_argument("name", choices=["green", "chi3", "chi3_pump", "ragged", "adjoint", "adjoint_cluster", "gnlse",
+    ap.add_argument("name", choices=["green", "cascade", "chi3", "chi3_pump", "ragged", "adjoint", "adjoint_cluster", "gnlse",
                                      "gnlse_grad", "signal", "gnlse_signal"])
     ap.add_argument("--zprecision", type=int, default=0, help="zPrecision override (0: the workload's own)")
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")

@@ -18,7 +18,7 @@ def _rows(n, rows, seed):
     return np.fft.fft(base[None, :] + cases.noise(rng, rows * n, 0.05).reshape(rows, n), axis=1)
 
 
-@pytest.mark.parametrize("rows", [320, 321])
+@pytest.mark.parametrize("rows", [153, 320, 321])
 def test_paired_rows_match_oracle_and_one_row_kernel(nlm, oracle, rows):
     kw = dict(cases.CASES["Chi3GNLSE"])
     med, ref = nlm.Chi3GNLSE(**kw), oracle.Chi3GNLSE(**kw)
@@ -35,6 +35,10 @@ def test_paired_rows_match_oracle_and_one_row_kernel(nlm, oracle, rows):
     assert not np.array_equal(out, single)        # two kernels (the Raman result is taken real)
     # each row on its own: the unpaired last row of an odd count is computed like the others
     assert cases.rel_l2(out[-1], single[-1]) < 1e-12
+    # time-domain inputs and outputs
+    xt = np.fft.ifft(x, axis=1)
+    out_t = med.batchSignalSimulation(xt, inTimeDomain=True)
+    assert cases.rel_l2(out_t, ref.batch_signal_simulation(xt, True)) < TOL
 
 
 def test_paired_forward_under_the_adjoint(nlm):

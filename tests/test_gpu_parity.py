@@ -140,9 +140,12 @@ def test_set_pump_from_other_medium(nlm, oracle):
         nlm.Chi2PDC(**dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10)).setPump(a, 1)   # this medium's modes
 
 
-def test_cascade_matches_oracle(nlm, oracle):
-    kwa = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10)
-    kwb = dict(cases.CASES["Chi2PDC"], tPrecision=32, tMax=10, beta1s=-1, diffBeta0=0.2)
+@pytest.mark.parametrize("n", [16, 32, 128])
+def test_cascade_matches_oracle(nlm, oracle, n):
+    """Green's functions, signal and batch through a cascade of two media; the composition's 32 x 32
+    tiles are partial (16), whole (32) and several (128)."""
+    kwa = dict(cases.CASES["Chi2PDC"], tPrecision=n, tMax=10)
+    kwb = dict(cases.CASES["Chi2PDC"], tPrecision=n, tMax=10, beta1s=-1, diffBeta0=0.2)
     a, b = nlm.Chi2PDC(**kwa), nlm.Chi2PDC(**kwb)
     ra, rb = oracle.Chi2PDC(**kwa), oracle.Chi2PDC(**kwb)
     c = nlm.Cascade([a, b], [{0: 0}], True)
@@ -150,11 +153,11 @@ def test_cascade_matches_oracle(nlm, oracle):
     C, S = c.computeGreensFunction()
     Cr, Sr = rc.compute_greens_function()
     assert cases.rel_l2_pair(C, S, Cr, Sr) < TOL
-    x = cases.signal_input("Chi2PDC", 32, 1, seed=9)
+    x = cases.signal_input("Chi2PDC", n, 1, seed=9)
     c.runSignalSimulation(x)
     rc.run_signal_simulation(x)
     assert cases.rel_l2(b.signalFreq, rb.signal_freq[0]) < TOL
-    xb = np.stack([cases.signal_input("Chi2PDC", 32, 1, seed=k) for k in range(3)])
+    xb = np.stack([cases.signal_input("Chi2PDC", n, 1, seed=k) for k in range(3)])
     assert cases.rel_l2(c.batchSignalSimulation(xb), rc.batch_signal_simulation(xb)) < TOL
 
 
