@@ -695,6 +695,7 @@ def run_ours(args):
     med._set_stream(stream.cuda_stream)
     peak = nlm.fp64_peak_tflops()
     peak_mma = nlm.fp64_mma_peak_tflops()
+    per_warps = {str(w): nlm.fp64_warps_rate_tflops(w) for w in (1, 2, 4, 8)}
     C = torch.empty((n, n), dtype=torch.complex128, device="cuda")
     S = torch.empty_like(C)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
@@ -817,6 +818,7 @@ def run_ours(args):
                              "source": "L2 and DRAM bytes per launch from the committed ncu summary "
                                        "(small-case capture scaled to the full step count) over the "
                                        "kernel's CUDA-event time"},
+                         "fp64_tflops_by_warps_per_sm": per_warps,
                          "fp64_tensor_peak": peak_mma,
                          "fp64_tensor_peak_source": "m16n8k16 f64 MMAs (DMMA) measured in this run: the rate a "
                                                     "DFT-as-GEMM schedule could draw on"},

@@ -264,6 +264,9 @@ nlm_status nlm_fp64_peak(double* tflops);
 /* Measured FP64 tensor-core (DMMA, m16n8k16) throughput of the current device in TFLOP/s: what a
  * DFT-as-GEMM schedule could draw on in FP64.  No counterpart in the reference (measurement support). */
 nlm_status nlm_fp64_mma_peak(double* tflops);
+/* FP64 FMA throughput of the device with one CTA of warps_per_sm warps on every SM (TFLOP/s): shows
+ * how many warps an SM needs to reach its FP64 rate (one per scheduler).  Measurement support. */
+nlm_status nlm_fp64_warps_rate(int warps_per_sm, double* tflops);
 
 /* --- Green's-function consumers (multimode.py:15-47) -------------------------------------------
  * Device pointers, row-major, on the given CUDA stream (NULL: the legacy default stream); the call

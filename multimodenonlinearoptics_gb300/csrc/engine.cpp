@@ -753,6 +753,35 @@ nlm_status nlm_abasis_greens(const void* green_c_dev, const void* green_s_dev, s
   });
 }
 
+nlm_status nlm_fp64_warps_rate(int warps_per_sm, double* tflops) {
+  return guarded([&] {
+    nlm::require_device();
+    if (warps_per_sm < 1 || warps_per_sm > 32) throw std::invalid_argument("warps_per_sm must be 1..32");
+    int dev = 0, sms = 1;
+    nlm::ck(cudaGetDevice(&dev), "device");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 32 * warps_per_sm, iters = 2000;
+    nlm::DevBuf<double> out;
+    out.alloc((size_t)sms * threads);
+    cudaEvent_t a, b;
+    nlm::ck(cudaEventCreate(&a), "event");
+    nlm::ck(cudaEventCreate(&b), "event");
+    double best = 0;
+    for (int rep = 0; rep < 4; rep++) {
+      nlm::ck(cudaEventRecord(a, 0), "event");
+      nlm::ck(nlm::launch_fp64_peak(out.p, iters, sms, threads, 0), "fp64 rate");
+      nlm::ck(cudaEventRecord(b, 0), "event");
+      nlm::ck(cudaEventSynchronize(b), "event");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (rep > 0) best = std::max(best, 64.0 * iters * (double)sms * threads / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *tflops = best;
+  });
+}
+
 nlm_status nlm_fp64_mma_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();

@@ -84,6 +84,7 @@ def _load():
         "nlm_adjoint_backward": (i, [vp, vp, vp, vp, P(d)]),
         "nlm_fp64_peak": (i, [P(d)]),
         "nlm_fp64_mma_peak": (i, [P(d)]),
+        "nlm_fp64_warps_rate": (i, [i, P(d)]),
         "nlm_quadrature_greens": (i, [vp, vp, sz, sz, vp, vp]),
         "nlm_abasis_greens": (i, [vp, vp, sz, sz, vp, vp]),
     }
@@ -155,6 +156,13 @@ def fp64_peak_tflops():
     """Measured FP64 FMA throughput of the current device (TFLOP/s, FMA = 2 flops)."""
     v = ctypes.c_double()
     _check(_lib.nlm_fp64_peak(ctypes.byref(v)))
+    return v.value
+
+
+def fp64_warps_rate_tflops(warps_per_sm):
+    """Measured FP64 FMA throughput (TFLOP/s) with one CTA of `warps_per_sm` warps on every SM."""
+    v = ctypes.c_double()
+    _check(_lib.nlm_fp64_warps_rate(int(warps_per_sm), ctypes.byref(v)))
     return v.value
 
 
