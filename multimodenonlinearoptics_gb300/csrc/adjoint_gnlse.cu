@@ -6,8 +6,9 @@
 //     g_u3 = F^H(conj(St') F g_k),  g_y += conj(u2) g_u3,  g_u2 = conj(y) g_u3,
 //     g_u1 = Re F^H(conj(R') F g_u2),  g_y += 2 r g_u1 y,  g_x += g_y,  g_k_{s-1} += fac_s g_y.
 // For every step the stage inputs y_s and convolutions u2_s are recomputed from the state before the
-// step (16 transforms), then the 16 transforms of the reverse stages and the dispersion pair run.
-// States come from checkpoints every K steps; segments between checkpoints are recomputed.
+// step (14 transforms: the last stage's self-steepening pair is not needed), then the 16 transforms
+// of the reverse stages and the dispersion pair run.  States come from checkpoints every K steps;
+// segments between checkpoints are recomputed.
 // Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and SEG[K][N] when K > 1.
 #include <vector>
 
@@ -276,9 +277,12 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pipe(const PropAr
 // reverse step only uses Re L(g_u2) = L(Re g_u2): so two rows' Raman transforms run as one complex
 // pair, L(a + i b) = L(a) + i L(b).  Per row and step: 10 transforms to recompute the stages (4
 // shared Raman pairs, 3 self-steepening pairs) and 14 to reverse the step (the dispersion pair, 4 x
-// the self-steepening pair and 4 shared Raman pairs), against 14 + 18.  Per-row scratch (each thread
-// touches only its own points): Y[4], U2[4] (real, stored as complex), K, GX, GXP, G, GY, GKE, ZR
-// (real, stored as complex), ACC: 16 N, and SEG[K] for checkpoint intervals K > 1.
+// the self-steepening pair and 4 shared Raman pairs), against 14 + 18.  With checkpoint intervals
+// K > 1 the segment's forward recomputation (14 per row and step) stores the stage values of its K
+// steps and the reverse steps read them: 14 + 14 instead of 14 + 10 + 14.  Per-row scratch (each
+// thread touches only its own points): Y[4], U2[4] (real, stored as complex), K, GX, GXP, G, GY, GKE,
+// ZR (real, stored as complex), ACC: 16 N; for K > 1 also the state being recomputed and the stage
+// store STG[K][8]: (1 + 8 K) N.
 namespace {
 
 constexpr int kPairRowSlot = 16;   // per-row scratch values in units of N
@@ -299,6 +303,8 @@ __device__ __forceinline__ PairRow pair_row(double2* base, int N, int K) {
   r.GKE = base + 13LL * N;
   r.ZR = base + 14LL * N;
   r.ACC = base + 15LL * N;
+  // checkpoint intervals K > 1: the state being recomputed, then the stage values of the K steps of
+  // the segment (y_s and u2_s of step q at SEG + N + q 8 N)
   r.SEG = K > 1 ? base + (long long)kPairRowSlot * N : nullptr;
   return r;
 }
@@ -450,7 +456,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pair(const PropAr
   const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
   double2* buf = bufs + (long long)g * N;
   const int K = d.K;
-  const long long perRow = (long long)(kPairRowSlot + (K > 1 ? K : 0)) * N;
+  const long long perRow = (long long)(kPairRowSlot + (K > 1 ? 1 + 8 * K : 0)) * N;
   double2* slot = d.seg + ((long long)blockIdx.x * a.ipc + g) * 2 * perRow;
   PairRow row[2] = {pair_row(slot, N, K), pair_row(slot + perRow, N, K)};
   const long long nPairs = (a.nInst + 1) / 2;
@@ -472,34 +478,59 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pair(const PropAr
       const int jseg = (segEnd - 1) / K;
       const int s0 = jseg * K;
       if (K > 1) {
-        // recompute both rows' states of the segment: SEG[q] = s_{s0 + q}
+        // recompute the segment's steps from its checkpoint, storing each step's stage values: step
+        // s0 + 1 + q at STG q (the state being advanced in SEG)
 #pragma unroll 1
         for (int r = 0; r < 2; r++) {
 #pragma unroll
           for (int v = 0; v < R; v++) row[r].SEG[j + v * T] = ck[r][(long long)jseg * N + j + v * T];
         }
-        for (int i = s0 + 1; i < segEnd; i++) {
+        double2* const y0[2] = {row[0].Y, row[1].Y};
+        double2* const u0[2] = {row[0].U2, row[1].U2};
+        for (int i = s0 + 1; i <= segEnd; i++) {
           const long long q = i - 1 - s0;
-          pair_stages<R>(a, i, j, buf, tw, row[0].SEG + q * N, row[1].SEG + q * N, row, true);
+          const bool more = i < segEnd;
 #pragma unroll 1
           for (int r = 0; r < 2; r++) {
-            double2 x[R];
+            row[r].Y = row[r].SEG + N + q * 8 * N;
+            row[r].U2 = row[r].Y + 4LL * N;
+          }
+          pair_stages<R>(a, i, j, buf, tw, row[0].SEG, row[1].SEG, row, more);
+          if (more) {
+#pragma unroll 1
+            for (int r = 0; r < 2; r++) {
+              double2 x[R];
 #pragma unroll
-            for (int v = 0; v < R; v++) x[v] = caxpy(row[r].SEG[q * N + j + v * T], 1.0 / 6.0, row[r].ACC[j + v * T]);
-            fft_regs<R, false>(x, buf, tw, plan, j);
+              for (int v = 0; v < R; v++) x[v] = caxpy(row[r].SEG[j + v * T], 1.0 / 6.0, row[r].ACC[j + v * T]);
+              fft_regs<R, false>(x, buf, tw, plan, j);
 #pragma unroll
-            for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
-            fft_regs<R, true>(x, buf, tw, plan, j);
+              for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+              fft_regs<R, true>(x, buf, tw, plan, j);
 #pragma unroll
-            for (int v = 0; v < R; v++) row[r].SEG[(q + 1) * N + j + v * T] = x[v];
+              for (int v = 0; v < R; v++) row[r].SEG[j + v * T] = x[v];
+            }
           }
         }
-      }
-      for (int i = segEnd; i > s0; i--) {
-        const double2* p0 = K > 1 ? row[0].SEG + (long long)(i - 1 - s0) * N : ck[0] + (long long)(i - 1) * N;
-        const double2* p1 = K > 1 ? row[1].SEG + (long long)(i - 1 - s0) * N : ck[1] + (long long)(i - 1) * N;
-        pair_stages<R>(a, i, j, buf, tw, p0, p1, row, false);
-        pair_reverse_step<R>(a, i, j, buf, tw, row);
+        // reverse the segment from the stored stage values
+        for (int i = segEnd; i > s0; i--) {
+          const long long q = i - 1 - s0;
+#pragma unroll 1
+          for (int r = 0; r < 2; r++) {
+            row[r].Y = row[r].SEG + N + q * 8 * N;
+            row[r].U2 = row[r].Y + 4LL * N;
+          }
+          pair_reverse_step<R>(a, i, j, buf, tw, row);
+        }
+#pragma unroll 1
+        for (int r = 0; r < 2; r++) {
+          row[r].Y = y0[r];
+          row[r].U2 = u0[r];
+        }
+      } else {
+        for (int i = segEnd; i > s0; i--) {
+          pair_stages<R>(a, i, j, buf, tw, ck[0] + (long long)(i - 1) * N, ck[1] + (long long)(i - 1) * N, row, false);
+          pair_reverse_step<R>(a, i, j, buf, tw, row);
+        }
       }
       segEnd = s0;
     }
