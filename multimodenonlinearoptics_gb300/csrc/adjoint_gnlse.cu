@@ -9,7 +9,9 @@
 // step (14 transforms: the last stage's self-steepening pair is not needed), then the 16 transforms
 // of the reverse stages and the dispersion pair run.  States come from checkpoints every K steps;
 // segments between checkpoints are recomputed.
-// Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and SEG[K][N] when K > 1.
+// With K > 1 the segment's recomputation stores the stage values of its steps, which its reverse
+// steps then read.  Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and for K > 1 the
+// state being recomputed and STG[K][8][N].
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -138,12 +140,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a,
   double2* bufs;
   const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
   double2* buf = bufs + (long long)g * N;
-  double2* slot = d.seg + ((long long)blockIdx.x * a.ipc + g) * (long long)(10 + (d.K > 1 ? d.K : 0)) * N;
+  double2* slot = d.seg + ((long long)blockIdx.x * a.ipc + g) * (long long)(10 + (d.K > 1 ? 1 + 8 * d.K : 0)) * N;
   double2* Y = slot;
   double2* U2 = slot + 4LL * N;
   double2* GX = slot + 8LL * N;
   double2* GXP = slot + 9LL * N;
-  double2* SEG = slot + 10LL * N;
+  double2* XS = slot + 10LL * N;    // K > 1: the state being recomputed
+  double2* STG = slot + 11LL * N;   // K > 1: y_s, u2_s of the segment's step q at STG + q 8 N
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
   for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
     const long long local = cg * a.ipc + g;
@@ -161,27 +164,35 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a,
       const int jseg = (segEnd - 1) / d.K;
       const int s0 = jseg * d.K;
       if (d.K > 1) {
-        // recompute the states of the segment: SEG[q] = s_{s0 + q}
+        // recompute the segment's steps from its checkpoint, storing each step's stage values, then
+        // reverse them from the store (no second recomputation of the stages)
 #pragma unroll
-        for (int v = 0; v < R; v++) SEG[j + v * T] = ck[(long long)jseg * N + j + v * T];
-        for (int i = s0 + 1; i < segEnd; i++) {
-          const double2* xs = SEG + (long long)(i - 1 - s0) * N;
-          gnlse_stages<R>(a, i, j, buf, tw, xs, Y, U2, GX);   // GX holds the stage sum here
-          double2 x[R];
+        for (int v = 0; v < R; v++) XS[j + v * T] = ck[(long long)jseg * N + j + v * T];
+        for (int i = s0 + 1; i <= segEnd; i++) {
+          double2* Yq = STG + (long long)(i - 1 - s0) * 8 * N;
+          const bool more = i < segEnd;
+          gnlse_stages<R>(a, i, j, buf, tw, XS, Yq, Yq + 4LL * N, more ? GX : nullptr);   // GX: stage sum
+          if (more) {
+            double2 x[R];
 #pragma unroll
-          for (int v = 0; v < R; v++) x[v] = caxpy(xs[j + v * T], 1.0 / 6.0, GX[j + v * T]);
-          fft_regs<R, false>(x, buf, tw, plan, j);
+            for (int v = 0; v < R; v++) x[v] = caxpy(XS[j + v * T], 1.0 / 6.0, GX[j + v * T]);
+            fft_regs<R, false>(x, buf, tw, plan, j);
 #pragma unroll
-          for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
-          fft_regs<R, true>(x, buf, tw, plan, j);
+            for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(a.dstep + j + v * T));
+            fft_regs<R, true>(x, buf, tw, plan, j);
 #pragma unroll
-          for (int v = 0; v < R; v++) SEG[(long long)(i - s0) * N + j + v * T] = x[v];
+            for (int v = 0; v < R; v++) XS[j + v * T] = x[v];
+          }
         }
-      }
-      for (int i = segEnd; i > s0; i--) {
-        const double2* prev = d.K > 1 ? SEG + (long long)(i - 1 - s0) * N : ck + (long long)(i - 1) * N;
-        gnlse_stages<R>(a, i, j, buf, tw, prev, Y, U2, nullptr);
-        gnlse_reverse_step<R>(a, i, j, buf, tw, Y, U2, GX, GXP, gv);
+        for (int i = segEnd; i > s0; i--) {
+          const double2* Yq = STG + (long long)(i - 1 - s0) * 8 * N;
+          gnlse_reverse_step<R>(a, i, j, buf, tw, Yq, Yq + 4LL * N, GX, GXP, gv);
+        }
+      } else {
+        for (int i = segEnd; i > s0; i--) {
+          gnlse_stages<R>(a, i, j, buf, tw, ck + (long long)(i - 1) * N, Y, U2, nullptr);
+          gnlse_reverse_step<R>(a, i, j, buf, tw, Y, U2, GX, GXP, gv);
+        }
       }
       segEnd = s0;
     }

@@ -2023,7 +2023,7 @@ struct Medium {
     if (kp && gn) {
       adjSeg.reserve((size_t)adjRows * (2 * (size_t)adjK * 8 + 4) * N);   // per cluster: STG[2][K][8][N], 4 N
     } else {
-      size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? adjK : 0)) * N : (size_t)adjK * N;
+      size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? 1 + 8 * adjK : 0)) * N : (size_t)adjK * N;
       if (kq) perSlot = 2 * (size_t)(16 + (adjK > 1 ? 1 + 8 * adjK : 0)) * N;   // two rows of the pair kernel's scratch
       if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
     }
