@@ -7,15 +7,22 @@
 2. ``multimode_golden.npz`` -- pinned to the reference itself: outputs of the reference's
    ``multimode.py`` and ``decompositions.py`` (imported from the checkout) on a Green's pair of the
    oracle and seeded matrices.
-3. ``oracle_golden.npz`` -- outputs of the numpy oracle (oracle/nlm_oracle.py) for the small
+3. ``frontends_golden.npz`` -- pinned to the reference itself: the poling generators of the
+   reference's ``poling.py`` and its ``nlMaterial`` decorator (applied to the synthetic Sellmeier
+   expressions of frontend_cases.py), imported from the checkout and run on the seeded cases there.
+4. ``oracle_golden.npz`` -- outputs of the numpy oracle (oracle/nlm_oracle.py) for the small
    configurations of tests/cases.py: pump grids, signal grids, Green's matrices and batch rows
    of every solver.  They pin the oracle over time and give the GPU tests fixed expectations.
 
 Usage:  python tests/golden/make_golden.py
 """
 
+import contextlib
+import importlib.util
+import io
 import os
 import sys
+import types
 
 import numpy as np
 
@@ -120,6 +127,63 @@ def make_multimode(ref_root):
     np.savez_compressed(os.path.join(HERE, "multimode_golden.npz"), **out)
 
 
+class _Numpy2Shim(types.ModuleType):
+    """numpy for the reference's poling module, as the numpy its code was written for behaves.
+
+    Current numpy refuses to store a one-element array in a scalar slot, which poling.py:152-156 does
+    with the rows of ``np.argwhere``; handing it each row as a tuple indexes a scalar instead, which is
+    the value older numpy stored."""
+
+    def __init__(self):
+        super().__init__("numpy")
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def argwhere(a):
+        return [tuple(r) for r in np.argwhere(a)]
+
+
+def _outcome(fn, args, kwargs):
+    try:
+        with contextlib.redirect_stdout(io.StringIO()):   # linearPolingContinuous prints a flag
+            return np.asarray(fn(*args, **kwargs), dtype=np.float64), None
+    except Exception as e:   # recorded: the front end must raise the same
+        return None, "%s: %s" % (type(e).__name__, e)
+
+
+def make_frontends(ref_root):
+    """Outputs of the reference's poling generators and material decorator on frontend_cases.py."""
+    import frontend_cases as FC
+    sys.path.insert(0, ref_root)
+    if not hasattr(np, "float_"):
+        np.float_ = np.float64
+    import poling as ref_poling  # the reference's module
+    ref_poling.np = _Numpy2Shim()
+    out = {}
+    for name, fn, args, kwargs in FC.poling_cases():
+        args = tuple(FC.NLF[a] if isinstance(a, str) else a for a in args)
+        val, err = _outcome(getattr(ref_poling, fn), args, kwargs)
+        out["pol_" + name] = val if err is None else np.array(err)
+    for name, a, b, ml, tol in FC.combine_cases(ref_poling.periodicPoling):
+        out["in_%s_a" % name], out["in_%s_b" % name] = a, b
+        val, err = _outcome(ref_poling.combinePoling, (a, b, ml, tol), {})
+        out["pol_" + name] = val if err is None else np.array(err)
+    spec = importlib.util.spec_from_file_location("ref_nlMaterial", os.path.join(ref_root, "materials", "nlMaterial.py"))
+    ref_mat = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ref_mat)
+    import sympy
+    sym = {"l0": ref_mat.l0, "T": ref_mat.T, "th": ref_mat.th, "sqrt": sympy.sqrt, "Piecewise": sympy.Piecewise}
+    for name, expr, kw, grid in FC.sellmeier_cases(sym, ref_mat.angledRefractiveIndex):
+        cls = ref_mat.nlMaterial(**kw)(type(name, (), {"ind": expr}))
+        out["mat_%s_grid" % name] = np.array(grid, dtype=np.float64)
+        fns = FC.MATERIAL_FUNCTIONS + (["walkoff"] if kw.get("angleTuning") else [])
+        for f in fns:
+            out["mat_%s_%s" % (name, f)] = np.array([float(getattr(cls, f)(*pt)) for pt in grid])
+    np.savez_compressed(os.path.join(HERE, "frontends_golden.npz"), **out)
+
+
 def oracle_case(name):
     kw = cases.oracle_kwargs(name)
     med = O.SOLVERS[name](**kw)
@@ -166,6 +230,8 @@ if __name__ == "__main__":
     if os.path.exists(os.path.join(ref_root, "poling.py")):
         make_poling(ref_root)
         make_multimode(ref_root)
+        make_frontends(ref_root)
     else:
-        print("reference checkout not found; poling and multimode fixtures left unchanged", file=sys.stderr)
+        print("reference checkout not found; poling, multimode and front-end fixtures left unchanged",
+              file=sys.stderr)
     make_oracle()
