@@ -692,31 +692,52 @@ nlm_status nlm_kernel_timing(nlm_medium* h, int enable, double* total_ms, long* 
 }
 
 namespace {
-// Best of three timed launches (after one warm-up) of a peak kernel; flops per launch given.
-double time_peak(const std::function<cudaError_t(double*, int, int, int)>& launch, int iters, double flopsPerThreadIter) {
+// Two CUDA events, destroyed however the scope is left.
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    nlm::ck(cudaEventCreate(&a), "event");
+    if (cudaEventCreate(&b) != cudaSuccess) {
+      cudaEventDestroy(a);
+      throw std::runtime_error("event: cudaEventCreate failed");
+    }
+  }
+  ~EventPair() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+  EventPair(const EventPair&) = delete;
+  EventPair& operator=(const EventPair&) = delete;
+};
+
+// Best of three timed launches (after one warm-up) of a peak kernel on blocksPerSM CTAs of `threads`
+// threads per SM; flopsPerThreadIter flops per thread and iteration.
+double time_peak(const std::function<cudaError_t(double*, int, int, int)>& launch, int iters, double flopsPerThreadIter,
+                 int blocksPerSM = 4, int threads = 256) {
   int dev = 0, sms = 1;
   nlm::ck(cudaGetDevice(&dev), "device");
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = sms * 4, threads = 256;
+  const int blocks = sms * blocksPerSM;
   nlm::DevBuf<double> out;
   out.alloc((size_t)blocks * threads);
-  cudaEvent_t a, b;
-  nlm::ck(cudaEventCreate(&a), "event");
-  nlm::ck(cudaEventCreate(&b), "event");
+  EventPair ev;
   double best = 0;
   for (int rep = 0; rep < 4; rep++) {
-    nlm::ck(cudaEventRecord(a, 0), "event");
+    nlm::ck(cudaEventRecord(ev.a, 0), "event");
     nlm::ck(launch(out.p, iters, blocks, threads), "peak kernel");
-    nlm::ck(cudaEventRecord(b, 0), "event");
-    nlm::ck(cudaEventSynchronize(b), "event");
+    nlm::ck(cudaEventRecord(ev.b, 0), "event");
+    nlm::ck(cudaEventSynchronize(ev.b), "event");
     float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
+    nlm::ck(cudaEventElapsedTime(&ms, ev.a, ev.b), "event");
     const double flops = flopsPerThreadIter * iters * (double)blocks * threads;
     if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
   return best;
+}
+
+double* out_arg(double* p) {
+  if (!p) throw std::invalid_argument("null output pointer");
+  return p;
 }
 }  // namespace
 
@@ -724,8 +745,8 @@ nlm_status nlm_fp64_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();
     // 32 FMAs (64 flops) per thread and iteration
-    *tflops = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
-                        2000, 64.0);
+    *out_arg(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
+                                 2000, 64.0);
   });
 }
 
@@ -757,28 +778,9 @@ nlm_status nlm_fp64_warps_rate(int warps_per_sm, double* tflops) {
   return guarded([&] {
     nlm::require_device();
     if (warps_per_sm < 1 || warps_per_sm > 32) throw std::invalid_argument("warps_per_sm must be 1..32");
-    int dev = 0, sms = 1;
-    nlm::ck(cudaGetDevice(&dev), "device");
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = 32 * warps_per_sm, iters = 2000;
-    nlm::DevBuf<double> out;
-    out.alloc((size_t)sms * threads);
-    cudaEvent_t a, b;
-    nlm::ck(cudaEventCreate(&a), "event");
-    nlm::ck(cudaEventCreate(&b), "event");
-    double best = 0;
-    for (int rep = 0; rep < 4; rep++) {
-      nlm::ck(cudaEventRecord(a, 0), "event");
-      nlm::ck(nlm::launch_fp64_peak(out.p, iters, sms, threads, 0), "fp64 rate");
-      nlm::ck(cudaEventRecord(b, 0), "event");
-      nlm::ck(cudaEventSynchronize(b), "event");
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      if (rep > 0) best = std::max(best, 64.0 * iters * (double)sms * threads / (ms * 1e-3) / 1e12);
-    }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    *tflops = best;
+    // one CTA of warps_per_sm warps on every SM, 32 FMAs per thread and iteration
+    *out_arg(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
+                                 2000, 64.0, 1, 32 * warps_per_sm);
   });
 }
 
@@ -786,8 +788,9 @@ nlm_status nlm_fp64_mma_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();
     // 4 m16n8k16 MMAs per warp and iteration: 4 x 2 x 16 x 8 x 16 flops over 32 threads
-    *tflops = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_mma_peak(o, it, bl, th, 0); },
-                        200, 4.0 * 2 * 16 * 8 * 16 / 32);
+    *out_arg(tflops) = time_peak(
+        [](double* o, int it, int bl, int th) { return nlm::launch_fp64_mma_peak(o, it, bl, th, 0); }, 200,
+        4.0 * 2 * 16 * 8 * 16 / 32);
   });
 }
 
