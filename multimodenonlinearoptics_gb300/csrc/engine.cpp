@@ -57,6 +57,13 @@ static Medium* create_medium(int s, const double* args, const double* pump, size
 using nlm::guarded;
 using nlm::Medium;
 
+// An output pointer of the C ABI, checked before it is written.
+template <class T>
+static T* out_ptr(T* p) {
+  if (!p) throw std::invalid_argument("null output pointer");
+  return p;
+}
+
 
 nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows, int inTime, void* out,
                                       size_t scratchElems, PropArgs* args, int* grid, int* block, size_t* smem,
@@ -97,12 +104,12 @@ nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows
     a.nInst = (long long)rows;
     a.ipc = s.ipc;
     a.work = nullptr;   // static round robin: no counter to allocate
-    *args = a;
-    *grid = s.grid;
-    *block = s.block;
-    *smem = s.smem;
-    *fn = k->fn;
-    *stream = m->stream;
+    *out_ptr(args) = a;
+    *out_ptr(grid) = s.grid;
+    *out_ptr(block) = s.block;
+    *out_ptr(smem) = s.smem;
+    *out_ptr(fn) = k->fn;
+    *out_ptr(stream) = m->stream;
   });
 }
 
@@ -276,11 +283,11 @@ nlm_status nlm_green_dims(nlm_medium* h, unsigned n_threads, const uint8_t* use_
         if (ci != r) throw std::invalid_argument("Cascade Green's function dimensions do not chain");
         r = ri;
       }
-      *rows = r;
-      *cols = cols0;
+      *out_ptr(rows) = r;
+      *out_ptr(cols) = cols0;
       return;
     }
-    m->greenDims(n_threads, use_input, n_use_input, use_output, n_use_output, rows, cols);
+    m->greenDims(n_threads, use_input, n_use_input, use_output, n_use_output, out_ptr(rows), out_ptr(cols));
   });
 }
 
@@ -370,12 +377,12 @@ nlm_status nlm_batch_dims(nlm_medium* h, size_t rows, size_t cols, unsigned n_th
       std::vector<int> outs;
       m->media[0]->batchModes(rows, cols, n_threads, input_mode, nullptr, 0, outs);
       last->batchModes(rows, last->N, n_threads, 0, use_output, n_use_output, outs);
-      *out_cols = outs.size() * last->N;
+      *out_ptr(out_cols) = outs.size() * last->N;
       return;
     }
     std::vector<int> outs;
     m->batchModes(rows, cols, n_threads, input_mode, use_output, n_use_output, outs);
-    *out_cols = outs.size() * m->N;
+    *out_ptr(out_cols) = outs.size() * m->N;
   });
 }
 
@@ -451,6 +458,7 @@ nlm_status nlm_get_grid(nlm_medium* h, int which, unsigned index, const double**
     Medium* m = M(h);
     if (which == 4) throw nlm::IndexError("vector::_M_range_check: field index out of range");  // no solver has fields
     size_t r = 0;
+    out_ptr(data), out_ptr(rows), out_ptr(cols);
     const std::vector<double>& v = m->mirror(which, index, &r);
     *data = v.data();
     *rows = r;
@@ -461,6 +469,7 @@ nlm_status nlm_get_grid(nlm_medium* h, int which, unsigned index, const double**
 nlm_status nlm_get_axis(nlm_medium* h, int which, unsigned index, const double** data, size_t* n) {
   return guarded([&] {
     Medium* m = M(h);
+    out_ptr(data), out_ptr(n);
     if (m->isCascade) m = m->media.at(0);
     switch (which) {
       case 0: *data = m->tau.data(); *n = m->tau.size(); break;
@@ -553,7 +562,7 @@ nlm_status nlm_cascade_add(nlm_medium* cascade, nlm_medium* medium, const unsign
 nlm_status nlm_cascade_media(const nlm_medium* cascade, size_t* n_media) {
   return guarded([&] {
     const Medium* c = CM(cascade);
-    *n_media = c->isCascade ? c->media.size() : 0;
+    *out_ptr(n_media) = c->isCascade ? c->media.size() : 0;
   });
 }
 
@@ -735,17 +744,13 @@ double time_peak(const std::function<cudaError_t(double*, int, int, int)>& launc
   return best;
 }
 
-double* out_arg(double* p) {
-  if (!p) throw std::invalid_argument("null output pointer");
-  return p;
-}
 }  // namespace
 
 nlm_status nlm_fp64_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();
     // 32 FMAs (64 flops) per thread and iteration
-    *out_arg(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
+    *out_ptr(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
                                  2000, 64.0);
   });
 }
@@ -779,7 +784,7 @@ nlm_status nlm_fp64_warps_rate(int warps_per_sm, double* tflops) {
     nlm::require_device();
     if (warps_per_sm < 1 || warps_per_sm > 32) throw std::invalid_argument("warps_per_sm must be 1..32");
     // one CTA of warps_per_sm warps on every SM, 32 FMAs per thread and iteration
-    *out_arg(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
+    *out_ptr(tflops) = time_peak([](double* o, int it, int bl, int th) { return nlm::launch_fp64_peak(o, it, bl, th, 0); },
                                  2000, 64.0, 1, 32 * warps_per_sm);
   });
 }
@@ -788,7 +793,7 @@ nlm_status nlm_fp64_mma_peak(double* tflops) {
   return guarded([&] {
     nlm::require_device();
     // 4 m16n8k16 MMAs per warp and iteration: 4 x 2 x 16 x 8 x 16 flops over 32 threads
-    *out_arg(tflops) = time_peak(
+    *out_ptr(tflops) = time_peak(
         [](double* o, int it, int bl, int th) { return nlm::launch_fp64_mma_peak(o, it, bl, th, 0); }, 200,
         4.0 * 2 * 16 * 8 * 16 / 32);
   });

@@ -91,3 +91,19 @@ def test_single_z_step(nlm, oracle, name):
         assert cases.rel_l2_pair(C, S, Cr, Sr) < TOL
     out, want = _batch_pair(med, ref, 4, 9, fnl)
     assert cases.rel_l2(out, want) < TOL
+
+
+def test_null_output_pointers(nlm):
+    """C-ABI queries given a null output pointer return an error status and leave the handle usable."""
+    import ctypes
+    lib = nlm._lib
+    med = nlm.Chi2PDC(**dict(PDC, tPrecision=64))
+    rows, cols = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.nlm_green_dims(med._h(), 1, None, 0, None, 0, None, ctypes.byref(cols)) != 0
+    assert "null output pointer" in lib.nlm_last_error().decode()
+    data = ctypes.POINTER(ctypes.c_double)()
+    assert lib.nlm_get_grid(med._h(), 0, 0, ctypes.byref(data), None, ctypes.byref(cols)) != 0
+    assert lib.nlm_cascade_media(med._h(), None) != 0
+    assert lib.nlm_fp64_peak(None) != 0
+    assert lib.nlm_green_dims(med._h(), 1, None, 0, None, 0, ctypes.byref(rows), ctypes.byref(cols)) == 0
+    assert rows.value == cols.value == 64
