@@ -311,19 +311,25 @@ def measure_configs(nlm, torch, cpu=True):
     res = {}
     # 1. Chi3 N=1 soliton pump + seeded-noise signal, N=512, nZSteps=200: latency through the API
     kw1 = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=512, zPrecision=200)
-    m1 = nlm.Chi3(**kw1)
     rng = np.random.default_rng(1)
     sig = (rng.standard_normal(512) + 1j * rng.standard_normal(512)) * 1e-3 / np.sqrt(2)
-    m1.runPumpSimulation()
-    m1.runSignalSimulation(sig)
-    lat = []
-    for _ in range(5):
-        t0 = time.perf_counter()
+
+    def chi3_latency(mode):
+        # mode 1 (default): both marches on four SMs with one point per thread; 0: one CTA each
+        m1 = nlm.Chi3(**kw1)
+        m1._set_cluster(mode)
         m1.runPumpSimulation()
         m1.runSignalSimulation(sig)
-        _ = m1.signalTime
-        lat.append(time.perf_counter() - t0)
-    res["chi3_pump_signal_n512"] = {"gpu_latency_ms": 1e3 * min(lat)}
+        lat = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            m1.runPumpSimulation()
+            m1.runSignalSimulation(sig)
+            _ = m1.signalTime
+            lat.append(time.perf_counter() - t0)
+        return 1e3 * min(lat)
+
+    res["chi3_pump_signal_n512"] = {"gpu_latency_ms": chi3_latency(1), "gpu_latency_ms_one_cta": chi3_latency(0)}
     if cpu:
         from oracle import nlm_oracle as O
         o1 = O.Chi3(**kw1)
@@ -331,14 +337,16 @@ def measure_configs(nlm, torch, cpu=True):
         o1.run_pump_simulation()
         o1.run_signal_simulation(sig)
         res["chi3_pump_signal_n512"]["cpu_oracle_latency_ms"] = 1e3 * (time.perf_counter() - t0)
-    # single propagations on large grids (runSignalSimulation, full grids): one CTA against a
-    # 4-CTA cluster per propagation
+    # single propagations (runSignalSimulation, full grids): one CTA against a 4-CTA cluster per
+    # propagation; at 1024 points with one point per thread (the default) and with four
     single = {}
-    for n in (2048, 8192):
+    for n in (1024, 2048, 8192):
         kw = dict(CONFIG, tPrecision=n, zPrecision=500)
         a = (np.random.default_rng(n).standard_normal(n) + 0j) * 0.1
         row = {"n_freqs": n}
-        for use, label in ((0, "one_cta_ms"), (1, "cluster_ms")):
+        forms = ((0, "one_cta_ms"), (1, "spread_ms"), (2, "cluster_ms")) if n == 1024 else \
+            ((0, "one_cta_ms"), (1, "cluster_ms"))
+        for use, label in forms:
             m = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kw)
             m._set_cluster(use)
             m.runPumpSimulation()

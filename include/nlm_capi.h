@@ -233,8 +233,11 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 /* 1 (default): a launch of at most SMs/4 propagations on a grid of 1024 to 8192 points spreads
  * each propagation over a cluster of 4 CTAs (one per SM, four-step FFT through distributed
  * shared memory); so do the Chi3 pump march and the reverse sweeps of nlm_adjoint_backward (on 4
- * or, pipelined, 8 CTAs) on such grids.  0: one CTA per propagation.  Also used by
- * nlm_ragged_batch for the costliest media.  No counterpart in the reference. */
+ * or, pipelined, 8 CTAs) on such grids.  On grids of 256 to 1024 points, full-grid propagations
+ * (nlm_run_signal) and the Chi3 pump march use clusters with one point per thread instead.
+ * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  Also used by
+ * nlm_ragged_batch for the costliest media.  Other values: NLM_ERR_VALUE.  No counterpart in the
+ * reference. */
 nlm_status nlm_set_cluster(nlm_medium* m, int enable);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float

@@ -1142,7 +1142,11 @@ struct Medium {
     upload(dd, dP);
     upload(db, bP);
     upload(dr, rel);
-    if (useCluster && N >= 1024) {
+    if (spreadGrid()) {
+      // the march on four SMs with one point per thread (prop_spread.cu)
+      ck(launch_pump_chi3_spread(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, (int)N, tw, stream),
+         "chi3 pump (spread)");
+    } else if (useCluster && N >= 1024) {
       // 1024..8192 points: the march on four SMs (prop_cluster_pump.cu), four points per thread
       const FFTPlanH local = make_plan((int)N / kClusterSize, kClusterSize);
       ck(launch_pump_chi3_cluster(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, local, tw, stream),
@@ -1445,35 +1449,52 @@ struct Medium {
 
   // ---- cluster-distributed propagation (prop_cluster.cu) -------------------------------------
   static constexpr int kClusterSize = 4;   // CTAs per propagation; also the points per thread
+  // 1: clusters, with one point per thread on the grids of spreadGrid(); 2: four points per thread
+  // only; 0: one CTA per propagation
   int useCluster = 1;
+  static constexpr uint kSpreadMinN = 256, kSpreadMaxN = 1024;
+
+  // A grid whose single propagations run on a 4-CTA cluster with one point per thread (prop_spread.cu):
+  // M = N/4 threads per CTA gives two to eight warps per SM, where the four-points-per-thread cluster
+  // form would give at most two (or, below 1024 points, is not built) and one CTA has one SM's FP64.
+  bool spreadGrid() const {
+    return useCluster == 1 && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;
+  }
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
     // checkpointed forwards (the adjoint's, Chi2PDC and Chi3GNLSE) run on clusters too: their reverse
     // sweeps have cluster forms that read the same checkpoints
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
-    if (!is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return nullptr;
+    if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
     if (nInst * kClusterSize > smCount()) return nullptr;
+    // full-grid propagations (runSignalSimulation) on the spread grids: one point per thread.  Batches
+    // and the adjoint's checkpointed forwards keep the kernels their reverse sweeps pair with.
+    if (spreadGrid() && (a.gridF || a.gridT) && !a.ckpt && !a.stages)
+      if (const KernelEntry* ks = findKernel(kKindCluster, solver, 1)) return ks;
+    if (N < 1024) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);
   }
 
   void launchCluster(const KernelEntry* k, PropArgs a, long long nInst) {
     constexpr int C = kClusterSize;
     const int M = (int)N / C;
-    a.plan = make_plan(M, C);
-    a.R = C;
+    const bool spread = k->R == 1;   // one point per thread (prop_spread.cu)
+    a.plan = make_plan(M, spread ? 1 : C);
+    a.R = spread ? 1 : C;
     a.nInst = nInst;
     a.ipc = 1;
     a.work = nullptr;
-    const int T = a.plan.T;
-    // M-point twiddles x2, exchange buffer, 2 x C x T receive; each CTA alone on its SM, e.g. beside
-    // the CTAs of a ragged launch
+    const int T = spread ? M : a.plan.T;
+    // four points per thread: M-point twiddles x2, exchange buffer, 2 x C x T receive; one point per
+    // thread: kSpreadSmemPerPoint values per point.  Each CTA alone on its SM, e.g. beside the CTAs of a ragged launch
     size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    const size_t need = (size_t)(spread ? kSpreadSmemPerPoint : 5LL) * M * sizeof(double2);
+    ck(exclusive_smem(k->fn, need, &smem, &fa), "smem attribute");
     if (smem == 0) throw Unsupported("grid too large for the cluster kernel");
     const long long clusters = std::min<long long>(nInst, smCount() / C);
     lastSchedule = Schedule{(int)(C * clusters), T, 1, smem, 1, 1};
-    lastR = C;
+    lastR = a.R;
     lastTuned = 0;
     lastRegs = fa.numRegs;
     auto record = [&] {

@@ -128,6 +128,15 @@ cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2
 cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                                      const double2* dstepP, const double2* backP, const double2* rel, int nRows,
                                      const FFTPlanH& localPlan, const double2* tw, cudaStream_t s);
+// Shared memory of a CTA of the one-point-per-thread cluster kernels (prop_spread.cu), in double2
+// values per point of the CTA: M-point twiddles, two exchange buffers, two halves of 4 receive rows.
+constexpr long long kSpreadSmemPerPoint = 11;
+
+// Chi3 pump march on a 4-CTA cluster with one point per thread (prop_spread.cu); N = 4 M, M a power of
+// two from 32 to 1024.
+cudaError_t launch_pump_chi3_spread(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
+                                    const double2* dstepP, const double2* backP, const double2* rel, int nRows, int N,
+                                    const double2* tw, cudaStream_t s);
 cudaError_t launch_green_epilogue(const double2* raw, long long rawStride, int N, int nIn, int nOut,
                                   const double2* blockScale, const uint8_t* blockShift, double2* C,
                                   double2* S, cudaStream_t s);

@@ -338,8 +338,10 @@ class _NonlinearMedium:
         _check(_lib.nlm_set_schedule(self._h(), int(cta_per_sm), int(use_propagator), int(use_graph)))
 
     def _set_cluster(self, enable):
-        """Spread each propagation of small launches on large grids over a 4-CTA cluster (default on)."""
-        _check(_lib.nlm_set_cluster(self._h(), int(bool(enable))))
+        """Spread each propagation of small launches over a 4-CTA cluster: 1 (default) with one point
+        per thread on 256..1024-point grids for full-grid propagations and the Chi3 pump march, 2 with
+        four points per thread only (grids of 1024 points and more), 0 one CTA per propagation."""
+        _check(_lib.nlm_set_cluster(self._h(), int(enable)))
 
     def _set_precision(self, precision):
         """"f64" (default) or "ff": double-float arithmetic (FP32 pairs, ~48-bit significand) for the

@@ -1,6 +1,8 @@
 """Propagations spread over a 4-CTA cluster (four-step FFT through distributed shared memory): the
-full grids of runSignalSimulation and small batches on grids of 1024 to 8192 points, against the
-oracle and against the one-CTA kernels."""
+full grids of runSignalSimulation and small batches on grids of 1024 to 8192 points with four points
+per thread (cluster mode 2, and the default from 2048 points), the full grids and the Chi3 pump march
+on grids of 256 to 1024 points with one point per thread (the default there), against the oracle and
+against the one-CTA kernels."""
 import numpy as np
 import pytest
 
@@ -25,6 +27,7 @@ MEDIA = {"Chi2PDC": PDC, "Chi2SFG": SFG, "Chi3": CHI3, "Chi2SHG": SHG}
 def test_cluster_signal_grids_match_oracle(nlm, oracle, name, n):
     kw = dict(MEDIA[name], tPrecision=n)
     med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw)
+    med._set_cluster(2)
     med.runPumpSimulation()
     ref.run_pump_simulation()
     a = cases.noise(np.random.default_rng(n), n, 0.2)
@@ -74,19 +77,23 @@ def test_cluster_equals_one_cta_kernels(nlm):
     assert cases.rel_l2(res[0][0], res[1][0]) < 1e-12 and cases.rel_l2(res[0][1], res[1][1]) < 1e-12
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
-def test_cluster_every_solver_matches_oracle(nlm, oracle, name):
-    """runSignalSimulation of each DiffEq solver on a 1024-point grid runs on a 4-CTA cluster and
-    matches the oracle's full grids."""
+def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
+    """runSignalSimulation of each DiffEq solver on a 1024-point grid runs on a 4-CTA cluster, with one
+    point per thread (mode 1, the default) or four (mode 2), and matches the oracle's full grids."""
     kw = dict(cases.CASES[name], tPrecision=1024)
     med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**cases.oracle_kwargs(name) | {"tPrecision": 1024})
+    med._set_cluster(mode)
     if name not in cases.FULLY_NONLINEAR:
         med.runPumpSimulation()
         ref.run_pump_simulation()
     a = cases.noise(np.random.default_rng(5), 1024, 0.3)
     med.runSignalSimulation(a, True, 0)
     ref.run_signal_simulation(a, True, 0)
-    assert med._last_schedule()["grid"] == 4 and med._last_schedule()["R"] == 4
+    sched = med._last_schedule()
+    assert sched["grid"] == 4 and sched["R"] == (1 if mode == 1 else 4)
+    assert sched["block"] == (256 if mode == 1 else 64)
     for m in range(med._dims["nSignalModes"]):
         assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
@@ -134,3 +141,62 @@ def test_cluster_chi3_pump_march(nlm, oracle, n):
     assert cases.rel_l2(med.pumpFreq, ref.pump_freq[0]) < TOL
     assert cases.rel_l2(med.pumpTime, one.pumpTime) < 1e-12
     assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024])
+@pytest.mark.parametrize("name", ["Chi2PDC", "Chi3", "Chi2SFG"])
+def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
+    """runSignalSimulation on 256..1024 points: one point per thread on four SMs, both input domains,
+    against the oracle and against the one-CTA kernels (same arithmetic, other transform order)."""
+    kw = dict(MEDIA[name], tPrecision=n)
+    med, ref, one = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
+    one._set_cluster(0)
+    for m in (med, one):
+        m.runPumpSimulation()
+    ref.run_pump_simulation()
+    modes = 2 if name == "Chi2SFG" else 1
+    a = cases.noise(np.random.default_rng(n + 1), n, 0.2)
+    for in_time in (True, False):
+        med.runSignalSimulation(a, in_time)
+        one.runSignalSimulation(a, in_time)
+        ref.run_signal_simulation(a, in_time)
+        sched = med._last_schedule()
+        assert sched["R"] == 1 and sched["grid"] == 4 and sched["block"] == n // 4
+        assert one._last_schedule()["grid"] == 1
+        for m in range(modes):
+            assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
+            assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL
+            assert cases.rel_l2(med.signalTimes(m), one.signalTimes(m)) < 1e-12
+            assert cases.rel_l2(med.signalFreqs(m), one.signalFreqs(m)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [256, 512])
+def test_spread_chi3_pump_march(nlm, oracle, n):
+    """The self-phase-modulation pump march with one point per thread on four SMs (the default on 256
+    to 1024 points; 1024 is covered by test_cluster_chi3_pump_march)."""
+    kw = dict(CHI3, tPrecision=n, zPrecision=15)
+    med, ref, one = nlm.Chi3(**kw), oracle.Chi3(**kw), nlm.Chi3(**kw)
+    one._set_cluster(0)
+    for m in (med, one):
+        m.runPumpSimulation()
+    ref.run_pump_simulation()
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(med.pumpFreq, ref.pump_freq[0]) < TOL
+    assert cases.rel_l2(med.pumpTime, one.pumpTime) < 1e-12
+    assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12
+
+
+def test_spread_config_chi3_n512(nlm, oracle):
+    """The Chi3 pump + signal configuration (N=512, nZSteps=200, nZStepsP=399): pump march and signal
+    march both on the spread kernels, full grids against the oracle."""
+    kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=512, zPrecision=200)
+    med, ref = nlm.Chi3(**kw), oracle.Chi3(**kw)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    a = cases.noise(np.random.default_rng(1), 512, 1e-3)
+    med.runSignalSimulation(a, True)
+    ref.run_signal_simulation(a, True)
+    assert med._last_schedule()["R"] == 1 and med._last_schedule()["grid"] == 4
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
+    assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
