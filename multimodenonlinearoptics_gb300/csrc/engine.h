@@ -1467,9 +1467,9 @@ struct Medium {
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
     if (nInst * kClusterSize > smCount()) return nullptr;
-    // full-grid propagations (runSignalSimulation) on the spread grids: one point per thread.  Batches
-    // and the adjoint's checkpointed forwards keep the kernels their reverse sweeps pair with.
-    if (spreadGrid() && (a.gridF || a.gridT) && !a.ckpt && !a.stages)
+    // the spread grids: one point per thread (the Chi2PDC reverse sweep has the same form,
+    // adjoint_spread.cu; Chi3GNLSE, whose forward stores stage values, has no spread kernel)
+    if (spreadGrid() && !a.stages)
       if (const KernelEntry* ks = findKernel(kKindCluster, solver, 1)) return ks;
     if (N < 1024) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);
@@ -1924,21 +1924,27 @@ struct Medium {
   }
 
   // Chi2PDC with few rows on a cluster grid (the forward ran on 4-CTA clusters): the reverse sweep
-  // over 4-CTA clusters too (adjoint_cluster.cu); false when it does not apply.
+  // over 4-CTA clusters too, with one point per thread on the spread grids (adjoint_spread.cu) and four
+  // above (adjoint_cluster.cu); false when it does not apply.
   bool adjointClusterPdc(const double2* gout, double2* gin) {
     constexpr int C = kClusterSize;
-    if (solver != kChi2PDC || !useCluster || !is_pow2((int)N) || N < 1024 || N > (uint)kMaxFFT) return false;
+    if (solver != kChi2PDC || !useCluster || !is_pow2((int)N) || N > (uint)kMaxFFT) return false;
+    const bool spread = spreadGrid();
+    if (!spread && N < 1024) return false;
     if (adjRows * C > smCount()) return false;
-    const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
+    const int Rk = spread ? 1 : C;   // points per thread
+    const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, Rk);
     if (!k) return false;
     const int M = (int)N / C;
+    const size_t need = (size_t)(spread ? kSpreadSmemPerPoint : 5LL) * M * sizeof(double2);
     size_t smem = 0;
     cudaFuncAttributes fa;
-    ck(exclusive_smem(k->fn, (size_t)5 * M * sizeof(double2), &smem, &fa), "smem attribute");
+    ck(exclusive_smem(k->fn, need, &smem, &fa), "smem attribute");
     if (smem == 0) return false;
     PropArgs a = baseArgs(C);
-    a.plan = make_plan(M, C);
-    a.R = C;
+    a.plan = make_plan(M, Rk);
+    a.R = Rk;
+    const int T = spread ? M : a.plan.T;   // threads per CTA
     a.nInst = adjRows;
     a.ipc = 1;
     a.work = nullptr;
@@ -1954,11 +1960,11 @@ struct Medium {
     int group = C;
     long long clusters = adjRows;
     if (adjK > 1) {
-      if (const KernelEntry* kp = findKernel(kKindAdjoint, solver + 200, C)) {
+      if (const KernelEntry* kp = findKernel(kKindAdjoint, solver + 200, Rk)) {
         size_t smemP = 0;
         cudaFuncAttributes faP;
-        ck(exclusive_smem(kp->fn, (size_t)5 * M * sizeof(double2), &smemP, &faP), "smem attribute");
-        const int fit = smemP ? maxActiveClusters(kp->fn, 2 * C, a.plan.T, smemP) : 0;
+        ck(exclusive_smem(kp->fn, need, &smemP, &faP), "smem attribute");
+        const int fit = smemP ? maxActiveClusters(kp->fn, 2 * C, T, smemP) : 0;
         if (fit >= 1 && adjRows <= 3LL * fit) {
           const long long waves = (adjRows + fit - 1) / fit;
           clusters = (adjRows + waves - 1) / waves;
@@ -1984,11 +1990,11 @@ struct Medium {
       d.gp = adjGPS.p;
     }
     void* args[] = {(void*)&a, (void*)&d};
-    lastSchedule = Schedule{(int)(group * clusters), a.plan.T, 1, smem, 1, 1};
-    lastR = C;
+    lastSchedule = Schedule{(int)(group * clusters), T, 1, smem, 1, 1};
+    lastR = Rk;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(launch_clustered(k->fn, (int)(group * clusters), a.plan.T, smem, stream, group, args), "adjoint (cluster)");
+    ck(launch_clustered(k->fn, (int)(group * clusters), T, smem, stream, group, args), "adjoint (cluster)");
     launches++;
     if (march) {
       ck(launch_adj_stage_grads(a, d, (int)N, adjRows, stream), "stage gradients");

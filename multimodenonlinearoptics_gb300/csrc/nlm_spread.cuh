@@ -37,6 +37,7 @@ struct SpreadFFT {
   double2* recv;        // [2][4][M] cluster receive buffers
   int M, rank, j;
   int sel, phase;       // next exchange buffer / receive half
+  int base;             // cluster rank of the group's first CTA (clusters holding two groups of four)
 };
 
 // Sets up the spread transform of this CTA: the M-point twiddles (every C-th entry of the N-point
@@ -48,6 +49,7 @@ __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const d
   f.j = threadIdx.x;
   f.sel = 0;
   f.phase = 0;
+  f.base = 0;
   double2* twM = smem;
   f.buf = smem + M;
   f.recv = smem + 3 * M;
@@ -97,7 +99,7 @@ __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::
   const int M = f.M;
   double2* half = f.recv + (long long)f.phase * kSpreadC * M;
 #pragma unroll
-  for (int v = 0; v < kSpreadC; v++) *cl.map_shared_rank(half + f.rank * M + f.j, v) = y;
+  for (int v = 0; v < kSpreadC; v++) *cl.map_shared_rank(half + f.rank * M + f.j, f.base + v) = y;
   cl.sync();
   const double2 r0 = half[f.j], r1 = half[M + f.j], r2 = half[2 * M + f.j], r3 = half[3 * M + f.j];
   f.phase ^= 1;
@@ -114,6 +116,12 @@ __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::
     case 2: return make_double2(a.x - b.x, a.y - b.y);
     default: return make_double2(a.x - b.y, a.y + b.x);   // a + i b
   }
+}
+
+// n bare cluster barriers: the transform slots of a group that has no transform to do while the other
+// group of the same cluster does (every exchange ends with a barrier of the whole cluster)
+__device__ __forceinline__ void spread_idle(cg::cluster_group& cl, int n) {
+  for (int q = 0; q < n; q++) cl.sync();
 }
 
 // time-domain ownership -> frequency-domain ownership

@@ -343,23 +343,25 @@ def test_gnlse_cluster_sweep(nlm, n):
     assert abs(adj - fd) < 1e-6 * abs(fd)
 
 
-@pytest.mark.parametrize("n", [1024, 4096])
+@pytest.mark.parametrize("n", [512, 1024, 4096])
 def test_pdc_cluster_sweep(nlm, oracle, n):
-    """Few rows on grids of 1024+ points: the checkpointed forward runs on 4-CTA clusters, and so does
-    the reverse sweep for checkpoint interval 1; interval 7 (segments recomputed with the cluster
-    transforms) runs pipelined on clusters of eight CTAs.  The input, pump and poling gradients agree
-    with the one-CTA sweeps, and match directional central differences of the oracle's forward."""
+    """Few rows on grids of 256+ points: the checkpointed forward runs on 4-CTA clusters (one point per
+    thread up to 1024 points, four above; cluster mode 2 keeps four at 1024), and so does the reverse
+    sweep for checkpoint interval 1; interval 7 (segments recomputed with the cluster transforms) runs
+    pipelined on clusters of eight CTAs.  The input, pump and poling gradients agree with the one-CTA
+    sweeps, and match directional central differences of the oracle's forward."""
     kw = dict(KW, tPrecision=n, zPrecision=30)
     nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
     x, f0, d, target = _problem(n, nz, rows=2, seed=n)
     res = {}
-    for cluster in (1, 0):
+    for cluster in ((1, 2, 0) if n == 1024 else (1, 0)):
         for k in (1, 7):
             res[cluster, k] = _engine_grads(nlm, kw, x, f0, d, target, interval=k, cluster=cluster)
             if cluster:
                 sched = res[cluster, k][4]._last_schedule()
-                assert sched["grid"] == (8 if k == 1 else 16) and sched["R"] == 4
-    for key in ((1, 7), (0, 1), (0, 7)):
+                assert sched["grid"] == (8 if k == 1 else 16)
+                assert sched["R"] == (1 if cluster == 1 and n <= 1024 else 4)
+    for key in [(1, 7), (0, 1), (0, 7)] + ([(2, 1), (2, 7)] if n == 1024 else []):
         for ga, gb in zip(res[1, 1][1:4], res[key][1:4]):
             assert cases.rel_l2(gb, ga) < 1e-11
     out, gx, gf, gd, _ = res[1, 1]
