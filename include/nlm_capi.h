@@ -233,8 +233,8 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 /* 1 (default): a launch of at most SMs/4 propagations on a grid of 1024 to 8192 points spreads
  * each propagation over a cluster of 4 CTAs (one per SM, four-step FFT through distributed
  * shared memory); so do the Chi3 pump march and the reverse sweeps of nlm_adjoint_backward (on 4
- * or, pipelined, 8 CTAs) on such grids.  On grids of 256 to 1024 points, full-grid propagations
- * (nlm_run_signal) and the Chi3 pump march use clusters with one point per thread instead.
+ * or, pipelined, 8 CTAs) on such grids.  On grids of 256 to 1024 points, such launches (and the
+ * Chi2PDC reverse sweeps) and the Chi3 pump march use clusters with one point per thread instead.
  * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  Also used by
  * nlm_ragged_batch for the costliest media.  Other values: NLM_ERR_VALUE.  No counterpart in the
  * reference. */
