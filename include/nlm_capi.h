@@ -241,7 +241,8 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 nlm_status nlm_set_cluster(nlm_medium* m, int enable);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float
- * (pairs of FP32 values, ~48-bit significand, on the FP32 units).  Other paths stay FP64.
+ * (pairs of FP32 values, ~48-bit significand, on the FP32 units).  Other paths stay FP64, among
+ * them launches of at most SMs/4 propagations on cluster grids (see nlm_set_cluster).
  * No counterpart in the reference (its arithmetic is always FP64). */
 nlm_status nlm_set_precision(nlm_medium* m, int precision);
 /* Run computeGreensFunction's propagations one per kernel launch (the "plain" form),
