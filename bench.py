@@ -337,14 +337,16 @@ def measure_configs(nlm, torch, cpu=True):
         o1.run_pump_simulation()
         o1.run_signal_simulation(sig)
         res["chi3_pump_signal_n512"]["cpu_oracle_latency_ms"] = 1e3 * (time.perf_counter() - t0)
-    # single propagations (runSignalSimulation, full grids): one CTA against a 4-CTA cluster per
-    # propagation; at 1024 points with one point per thread (the default) and with four
+    # single propagations (runSignalSimulation, full grids): one CTA against a cluster per propagation;
+    # at 1024 and 2048 points with one point per thread (the default) and with four
     single = {}
     for n in (1024, 2048, 8192):
         kw = dict(CONFIG, tPrecision=n, zPrecision=500)
         a = (np.random.default_rng(n).standard_normal(n) + 0j) * 0.1
         row = {"n_freqs": n}
-        forms = ((0, "one_cta_ms"), (1, "spread_ms"), (2, "cluster_ms")) if n == 1024 else \
+        # mode 1: one point per thread (four CTAs at 1024 points, eight at 2048); mode 2: four points
+        # per thread on four CTAs, the only cluster form at 8192 points
+        forms = ((0, "one_cta_ms"), (1, "spread_ms"), (2, "cluster_ms")) if n <= 2048 else \
             ((0, "one_cta_ms"), (1, "cluster_ms"))
         for use, label in forms:
             m = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kw)

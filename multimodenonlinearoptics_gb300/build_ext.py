@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libnlm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_gnlse.cu", "kernels_misc.cu",
-                "nlm_noalloc.cu", "adjoint.cu", "prop_ragged.cu", "adjoint_gnlse.cu", "prop_ff.cu", "prop_direct_c.cu", "prop_cluster.cu", "prop_cluster_b.cu", "prop_cluster_gnlse.cu", "prop_cluster_pump.cu", "prop_spread.cu",
+                "nlm_noalloc.cu", "adjoint.cu", "prop_ragged.cu", "adjoint_gnlse.cu", "prop_ff.cu", "prop_direct_c.cu", "prop_cluster.cu", "prop_cluster_b.cu", "prop_cluster_gnlse.cu", "prop_cluster_pump.cu", "prop_spread.cu", "prop_spread_b.cu",
                 "adjoint_gnlse_cluster.cu", "adjoint_cluster.cu", "adjoint_spread.cu",
                 "greens_quadrature.cu"]
 CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]

@@ -1142,8 +1142,8 @@ struct Medium {
     upload(dd, dP);
     upload(db, bP);
     upload(dr, rel);
-    if (spreadGrid()) {
-      // the march on four SMs with one point per thread (prop_spread.cu)
+    if (spreadGrid() || wideGrid()) {
+      // the march on four (up to 1024 points) or eight SMs with one point per thread (prop_spread.cu)
       ck(launch_pump_chi3_spread(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, (int)N, tw, stream),
          "chi3 pump (spread)");
     } else if (useCluster && N >= 1024) {
@@ -1452,7 +1452,7 @@ struct Medium {
   // 1: clusters, with one point per thread on the grids of spreadGrid(); 2: four points per thread
   // only; 0: one CTA per propagation
   int useCluster = 1;
-  static constexpr uint kSpreadMinN = 256, kSpreadMaxN = 1024;
+  static constexpr uint kSpreadMinN = 256, kSpreadMaxN = 1024, kWideMaxN = 4096;
 
   // A grid whose single propagations run on a 4-CTA cluster with one point per thread (prop_spread.cu):
   // M = N/4 threads per CTA gives two to eight warps per SM, where the four-points-per-thread cluster
@@ -1460,12 +1460,24 @@ struct Medium {
   bool spreadGrid() const {
     return useCluster == 1 && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;
   }
+  // 2048- and 4096-point grids: one point per thread on eight CTAs (prop_spread_b.cu), twice the SMs of
+  // the four-points-per-thread cluster, for the launches that no reverse sweep pairs with (full grids,
+  // the media of ragged batches marked by raggedWide) and the Chi3 pump march.
+  bool wideGrid() const {
+    return useCluster == 1 && is_pow2((int)N) && N > kSpreadMaxN && N <= kWideMaxN;
+  }
+  bool wideLaunch(const PropArgs& a) const {
+    return wideGrid() && !a.ckpt && !a.stages && (a.gridF || a.gridT || raggedWide);
+  }
+  bool raggedWide = false;   // set by nlm_ragged_batch around the propagation of a medium given 8 CTAs
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
     // checkpointed forwards (the adjoint's, Chi2PDC and Chi3GNLSE) run on clusters too: their reverse
     // sweeps have cluster forms that read the same checkpoints
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
+    if (wideLaunch(a) && nInst * 8 <= smCount())
+      if (const KernelEntry* kw = findKernel(kKindCluster, solver + kSpreadWideKey, 1)) return kw;
     if (nInst * kClusterSize > smCount()) return nullptr;
     // the spread grids: one point per thread (the Chi2PDC reverse sweep has the same form,
     // adjoint_spread.cu; Chi3GNLSE, whose forward stores stage values, has no spread kernel)
@@ -1476,9 +1488,9 @@ struct Medium {
   }
 
   void launchCluster(const KernelEntry* k, PropArgs a, long long nInst) {
-    constexpr int C = kClusterSize;
+    const bool spread = k->R == 1;   // one point per thread (prop_spread.cu, prop_spread_b.cu)
+    const int C = k->key >= kSpreadWideKey ? 8 : kClusterSize;
     const int M = (int)N / C;
-    const bool spread = k->R == 1;   // one point per thread (prop_spread.cu)
     a.plan = make_plan(M, spread ? 1 : C);
     a.R = spread ? 1 : C;
     a.nInst = nInst;
@@ -1486,10 +1498,11 @@ struct Medium {
     a.work = nullptr;
     const int T = spread ? M : a.plan.T;
     // four points per thread: M-point twiddles x2, exchange buffer, 2 x C x T receive; one point per
-    // thread: kSpreadSmemPerPoint values per point.  Each CTA alone on its SM, e.g. beside the CTAs of a ragged launch
+    // thread: spread_smem_per_point(C) values per point.  Each CTA alone on its SM, e.g. beside the
+    // CTAs of a ragged launch
     size_t smem = 0;
     cudaFuncAttributes fa;
-    const size_t need = (size_t)(spread ? kSpreadSmemPerPoint : 5LL) * M * sizeof(double2);
+    const size_t need = (size_t)(spread ? spread_smem_per_point(C) : 5LL) * M * sizeof(double2);
     ck(exclusive_smem(k->fn, need, &smem, &fa), "smem attribute");
     if (smem == 0) throw Unsupported("grid too large for the cluster kernel");
     const long long clusters = std::min<long long>(nInst, smCount() / C);

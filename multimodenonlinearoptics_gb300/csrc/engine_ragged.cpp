@@ -99,6 +99,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       // clusters leave the ragged launch about one SM per two remaining media: it claims its media
       // largest first from a work counter, so the smallest ones queue behind the others.
       std::vector<size_t> clustered;
+      std::vector<bool> wide(n_media, false);
       {
         const int sms = Medium::smCount();
         std::vector<size_t> others;
@@ -113,6 +114,17 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
             others.push_back(k);   // still largest first
         }
         ks.swap(others);
+        // the costliest of them on 2048- and 4096-point grids take eight CTAs (one point per thread,
+        // twice the SMs) while the SMs allow, largest first
+        size_t used = clustered.size() * Medium::kClusterSize + (ks.size() + 1) / 2;
+        for (size_t k : clustered) {
+          Medium* m = ms[k];
+          if (m->wideGrid() && m->findKernel(kKindCluster, m->solver + kSpreadWideKey, 1) &&
+              used + (8 - Medium::kClusterSize) <= (size_t)sms) {
+            wide[k] = true;
+            used += 8 - Medium::kClusterSize;
+          }
+        }
       }
       if (!clustered.empty()) {
         // Each cluster propagation runs on its medium's own stream: input copy (page-locked source),
@@ -136,7 +148,14 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
           for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
           a.out = g_ragged.cout.p + oo;
           a.outStride = (long long)m->nSignal * m->N;
-          m->propagate(a, 1, m->raggedPropagator());
+          m->raggedWide = wide[k];
+          try {
+            m->propagate(a, 1, m->raggedPropagator());
+          } catch (...) {
+            m->raggedWide = false;
+            throw;
+          }
+          m->raggedWide = false;
           pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
                                 (size_t)m->nSignal * m->N * sizeof(double2), m->stream});
           clusterSync.push_back(m->stream);

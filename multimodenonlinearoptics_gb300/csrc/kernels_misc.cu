@@ -21,6 +21,7 @@ void add_kernels_direct_c(std::vector<KernelEntry>& t);
 void add_kernels_cluster(std::vector<KernelEntry>& t);
 void add_kernels_cluster_b(std::vector<KernelEntry>& t);
 void add_kernels_spread(std::vector<KernelEntry>& t);
+void add_kernels_spread_b(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_spread(std::vector<KernelEntry>& t);
 void add_kernels_cluster_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse_cluster(std::vector<KernelEntry>& t);
@@ -42,6 +43,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_cluster(table);
     add_kernels_cluster_b(table);
     add_kernels_spread(table);
+    add_kernels_spread_b(table);
     add_kernels_adjoint_spread(table);
     add_kernels_cluster_gnlse(table);
     add_kernels_adjoint_gnlse_cluster(table);

@@ -128,9 +128,13 @@ cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2
 cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                                      const double2* dstepP, const double2* backP, const double2* rel, int nRows,
                                      const FFTPlanH& localPlan, const double2* tw, cudaStream_t s);
-// Shared memory of a CTA of the one-point-per-thread cluster kernels (prop_spread.cu), in double2
-// values per point of the CTA: M-point twiddles, two exchange buffers, two halves of 4 receive rows.
-constexpr long long kSpreadSmemPerPoint = 11;
+// Shared memory of a CTA of the one-point-per-thread cluster kernels (prop_spread.cu) of C CTAs, in
+// double2 values per point of the CTA: M-point twiddles, two exchange buffers, two halves of C receive
+// rows.
+constexpr long long spread_smem_per_point(int C) { return 3 + 2LL * C; }
+constexpr long long kSpreadSmemPerPoint = spread_smem_per_point(4);
+// Registry key offset (kKindCluster) of the one-point-per-thread kernels on eight CTAs.
+constexpr int kSpreadWideKey = 800;
 
 // Chi3 pump march on a 4-CTA cluster with one point per thread (prop_spread.cu); N = 4 M, M a power of
 // two from 32 to 1024.

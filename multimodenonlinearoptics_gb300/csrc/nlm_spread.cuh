@@ -1,22 +1,23 @@
-// nlm_spread.cuh -- one propagation on a cluster of four CTAs with ONE point per thread.
+// nlm_spread.cuh -- one propagation on a cluster of four (or eight) CTAs with ONE point per thread.
 //
 // The FP64 units of an SM belong to its four schedulers: each issues at most 0.5 DFMA lanes per
 // clock, and only for its own warps.  The four-points-per-thread cluster transforms (nlm_cluster.cuh)
 // give a grid of N points N/16 threads per CTA: below N = 2048 that is fewer than four warps per SM,
 // so some schedulers idle.  Here every CTA holds M = N/4 points, one per thread: N = 512 gives four
-// warps on each of the four SMs, four times the FP64 issue of one SM.  The transforms:
-//   time domain:       CTA c, thread j  <->  point n = c + 4 j
+// warps on each of the four SMs, four times the FP64 issue of one SM.  With C = 8 CTAs (M = N/8) the
+// same form doubles the SMs of a 2048- or 4096-point propagation.  The transforms:
+//   time domain:       CTA c, thread j  <->  point n = c + C j
 //   frequency domain:  CTA c, thread j  <->  bin   k = j + M c
 // forward:  M-point DFT over j of the CTA's strided points (radix-2 Stockham through shared memory,
 //           one output per thread and stage: out = e + W o as two FMAs per component), twiddle
-//           exp(-2 pi i c j / N), then the 4-point DFT over the CTAs: every thread pushes its value to
-//           all four CTAs through distributed shared memory, one cluster barrier, and each thread
-//           combines the four values of its own column for its CTA's output row;
-// inverse:  the 4-point inverse DFT over the CTAs first, the conjugate twiddle, then the local inverse
+//           exp(-2 pi i c j / N), then the C-point DFT over the CTAs: every thread pushes its value to
+//           all C CTAs through distributed shared memory, one cluster barrier, and each thread
+//           combines the C values of its own column for its CTA's output row;
+// inverse:  the C-point inverse DFT over the CTAs first, the conjugate twiddle, then the local inverse
 //           DFT (unscaled; 1/N is in the tables).
 // Shared memory: M twiddles, two M-point exchange buffers (alternating, one barrier per stage: a thread
 // writes a buffer only after the barrier that every reader of that buffer's previous contents has
-// passed), and two halves of 4 x M cluster receive buffers (alternating per transform: a CTA writes a
+// passed), and two halves of C x M cluster receive buffers (alternating per transform: a CTA writes a
 // half only after the cluster barrier that its readers passed after their last read of it).
 #pragma once
 #include <cooperative_groups.h>
@@ -28,13 +29,13 @@ namespace cg = cooperative_groups;
 namespace nlm {
 
 constexpr int kSpreadC = 4;
-static_assert(kSpreadSmemPerPoint == 1 + 2 + 2 * kSpreadC, "twiddles, exchange buffers, receive halves");
+static_assert(kSpreadSmemPerPoint == spread_smem_per_point(kSpreadC), "twiddles, exchange buffers, receive halves");
 
 struct SpreadFFT {
   const double2* twM;   // [M] exp(-2 pi i m / M), shared memory
   double2 twC;          // exp(-2 pi i c j / N) of this thread (rank c, thread j)
   double2* buf;         // [2][M] exchange buffers of the local transform
-  double2* recv;        // [2][4][M] cluster receive buffers
+  double2* recv;        // [2][C][M] cluster receive buffers
   int M, rank, j;
   int sel, phase;       // next exchange buffer / receive half
   int base;             // cluster rank of the group's first CTA (clusters holding two groups of four)
@@ -42,6 +43,7 @@ struct SpreadFFT {
 
 // Sets up the spread transform of this CTA: the M-point twiddles (every C-th entry of the N-point
 // table `tw`) and this thread's cluster twiddle.  Ends with a CTA barrier.
+template <int C = kSpreadC>
 __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const double2* __restrict__ tw, int M,
                                             int rank) {
   f.M = M;
@@ -53,7 +55,7 @@ __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const d
   double2* twM = smem;
   f.buf = smem + M;
   f.recv = smem + 3 * M;
-  for (int k = threadIdx.x; k < M; k += blockDim.x) twM[k] = tw[(long long)k * kSpreadC];
+  for (int k = threadIdx.x; k < M; k += blockDim.x) twM[k] = tw[(long long)k * C];
   f.twM = twM;
   f.twC = tw[(long long)rank * f.j];
   __syncthreads();
@@ -92,29 +94,48 @@ __device__ __forceinline__ double2 spread_local(SpreadFFT& f, double2 x) {
   return x;
 }
 
-// 4-point DFT over the cluster's CTAs: thread j of every CTA pushes y to column j of row `rank` in all
-// four CTAs; after the barrier thread j of CTA r returns sum_c W_4^(+-r c) recv[c][j].
-template <bool INV>
+// C-point DFT over the cluster's CTAs: thread j of every CTA pushes y to column j of row `rank` in all
+// C CTAs; after the barrier thread j of CTA r returns sum_c W_C^(+-r c) recv[c][j].
+template <bool INV, int C = kSpreadC>
 __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::cluster_group& cl) {
+  static_assert(C == 4 || C == 8, "four or eight CTAs");
   const int M = f.M;
-  double2* half = f.recv + (long long)f.phase * kSpreadC * M;
+  double2* half = f.recv + (long long)f.phase * C * M;
 #pragma unroll
-  for (int v = 0; v < kSpreadC; v++) *cl.map_shared_rank(half + f.rank * M + f.j, f.base + v) = y;
+  for (int v = 0; v < C; v++) *cl.map_shared_rank(half + f.rank * M + f.j, f.base + v) = y;
   cl.sync();
-  const double2 r0 = half[f.j], r1 = half[M + f.j], r2 = half[2 * M + f.j], r3 = half[3 * M + f.j];
+  double2 r[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) r[c] = half[c * M + f.j];
   f.phase ^= 1;
-  // a = r0 + (-1)^r r2, b = r1 + (-1)^r r3, out = a + W_4^(+-r) b with W_4 = -i (forward)
-  const int r = f.rank;
-  const double sg = (r & 1) ? -1.0 : 1.0;
-  const double2 a = make_double2(fma(sg, r2.x, r0.x), fma(sg, r2.y, r0.y));
-  const double2 b = make_double2(fma(sg, r3.x, r1.x), fma(sg, r3.y, r1.y));
-  // W_4^(r) for r = 0..3: 1, -i, -1, i (forward); conjugates for the inverse
-  const int q = INV ? (4 - r) & 3 : r;
-  switch (q) {
-    case 0: return make_double2(a.x + b.x, a.y + b.y);
-    case 1: return make_double2(a.x + b.y, a.y - b.x);    // a - i b
-    case 2: return make_double2(a.x - b.x, a.y - b.y);
-    default: return make_double2(a.x - b.y, a.y + b.x);   // a + i b
+  const int rk = f.rank;
+  const double sg = (rk & 1) ? -1.0 : 1.0;   // W_C^(r C/2) = (-1)^r
+  // W_4^(+-r) b for the four quarter turns: 1, -i, -1, i (forward); conjugates for the inverse
+  const int q = INV ? (4 - (rk & 3)) & 3 : (rk & 3);
+  auto quarter = [q](double2 b) {
+    switch (q) {
+      case 0: return b;
+      case 1: return make_double2(b.y, -b.x);    // -i b
+      case 2: return make_double2(-b.x, -b.y);
+      default: return make_double2(-b.y, b.x);   // i b
+    }
+  };
+  if constexpr (C == 4) {
+    // a = r0 + (-1)^r r2, b = r1 + (-1)^r r3, out = a + W_4^(+-r) b
+    const double2 a = make_double2(fma(sg, r[2].x, r[0].x), fma(sg, r[2].y, r[0].y));
+    const double2 b = quarter(make_double2(fma(sg, r[3].x, r[1].x), fma(sg, r[3].y, r[1].y)));
+    return make_double2(a.x + b.x, a.y + b.y);
+  } else {
+    // u_c = r_c + (-1)^r r_(c+4); v0 = u0 + W_4^r u2, v1 = u1 + W_4^r u3; out = v0 + W_8^r v1
+    double2 u[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) u[c] = make_double2(fma(sg, r[c + 4].x, r[c].x), fma(sg, r[c + 4].y, r[c].y));
+    const double2 q2 = quarter(u[2]), q3 = quarter(u[3]);
+    const double2 v0 = make_double2(u[0].x + q2.x, u[0].y + q2.y);
+    const double2 v1 = make_double2(u[1].x + q3.x, u[1].y + q3.y);
+    const double2 w = f.twM[rk * (M / 8)];      // W_8^r = W_M^(r M / 8)
+    const double wy = INV ? -w.y : w.y;
+    return make_double2(fma(-wy, v1.y, fma(w.x, v1.x, v0.x)), fma(wy, v1.x, fma(w.x, v1.y, v0.y)));
   }
 }
 
@@ -125,14 +146,16 @@ __device__ __forceinline__ void spread_idle(cg::cluster_group& cl, int n) {
 }
 
 // time-domain ownership -> frequency-domain ownership
+template <int C = kSpreadC>
 __device__ __forceinline__ double2 spread_fwd(SpreadFFT& f, double2 x, cg::cluster_group& cl) {
   x = spread_local<false>(f, x);
-  return spread_exchange<false>(f, cmul(x, f.twC), cl);
+  return spread_exchange<false, C>(f, cmul(x, f.twC), cl);
 }
 
 // frequency-domain ownership -> time-domain ownership (unscaled)
+template <int C = kSpreadC>
 __device__ __forceinline__ double2 spread_inv(SpreadFFT& f, double2 x, cg::cluster_group& cl) {
-  x = cmulc(spread_exchange<true>(f, x, cl), f.twC);
+  x = cmulc(spread_exchange<true, C>(f, x, cl), f.twC);
   return spread_local<true>(f, x);
 }
 

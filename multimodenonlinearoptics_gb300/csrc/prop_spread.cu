@@ -1,211 +1,48 @@
-// prop_spread.cu -- single propagations and the Chi3 pump march on a cluster of four CTAs with one
-// point per thread (nlm_spread.cuh), for grids whose four-points-per-thread cluster form would leave
-// schedulers idle or is not built (N = 256 to 1024: M = N/4 threads per CTA).
-//
-// k_pump_chi3_spread has the arithmetic of k_pump_chi3 / k_pump_chi3_cluster (solvers/Chi3.cpp:41-70);
-// k_propagate_spread<S> that of k_propagate_cluster<S> (src/_NonlinearMedium.hpp:160-239): the same
-// tables, the same order of operations per point, only the ownership of the points differs.
+// prop_spread.cu -- single propagations, small batches and the Chi3 pump march on a cluster of four CTAs
+// with one point per thread (prop_spread.cuh), for grids whose four-points-per-thread cluster form
+// would leave schedulers idle or is not built (N = 256 to 1024: M = N/4 threads per CTA); the pump
+// march also on eight CTAs for 2048 and 4096 points.
 #include <vector>
 
 #include "nlm_launch.h"
-#include "nlm_spread.cuh"
+#include "prop_spread.cuh"
 
 namespace nlm {
-
-// tw: the N-point table; M = N / 4 threads per CTA.
-__global__ void __launch_bounds__(kMaxThreads) k_pump_chi3_spread(double2* __restrict__ pf, double2* __restrict__ pt,
-                                                                  const double2* __restrict__ env,
-                                                                  const double2* __restrict__ halfP,
-                                                                  const double2* __restrict__ dstepP,
-                                                                  const double2* __restrict__ backP,
-                                                                  const double2* __restrict__ rel, int nRows, int M,
-                                                                  const double2* __restrict__ tw) {
-  extern __shared__ double2 smem[];
-  cg::cluster_group cl = cg::this_cluster();
-  SpreadFFT f;
-  const int rank = (int)cl.block_rank();
-  spread_init(f, smem, tw, M, rank);
-  const int N = M * kSpreadC;
-  const int tn = rank + kSpreadC * f.j;   // time-domain point of this thread
-  const int fk = f.j + M * rank;          // frequency bin of this thread
-  const double invN = 1.0 / N;
-  const double2 hp = halfP[fk], dp = dstepP[fk];
-  double2 x = spread_fwd(f, env[tn], cl);
-  x = cmul(x, hp);
-  pf[fk] = x;
-  x = cscale(spread_inv(f, x, cl), invN);
-  pt[tn] = x;
-  for (int i = 1; i < nRows; i++) {
-    const double2 r = rel[i - 1];
-    const double a2 = cabs2(x);
-    x = cmul(x, spm_factor(r.x * a2, r.y * a2));
-    x = cmul(spread_fwd(f, x, cl), dp);
-    pf[(long long)i * N + fk] = x;
-    x = cscale(spread_inv(f, x, cl), invN);
-    pt[(long long)i * N + tn] = x;
-  }
-  // last row: undo half of the last pump dispersion step (each thread rereads its own bin)
-  const long long last = (long long)(nRows - 1) * N;
-  x = cmul(pf[last + fk], backP[fk]);
-  pf[last + fk] = x;
-  pt[last + tn] = cscale(spread_inv(f, x, cl), invN);
-}
 
 cudaError_t launch_pump_chi3_spread(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                                     const double2* dstepP, const double2* backP, const double2* rel, int nRows, int N,
                                     const double2* tw, cudaStream_t s) {
-  int M = N / kSpreadC;
-  if (N % kSpreadC != 0 || M < 32 || M > kMaxThreads || (M & (M - 1)) != 0) return cudaErrorInvalidValue;
+  // four CTAs up to 1024 points, eight above (M = N / C threads per CTA)
+  const int C = N <= 1024 ? 4 : 8;
+  int M = N / C;
+  if (N % C != 0 || M < 32 || M > kMaxThreads || (M & (M - 1)) != 0) return cudaErrorInvalidValue;
+  const void* fn = C == 4 ? (const void*)k_pump_chi3_spread<4> : (const void*)k_pump_chi3_spread<8>;
   // each CTA alone on its SM: its M/32 warps are then the only ones on their schedulers
   size_t smem = 0;
-  cudaError_t e = exclusive_smem((const void*)k_pump_chi3_spread, (size_t)kSpreadSmemPerPoint * M * sizeof(double2), &smem);
+  cudaError_t e = exclusive_smem(fn, (size_t)spread_smem_per_point(C) * M * sizeof(double2), &smem);
   if (e != cudaSuccess) return e;
   if (smem == 0) return cudaErrorInvalidValue;
   void* args[] = {(void*)&pumpFreq, (void*)&pumpTime, (void*)&env, (void*)&halfP, (void*)&dstepP, (void*)&backP,
                   (void*)&rel, (void*)&nRows, (void*)&M, (void*)&tw};
-  return launch_clustered((const void*)k_pump_chi3_spread, kSpreadC, M, smem, s, kSpreadC, args);
+  return launch_clustered(fn, C, M, smem, s, C, args);
 }
 
-// One propagation per cluster (clusters take instances in turn); a.plan.N = M, a.tw the N-point table.
-// Point-wise work: the pump-driven solvers' RK4 matrices (a.prop) or the solver's DiffEq.
-template <class S>
-__global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs a) {
-  constexpr int MD = S::kM, P = S::kP > 0 ? S::kP : 1;
-  extern __shared__ double2 smem[];
-  cg::cluster_group cl = cg::this_cluster();
-  SpreadFFT f;
-  const int rank = (int)cl.block_rank();
-  const int M = a.plan.N;
-  spread_init(f, smem, a.tw, M, rank);
-  const int N = M * kSpreadC;
-  const int tn = rank + kSpreadC * f.j;
-  const int fk = f.j + M * rank;
-  const long long clusterId = blockIdx.x / kSpreadC, nClusters = gridDim.x / kSpreadC;
-  const long long ms = (long long)a.nZ * N;
-  for (long long local = clusterId; local < a.nInst; local += nClusters) {
-    const long long inst = a.instBase + local;
-    double2 x[MD];
-    const double2* row = a.in + inst * a.inStride;
-#pragma unroll
-    for (int m = 0; m < MD; m++) {
-      int seg = -1;
-      if (m == a.inputMode) seg = 0;
-      else if (a.inputMode < 1 && m < a.inChannels) seg = m;
-      x[m] = seg >= 0 ? row[(long long)seg * N + (a.inTime ? tn : fk)] : czero();
-      if (a.inTime) x[m] = spread_fwd(f, x[m], cl);
-      x[m] = cmul(x[m], __ldg(a.half + (long long)m * N + fk));
-    }
-    if (a.gridF) {
-#pragma unroll
-      for (int m = 0; m < MD; m++) a.gridF[m * ms + fk] = cscale(x[m], (double)N);
-    }
-#pragma unroll
-    for (int m = 0; m < MD; m++) x[m] = spread_inv(f, x[m], cl);
-    if (a.gridT) {
-#pragma unroll
-      for (int m = 0; m < MD; m++) a.gridT[m * ms + tn] = x[m];
-    }
-    // checkpoints for a reverse sweep: the time-domain state before steps 1, K + 1, 2 K + 1, ...
-    double2* ckRow = a.ckpt ? a.ckpt + inst * a.ckN * MD * (long long)N : nullptr;
-    if (ckRow && a.nZ > 1) {
-#pragma unroll
-      for (int m = 0; m < MD; m++) ckRow[(long long)m * N + tn] = x[m];
-    }
-    for (int i = 1; i < a.nZ; i++) {
-      if (a.prop) {
-        // the RK4 step as its per-point real (2M)x(2M) matrix, stored as pairs (row r, columns 2c and
-        // 2c+1) at [step][r * M + c][N]
-        constexpr int D = 2 * MD;
-        const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (D * D / 2) * N;
-        double in[D], outv[D];
-#pragma unroll
-        for (int m = 0; m < MD; m++) {
-          in[2 * m] = x[m].x;
-          in[2 * m + 1] = x[m].y;
-        }
-#pragma unroll
-        for (int r = 0; r < D; r++) {
-          double acc = 0.0;
-#pragma unroll
-          for (int cc = 0; cc < D / 2; cc++) {
-            const double2 e = __ldg(mat + (long long)(r * (D / 2) + cc) * N + tn);
-            acc = fma(e.x, in[2 * cc], acc);
-            acc = fma(e.y, in[2 * cc + 1], acc);
-          }
-          outv[r] = acc;
-        }
-#pragma unroll
-        for (int m = 0; m < MD; m++) x[m] = make_double2(outv[2 * m], outv[2 * m + 1]);
-      } else {
-        const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-        double2 p[3][P];
-#pragma unroll
-        for (int q = 0; q < P; q++) {
-          if (S::kP > 0) {
-            const double2* pr = a.pump + q * a.pumpStride + (long long)(2 * i - 2) * N + tn;
-            p[0][q] = __ldg(pr);
-            p[1][q] = __ldg(pr + N);
-            p[2][q] = __ldg(pr + 2 * N);
-          } else {
-            p[0][q] = p[1][q] = p[2][q] = czero();
-          }
-        }
-        rk4_point<S>(x, p, c);
-      }
-      const bool last = i == a.nZ - 1;
-      const double2* table = last ? a.dlast : a.dstep;
-      const bool wantTime = !last || a.inTime || a.gridT != nullptr;
-#pragma unroll
-      for (int m = 0; m < MD; m++) {
-        x[m] = cmul(spread_fwd(f, x[m], cl), __ldg(table + (long long)m * N + fk));
-        if (a.gridF) a.gridF[m * ms + (long long)i * N + fk] = cscale(x[m], (double)N);
-        if (wantTime) {
-          x[m] = spread_inv(f, x[m], cl);
-          if (a.gridT) a.gridT[m * ms + (long long)i * N + tn] = x[m];
-        }
-        if (ckRow && !last && i % a.ckK == 0) ckRow[((long long)(i / a.ckK) * MD + m) * N + tn] = x[m];
-      }
-    }
-    if (a.nZ == 1) {
-#pragma unroll
-      for (int m = 0; m < MD; m++) {
-        x[m] = cmul(spread_fwd(f, x[m], cl), __ldg(a.back + (long long)m * N + fk));
-        if (a.gridF) a.gridF[m * ms + fk] = cscale(x[m], (double)N);
-        if (a.inTime || a.gridT) {
-          x[m] = spread_inv(f, x[m], cl);
-          if (a.gridT) a.gridT[m * ms + tn] = x[m];
-        }
-      }
-    }
-    // the last row is in the time domain when the input was, else in the frequency domain
-    if (a.out) {
-      double2* o = a.out + inst * a.outStride;
-      const double sc = a.inTime ? 1.0 : (double)N;
-      for (int om = 0; om < a.nOut; om++) {
-#pragma unroll
-        for (int m = 0; m < MD; m++)
-          if (m == a.outModes[om]) o[(long long)om * N + (a.inTime ? tn : fk)] = cscale(x[m], sc);
-      }
-    }
-  }
-}
-
-// key = solver id, R = 1 (one point per thread); cluster of kSpreadC CTAs of N / kSpreadC threads
+// key = solver id, R = 1 (one point per thread); cluster of four CTAs of N / 4 threads
 void add_kernels_spread(std::vector<KernelEntry>& t) {
-  t.push_back({kKindCluster, kChi3, 1, (const void*)k_propagate_spread<FChi3>});
-  t.push_back({kKindCluster, kChi2PDC, 1, (const void*)k_propagate_spread<FChi2PDC>});
-  t.push_back({kKindCluster, kChi2SFG, 1, (const void*)k_propagate_spread<FChi2SFG>});
-  t.push_back({kKindCluster, kChi2AFC, 1, (const void*)k_propagate_spread<FChi2AFC>});
-  t.push_back({kKindCluster, kChi2SFGPDC, 1, (const void*)k_propagate_spread<FChi2SFGPDC>});
-  t.push_back({kKindCluster, kChi2PDCII, 1, (const void*)k_propagate_spread<FChi2PDCII>});
-  t.push_back({kKindCluster, kChi2SFGOPA, 1, (const void*)k_propagate_spread<FChi2SFGOPA>});
-  t.push_back({kKindCluster, kChi2SFGXPM, 1, (const void*)k_propagate_spread<FChi2SFGXPM>});
-  t.push_back({kKindCluster, kChi2SFGII, 1, (const void*)k_propagate_spread<FChi2SFGII>});
-  t.push_back({kKindCluster, kChi2SHG, 1, (const void*)k_propagate_spread<FChi2SHG>});
-  t.push_back({kKindCluster, kChi2ASHG, 1, (const void*)k_propagate_spread<FChi2ASHG>});
-  t.push_back({kKindCluster, kChi2SHGXPM, 1, (const void*)k_propagate_spread<FChi2SHGXPM>});
-  t.push_back({kKindCluster, kChi2SHGOPA, 1, (const void*)k_propagate_spread<FChi2SHGOPA>});
-  t.push_back({kKindCluster, kChi2DSFG, 1, (const void*)k_propagate_spread<FChi2DSFG>});
+  t.push_back({kKindCluster, kChi3, 1, (const void*)k_propagate_spread<FChi3, 4>});
+  t.push_back({kKindCluster, kChi2PDC, 1, (const void*)k_propagate_spread<FChi2PDC, 4>});
+  t.push_back({kKindCluster, kChi2SFG, 1, (const void*)k_propagate_spread<FChi2SFG, 4>});
+  t.push_back({kKindCluster, kChi2AFC, 1, (const void*)k_propagate_spread<FChi2AFC, 4>});
+  t.push_back({kKindCluster, kChi2SFGPDC, 1, (const void*)k_propagate_spread<FChi2SFGPDC, 4>});
+  t.push_back({kKindCluster, kChi2PDCII, 1, (const void*)k_propagate_spread<FChi2PDCII, 4>});
+  t.push_back({kKindCluster, kChi2SFGOPA, 1, (const void*)k_propagate_spread<FChi2SFGOPA, 4>});
+  t.push_back({kKindCluster, kChi2SFGXPM, 1, (const void*)k_propagate_spread<FChi2SFGXPM, 4>});
+  t.push_back({kKindCluster, kChi2SFGII, 1, (const void*)k_propagate_spread<FChi2SFGII, 4>});
+  t.push_back({kKindCluster, kChi2SHG, 1, (const void*)k_propagate_spread<FChi2SHG, 4>});
+  t.push_back({kKindCluster, kChi2ASHG, 1, (const void*)k_propagate_spread<FChi2ASHG, 4>});
+  t.push_back({kKindCluster, kChi2SHGXPM, 1, (const void*)k_propagate_spread<FChi2SHGXPM, 4>});
+  t.push_back({kKindCluster, kChi2SHGOPA, 1, (const void*)k_propagate_spread<FChi2SHGOPA, 4>});
+  t.push_back({kKindCluster, kChi2DSFG, 1, (const void*)k_propagate_spread<FChi2DSFG, 4>});
 }
 
 }  // namespace nlm

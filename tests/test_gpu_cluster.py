@@ -52,7 +52,7 @@ def test_cluster_two_modes_match_oracle(nlm, oracle, name, n):
     a = cases.noise(np.random.default_rng(3), n, 0.2)
     med.runSignalSimulation(a)
     ref.run_signal_simulation(a)
-    assert med._last_schedule()["grid"] == 4
+    assert med._last_schedule()["grid"] == (8 if n > 1024 else 4)   # full grids: eight CTAs from 2048
     for m in range(2):
         assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL
@@ -67,7 +67,7 @@ def test_cluster_equals_one_cta_kernels(nlm):
     kw = dict(PDC, tPrecision=2048, zPrecision=40)
     a = cases.noise(np.random.default_rng(9), 2048, 0.3)
     res = []
-    for use in (1, 0):
+    for use in (2, 0):
         med = nlm.Chi2PDC(**kw)
         med._set_cluster(use)
         med.runPumpSimulation()
@@ -143,11 +143,12 @@ def test_cluster_chi3_pump_march(nlm, oracle, n):
     assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12
 
 
-@pytest.mark.parametrize("n", [256, 512, 1024])
+@pytest.mark.parametrize("n", [256, 512, 1024, 2048, 4096])
 @pytest.mark.parametrize("name", ["Chi2PDC", "Chi3", "Chi2SFG"])
 def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
-    """runSignalSimulation on 256..1024 points: one point per thread on four SMs, both input domains,
-    against the oracle and against the one-CTA kernels (same arithmetic, other transform order)."""
+    """runSignalSimulation on 256..4096 points: one point per thread on four SMs (eight from 2048
+    points), both input domains, against the oracle and against the one-CTA kernels (same arithmetic,
+    other transform order)."""
     kw = dict(MEDIA[name], tPrecision=n)
     med, ref, one = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
     one._set_cluster(0)
@@ -161,7 +162,8 @@ def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
         one.runSignalSimulation(a, in_time)
         ref.run_signal_simulation(a, in_time)
         sched = med._last_schedule()
-        assert sched["R"] == 1 and sched["grid"] == 4 and sched["block"] == n // 4
+        ctas = 4 if n <= 1024 else 8
+        assert sched["R"] == 1 and sched["grid"] == ctas and sched["block"] == n // ctas
         assert one._last_schedule()["grid"] == 1
         for m in range(modes):
             assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
@@ -170,10 +172,11 @@ def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
             assert cases.rel_l2(med.signalFreqs(m), one.signalFreqs(m)) < 1e-12
 
 
-@pytest.mark.parametrize("n", [256, 512])
+@pytest.mark.parametrize("n", [256, 512, 4096])
 def test_spread_chi3_pump_march(nlm, oracle, n):
     """The self-phase-modulation pump march with one point per thread on four SMs (the default on 256
-    to 1024 points; 1024 is covered by test_cluster_chi3_pump_march)."""
+    to 1024 points) or eight (2048 and 4096 points; 1024 and 2048 are covered by
+    test_cluster_chi3_pump_march)."""
     kw = dict(CHI3, tPrecision=n, zPrecision=15)
     med, ref, one = nlm.Chi3(**kw), oracle.Chi3(**kw), nlm.Chi3(**kw)
     one._set_cluster(0)

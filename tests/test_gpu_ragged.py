@@ -58,8 +58,9 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
 
 
 def test_ragged_set_with_cluster_propagations(nlm, oracle):
-    """The costliest media on grids of 1024+ points run as 4-CTA cluster propagations beside the ragged
-    launch of the others; every output matches the oracle."""
+    """The costliest media on grids of 1024+ points run as cluster propagations beside the ragged
+    launch of the others (one point per thread on four CTAs at 1024 points, on eight at 2048); every
+    output matches the oracle."""
     kw0 = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=0.4, beta2s=-0.3, beta2o=0, beta1=0, beta1s=1.2,
                beta1o=0, beta3=0, beta3s=0.05, beta3o=0, diffBeta0=0, tMax=10)
     rng = np.random.default_rng(21)
@@ -77,10 +78,12 @@ def test_ragged_set_with_cluster_propagations(nlm, oracle):
         ins.append(cases.noise(rng, n, 1e-2))
     outs = nlm.ragged_batch(media, ins)
     for m in media:
-        # 1024 points: one point per thread; 2048: four
-        want_r = 1 if m._dims["nFreqs"] == 1024 else 4
-        on_cluster = m._last_schedule()["grid"] == 4 and m._last_schedule()["R"] == want_r
-        assert on_cluster == (m._dims["nFreqs"] >= 1024)
+        s, n = m._last_schedule(), m._dims["nFreqs"]
+        want = {1024: (4, 1, 256), 2048: (8, 1, 256)}.get(n)
+        if want:
+            assert (s["grid"], s["R"], s["block"]) == want
+        else:
+            assert (s["grid"], s["R"]) not in ((4, 1), (8, 1), (4, 4))
     for r, x, o in zip(refs, ins, outs):
         f, _ = r.propagate(x[None, :], False, 0)
         assert cases.rel_l2(o, f[0]) < TOL
