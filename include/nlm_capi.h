@@ -233,7 +233,7 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
 /* 1 (default): a launch of at most SMs/4 propagations on a grid of 1024 to 8192 points spreads
  * each propagation over a cluster of 4 CTAs (one per SM, four-step FFT through distributed
  * shared memory); so do the Chi3 pump march and the reverse sweeps of nlm_adjoint_backward (on 4
- * or, pipelined, 8 CTAs) on such grids.  On grids of 256 to 1024 points, such launches (and the
+ * or, pipelined, 8 CTAs) on such grids.  On grids of 128 to 1024 points, such launches (and the
  * Chi2PDC reverse sweeps) and the Chi3 pump march use clusters with one point per thread instead;
  * on 2048 and 4096 points, full-grid propagations, the costliest ragged media and the Chi3 pump
  * march use eight CTAs with one point per thread.

@@ -1,6 +1,6 @@
 // adjoint_spread.cu -- the Chi2PDC reverse sweep (adjoint.cu) with each propagation on a cluster of four
 // CTAs holding one point per thread (nlm_spread.cuh): the reverse of the forwards that run on the
-// spread kernels (few rows on grids of 256 to 1024 points), whose checkpoints it reads.  Same steps as
+// spread kernels (few rows on grids of 128 to 1024 points), whose checkpoints it reads.  Same steps as
 // adjoint_cluster.cu: per segment between checkpoints the states are recomputed into per-cluster scratch
 // (K > 1), then the reverse steps run: the dispersion pair as spread transforms, the transposed RK4 step
 // point-wise in the time-domain ownership (the marching form with every state stored: P^T per point,

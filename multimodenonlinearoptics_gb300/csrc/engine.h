@@ -1452,10 +1452,10 @@ struct Medium {
   // 1: clusters, with one point per thread on the grids of spreadGrid(); 2: four points per thread
   // only; 0: one CTA per propagation
   int useCluster = 1;
-  static constexpr uint kSpreadMinN = 256, kSpreadMaxN = 1024, kWideMaxN = 4096;
+  static constexpr uint kSpreadMinN = 128, kSpreadMaxN = 1024, kWideMaxN = 4096;
 
   // A grid whose single propagations run on a 4-CTA cluster with one point per thread (prop_spread.cu):
-  // M = N/4 threads per CTA gives two to eight warps per SM, where the four-points-per-thread cluster
+  // M = N/4 threads per CTA gives one to eight warps per SM, where the four-points-per-thread cluster
   // form would give at most two (or, below 1024 points, is not built) and one CTA has one SM's FP64.
   bool spreadGrid() const {
     return useCluster == 1 && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;

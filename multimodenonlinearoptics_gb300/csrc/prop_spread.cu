@@ -1,6 +1,6 @@
 // prop_spread.cu -- single propagations, small batches and the Chi3 pump march on a cluster of four CTAs
 // with one point per thread (prop_spread.cuh), for grids whose four-points-per-thread cluster form
-// would leave schedulers idle or is not built (N = 256 to 1024: M = N/4 threads per CTA); the pump
+// would leave schedulers idle or is not built (N = 128 to 1024: M = N/4 threads per CTA); the pump
 // march also on eight CTAs for 2048 and 4096 points.
 #include <vector>
 

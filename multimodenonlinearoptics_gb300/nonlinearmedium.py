@@ -339,7 +339,7 @@ class _NonlinearMedium:
 
     def _set_cluster(self, enable):
         """Spread each propagation of small launches over a 4-CTA cluster: 1 (default) with one point
-        per thread on 256..1024-point grids (and the Chi3 pump march there), 2 with
+        per thread on 128..1024-point grids (and the Chi3 pump march there), 2 with
         four points per thread only (grids of 1024 points and more), 0 one CTA per propagation."""
         _check(_lib.nlm_set_cluster(self._h(), int(enable)))
 

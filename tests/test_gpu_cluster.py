@@ -143,10 +143,10 @@ def test_cluster_chi3_pump_march(nlm, oracle, n):
     assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12
 
 
-@pytest.mark.parametrize("n", [256, 512, 1024, 2048, 4096])
+@pytest.mark.parametrize("n", [128, 256, 512, 1024, 2048, 4096])
 @pytest.mark.parametrize("name", ["Chi2PDC", "Chi3", "Chi2SFG"])
 def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
-    """runSignalSimulation on 256..4096 points: one point per thread on four SMs (eight from 2048
+    """runSignalSimulation on 128..4096 points: one point per thread on four SMs (eight from 2048
     points), both input domains, against the oracle and against the one-CTA kernels (same arithmetic,
     other transform order)."""
     kw = dict(MEDIA[name], tPrecision=n)
@@ -172,9 +172,9 @@ def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
             assert cases.rel_l2(med.signalFreqs(m), one.signalFreqs(m)) < 1e-12
 
 
-@pytest.mark.parametrize("n", [256, 512, 4096])
+@pytest.mark.parametrize("n", [128, 256, 512, 4096])
 def test_spread_chi3_pump_march(nlm, oracle, n):
-    """The self-phase-modulation pump march with one point per thread on four SMs (the default on 256
+    """The self-phase-modulation pump march with one point per thread on four SMs (the default on 128
     to 1024 points) or eight (2048 and 4096 points; 1024 and 2048 are covered by
     test_cluster_chi3_pump_march)."""
     kw = dict(CHI3, tPrecision=n, zPrecision=15)
