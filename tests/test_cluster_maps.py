@@ -1,4 +1,6 @@
-"""The index arithmetic of the one-point-per-thread cluster transforms, replayed in numpy.
+"""The index arithmetic of the cluster transforms, replayed in numpy.
+
+One point per thread (`nlm_spread.cuh`):
 
 multimodenonlinearoptics_gb300/csrc/nlm_spread.cuh spreads an N-point transform over C = 4 or 8 CTAs
 of M = N / C threads: thread j of CTA c holds time point c + C j and frequency bin j + M c.  The local
@@ -6,7 +8,15 @@ M-point DFT is a radix-2 Stockham pass per stage (output t = e + W o with e = y[
 partner M/2 further, W = twM[k' M / 2L]); the C-point DFT across the CTAs combines the received
 column per output row (4 points: a + W_4^r b; 8 points: v0 + W_8^r v1).  This test executes exactly
 those index expressions for every thread, checks every shared-memory index against its buffer, and
-compares the result with numpy's FFT: forward, and the unscaled inverse round trip.  No GPU needed.
+compares the result with numpy's FFT: forward, and the unscaled inverse round trip.
+
+Four points per thread (`nlm_cluster.cuh`, C = R = 4): thread j of CTA c, register v holds time point
+c + C (j + v T) and frequency bin j + c T + M v (T = M / C).  The local M-point transform is the one-CTA
+register FFT, which keeps the ownership j + v T of its input for its output (tested against the oracle
+by the one-CTA kernels' own parity tests; here an exact DFT).  The test replays the twiddle
+exp(-2 pi i c k2 / N), the transpose through distributed shared memory (thread j of CTA c writes its
+register v to slot c T + j of CTA v's receive half; thread j then reads register c' from slot
+c' T + j) and the C-point DFT over the registers.  No GPU needed.
 """
 import numpy as np
 import pytest
@@ -101,3 +111,40 @@ def test_shared_memory_layout():
         m = n // c_count
         values = m * (1 + 2 + 2 * c_count)
         assert values * 16 <= 227 * 1024
+
+
+def _four_point_forward(x, c_count=4):
+    n = x.size
+    m = n // c_count
+    t = m // c_count                                    # threads per CTA
+    tw = np.exp(-2j * np.pi * np.arange(n) / n)
+    j = np.arange(t)
+    # regs[c][v][j]: register v of thread j in CTA c after the local transform and the twiddle
+    regs = np.empty((c_count, c_count, t), complex)
+    for c in range(c_count):
+        local = np.fft.fft(x[c + c_count * np.arange(m)])   # bin k2 at ownership k2 = j + v T
+        for v in range(c_count):
+            k2 = j + v * t
+            regs[c, v] = local[k2] * tw[c * k2]
+    recv = np.full((c_count, c_count * t), np.nan + 0j)   # one receive half per CTA
+    for c in range(c_count):
+        for v in range(c_count):
+            dst = c * t + j
+            assert dst.max() < c_count * t
+            recv[v, dst] = regs[c, v]
+    assert not np.isnan(recv).any()                       # every slot written exactly by the plan
+    out = np.empty(n, complex)
+    w_c = np.exp(-2j * np.pi / c_count)
+    for v in range(c_count):                               # CTA v after the barrier
+        r = np.array([recv[v, cp * t + j] for cp in range(c_count)])
+        for k1 in range(c_count):
+            out[j + v * t + m * k1] = sum(w_c ** (cp * k1) * r[cp] for cp in range(c_count))
+    return out
+
+
+@pytest.mark.parametrize("n", [1024, 2048, 8192])
+def test_four_point_cluster_transform_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = np.fft.fft(x)
+    assert np.max(np.abs(_four_point_forward(x) - ref)) <= 1e-12 * np.max(np.abs(ref))
