@@ -159,4 +159,14 @@ __device__ __forceinline__ double2 spread_inv(SpreadFFT& f, double2 x, cg::clust
   return spread_local<true>(f, x);
 }
 
+// spread_inv, with `store(x)` (the global store of the frequency-domain value) issued right after the
+// exchange's cluster barrier instead of before it: the barrier's release fence then does not wait for
+// the store, which drains during the local transform.
+template <int C = kSpreadC, class Store>
+__device__ __forceinline__ double2 spread_inv_store(SpreadFFT& f, double2 x, cg::cluster_group& cl, Store store) {
+  const double2 y = spread_exchange<true, C>(f, x, cl);
+  store(x);
+  return spread_local<true>(f, cmulc(y, f.twC));
+}
+
 }  // namespace nlm

@@ -30,23 +30,20 @@ __global__ void __launch_bounds__(kMaxThreads) k_pump_chi3_spread(double2* __res
   const double2 hp = halfP[fk], dp = dstepP[fk];
   double2 x = spread_fwd<C>(f, env[tn], cl);
   x = cmul(x, hp);
-  pf[fk] = x;
-  x = cscale(spread_inv<C>(f, x, cl), invN);
+  x = cscale(spread_inv_store<C>(f, x, cl, [&](double2 v) { pf[fk] = v; }), invN);
   pt[tn] = x;
   for (int i = 1; i < nRows; i++) {
     const double2 r = rel[i - 1];
     const double a2 = cabs2(x);
     x = cmul(x, spm_factor(r.x * a2, r.y * a2));
     x = cmul(spread_fwd<C>(f, x, cl), dp);
-    pf[(long long)i * N + fk] = x;
-    x = cscale(spread_inv<C>(f, x, cl), invN);
+    x = cscale(spread_inv_store<C>(f, x, cl, [&](double2 v) { pf[(long long)i * N + fk] = v; }), invN);
     pt[(long long)i * N + tn] = x;
   }
   // last row: undo half of the last pump dispersion step (each thread rereads its own bin)
   const long long last = (long long)(nRows - 1) * N;
   x = cmul(pf[last + fk], backP[fk]);
-  pf[last + fk] = x;
-  pt[last + tn] = cscale(spread_inv<C>(f, x, cl), invN);
+  pt[last + tn] = cscale(spread_inv_store<C>(f, x, cl, [&](double2 v) { pf[last + fk] = v; }), invN);
 }
 
 // One propagation per cluster (clusters take instances in turn); a.plan.N = M, a.tw the N-point table.
@@ -78,12 +75,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs
       if (a.inTime) x[m] = spread_fwd<C>(f, x[m], cl);
       x[m] = cmul(x[m], __ldg(a.half + (long long)m * N + fk));
     }
-    if (a.gridF) {
 #pragma unroll
-      for (int m = 0; m < MD; m++) a.gridF[m * ms + fk] = cscale(x[m], (double)N);
-    }
-#pragma unroll
-    for (int m = 0; m < MD; m++) x[m] = spread_inv<C>(f, x[m], cl);
+    for (int m = 0; m < MD; m++)
+      x[m] = spread_inv_store<C>(f, x[m], cl, [&](double2 v) {
+        if (a.gridF) a.gridF[m * ms + fk] = cscale(v, (double)N);
+      });
     if (a.gridT) {
 #pragma unroll
       for (int m = 0; m < MD; m++) a.gridT[m * ms + tn] = x[m];
@@ -141,10 +137,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs
 #pragma unroll
       for (int m = 0; m < MD; m++) {
         x[m] = cmul(spread_fwd<C>(f, x[m], cl), __ldg(table + (long long)m * N + fk));
-        if (a.gridF) a.gridF[m * ms + (long long)i * N + fk] = cscale(x[m], (double)N);
+        auto storeF = [&](double2 v) {
+          if (a.gridF) a.gridF[m * ms + (long long)i * N + fk] = cscale(v, (double)N);
+        };
         if (wantTime) {
-          x[m] = spread_inv<C>(f, x[m], cl);
+          x[m] = spread_inv_store<C>(f, x[m], cl, storeF);
           if (a.gridT) a.gridT[m * ms + (long long)i * N + tn] = x[m];
+        } else {
+          storeF(x[m]);
         }
         if (ckRow && !last && i % a.ckK == 0) ckRow[((long long)(i / a.ckK) * MD + m) * N + tn] = x[m];
       }
