@@ -1,6 +1,6 @@
 """Parity of the CUDA engine with the oracle, through the drop-in API and its C ABI.
 
-Tolerance: relative L2 error <= 1e-9 over every output array (the benchmark spec's bound for FP64
+Tolerance: relative L2 error <= 1e-9 over every output array (the required bound for FP64
 propagation); the expected level is ~1e-13 since both sides compute in double precision.
 """
 import numpy as np
