@@ -178,10 +178,13 @@ nlm_status nlm_adjoint_backward(nlm_medium* m, const void* grad_out_dev, void* g
  * medium (rows x N complex inputs on the device, one N-point output row each, frequency or time
  * domain as in_time_domain), with the kernel's scratch taken from one 16 MiB file-scope device array
  * instead of an allocation.  The medium must have run one GPU call before (its device tables are
- * built there).  Grids needing more than the array per CTA are rejected.  The call is asynchronous
- * on cuda_stream (a cudaStream_t; NULL is the legacy default stream).  All calls share the array: calls that overlap on the
- * GPU race.  The first call on a device looks up the array's address; make it before any stream
- * capture. */
+ * built there), with the same device current as now.  The array holds a slot of 2 N values per
+ * resident propagation, so it bounds how many CTAs run at once, not the number of rows; grids the
+ * one-CTA Chi3GNLSE kernel does not take (power of two, 8 to 4096 points) are rejected with
+ * NLM_ERR_UNSUPPORTED.  The call is asynchronous on cuda_stream (a cudaStream_t; NULL is the legacy
+ * default stream).  All calls share the array: calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's address (again on every call outside stream capture); make it
+ * before any stream capture. */
 nlm_status nlm_batch_gnlse_noalloc(nlm_medium* m, const void* inputs_dev, size_t rows,
                                    int in_time_domain, void* out_dev, void* cuda_stream);
 

@@ -77,11 +77,20 @@ nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows
                                "before the allocation-free entry point");
     if (!in || !out) throw std::invalid_argument("null input or output pointer");
     if (rows == 0) throw std::invalid_argument("Too many threads requested!");
+    int dev = -1;
+    ck(cudaGetDevice(&dev), "device");
+    if (dev != m->devOrdinal)
+      throw std::invalid_argument("the medium's tables live on device " + std::to_string(m->devOrdinal) +
+                                  " but device " + std::to_string(dev) + " is current");
     const int R = m->chooseR();
-    m->checkGrid(R);
+    // only the one-CTA kernel takes its scratch from the caller: grids it cannot hold (more than
+    // 512 threads of R points, or a grid the fused kernels do not take) are rejected here
+    m->checkGridStrict(R);
     const KernelEntry* k = m->findKernel(kKindGnlse, m->solver, R);
-    if (!k) throw Unsupported("no fused kernel for this grid");
+    if (!k) throw Unsupported("no one-CTA Chi3GNLSE kernel for a grid of " + std::to_string(m->N) + " points");
     Medium::Schedule s = m->schedule(k, (long long)rows, R);
+    // the array bounds how many CTAs run at once (2 N values per resident propagation); more rows
+    // than the resident propagations only means more rounds of the persistent grid
     const size_t perSlot = 2 * (size_t)m->N;
     const size_t slots = scratchElems / perSlot;
     if (slots < (size_t)s.ipc)

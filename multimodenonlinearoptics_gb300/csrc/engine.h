@@ -586,6 +586,7 @@ struct Medium {
 
   // device state
   bool devReady = false;
+  int devOrdinal = -1;   // the device holding this medium's tables (current device at set-up)
   cudaStream_t stream = nullptr;
   bool ownStream = false;
   const double2* tw = nullptr;
@@ -739,6 +740,7 @@ struct Medium {
   void ensureDevice() {
     if (devReady) return;
     require_device();
+    ck(cudaGetDevice(&devOrdinal), "device");
     if (!stream) {
       ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
       ownStream = true;

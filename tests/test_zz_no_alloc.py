@@ -45,6 +45,31 @@ def test_noalloc_batch_matches_batch_entry_point(nlm):
             assert cases.rel_l2(out.cpu().numpy(), expected) < TOL
 
 
+def test_noalloc_rounds_over_capped_grid(nlm):
+    """At N=4096 the array holds 128 slots of 2N values, fewer than the SMs: the grid is capped at
+    128 CTAs, and 300 rows make the CTAs walk several rows each in the static round robin, reusing
+    their slot.  Two calls in a row must match the ordinary batch entry point."""
+    torch = pytest.importorskip("torch")
+    fn = _bind(nlm)
+    kw = dict(cases.CASES["Chi3GNLSE"], tMax=40, tPrecision=4096, zPrecision=10)
+    med = nlm.Chi3GNLSE(**kw)
+    n = med._dims["nFreqs"]
+    rows = 300
+    t = np.fft.fftshift(np.linspace(-40, 40, n, endpoint=False))
+    rng = np.random.default_rng(30)
+    x = 2.0 / np.cosh(t)[None, :] + cases.noise(rng, rows * n, 1e-3).reshape(rows, n)
+    expected = med.batchSignalSimulation(x, True)
+    xin = torch.from_numpy(x).to("cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        out = torch.full((rows, n), float("nan"), dtype=torch.complex128, device="cuda")
+        status = fn(med._h(), ctypes.c_void_p(xin.data_ptr()), rows, 1, ctypes.c_void_p(out.data_ptr()),
+                    ctypes.c_void_p(stream.cuda_stream))
+        assert status == 0, nlm._lib.nlm_last_error().decode()
+        torch.cuda.synchronize()
+        assert cases.rel_l2(out.cpu().numpy(), expected) < TOL
+
+
 def test_noalloc_rejects_other_solvers(nlm):
     torch = pytest.importorskip("torch")
     fn = _bind(nlm)
@@ -53,3 +78,17 @@ def test_noalloc_rejects_other_solvers(nlm):
     status = fn(med._h(), ctypes.c_void_p(buf.data_ptr()), 1, 0, ctypes.c_void_p(buf.data_ptr()), None)
     assert status == 1
     assert "Chi3GNLSE" in nlm._lib.nlm_last_error().decode()
+
+
+def test_noalloc_rejects_grids_of_the_cluster_kernels(nlm):
+    """8192 points need more than the one-CTA kernel's 512 threads: rejected as unsupported
+    (status 6) with the reason, before anything is launched."""
+    torch = pytest.importorskip("torch")
+    fn = _bind(nlm)
+    med = nlm.Chi3GNLSE(**dict(cases.CASES["Chi3GNLSE"], tMax=40, tPrecision=8192, zPrecision=4))
+    n = med._dims["nFreqs"]
+    med.batchSignalSimulation(np.ones((1, n), dtype=np.complex128), False)
+    buf = torch.zeros((1, n), dtype=torch.complex128, device="cuda")
+    status = fn(med._h(), ctypes.c_void_p(buf.data_ptr()), 1, 0, ctypes.c_void_p(buf.data_ptr()), None)
+    assert status == 6
+    assert "8192" in nlm._lib.nlm_last_error().decode()
