@@ -2,8 +2,9 @@
 
 1. ``poling_golden.npz`` -- pinned to the reference itself: the reference's Python twin of
    ``setPoling`` (poling.py:439-471, ``domainsToSpace``) is imported from a checkout of the
-   reference and run on seeded domain-length arrays.  Run with REFERENCE_ROOT pointing at the
-   reference checkout (default: /root/reference).
+   reference and run on seeded domain-length arrays.  Run with REFERENCE_ROOT (environment) or
+   --reference-root pointing at the reference checkout; without one only the oracle fixture below
+   is regenerated.
 2. ``multimode_golden.npz`` -- pinned to the reference itself: outputs of the reference's
    ``multimode.py`` and ``decompositions.py`` (imported from the checkout) on a Green's pair of the
    oracle and seeded matrices.
@@ -226,12 +227,17 @@ def make_oracle():
 
 
 if __name__ == "__main__":
-    ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
-    if os.path.exists(os.path.join(ref_root, "poling.py")):
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference-root", default=os.environ.get("REFERENCE_ROOT"),
+                    help="checkout of the reference (also REFERENCE_ROOT)")
+    ref_root = ap.parse_args().reference_root
+    if ref_root and os.path.exists(os.path.join(ref_root, "poling.py")):
         make_poling(ref_root)
         make_multimode(ref_root)
         make_frontends(ref_root)
     else:
-        print("reference checkout not found; poling, multimode and front-end fixtures left unchanged",
+        print("no reference checkout given (REFERENCE_ROOT or --reference-root); poling, multimode and "
+              "front-end fixtures left unchanged",
               file=sys.stderr)
     make_oracle()

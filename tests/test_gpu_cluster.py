@@ -104,7 +104,7 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     """Chi3GNLSE on a 4-CTA cluster (all 16 stage transforms and the dispersion pair as cluster
     FFTs): full grids of one propagation and a small batch, against the oracle and the one-CTA kernel
     (N=8192 has no one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
-    self-steepening) over 0.2 of its length with its z step (199 steps); at N=8192 the time window
+    self-steepening) over 0.2 of its length with its z step (1999 steps); at N=8192 the time window
     doubles so that the RK4 step stays stable for the self-steepening term at the highest frequency."""
     from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG
     kw = dict(GNLSE_CONFIG, tPrecision=n, relativeLength=0.2, tMax=t_max)
