@@ -290,6 +290,16 @@ nlm_status nlm_quadrature_greens(const void* green_c_dev, const void* green_s_de
 nlm_status nlm_abasis_greens(const void* green_c_dev, const void* green_s_dev, size_t rows, size_t cols, void* z_dev,
                              void* cuda_stream);
 
+/* --- Cascade composition (src/Cascade.cpp:128-129) --------------------------------------------
+ * The Green's-function composition of two chained media, on device pointers (row-major complex128)
+ * and the given CUDA stream: c_out = C2 C1 + S2 conj(S1), s_out = C2 S1 + S2 conj(C1), with C2, S2
+ * rows x inner and C1, S1 inner x cols.  nlm_green of a cascade runs the same kernel between its
+ * media; exported so that the composition can be timed and checked on its own.  Outputs must not
+ * alias inputs. */
+nlm_status nlm_cascade_compose(const void* c2_dev, const void* s2_dev, const void* c1_dev, const void* s1_dev,
+                               size_t rows, size_t inner, size_t cols, void* c_out_dev, void* s_out_dev,
+                               void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

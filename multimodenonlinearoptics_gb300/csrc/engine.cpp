@@ -789,6 +789,24 @@ nlm_status nlm_abasis_greens(const void* green_c_dev, const void* green_s_dev, s
   });
 }
 
+nlm_status nlm_cascade_compose(const void* c2_dev, const void* s2_dev, const void* c1_dev, const void* s1_dev,
+                               size_t rows, size_t inner, size_t cols, void* c_out_dev, void* s_out_dev,
+                               void* cuda_stream) {
+  return guarded([&] {
+    nlm::require_device();
+    if (!c2_dev || !s2_dev || !c1_dev || !s1_dev || !c_out_dev || !s_out_dev)
+      throw std::invalid_argument("null device pointer");
+    if (rows == 0 || inner == 0 || cols == 0) throw std::invalid_argument("empty matrices");
+    if (rows > (size_t)INT32_MAX || inner > (size_t)INT32_MAX || cols > (size_t)INT32_MAX)
+      throw std::invalid_argument("matrix dimension too large");
+    nlm::ck(nlm::launch_cgemm_compose(reinterpret_cast<const double2*>(c2_dev), reinterpret_cast<const double2*>(s2_dev),
+                                      reinterpret_cast<const double2*>(c1_dev), reinterpret_cast<const double2*>(s1_dev),
+                                      (int)rows, (int)inner, (int)cols, nlm::d2(c_out_dev), nlm::d2(s_out_dev),
+                                      static_cast<cudaStream_t>(cuda_stream)),
+            "compose");
+  });
+}
+
 nlm_status nlm_fp64_warps_rate(int warps_per_sm, double* tflops) {
   return guarded([&] {
     nlm::require_device();

@@ -87,6 +87,7 @@ def _load():
         "nlm_fp64_warps_rate": (i, [i, P(d)]),
         "nlm_quadrature_greens": (i, [vp, vp, sz, sz, vp, vp]),
         "nlm_abasis_greens": (i, [vp, vp, sz, sz, vp, vp]),
+        "nlm_cascade_compose": (i, [vp, vp, vp, vp, sz, sz, sz, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -161,6 +161,31 @@ def test_cascade_matches_oracle(nlm, oracle, n):
     assert cases.rel_l2(c.batchSignalSimulation(xb), rc.batch_signal_simulation(xb)) < TOL
 
 
+@pytest.mark.parametrize("rows,inner,cols", [(16, 16, 16), (40, 72, 24), (256, 256, 256)])
+def test_cascade_compose_matches_torch(nlm, rows, inner, cols):
+    """The composition kernel on its own (partial and whole 32 x 32 tiles, rectangular shapes) against
+    torch's complex128 matmul: C2 C1 + S2 conj(S1), C2 S1 + S2 conj(C1)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    g = torch.Generator().manual_seed(rows + inner + cols)
+
+    def mat(r, c):
+        return torch.complex(torch.randn(r, c, generator=g, dtype=torch.float64),
+                             torch.randn(r, c, generator=g, dtype=torch.float64)).cuda()
+    c2, s2, c1, s1 = mat(rows, inner), mat(rows, inner), mat(inner, cols), mat(inner, cols)
+    co = torch.empty(rows, cols, dtype=torch.complex128, device="cuda")
+    so = torch.empty_like(co)
+    vp = ctypes.c_void_p
+    nlm._check(nlm._lib.nlm_cascade_compose(vp(c2.data_ptr()), vp(s2.data_ptr()), vp(c1.data_ptr()), vp(s1.data_ptr()),
+                                            rows, inner, cols, vp(co.data_ptr()), vp(so.data_ptr()),
+                                            vp(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    ce = c2 @ c1 + s2 @ s1.conj()
+    se = c2 @ s1 + s2 @ c1.conj()
+    assert cases.rel_l2(co.cpu().numpy(), ce.cpu().numpy()) < 1e-13
+    assert cases.rel_l2(so.cpu().numpy(), se.cpu().numpy()) < 1e-13
+
+
 def test_plain_equals_batched(nlm):
     med = make(nlm, "Chi2PDC")
     med.runPumpSimulation()
