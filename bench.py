@@ -248,7 +248,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": bench_config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "the whole workload every step: computeGreensFunction with the pump grid, "
@@ -442,11 +442,16 @@ def measure_configs(nlm, torch, cpu=True):
         row[label] = 1e3 * (time.perf_counter() - t0)
         row["z_steps"] = m._dims["nZSteps"]
     if cpu:
+        # the same propagation (999 steps of the medium's own z step) with the C++ restatement, one thread
+        from oracle import build_oracle, cpu_port
         from oracle import nlm_oracle as O
-        o = O.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=12))
+        build_oracle.build()
+        o = O.Chi3GNLSE(**kw)
         t0 = time.perf_counter()
-        o.run_signal_simulation(a)
-        row["cpu_oracle_ms_estimate"] = 1e3 * (time.perf_counter() - t0) * (row["z_steps"] - 1) / (o.n_z_steps - 1)
+        out = cpu_port.gnlse_batch(o, a[None, :], True, 1)
+        row["cpu_port_ms"] = 1e3 * (time.perf_counter() - t0)
+        if not np.all(np.isfinite(out)):
+            raise RuntimeError("the CPU restatement diverged on the GNLSE medium")
     single["gnlse_run_signal_n4096"] = row
     # the Chi3 self-phase-modulation pump march (runPumpSimulation) on 8192 points, 1000 rows
     kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0.02, tMax=40, tPrecision=8192,
@@ -849,7 +854,16 @@ def run_ours(args):
     S = torch.empty_like(C)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
 
+    def green_local():
+        nlm._check(nlm._lib.nlm_green_device(med._h(), 0, 1, 1, 0, None, 0, None, 0, C.data_ptr(), S.data_ptr()))
+
     def green_device():
+        if world > 1:
+            # one Green's function split over the ranks (strong scaling): rows on each GPU, one NCCL
+            # gather of device buffers, C and S on rank 0's GPU
+            from multimodenonlinearoptics_gb300 import sharding
+            sharding.green_sharded_device(med, C, S)
+            return
         nlm._check(nlm._lib.nlm_green_device(med._h(), 0, 1, 1, 0, None, 0, None, 0, C.data_ptr(), S.data_ptr()))
 
     # warm-up (also builds the kernel schedule and the propagator)
@@ -878,7 +892,7 @@ def run_ours(args):
     sched = med._last_schedule()
     barrier()
     t_dev = max_over_ranks(elapsed)
-    value = world * n_inst * args.steps / t_dev
+    value = n_inst * args.steps / t_dev   # the whole Green's function per step, over all ranks
 
     # end to end through the public API: numpy C and S on the host every step
     barrier()
@@ -889,17 +903,22 @@ def run_ours(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        Ch, Sh = med.computeGreensFunction()
+        if world > 1:
+            from multimodenonlinearoptics_gb300 import sharding
+            res = sharding.compute_greens_function_sharded(med)
+            Ch, Sh = res if res is not None else (None, None)
+        else:
+            Ch, Sh = med.computeGreensFunction()
         e1.record(stream)
         e1.synchronize()
         e2e_elapsed += e0.elapsed_time(e1) / 1e3
     barrier()
     t_e2e = max_over_ranks(e2e_elapsed)
-    e2e_value = world * n_inst * args.steps / t_e2e
+    e2e_value = n_inst * args.steps / t_e2e
 
     # plain form: one propagation per kernel launch, on a sample of the impulses
     plain = None
-    if args.plain_sample > 0:
+    if args.plain_sample > 0 and rank == 0:
         Cp = np.empty((n, n), dtype=np.complex128)
         Sp = np.empty_like(Cp)
         nlm._check(nlm._lib.nlm_green_plain(med._h(), 0, 0, 2, nlm._dptr(Cp.view(np.float64)),
@@ -911,12 +930,15 @@ def run_ours(args):
         t_plain = time.perf_counter() - t0
         plain = args.plain_sample / t_plain
 
-    ff = measure_ff(nlm, torch, args, stream, flush, C, S, value, kernel_ms / max(kernel_count, 1)) if args.ff else None
-    adjoint = measure_adjoint(nlm, torch, check=args.cpu_bins > 0) if args.adjoint else None
-    configs = measure_configs(nlm, torch, cpu=args.cpu_bins > 0) if args.configs else None
+    # the secondary measurements run on rank 0 only (the other ranks wait at the final barrier)
+    main = rank == 0
+    ff = measure_ff(nlm, torch, args, stream, flush, C, S, value, kernel_ms / max(kernel_count, 1)) \
+        if args.ff and main and world == 1 else None
+    adjoint = measure_adjoint(nlm, torch, check=args.cpu_bins > 0) if args.adjoint and main else None
+    configs = measure_configs(nlm, torch, cpu=args.cpu_bins > 0) if args.configs and main else None
     if configs is not None:
         with torch.cuda.stream(stream):
-            configs["green_consumers_n1024"] = measure_consumers(nlm, torch, green_device, C, S,
+            configs["green_consumers_n1024"] = measure_consumers(nlm, torch, green_local, C, S,
                                                                  cpu=args.cpu_bins > 0)
 
     line = None
@@ -958,16 +980,16 @@ def run_ours(args):
                                 "sample": "%d impulse propagations, 1 thread" % (2 * args.cpu_bins)}}
         config = bench_config()
         if world > 1:
-            config = dict(config, global_batch=n_inst * world,
-                          parallelism="%d replicas of the workload, one per GPU" % world)
-        flops = algorithmic_flops(n_inst, n_z, n)
+            config = dict(config, parallelism="2048 impulse propagations split over %d GPUs in contiguous row "
+                                              "blocks, one NCCL gather to rank 0" % world)
+        flops = algorithmic_flops(n_inst // world, n_z, n)   # one launch: this rank's share of the rows
         avg_kernel_s = kernel_ms / max(kernel_count, 1) / 1e3
         achieved = flops / avg_kernel_s / 1e12
         traffic = read_profile_traffic()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16,
                     "d2h_bytes_per_step": 2 * n * n * 16,

@@ -123,6 +123,14 @@ nlm_status nlm_green_rows(nlm_medium* m, int in_time_domain, int run_pump, size_
                           double* raw_out);
 nlm_status nlm_green_finish(nlm_medium* m, const double* raw, int normalize, double* green_c,
                             double* green_s);
+/* The same two steps on device memory of the handle's GPU (row-major complex128, the layouts above):
+ * the rows are written, and C and S computed, in place on the device, so that a gather between the
+ * GPUs (NCCL) reads and writes device buffers with no host round trip.  Both return after the work
+ * on the handle's stream has finished.  No counterpart in the reference (its threads share memory). */
+nlm_status nlm_green_rows_device(nlm_medium* m, int in_time_domain, int run_pump, size_t first, size_t count,
+                                 void* raw_out_dev);
+nlm_status nlm_green_finish_device(nlm_medium* m, const void* raw_dev, int normalize, void* green_c_dev,
+                                   void* green_s_dev);
 
 /* --- batchSignalSimulation (src/_NonlinearMedium.cpp:378-444;
  *     src/_FullyNonlinearMedium.hpp:8-11 where run_pump is ignored) -------------------

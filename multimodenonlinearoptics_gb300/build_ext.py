@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_gnlse.cu", "kernels_misc.cu",
                 "nlm_noalloc.cu", "adjoint.cu", "prop_ragged.cu", "adjoint_gnlse.cu", "prop_ff.cu", "prop_direct_c.cu", "prop_cluster.cu", "prop_cluster_b.cu", "prop_cluster_gnlse.cu", "prop_cluster_pump.cu", "prop_spread.cu", "prop_spread_b.cu",
                 "adjoint_gnlse_cluster.cu", "adjoint_cluster.cu", "adjoint_spread.cu",
-                "greens_quadrature.cu"]
+                "greens_quadrature.cu", "prop_gen_a.cu", "prop_gen_b.cu",
+                "prop_gen_c.cu", "prop_gen_d.cu", "prop_gen_e.cu"]
 CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]
 
 

@@ -592,6 +592,27 @@ nlm_status nlm_green_finish(nlm_medium* h, const double* raw, int normalize, dou
   });
 }
 
+nlm_status nlm_green_rows_device(nlm_medium* h, int in_time_domain, int run_pump, size_t first, size_t count,
+                                 void* raw_out_dev) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (count > 0 && !raw_out_dev) throw std::invalid_argument("null device pointer");
+    m->greenRows(in_time_domain, run_pump, (long long)first, (long long)count, nlm::d2(raw_out_dev), true);
+  });
+}
+
+nlm_status nlm_green_finish_device(nlm_medium* h, const void* raw_dev, int normalize, void* green_c_dev,
+                                   void* green_s_dev) {
+  return guarded([&] {
+    Medium* m = M(h);
+    m->launches = 0;
+    if (!raw_dev || !green_c_dev || !green_s_dev) throw std::invalid_argument("null device pointer");
+    m->greenFinish(reinterpret_cast<const double2*>(raw_dev), normalize, nlm::d2(green_c_dev), nlm::d2(green_s_dev),
+                   true);
+  });
+}
+
 nlm_status nlm_set_poling_profile(nlm_medium* h, const double* profile, size_t n) {
   return guarded([&] { M(h)->setPolingProfile(profile, n); });
 }

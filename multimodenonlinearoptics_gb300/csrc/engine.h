@@ -187,7 +187,7 @@ struct GraphKey {
 
 // Key bytes of a PropArgs, field by field (the struct has padding, whose bytes are unspecified).
 inline void add_prop_key(GraphKey& k, const PropArgs& a) {
-  k.add(a.plan.N).add(a.plan.T).add(a.plan.nPass);
+  k.add(a.plan.N).add(a.plan.T).add(a.plan.nPass).add(a.plan.gen).add(a.plan.R);
   for (int i = 0; i < a.plan.nPass && i < 16; i++) k.add(a.plan.radix[i]);
   k.add(a.R).add(a.nModes).add(a.nZ).add(a.nInst).add(a.instBase).add(a.ipc).add(a.work);
   k.add(a.inKind).add(a.inTime).add(a.in).add(a.inStride).add(a.inChannels).add(a.inputMode);
@@ -299,9 +299,42 @@ inline TwiddleCache g_twiddles;
 
 inline bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
-inline FFTPlanH make_plan(int N, int R) {
+// The general plan (FFTPlanH::gen == 1) of an N-point transform with R points per thread: T = ceil(N/R)
+// threads, passes of radix 8 (then one of 4 or 2) for the power-of-two factor and one per odd prime
+// factor, in ascending order.  Any N >= 2 up to kMaxFFT.
+inline FFTPlanH make_plan_gen(int N, int R) {
   FFTPlanH p{};
   p.N = N;
+  p.R = R;
+  p.gen = 1;
+  p.T = (N + R - 1) / R;
+  std::vector<int> rad;
+  int n = N, twos = 0;
+  while (n % 2 == 0) {
+    n /= 2;
+    twos++;
+  }
+  for (; twos >= 3; twos -= 3) rad.push_back(8);
+  if (twos) rad.push_back(1 << twos);
+  for (int q = 3; n > 1; q += 2)
+    while (n % q == 0) {
+      rad.push_back(q);
+      n /= q;
+    }
+  if (rad.size() > 16) throw Unsupported("transform of " + std::to_string(N) + " points has too many factors");
+  p.nPass = (int)rad.size();
+  for (int i = 0; i < p.nPass; i++) p.radix[i] = rad[i];
+  return p;
+}
+
+// Plan of an N-point transform with R points per thread: the register plan (gen == 0, radix-8 passes
+// with one radix-2/4 pass, T = N/R) when N is a power of two of at least R points, the general plan
+// otherwise.
+inline FFTPlanH make_plan(int N, int R) {
+  if (!is_pow2(N) || N < R) return make_plan_gen(N, R);
+  FFTPlanH p{};
+  p.N = N;
+  p.R = R;
   p.T = N / R;
   int n = 0;
   while ((1 << n) < N) n++;
@@ -748,8 +781,8 @@ struct Medium {
     tw = g_twiddles.get((int)N, stream);
     const size_t n = N;
     if (nPump > 0 && nZP > 0) {
-      pumpFreq.alloc((size_t)nPump * nZP * n);
-      pumpTime.alloc((size_t)nPump * nZP * n);
+      pumpFreq.alloc((size_t)nPump * nZP * n + kTablePad);
+      pumpTime.alloc((size_t)nPump * nZP * n + kTablePad);
       ck(cudaMemsetAsync(pumpFreq.p, 0, pumpFreq.n * sizeof(double2), stream), "memset");
       ck(cudaMemsetAsync(pumpTime.p, 0, pumpTime.n * sizeof(double2), stream), "memset");
     }
@@ -788,16 +821,27 @@ struct Medium {
     devReady = true;
   }
 
+  // Device tables carry kTablePad zeroed values after their data: a kernel on the general plan reads
+  // the points of its padded ownership (j + v T up to R - 1 past N) without a bound check, and the
+  // values it reads there only ever meet zeros.
   template <class V>
   void upload(DevBuf<double2>& d, const V& h) {
-    d.alloc(h.size());
-    if (!h.empty())
-      ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, stream), "upload");
+    if (h.empty()) {
+      d.alloc(0);
+      return;
+    }
+    d.alloc(h.size() + kTablePad);
+    ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, stream), "upload");
+    ck(cudaMemsetAsync(d.p + h.size(), 0, kTablePad * sizeof(double2), stream), "upload");
   }
   void uploadD(DevBuf<double>& d, const std::vector<double>& h) {
-    d.alloc(h.size());
-    if (!h.empty())
-      ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "upload");
+    if (h.empty()) {
+      d.alloc(0);
+      return;
+    }
+    d.alloc(h.size() + kTablePad);
+    ck(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream), "upload");
+    ck(cudaMemsetAsync(d.p + h.size(), 0, kTablePad * sizeof(double), stream), "upload");
   }
 
   // relativeAmplitude / relativeIntensity, src/_FullyNonlinearMedium.hpp:40-63
@@ -994,11 +1038,13 @@ struct Medium {
     uploadD(relIntD, rel);
   }
 
+  // Plan of the batched row transforms (pump grids, chirp and delay, Raman response): the register
+  // plan on power-of-two grids, the general plan on the others.
   FFTPlanH fftPlanRows() const {
-    if (is_pow2((int)N) && N >= 8 && N <= (uint)kMaxFFT) return make_plan((int)N, N <= 4096 ? 8 : 16);
+    if (N <= (uint)kMaxFFT) return make_plan((int)N, N <= 4096 ? 8 : 16);
     FFTPlanH p{};
     p.N = (int)N;
-    p.T = 1;
+    p.T = 0;   // no plan: the direct DFT
     return p;
   }
 
@@ -1111,8 +1157,10 @@ struct Medium {
 
   // solvers/Chi3.cpp:41-70
   void runPumpChi3() {
-    if (!(is_pow2((int)N) && N >= 8 && N <= (uint)kMaxFFT)) throw Unsupported("Chi3 pump march needs a power-of-two grid of 8..8192 points");
-    // one CTA marches the pump: N/4 threads up to N=512 so that all four schedulers of the SM issue
+    if (N < 2 || N > (uint)kMaxFFT)
+      throw Unsupported("the Chi3 pump march takes grids of 2 to " + std::to_string(kMaxFFT) + " points");
+    // one CTA marches the pump: N/4 threads up to N=512 so that all four schedulers of the SM issue;
+    // the general plan (ceil(N/R) threads) on grids that are not powers of two
     FFTPlanH plan = make_plan((int)N, N <= 512 ? 4 : (N <= 4096 ? 8 : 16));
     std::vector<double2> e(N), hP(N), dP(N), bP(N);
     for (uint k = 0; k < N; k++) {
@@ -1148,7 +1196,7 @@ struct Medium {
       // the march on four (up to 1024 points) or eight SMs with one point per thread (prop_spread.cu)
       ck(launch_pump_chi3_spread(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, (int)N, tw, stream),
          "chi3 pump (spread)");
-    } else if (useCluster && N >= 1024) {
+    } else if (useCluster && is_pow2((int)N) && N >= 1024) {
       // 1024..8192 points: the march on four SMs (prop_cluster_pump.cu), four points per thread
       const FFTPlanH local = make_plan((int)N / kClusterSize, kClusterSize);
       ck(launch_pump_chi3_cluster(pumpFreq.p, pumpTime.p, de.p, dh.p, dd.p, db.p, dr.p, (int)nZP, local, tw, stream),
@@ -1231,15 +1279,39 @@ struct Medium {
            findKernel(kKindCluster, solver, kClusterSize) != nullptr;
   }
 
+  // Grids some propagation kernel takes: cluster grids, register-plan grids, and every other grid of
+  // 2..kMaxFFT points on the general plan (propagate() picks the kernel).
   void checkGrid(int R) const {
-    if (clusterGrid()) return;
-    checkGridStrict(R);
+    if (clusterGrid() || registerGrid(R)) return;
+    if (N < 2 || N > (uint)kMaxFFT)
+      throw Unsupported("grid of " + std::to_string(N) + " points: the fused split-step kernels take 2 to " +
+                        std::to_string(kMaxFFT) + " points");
   }
 
   void checkGridStrict(int R) const {
     if (!is_pow2((int)N) || (int)N < R || N > (uint)kMaxFFT || N / R > 512)
       throw Unsupported("grid of " + std::to_string(N) + " points is not supported by the fused split-step kernels "
                         "(power of two, R=" + std::to_string(R) + " to 8192 points)");
+  }
+
+  // The register plan's one-CTA kernels take power-of-two grids of at least R points with N/R <= 512
+  // threads; every other grid up to kMaxFFT points runs on the general plan (FFTPlanH::gen).
+  bool registerGrid(int R) const { return is_pow2((int)N) && (int)N >= R && N <= (uint)kMaxFFT && N / R <= 512; }
+
+  // The general-plan kernel of `kind` for `key` (registered at key + kGenKey) with the fewest points
+  // per thread, from R up, whose CTA holds a propagation (ceil(N/R) <= 512 threads); sets *Rout.
+  const KernelEntry* genKernel(int kind, int key, int R, int* Rout) const {
+    if (N > (uint)kMaxFFT || N < 2)
+      throw Unsupported("grid of " + std::to_string(N) + " points: the fused split-step kernels take 2 to " +
+                        std::to_string(kMaxFFT) + " points");
+    for (int r : {4, 8, 16}) {
+      if (r < R || ((int)N + r - 1) / r > 512) continue;
+      if (const KernelEntry* k = findKernel(kind, key + kGenKey, r)) {
+        *Rout = r;
+        return k;
+      }
+    }
+    return nullptr;
   }
 
   struct Schedule {
@@ -1252,7 +1324,7 @@ struct Medium {
   // default enough for 128 threads, times ipcMul), `cta` resident CTAs per SM (0: the member
   // override or the occupancy maximum), grid = SMs x CTAs per SM, capped by the number of groups.
   Schedule schedule(const KernelEntry* k, long long nInst, int R, int cta = 0, int ipcMul = 1) {
-    const int T = (int)N / R;
+    const int T = ((int)N + R - 1) / R;   // N / R on the register plan, ceil(N / R) on the general one
     int ipc = (T >= 128 ? 1 : 128 / T) * ipcMul;
     if (ipc > nInst) ipc = (int)std::max<long long>(1, nInst);
     const int block = T * ipc;
@@ -1431,7 +1503,8 @@ struct Medium {
     const int M = (int)nSignal, E = 4 * M * M;
     const size_t count = (size_t)(nZ > 1 ? nZ - 1 : 0) * E * N;
     if (count == 0) return;
-    prop.alloc(count);
+    prop.alloc(count + 2 * kTablePad);   // doubles; the padding is zeroed like that of the tables
+    ck(cudaMemsetAsync(prop.p + count, 0, 2 * kTablePad * sizeof(double), on ? on : stream), "propagator");
     const KernelEntry* k = findKernel(kKindBuildProp, solver, 0);
     if (!k) throw Unsupported("no propagator kernel for this solver");
     PropArgs a = baseArgs(R);
@@ -1627,9 +1700,27 @@ struct Medium {
       return;
     }
     if (a.stages) throw std::logic_error("stage values are stored by the cluster kernels only");
-    checkGridStrict(R);
+    // grids the register plan does not take: the general-plan kernels (any N up to kMaxFFT)
+    const bool gen = !registerGrid(R);
     bool paired = false;
-    if (gnlse) {
+    if (gen) {
+      if (a.ckpt) throw Unsupported("the adjoint's forward takes power-of-two grids (register plan) only");
+      int Rg = R;
+      if (!gnlse && allowPropagator && wantPropagator(nInst)) {
+        k = genKernel(kKindLinear, (int)nSignal, R, &Rg);
+        if (k) {
+          buildPropagator(R);
+          a.prop = prop.p;
+        }
+      }
+      if (!k) k = genKernel(gnlse ? kKindGnlse : kKindDirect, solver, R, &Rg);
+      if (!k)
+        throw Unsupported("no fused kernel for a grid of " + std::to_string(N) + " points for this solver (" +
+                          std::to_string(nSignal) + " modes)");
+      a.plan = make_plan_gen((int)N, Rg);
+      a.R = Rg;
+    } else if (gnlse) {
+      checkGridStrict(R);
       k = findKernel(kKindGnlse, solver, R);
       // more rows than SMs (one row per thread group would take a second wave): two rows per thread
       // group, sharing their Raman transforms (k_propagate_gnlse_pair: 14 transforms per row and step
@@ -1641,6 +1732,7 @@ struct Medium {
         }
       }
     } else if (allowPropagator && wantPropagator(nInst)) {
+      checkGridStrict(R);
       buildPropagator(R);
       a.prop = prop.p;
       if (wantFF(R, a)) {
@@ -1661,6 +1753,7 @@ struct Medium {
         }
       }
     } else {
+      checkGridStrict(R);
       k = findKernel(kKindDirect, solver, R);
       // Launches with fewer propagations than SMs are latency-bound: one SM's FP64 units run each
       // propagation, and N/R threads below 128 leave some of its four schedulers idle.  Use the
@@ -1676,7 +1769,7 @@ struct Medium {
     if (!k) throw Unsupported("no fused kernel for this solver and grid");
     Schedule s{};
     lastTuned = 0;
-    if (!plainOne && !gnlse && tuneWanted(a, nInst)) {
+    if (!plainOne && !gnlse && !gen && tuneWanted(a, nInst)) {
       const TuneChoice c = autotune(k->kind, k->key, a, nInst, ff ? &ffT : nullptr);
       if (c.R != 0) {
         k = findKernelFn(c.fn);
@@ -1704,7 +1797,8 @@ struct Medium {
     }
     double2* sp = nullptr;
     if (gnlse) {
-      scratch.reserve((size_t)s.grid * s.ipc * (paired ? 7 : 2) * N);
+      // per thread group: 2 (7 when paired) parts of T R values (N on the register plan)
+      scratch.reserve((size_t)s.grid * s.ipc * (paired ? 7 : 2) * ((size_t)a.plan.T * a.R));
       sp = scratch.p;
     }
     // with kernel timing on, the tail runs after the timed region, outside the graph
@@ -1770,6 +1864,7 @@ struct Medium {
       throw Unsupported("the adjoint is implemented for Chi2PDC and Chi3GNLSE");
     if (rows == 0) throw std::invalid_argument("Too many threads requested!");
     if (nZ < 2) throw std::invalid_argument("the adjoint needs at least two z steps");
+    if (!is_pow2((int)N)) throw Unsupported("the adjoint takes power-of-two grids");
     ensureDevice();
     const int R = chooseR();
     checkGrid(R);
@@ -2292,7 +2387,8 @@ struct Medium {
   // Raw outputs of impulse propagations [first, first + count) of the Green's function over all modes
   // (instance 2 (im N + bin) + {0: impulse 1, 1: impulse i}); the row block of one rank when the
   // 2 N nIn propagations are split over several GPUs.
-  void greenRows(int inTime, int runPumpFlag, long long first, long long count, double2* rawOut) {
+  // rawOut: host memory, or (device = true) device memory written by the kernel directly.
+  void greenRows(int inTime, int runPumpFlag, long long first, long long count, double2* rawOut, bool device = false) {
     if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
     const long long total = 2LL * nSignal * N;
     if (first < 0 || count < 0 || first + count > total) throw std::invalid_argument("impulse range out of bounds");
@@ -2301,32 +2397,38 @@ struct Medium {
     const int R = chooseR();
     checkGrid(R);
     const long long outStride = (long long)nSignal * N;
-    raw.reserve((size_t)std::max<long long>(count, 1) * outStride);
+    if (!device) raw.reserve((size_t)std::max<long long>(count, 1) * outStride);
+    double2* dst = device ? rawOut : raw.p;
     PropArgs a = baseArgs(R);
     a.inKind = 0;
     a.inTime = inTime ? 1 : 0;
     for (uint m = 0; m < nSignal; m++) a.impModes[m] = (int)m;
     a.nOut = (int)nSignal;
     for (uint m = 0; m < nSignal; m++) a.outModes[m] = (int)m;
-    a.out = raw.p - first * outStride;   // the kernel indexes outputs by the global instance
+    a.out = dst - first * outStride;   // the kernel indexes outputs by the global instance
     a.outStride = outStride;
     a.instBase = first;
     if (count > 0) propagate(a, count, true);
-    if (count > 0)
+    if (count > 0 && !device)
       ck(cudaMemcpyAsync(rawOut, raw.p, (size_t)count * outStride * sizeof(double2), cudaMemcpyDeviceToHost, stream),
          "rows download");
     ck(cudaStreamSynchronize(stream), "green rows");
   }
 
   // C and S from the raw rows of all 2 N nSignal impulse propagations (the epilogue of green()).
-  void greenFinish(const double2* rawIn, int normalize, double2* Cdst, double2* Sdst) {
+  // rawIn, Cdst, Sdst: host memory, or (device = true) device memory read and written directly.
+  void greenFinish(const double2* rawIn, int normalize, double2* Cdst, double2* Sdst, bool device = false) {
     if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
     ensureDevice();
     const int nIn = (int)nSignal, nOut = (int)nSignal;
     const long long nInst = 2LL * nIn * N, outStride = (long long)nOut * N;
-    raw.reserve((size_t)nInst * outStride);
-    ck(cudaMemcpyAsync(raw.p, rawIn, (size_t)nInst * outStride * sizeof(double2), cudaMemcpyHostToDevice, stream),
-       "rows upload");
+    const double2* src = rawIn;
+    if (!device) {
+      raw.reserve((size_t)nInst * outStride);
+      ck(cudaMemcpyAsync(raw.p, rawIn, (size_t)nInst * outStride * sizeof(double2), cudaMemcpyHostToDevice, stream),
+         "rows upload");
+      src = raw.p;
+    }
     std::vector<uint8_t> flags((size_t)nOut * nIn, 1);
     std::vector<double2> scales((size_t)nOut * nIn, make_double2(1, 0));
     for (int im = 0; im < nIn; im++)
@@ -2340,12 +2442,15 @@ struct Medium {
     ck(cudaMemcpyAsync(flagsD.p, flags.data(), flags.size(), cudaMemcpyHostToDevice, stream), "flags");
     upload(scaleD, scales);
     const size_t mat = (size_t)nOut * N * nIn * N;
-    cs.reserve(2 * mat);
-    ck(launch_green_epilogue(raw.p, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, cs.p, cs.p + mat, stream),
-       "epilogue");
+    if (!device) cs.reserve(2 * mat);
+    double2* Cd = device ? Cdst : cs.p;
+    double2* Sd = device ? Sdst : cs.p + mat;
+    ck(launch_green_epilogue(src, outStride, (int)N, nIn, nOut, scaleD.p, flagsD.p, Cd, Sd, stream), "epilogue");
     launches++;
-    ck(cudaMemcpyAsync(Cdst, cs.p, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "C download");
-    ck(cudaMemcpyAsync(Sdst, cs.p + mat, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "S download");
+    if (!device) {
+      ck(cudaMemcpyAsync(Cdst, cs.p, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "C download");
+      ck(cudaMemcpyAsync(Sdst, cs.p + mat, mat * sizeof(double2), cudaMemcpyDeviceToHost, stream), "S download");
+    }
     ck(cudaStreamSynchronize(stream), "green finish");
   }
 

@@ -26,6 +26,11 @@ void add_kernels_adjoint_spread(std::vector<KernelEntry>& t);
 void add_kernels_cluster_gnlse(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_gnlse_cluster(std::vector<KernelEntry>& t);
 void add_kernels_adjoint_cluster(std::vector<KernelEntry>& t);
+void add_kernels_gen_a(std::vector<KernelEntry>& t);
+void add_kernels_gen_b(std::vector<KernelEntry>& t);
+void add_kernels_gen_c(std::vector<KernelEntry>& t);
+void add_kernels_gen_d(std::vector<KernelEntry>& t);
+void add_kernels_gen_e(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -48,6 +53,11 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_cluster_gnlse(table);
     add_kernels_adjoint_gnlse_cluster(table);
     add_kernels_adjoint_cluster(table);
+    add_kernels_gen_a(table);
+    add_kernels_gen_b(table);
+    add_kernels_gen_c(table);
+    add_kernels_gen_d(table);
+    add_kernels_gen_e(table);
   });
   *count = (int)table.size();
   return table.data();
@@ -56,7 +66,7 @@ const KernelEntry* kernel_table(int* count) {
 // ------------------------------------------------------------------------------------------
 // Batched transforms of contiguous rows: out = scale * FFT(in) [* post] (power-of-two N)
 // ------------------------------------------------------------------------------------------
-template <int R, bool INV>
+template <int R, bool INV, bool GEN = false>
 __global__ void __launch_bounds__(512) k_fft_rows(const double2* __restrict__ in, double2* __restrict__ out,
                                                   long long rows, FFTPlanH plan, const double2* __restrict__ tw,
                                                   double scale, const double2* __restrict__ post, int rpc) {
@@ -69,11 +79,12 @@ __global__ void __launch_bounds__(512) k_fft_rows(const double2* __restrict__ in
     const bool active = row < rows;
     double2 x[R];
 #pragma unroll
-    for (int v = 0; v < R; v++) x[v] = active ? in[row * N + j + v * T] : czero();
-    fft_regs<R, INV>(x, buf, tw, plan, j);
+    for (int v = 0; v < R; v++) x[v] = (active && (!GEN || j + v * T < N)) ? in[row * N + j + v * T] : czero();
+    fft_any<R, INV, GEN>(x, buf, tw, plan, j);
     if (active) {
 #pragma unroll
       for (int v = 0; v < R; v++) {
+        if (GEN && j + v * T >= N) continue;
         double2 y = cscale(x[v], scale);
         if (post) y = cmul(y, post[j + v * T]);
         out[row * N + j + v * T] = y;
@@ -135,7 +146,7 @@ static cudaError_t smem_optin(const void* fn) {
   return e;
 }
 
-template <int R, bool INV>
+template <int R, bool INV, bool GEN>
 static cudaError_t fft_rows_R(const double2* in, double2* out, long long rows, const FFTPlanH& plan,
                               const double2* tw, double scale, const double2* post, cudaStream_t s) {
   const int T = plan.T;
@@ -143,14 +154,25 @@ static cudaError_t fft_rows_R(const double2* in, double2* out, long long rows, c
   if (rpc > rows) rpc = (int)rows;
   if (rpc < 1) rpc = 1;
   const size_t smem = (size_t)rpc * plan.N * sizeof(double2);
-  const void* fn = (const void*)k_fft_rows<R, INV>;
+  const void* fn = (const void*)k_fft_rows<R, INV, GEN>;
   cudaError_t e = smem_optin(fn);
   if (e != cudaSuccess) return e;
   long long groups = (rows + rpc - 1) / rpc;
   int grid = (int)(groups < 8LL * sm_count() ? groups : 8LL * sm_count());
   if (grid < 1) grid = 1;
-  k_fft_rows<R, INV><<<grid, T * rpc, smem, s>>>(in, out, rows, plan, tw, scale, post, rpc);
+  k_fft_rows<R, INV, GEN><<<grid, T * rpc, smem, s>>>(in, out, rows, plan, tw, scale, post, rpc);
   return cudaGetLastError();
+}
+
+template <bool GEN>
+static cudaError_t fft_rows_plan(const double2* in, double2* out, long long rows, const FFTPlanH& plan,
+                                 const double2* tw, bool inverse, double scale, const double2* postMul,
+                                 cudaStream_t s) {
+  if (plan.R == 8) return inverse ? fft_rows_R<8, true, GEN>(in, out, rows, plan, tw, scale, postMul, s)
+                                  : fft_rows_R<8, false, GEN>(in, out, rows, plan, tw, scale, postMul, s);
+  if (plan.R == 16) return inverse ? fft_rows_R<16, true, GEN>(in, out, rows, plan, tw, scale, postMul, s)
+                                   : fft_rows_R<16, false, GEN>(in, out, rows, plan, tw, scale, postMul, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_fft_rows(const double2* in, double2* out, long long rows, const FFTPlanH& plan,
@@ -158,8 +180,8 @@ cudaError_t launch_fft_rows(const double2* in, double2* out, long long rows, con
                             cudaStream_t s) {
   if (rows <= 0) return cudaSuccess;
   const int N = plan.N;
-  const bool pow2 = N >= 8 && (N & (N - 1)) == 0 && N <= kMaxFFT;
-  if (!pow2) {
+  if (plan.T < 1 || plan.T > 512 || N > kMaxFFT) {
+    // grids no transform plan takes: the direct O(N^2) DFT of each row
     if (in == out) return cudaErrorInvalidValue;
     const long long total = rows * N;
     int grid = (int)((total + 255) / 256);
@@ -168,12 +190,8 @@ cudaError_t launch_fft_rows(const double2* in, double2* out, long long rows, con
     else k_dft_rows<false><<<grid, 256, 0, s>>>(in, out, rows, N, tw, scale, postMul);
     return cudaGetLastError();
   }
-  const int R = N / plan.T;
-  if (R == 8) return inverse ? fft_rows_R<8, true>(in, out, rows, plan, tw, scale, postMul, s)
-                             : fft_rows_R<8, false>(in, out, rows, plan, tw, scale, postMul, s);
-  if (R == 16) return inverse ? fft_rows_R<16, true>(in, out, rows, plan, tw, scale, postMul, s)
-                              : fft_rows_R<16, false>(in, out, rows, plan, tw, scale, postMul, s);
-  return cudaErrorInvalidValue;
+  return plan.gen ? fft_rows_plan<true>(in, out, rows, plan, tw, inverse, scale, postMul, s)
+                  : fft_rows_plan<false>(in, out, rows, plan, tw, inverse, scale, postMul, s);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -226,7 +244,8 @@ cudaError_t launch_scale_rows(double2* a, const double* scale, int nRows, int N,
 // ------------------------------------------------------------------------------------------
 // Chi3 pump: sequential self-phase-modulation march on one CTA (solvers/Chi3.cpp:41-70)
 // ------------------------------------------------------------------------------------------
-template <int R>
+// GEN: the general plan (padded ownership): points j + v*T at or past N are neither loaded nor stored.
+template <int R, bool GEN = false>
 __global__ void __launch_bounds__(512) k_pump_chi3(double2* __restrict__ pf, double2* __restrict__ pt,
                                                    const double2* __restrict__ env, const double2* __restrict__ halfP,
                                                    const double2* __restrict__ dstepP, const double2* __restrict__ backP,
@@ -235,18 +254,21 @@ __global__ void __launch_bounds__(512) k_pump_chi3(double2* __restrict__ pf, dou
   extern __shared__ double2 buf[];
   const int N = plan.N, T = plan.T, j = threadIdx.x;
   const double invN = 1.0 / N;
+  auto own = [&](int v) { return !GEN || j + v * T < N; };
   double2 x[R];
 #pragma unroll
-  for (int v = 0; v < R; v++) x[v] = env[j + v * T];
-  fft_regs<R, false>(x, buf, tw, plan, j);
+  for (int v = 0; v < R; v++) x[v] = own(v) ? env[j + v * T] : czero();
+  fft_any<R, false, GEN>(x, buf, tw, plan, j);
 #pragma unroll
   for (int v = 0; v < R; v++) {
+    if (!own(v)) continue;
     x[v] = cmul(x[v], halfP[j + v * T]);
     pf[j + v * T] = x[v];
   }
-  fft_regs<R, true>(x, buf, tw, plan, j);
+  fft_any<R, true, GEN>(x, buf, tw, plan, j);
 #pragma unroll
   for (int v = 0; v < R; v++) {
+    if (!own(v)) continue;
     x[v] = cscale(x[v], invN);
     pt[j + v * T] = x[v];
   }
@@ -257,15 +279,17 @@ __global__ void __launch_bounds__(512) k_pump_chi3(double2* __restrict__ pf, dou
       const double a2 = cabs2(x[v]);
       x[v] = cmul(x[v], spm_factor(r.x * a2, r.y * a2));
     }
-    fft_regs<R, false>(x, buf, tw, plan, j);
+    fft_any<R, false, GEN>(x, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) {
+      if (!own(v)) continue;
       x[v] = cmul(x[v], dstepP[j + v * T]);
       pf[(long long)i * N + j + v * T] = x[v];
     }
-    fft_regs<R, true>(x, buf, tw, plan, j);
+    fft_any<R, true, GEN>(x, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) {
+      if (!own(v)) continue;
       x[v] = cscale(x[v], invN);
       pt[(long long)i * N + j + v * T] = x[v];
     }
@@ -275,35 +299,43 @@ __global__ void __launch_bounds__(512) k_pump_chi3(double2* __restrict__ pf, dou
   const long long last = (long long)(nRows - 1) * N;
 #pragma unroll
   for (int v = 0; v < R; v++) {
+    if (!own(v)) {
+      x[v] = czero();
+      continue;
+    }
     x[v] = cmul(pf[last + j + v * T], backP[j + v * T]);
     pf[last + j + v * T] = x[v];
   }
-  fft_regs<R, true>(x, buf, tw, plan, j);
+  fft_any<R, true, GEN>(x, buf, tw, plan, j);
 #pragma unroll
-  for (int v = 0; v < R; v++) pt[last + j + v * T] = cscale(x[v], invN);
+  for (int v = 0; v < R; v++)
+    if (own(v)) pt[last + j + v * T] = cscale(x[v], invN);
+}
+
+template <int R, bool GEN>
+static cudaError_t pump_chi3_R(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
+                               const double2* dstepP, const double2* backP, const double2* rel, int nRows,
+                               const FFTPlanH& plan, const double2* tw, cudaStream_t s) {
+  const size_t smem = (size_t)plan.N * sizeof(double2);
+  cudaError_t e = smem_optin((const void*)k_pump_chi3<R, GEN>);
+  if (e != cudaSuccess) return e;
+  k_pump_chi3<R, GEN><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_pump_chi3(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                              const double2* dstepP, const double2* backP, const double2* rel, int nRows,
                              const FFTPlanH& plan, const double2* tw, cudaStream_t s) {
-  const int R = plan.N / plan.T;
-  const size_t smem = (size_t)plan.N * sizeof(double2);
-  if (R == 8) {
-    cudaError_t e = smem_optin((const void*)k_pump_chi3<8>);
-    if (e != cudaSuccess) return e;
-    k_pump_chi3<8><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
-  } else if (R == 4) {
-    cudaError_t e = smem_optin((const void*)k_pump_chi3<4>);
-    if (e != cudaSuccess) return e;
-    k_pump_chi3<4><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
-  } else if (R == 16) {
-    cudaError_t e = smem_optin((const void*)k_pump_chi3<16>);
-    if (e != cudaSuccess) return e;
-    k_pump_chi3<16><<<1, plan.T, smem, s>>>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw);
-  } else {
-    return cudaErrorInvalidValue;
+  if (plan.T < 1 || plan.T > 512) return cudaErrorInvalidValue;
+  switch (plan.R * 2 + (plan.gen ? 1 : 0)) {
+    case 8: return pump_chi3_R<4, false>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    case 16: return pump_chi3_R<8, false>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    case 32: return pump_chi3_R<16, false>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    case 9: return pump_chi3_R<4, true>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    case 17: return pump_chi3_R<8, true>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    case 33: return pump_chi3_R<16, true>(pumpFreq, pumpTime, env, halfP, dstepP, backP, rel, nRows, plan, tw, s);
+    default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------------------------------

@@ -179,6 +179,140 @@ __device__ __forceinline__ void fft_regs(double2 (&x)[R], double2* __restrict__ 
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// General transform (plan.gen == 1): any N, thread j owning the points j + v*T that are below N,
+// T = ceil(N/R).  The owned points go to the shared-memory buffer, every pass reads its inputs from
+// there and writes its outputs back, and the result comes back to the same ownership (points past N
+// read as zero).  Pass of radix r with L = product of the earlier radices and stride = N/(L r),
+// butterfly b < N/r, k = b mod L:
+//     y_s = sum_q x[b + q N/r] w_N^{q (k stride + s N/r)},   written to [(b - k) r + k + s L]
+// (the Stockham pass of the power-of-two kernels above, with any radix).  Radices 2, 4 and 8 run as
+// butterflies (each thread holds the outputs of at most ceil(R/r) of them until the barrier); every
+// other radix computes each output as its r-term sum, so a thread holds R outputs (one per owned
+// index, read as the pair (b, s)).  This path serves the grids that are not powers of two; its
+// barriers are CTA-wide in uniform control flow like those of stockham_pass.
+// ------------------------------------------------------------------------------------------
+template <int R, int r, bool INV>
+__device__ __forceinline__ void gen_pass_pow2(double2* __restrict__ buf, const double2* __restrict__ tw, int N, int T,
+                                              int j, int L) {
+  constexpr int U = (R + r - 1) / r;   // butterflies per thread: N/r / ceil(N/R) <= R/r
+  const int nb = N / r, stride = N / (L * r);
+  double2 y[U][r];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int b = j + u * T;
+    if (b < nb) {
+      const int k = b % L;
+      double2 a[r];
+#pragma unroll
+      for (int q = 0; q < r; q++) {
+        a[q] = buf[b + q * nb];
+        if (q > 0 && L > 1) {
+          const double2 w = tw[k * q * stride];
+          a[q] = INV ? cmulc(a[q], w) : cmul(a[q], w);
+        }
+      }
+      if constexpr (r == 2) dft2<INV>(a[0], a[1]);
+      else if constexpr (r == 4) dft4<INV>(a[0], a[1], a[2], a[3]);
+      else dft8<INV>(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]);
+#pragma unroll
+      for (int s = 0; s < r; s++) y[u][s] = a[s];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int b = j + u * T;
+    if (b < nb) {
+      const int k = b % L;
+      const int base = (b - k) * r + k;
+#pragma unroll
+      for (int s = 0; s < r; s++) buf[base + s * L] = y[u][s];
+    }
+  }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void gen_pass_any(double2* __restrict__ buf, const double2* __restrict__ tw, int N, int T,
+                                             int j, int L, int r) {
+  const int nb = N / r, stride = N / (L * r);
+  double2 y[R];
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    const int o = j + v * T;
+    y[v] = czero();
+    if (o < N) {
+      const int b = o % nb, s = o / nb, k = b % L;
+      const int step = (k * stride + s * nb) % N;
+      int e = 0;
+      double2 acc = czero();
+      for (int q = 0; q < r; q++) {
+        const double2 w = tw[e];
+        const double2 xq = buf[b + q * nb];
+        acc = INV ? cadd(acc, cmulc(xq, w)) : cadd(acc, cmul(xq, w));
+        e += step;
+        if (e >= N) e -= N;
+      }
+      y[v] = acc;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    const int o = j + v * T;
+    if (o < N) {
+      const int b = o % nb, s = o / nb, k = b % L;
+      buf[(b - k) * r + k + s * L] = y[v];
+    }
+  }
+}
+
+// The passes of the general plan, on the buffer alone: one out-of-line copy per (R, direction), so that
+// a kernel with many transforms carries a call at each of them rather than the passes inlined.  The
+// plan comes by value (its radices); every pass starts with a barrier and ends with its writes.
+template <int R, bool INV>
+__device__ __noinline__ void fft_general_passes(double2* __restrict__ buf, const double2* __restrict__ tw,
+                                                const FFTPlanH plan, int j) {
+  const int N = plan.N, T = plan.T;
+  int L = 1;
+  for (int p = 0; p < plan.nPass; p++) {
+    const int r = plan.radix[p];
+    __syncthreads();   // the previous pass's outputs (or the caller's scatter) are visible
+    if (r == 8) gen_pass_pow2<R, 8, INV>(buf, tw, N, T, j, L);
+    else if (r == 4) gen_pass_pow2<R, 4, INV>(buf, tw, N, T, j, L);
+    else if (r == 2) gen_pass_pow2<R, 2, INV>(buf, tw, N, T, j, L);
+    else gen_pass_any<R, INV>(buf, tw, N, T, j, L, r);
+    L *= r;
+  }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void fft_general(double2 (&x)[R], double2* __restrict__ buf, const double2* __restrict__ tw,
+                                            const FFTPlanH& plan, int j) {
+  const int N = plan.N, T = plan.T;
+  __syncthreads();   // earlier readers of the buffer are done
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    const int t = j + v * T;
+    if (t < N) buf[t] = x[v];
+  }
+  fft_general_passes<R, INV>(buf, tw, plan, j);
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < R; v++) {
+    const int t = j + v * T;
+    x[v] = t < N ? buf[t] : czero();
+  }
+}
+
+// The transform of the kernels that take both plans: GEN instantiations serve plan.gen == 1.
+template <int R, bool INV, bool GEN>
+__device__ __forceinline__ void fft_any(double2 (&x)[R], double2* __restrict__ buf, const double2* __restrict__ tw,
+                                        const FFTPlanH& plan, int j) {
+  if constexpr (GEN) fft_general<R, INV>(x, buf, tw, plan, j);
+  else fft_regs<R, INV>(x, buf, tw, plan, j);
+}
+
 // exp(re + i im), the self-phase factor of one pump row.  im is the nonlinear phase of half a z step,
 // small in practice: for |im| <= 1/4 sine and cosine come from their Taylor series (terms to x^13 and
 // x^14; the first omitted term is below 1e-21 of the result), otherwise from sincos.  re is zero

@@ -9,11 +9,18 @@ namespace nlm {
 constexpr int kMaxModes = 4;
 constexpr int kMaxPumps = 2;
 constexpr int kMaxCoefs = 8;
-constexpr int kMaxFFT = 8192;   // largest power-of-two grid of the fused kernels
+constexpr int kMaxFFT = 8192;   // largest grid of the fused kernels
+constexpr int kTablePad = 16;   // zeroed values after every per-point device table (padded ownership reads)
 
+// Plan of an N-point transform held by T threads of R points each.  gen == 0: N a power of two and
+// T = N / R, radix-8/4/2 passes on the register ownership (nlm_device.cuh, fft_regs).  gen == 1: any N,
+// T = ceil(N / R) (thread j owns the points j + v T that are below N), passes of any radix through
+// shared memory (fft_general).
 struct FFTPlanH {
   int N, T, nPass;
   int radix[16];
+  int gen;
+  int R;   // points per thread the plan was made for
 };
 
 // Arguments of every propagation kernel (batched impulses, dense rows, one full grid).
@@ -133,6 +140,9 @@ cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const
 // rows.
 constexpr long long spread_smem_per_point(int C) { return 3 + 2LL * C; }
 constexpr long long kSpreadSmemPerPoint = spread_smem_per_point(4);
+// Registry key offset of the instantiations for the general plan (FFTPlanH::gen == 1): grids that are
+// not powers of two (kKindDirect, kKindLinear, kKindGnlse).
+constexpr int kGenKey = 2000;
 // Registry key offset (kKindCluster) of the one-point-per-thread kernels on eight CTAs.
 constexpr int kSpreadWideKey = 800;
 

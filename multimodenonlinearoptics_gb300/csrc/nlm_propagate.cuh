@@ -50,7 +50,8 @@ __device__ __forceinline__ const double2* stage_twiddles(const double2* __restri
 
 // Input of one propagation, in the frequency domain and pre-multiplied by exp(+i dz/2 D)/N
 // (src/_NonlinearMedium.hpp:169-192).
-template <int M, int R>
+// GEN: the general plan (padded ownership): points j + v*T at or past N are not loaded or stored.
+template <int M, int R, bool GEN = false>
 __device__ __forceinline__ void load_input(const PropArgs& a, long long inst, bool active, int j,
                                            double2 (&x)[M][R], double2* buf, const FFTPlanH& plan,
                                            const double2* tw) {
@@ -75,19 +76,19 @@ __device__ __forceinline__ void load_input(const PropArgs& a, long long inst, bo
       else if (a.inputMode < 1 && m < a.inChannels) seg = m;
 #pragma unroll
       for (int v = 0; v < R; v++)
-        x[m][v] = (active && seg >= 0) ? row[(long long)seg * N + j + v * T] : czero();
+        x[m][v] = (active && seg >= 0 && (!GEN || j + v * T < N)) ? row[(long long)seg * N + j + v * T] : czero();
     }
   }
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    if (a.inTime) fft_regs<R, false>(x[m], buf, tw, plan, j);
+    if (a.inTime) fft_any<R, false, GEN>(x[m], buf, tw, plan, j);
     const double2* h = a.half + (long long)m * N;
 #pragma unroll
     for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(h + j + v * T));
   }
 }
 
-template <int M, int R>
+template <int M, int R, bool GEN = false>
 __device__ __forceinline__ void store_rows(double2* base, long long modeStride, int row, int N, int T, int j,
                                            const double2 (&x)[M][R], double scale, bool active) {
   if (!active) return;
@@ -95,10 +96,10 @@ __device__ __forceinline__ void store_rows(double2* base, long long modeStride, 
   for (int m = 0; m < M; m++)
 #pragma unroll
     for (int v = 0; v < R; v++)
-      base[m * modeStride + (long long)row * N + j + v * T] = cscale(x[m][v], scale);
+      if (!GEN || j + v * T < N) base[m * modeStride + (long long)row * N + j + v * T] = cscale(x[m][v], scale);
 }
 
-template <int M, int R>
+template <int M, int R, bool GEN = false>
 __device__ __forceinline__ void store_output(const PropArgs& a, long long inst, bool active, int j,
                                              const double2 (&x)[M][R], double scale) {
   if (!active || a.out == nullptr) return;
@@ -110,13 +111,14 @@ __device__ __forceinline__ void store_output(const PropArgs& a, long long inst, 
     for (int m = 0; m < M; m++) {
       if (m != mode) continue;
 #pragma unroll
-      for (int v = 0; v < R; v++) o[(long long)om * N + j + v * T] = cscale(x[m][v], scale);
+      for (int v = 0; v < R; v++)
+        if (!GEN || j + v * T < N) o[(long long)om * N + j + v * T] = cscale(x[m][v], scale);
     }
   }
 }
 
 // Dispersion half of a step for all modes: FFT, multiply, optional inverse FFT and grid rows.
-template <int M, int R>
+template <int M, int R, bool GEN = false>
 __device__ __forceinline__ void dispersion_step(const PropArgs& a, int i, bool last, int j, double2 (&x)[M][R],
                                                 double2* buf, const FFTPlanH& plan, bool active, const double2* table,
                                                 const double2* tw) {
@@ -124,17 +126,17 @@ __device__ __forceinline__ void dispersion_step(const PropArgs& a, int i, bool l
   const bool wantTime = !last || a.inTime || a.gridT != nullptr;
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    fft_regs<R, false>(x[m], buf, tw, plan, j);
+    fft_any<R, false, GEN>(x[m], buf, tw, plan, j);
     const double2* d = table + (long long)m * N;
 #pragma unroll
     for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(d + j + v * T));
   }
   const long long ms = (long long)a.nZ * N;
-  if (a.gridF) store_rows<M, R>(a.gridF, ms, i, N, T, j, x, (double)N, active);
+  if (a.gridF) store_rows<M, R, GEN>(a.gridF, ms, i, N, T, j, x, (double)N, active);
   if (wantTime) {
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
-    if (a.gridT) store_rows<M, R>(a.gridT, ms, i, N, T, j, x, 1.0, active);
+    for (int m = 0; m < M; m++) fft_any<R, true, GEN>(x[m], buf, tw, plan, j);
+    if (a.gridT) store_rows<M, R, GEN>(a.gridT, ms, i, N, T, j, x, 1.0, active);
   }
 }
 
@@ -173,7 +175,7 @@ __device__ __forceinline__ void rk4_point(double2 (&x)[S::kM], const double2 (&p
 // --------------------------------------------------------------------------------------------
 // Direct kernel: every solver except Chi3GNLSE.
 // --------------------------------------------------------------------------------------------
-template <class S, int R>
+template <class S, int R, bool GEN = false>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs a) {
   constexpr int M = S::kM, P = S::kP > 0 ? S::kP : 1;
   extern __shared__ double2 smem[];
@@ -190,13 +192,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[M][R];
-    load_input<M, R>(a, inst, active, j, x, buf, plan, tw);
+    load_input<M, R, GEN>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
-    if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+    if (a.gridF) store_rows<M, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
-    if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
-    if (a.ckpt && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
+    for (int m = 0; m < M; m++) fft_any<R, true, GEN>(x[m], buf, tw, plan, j);
+    if (a.gridT) store_rows<M, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+    if (a.ckpt && a.nZ > 1) store_rows<M, R, GEN>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
 #pragma unroll
@@ -222,26 +224,26 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
         for (int m = 0; m < M; m++) x[m][v] = xm[m];
       }
       const bool last = i == a.nZ - 1;
-      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      dispersion_step<M, R, GEN>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
       if (a.ckpt && !last && i % a.ckK == 0)
-        store_rows<M, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
+        store_rows<M, R, GEN>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     }
     if (a.nZ == 1) {
 #pragma unroll
-      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, tw, plan, j);
+      for (int m = 0; m < M; m++) fft_any<R, false, GEN>(x[m], buf, tw, plan, j);
       // x now holds X_in * exp(+i dz/2 D); the factor tables are pre-divided by N
 #pragma unroll
       for (int m = 0; m < M; m++)
 #pragma unroll
         for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(a.back + (long long)m * N + j + v * T));
-      if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+      if (a.gridF) store_rows<M, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
       if (a.inTime || a.gridT) {
 #pragma unroll
-        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
-        if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+        for (int m = 0; m < M; m++) fft_any<R, true, GEN>(x[m], buf, tw, plan, j);
+        if (a.gridT) store_rows<M, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
       }
     }
-    store_output<M, R>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
+    store_output<M, R, GEN>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
     __syncthreads();
   }
 }
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_direct(const PropArgs
 // --------------------------------------------------------------------------------------------
 // CK: the forward checkpoints of the adjoint (PropArgs::ckpt) are written; a separate instantiation,
 // so that the other launches carry no per-step test.
-template <int M, int R, bool CK = false>
+template <int M, int R, bool CK = false, bool GEN = false>
 __device__ __forceinline__ void linear_body(const PropArgs& a) {
   constexpr int D = 2 * M, E = D * D;
   extern __shared__ double2 smem[];
@@ -270,13 +272,13 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[M][R];
-    load_input<M, R>(a, inst, active, j, x, buf, plan, tw);
+    load_input<M, R, GEN>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
-    if (a.gridF) store_rows<M, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+    if (a.gridF) store_rows<M, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
 #pragma unroll
-    for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
-    if (a.gridT) store_rows<M, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
-    if (CK && a.nZ > 1) store_rows<M, R>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
+    for (int m = 0; m < M; m++) fft_any<R, true, GEN>(x[m], buf, tw, plan, j);
+    if (a.gridT) store_rows<M, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+    if (CK && a.nZ > 1) store_rows<M, R, GEN>(a.ckpt + inst * a.ckN * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       // entries stored as pairs (row r, columns 2c and 2c+1) so a point loads D*D/2 16-byte words
       const double2* mat = reinterpret_cast<const double2*>(a.prop) + (long long)(i - 1) * (E / 2) * N;
@@ -305,30 +307,30 @@ __device__ __forceinline__ void linear_body(const PropArgs& a) {
         for (int m = 0; m < M; m++) x[m][v] = make_double2(outv[2 * m], outv[2 * m + 1]);
       }
       const bool last = i == a.nZ - 1;
-      dispersion_step<M, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      dispersion_step<M, R, GEN>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
       if (CK && !last && i % a.ckK == 0)
-        store_rows<M, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
+        store_rows<M, R, GEN>(a.ckpt + (inst * a.ckN + i / a.ckK) * M * (long long)N, N, 0, N, T, j, x, 1.0, active);
     }
     if (a.nZ == 1) {
 #pragma unroll
-      for (int m = 0; m < M; m++) fft_regs<R, false>(x[m], buf, tw, plan, j);
+      for (int m = 0; m < M; m++) fft_any<R, false, GEN>(x[m], buf, tw, plan, j);
 #pragma unroll
       for (int m = 0; m < M; m++)
 #pragma unroll
         for (int v = 0; v < R; v++) x[m][v] = cmul(x[m][v], __ldg(a.back + (long long)m * N + j + v * T));
       if (a.inTime) {
 #pragma unroll
-        for (int m = 0; m < M; m++) fft_regs<R, true>(x[m], buf, tw, plan, j);
+        for (int m = 0; m < M; m++) fft_any<R, true, GEN>(x[m], buf, tw, plan, j);
       }
     }
-    store_output<M, R>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
+    store_output<M, R, GEN>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
     __syncthreads();
   }
 }
 
-template <int M, int R, bool CK = false>
+template <int M, int R, bool CK = false, bool GEN = false>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_linear(const PropArgs a) {
-  linear_body<M, R, CK>(a);
+  linear_body<M, R, CK, GEN>(a);
 }
 
 // The same kernel compiled for 128-thread CTAs with at least MINB of them resident per SM: fewer

@@ -12,7 +12,8 @@
 
 namespace nlm {
 
-template <int R>
+// GEN: the general plan (any N, padded ownership); the scratch slot then holds T R >= N values per part.
+template <int R, bool GEN = false>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs a, double2* __restrict__ scratch) {
   extern __shared__ double2 smem[];
   const FFTPlanH& plan = a.plan;
@@ -21,8 +22,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
   double2* bufs;
   const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
   double2* buf = bufs + (long long)g * N;
-  double2* X = scratch + ((long long)blockIdx.x * a.ipc + g) * 2 * N;   // state (time domain)
-  double2* ACC = X + N;                                                 // k1 + 2 k2 + 2 k3 + k4
+  const long long NS = (long long)T * R;                                // N for a power-of-two plan
+  double2* X = scratch + ((long long)blockIdx.x * a.ipc + g) * 2 * NS;  // state (time domain)
+  double2* ACC = X + NS;                                                // k1 + 2 k2 + 2 k3 + k4
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
   __shared__ long long s_group;
   for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
@@ -30,14 +32,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
     const bool active = local < a.nInst;
     const long long inst = a.instBase + local;
     double2 x[1][R];
-    load_input<1, R>(a, inst, active, j, x, buf, plan, tw);
+    load_input<1, R, GEN>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
-    if (a.gridF) store_rows<1, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
-    fft_regs<R, true>(x[0], buf, tw, plan, j);
-    if (a.gridT) store_rows<1, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+    if (a.gridF) store_rows<1, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+    fft_any<R, true, GEN>(x[0], buf, tw, plan, j);
+    if (a.gridT) store_rows<1, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
 #pragma unroll
     for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
-    if (a.ckpt && a.nZ > 1) store_rows<1, R>(a.ckpt + inst * a.ckN * (long long)N, N, 0, N, T, j, x, 1.0, active);
+    if (a.ckpt && a.nZ > 1) store_rows<1, R, GEN>(a.ckpt + inst * a.ckN * (long long)N, N, 0, N, T, j, x, 1.0, active);
     for (int i = 1; i < a.nZ; i++) {
       const double* rel = a.relInt + (long long)(i - 1) * 3;
       double2 k[R];
@@ -54,17 +56,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
           u[v] = make_double2(ri * cabs2(y[v]), 0.0);
         }
         // Raman convolution R~ * (rel |y|^2)
-        fft_regs<R, false>(u, buf, tw, plan, j);
+        fft_any<R, false, GEN>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.raman + j + v * T));
-        fft_regs<R, true>(u, buf, tw, plan, j);
+        fft_any<R, true, GEN>(u, buf, tw, plan, j);
         // times the field, then the self-steepening operator (g0 + g1 w)
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], y[v]);
-        fft_regs<R, false>(u, buf, tw, plan, j);
+        fft_any<R, false, GEN>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + j + v * T));
-        fft_regs<R, true>(u, buf, tw, plan, j);
+        fft_any<R, true, GEN>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) {
           k[v] = u[v];
@@ -75,25 +77,25 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
 #pragma unroll
       for (int v = 0; v < R; v++) x[0][v] = caxpy(X[j + v * T], 1.0 / 6.0, ACC[j + v * T]);
       const bool last = i == a.nZ - 1;
-      dispersion_step<1, R>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      dispersion_step<1, R, GEN>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
       if (!last) {
 #pragma unroll
         for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
         if (a.ckpt && i % a.ckK == 0)
-          store_rows<1, R>(a.ckpt + (inst * a.ckN + i / a.ckK) * (long long)N, N, 0, N, T, j, x, 1.0, active);
+          store_rows<1, R, GEN>(a.ckpt + (inst * a.ckN + i / a.ckK) * (long long)N, N, 0, N, T, j, x, 1.0, active);
       }
     }
     if (a.nZ == 1) {
-      fft_regs<R, false>(x[0], buf, tw, plan, j);
+      fft_any<R, false, GEN>(x[0], buf, tw, plan, j);
 #pragma unroll
       for (int v = 0; v < R; v++) x[0][v] = cmul(x[0][v], __ldg(a.back + j + v * T));
-      if (a.gridF) store_rows<1, R>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+      if (a.gridF) store_rows<1, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
       if (a.inTime || a.gridT) {
-        fft_regs<R, true>(x[0], buf, tw, plan, j);
-        if (a.gridT) store_rows<1, R>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
+        fft_any<R, true, GEN>(x[0], buf, tw, plan, j);
+        if (a.gridT) store_rows<1, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
       }
     }
-    store_output<1, R>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
+    store_output<1, R, GEN>(a, inst, active, j, x, a.inTime ? 1.0 : (double)N);
     __syncthreads();
   }
 }
@@ -222,6 +224,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
 
 void add_kernels_gnlse(std::vector<KernelEntry>& t) {
   t.push_back({kKindGnlse, kChi3GNLSE, 8, (const void*)k_propagate_gnlse<8>});
+  // key + kGenKey: grids that are not powers of two (general plan), up to 4096 and 8192 points
+  t.push_back({kKindGnlse, kChi3GNLSE + kGenKey, 8, (const void*)k_propagate_gnlse<8, true>});
+  t.push_back({kKindGnlse, kChi3GNLSE + kGenKey, 16, (const void*)k_propagate_gnlse<16, true>});
   // key + 400: two rows per thread group, shared Raman transforms
   t.push_back({kKindGnlse, kChi3GNLSE + 400, 8, (const void*)k_propagate_gnlse_pair<8>});
 }

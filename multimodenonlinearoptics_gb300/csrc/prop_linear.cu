@@ -16,6 +16,11 @@ void add_kernels_linear(std::vector<KernelEntry>& t) {
   // latency-bound launches (fewer propagations than SMs): N/4 threads, all four schedulers of the SM
   t.push_back({kKindLinear, 1, 4, (const void*)k_propagate_linear<1, 4>});
   t.push_back({kKindLinear, 2, 4, (const void*)k_propagate_linear<2, 4>});
+  // key + kGenKey: grids that are not powers of two (general plan)
+  t.push_back({kKindLinear, 1 + kGenKey, 8, (const void*)k_propagate_linear<1, 8, false, true>});
+  t.push_back({kKindLinear, 1 + kGenKey, 16, (const void*)k_propagate_linear<1, 16, false, true>});
+  t.push_back({kKindLinear, 2 + kGenKey, 8, (const void*)k_propagate_linear<2, 8, false, true>});
+  t.push_back({kKindLinear, 4 + kGenKey, 4, (const void*)k_propagate_linear<4, 4, false, true>});
   // key + 100: the adjoint's checkpointed forwards
   t.push_back({kKindLinear, 101, 4, (const void*)k_propagate_linear<1, 4, true>});
   t.push_back({kKindLinear, 101, 8, (const void*)k_propagate_linear<1, 8, true>});

@@ -80,6 +80,8 @@ def _load():
         "nlm_set_poling_profile": (i, [vp, P(d), sz]),
         "nlm_green_rows": (i, [vp, i, i, sz, sz, P(d)]),
         "nlm_green_finish": (i, [vp, P(d), i, P(d), P(d)]),
+        "nlm_green_rows_device": (i, [vp, i, i, sz, sz, vp]),
+        "nlm_green_finish_device": (i, [vp, vp, i, vp, vp]),
         "nlm_adjoint_forward": (i, [vp, vp, sz, vp, i, P(i)]),
         "nlm_adjoint_backward": (i, [vp, vp, vp, vp, P(d)]),
         "nlm_fp64_peak": (i, [P(d)]),
