@@ -148,13 +148,20 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
                             unsigned input_mode, const uint8_t* use_output, size_t n_use_output,
                             void* out_dev);
 
-/* --- ragged batch: several media, one seeded signal each, one launch --------------
+/* --- ragged batch: several media, one seeded signal each, one call ----------------
  * No counterpart method in the reference (it would loop over media calling
  * batchSignalSimulation one row at a time, src/_NonlinearMedium.cpp:378-444).
  * inputs[k] is an N_k complex row for media[k]; outputs[k] receives the last row of all
- * signal modes (nSignalModes_k*N_k complex).  Pumps must have been run.              */
+ * signal modes (nSignalModes_k*N_k complex).  Pumps must have been run.  The call plans
+ * each medium's form (one SM in a ragged launch, or a cluster of 4 or 8 SMs) for the
+ * shortest makespan and runs as one CUDA graph, replayed while the plan stays the same. */
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
+/* The plan of the last nlm_ragged_batch call: its estimated makespan (microseconds), the cluster
+ * slots of four and eight SMs, the CTAs of its one-SM ragged launches, and the CUDA-graph captures and
+ * replays of ragged calls so far.  No counterpart in the reference (measurement support). */
+nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
+                                long* graph_captures, long* graph_replays);
 
 /* --- gradients (no counterpart in the reference) -------------------------------------------
  * Reverse-mode gradients of a functional L of the output spectra of a Chi2PDC batch with respect to

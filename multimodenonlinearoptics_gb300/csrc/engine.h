@@ -224,11 +224,12 @@ struct GraphCache {
   // a graph: replay of the graph captured for `key`, else capture, instantiate and launch.  Streams
   // that cannot be captured (the legacy default stream, or one already being captured by the
   // caller) get the launches directly.
-  void run(const GraphKey& key, cudaStream_t stream, const std::function<void()>& record) {
+  // Returns true when it replayed a captured graph (the host code of `record` did not run).
+  bool run(const GraphKey& key, cudaStream_t stream, const std::function<void()>& record) {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     if (stream == nullptr || cudaStreamIsCapturing(stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
       record();
-      return;
+      return false;
     }
     clock++;
     for (auto& e : entries)
@@ -236,7 +237,7 @@ struct GraphCache {
         e.lastUse = clock;
         replays++;
         ck(cudaGraphLaunch(e.exec, stream), "graph launch");
-        return;
+        return true;
       }
     cudaGraph_t g = nullptr;
     ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -261,6 +262,7 @@ struct GraphCache {
     entries.push_back(Entry{key.bytes, ex, clock});
     captures++;
     ck(cudaGraphLaunch(ex, stream), "graph launch");
+    return false;
   }
 };
 
@@ -1495,6 +1497,14 @@ struct Medium {
     a.steep = steepD.p;
     a.relInt = relIntD.p;
     return a;
+  }
+
+  // The propagator's device buffer at its size, allocated ahead of a graph capture (which may not
+  // allocate); buildPropagator then finds it in place.
+  void reservePropagator() {
+    const int M = (int)nSignal, E = 4 * M * M;
+    const size_t count = (size_t)(nZ > 1 ? nZ - 1 : 0) * E * N;
+    if (count) prop.alloc(count + 2 * kTablePad);
   }
 
   // on: the stream of the build (default: the medium's own)

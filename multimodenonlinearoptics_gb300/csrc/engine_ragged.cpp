@@ -1,28 +1,160 @@
-// engine_ragged.cpp -- nlm_ragged_batch: one persistent launch over a ragged set of media (different
-// grids and step counts), with the costliest large-grid media as cluster propagations beside it.
+// engine_ragged.cpp -- nlm_ragged_batch: one call over a ragged set of media (different grids and step
+// counts), scheduled for its makespan over the SMs and captured into a CUDA graph.
+//
+// Every medium is a sequential z march; it can run in one of three forms:
+//   one  -- one CTA (one SM) in the ragged launch, whose CTAs claim media largest first;
+//   c4   -- a 4-CTA cluster on four SMs (one point per thread up to 1024 points, four from 2048);
+//   w8   -- an 8-CTA cluster on eight SMs, one point per thread (2048 and 4096 points).
+// The larger forms finish a medium sooner but spend more SM time on it.  The planner picks a target
+// makespan T by bisection: every medium takes the form of least SM time that finishes within T;
+// cluster-form media are packed first-fit, largest first, into slots (a stream running its media one
+// after another on 4 or 8 SMs); the one-SM media share the ragged launch.  T is feasible when the
+// slots and the ragged launch fit on the SMs at once.  The call is then enqueued on those streams
+// (inputs in one copy, outputs in one copy) and captured into a CUDA graph, replayed by later calls
+// with the same plan.
 #include "engine.h"
 
 using nlm::guarded;
 using nlm::Medium;
 
+namespace {
+
+using namespace nlm;
+
+enum Form { kOne = 0, kC4 = 1, kW8 = 2, kForms = 3 };
+constexpr int kFormSMs[kForms] = {1, 4, 8};
+
+// Per-step time (microseconds) of a two-mode pump-driven medium (Chi2SFG) in each form on a GB300,
+// measured with one propagation of 1199 steps per form: [RK4 propagator used][form][log2 N - 7] for
+// N = 128 .. 2048.  Zero: the form does not exist for that grid.  Larger grids scale as N log2 N from
+// the table's end, smaller ones take the 128-point time (latency-bound); other solvers scale with
+// their mode count.
+constexpr double kStepUs[2][kForms][5] = {
+    {{26.3, 27.8, 34.7, 67.8, 137.6}, {9.6, 10.8, 13.7, 24.4, 41.7}, {0, 0, 0, 0, 30.7}},
+    {{18.3, 19.7, 27.8, 51.8, 99.3}, {7.6, 8.8, 11.7, 20.0, 33.6}, {0, 0, 0, 0, 26.6}}};
+
+double step_us(int form, uint N, uint modes, bool prop) {
+  int lg = 0;
+  while ((1u << lg) < N) lg++;
+  const int i = std::min(std::max(lg - 7, 0), 4);
+  double t = kStepUs[prop ? 1 : 0][form][i];
+  if (t == 0) return -1;
+  if (lg > 11) t *= (double)N * lg / (2048.0 * 11);
+  return t * std::max(1u, modes) / 2.0;
+}
+
+struct Job {
+  size_t k;                  // index in the call's media
+  double t[kForms];          // estimated march time per form (us); < 0: form not available
+  double best() const {
+    double b = -1;
+    for (double x : t)
+      if (x >= 0 && (b < 0 || x < b)) b = x;
+    return b;
+  }
+};
+
+struct Plan {
+  std::vector<int> form;                    // per job
+  std::vector<std::vector<size_t>> slots;   // cluster slots: job indices in launch order
+  std::vector<int> slotForm;
+  int poolSMs = 0;                          // CTAs of the ragged launches
+  double makespan = 0;
+};
+
+// Plan for target makespan T (us); false when the slots and the ragged launch need more than `sms` SMs.
+bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
+  Plan p;
+  p.form.assign(jobs.size(), -1);
+  std::vector<double> slotLoad;
+  double pool = 0, poolMax = 0;
+  // largest first (by the time of the fastest form)
+  std::vector<size_t> order(jobs.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a].best() > jobs[b].best(); });
+  for (size_t i : order) {
+    const Job& j = jobs[i];
+    // the form of least SM time that finishes within T
+    int f = -1;
+    for (int c = 0; c < kForms; c++)
+      if (j.t[c] >= 0 && j.t[c] <= T && (f < 0 || j.t[c] * kFormSMs[c] < j.t[f] * kFormSMs[f])) f = c;
+    if (f < 0) return false;
+    p.form[i] = f;
+    if (f == kOne) {
+      pool += j.t[f];
+      poolMax = std::max(poolMax, j.t[f]);
+      continue;
+    }
+    size_t s = 0;
+    for (; s < slotLoad.size(); s++)
+      if (p.slotForm[s] == f && slotLoad[s] + j.t[f] <= T) break;
+    if (s == slotLoad.size()) {
+      slotLoad.push_back(0);
+      p.slotForm.push_back(f);
+      p.slots.emplace_back();
+    }
+    slotLoad[s] += j.t[f];
+    p.slots[s].push_back(i);
+  }
+  // the ragged launch's CTAs take their media largest first from a counter: with m CTAs the last
+  // medium starts by pool / m and runs at most poolMax more
+  int m = 0;
+  if (pool > 0) {
+    const double room = T - poolMax;
+    m = room > 0 ? (int)std::ceil(pool / room) : sms + 1;
+    m = std::max(m, 1);
+  }
+  int used = m;
+  for (int f : p.slotForm) used += kFormSMs[f];
+  if (used > sms) return false;
+  p.poolSMs = m;
+  p.makespan = T;
+  *out = p;
+  return true;
+}
+
+}  // namespace
+
 extern "C" {
 
-// Workspace of the ragged launch (process-wide; the launch is serialised by the mutex).
+// Workspace of the ragged call (process-wide; calls are serialised by the mutex).
 struct RaggedWorkspace {
   std::mutex mu;
-  nlm::DevBuf<double2> in, out;
-  nlm::DevBuf<double2> cin, cout;   // inputs and outputs of the media run as cluster propagations
-  nlm::DevBuf<nlm::PropArgs> items;
-  nlm::PinnedBuf<double2> hin, hout;   // host staging of every medium's input and output
+  nlm::DevBuf<double2> in, out;                 // every fused medium's input and output, one block each
+  nlm::DevBuf<nlm::PropArgs> items;             // the ragged launches' media
+  nlm::PinnedBuf<double2> hin, hout;            // host staging of the inputs and outputs
   nlm::PinnedBuf<nlm::PropArgs> hitems;
-  nlm::DevBuf<unsigned long long> counter;
+  nlm::DevBuf<unsigned long long> counters;     // one work counter per ragged launch
+  std::vector<cudaStream_t> streams;            // [0]: origin; then one per slot and ragged launch
+  std::vector<cudaEvent_t> events;
+  nlm::GraphCache graphs;
+  std::vector<unsigned char> lastKey;           // the previous call's plan
+  void ensureStreams(size_t n) {
+    while (streams.size() < n) {
+      cudaStream_t st = nullptr;
+      ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "ragged stream");
+      streams.push_back(st);
+    }
+    while (events.size() < n) {
+      cudaEvent_t e = nullptr;
+      ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "ragged event");
+      events.push_back(e);
+    }
+  }
 };
 static RaggedWorkspace g_ragged;
+
+// What the last call planned and ran (nlm_ragged_last_plan).
+struct RaggedStats {
+  double makespan;
+  int slotsC4, slotsW8, raggedCTAs;
+  long captures, replays;
+};
+static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0};
 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
                             double* const* outputs) {
   return guarded([&] {
-    using namespace nlm;
     if (n_media == 0) return;
     std::vector<Medium*> ms(n_media);
     for (size_t k = 0; k < n_media; k++) {
@@ -30,7 +162,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       if (ms[k]->isCascade) throw std::invalid_argument("ragged batches take single media");
       ms[k]->launches = 0;
     }
-    // media without a ragged kernel (or with a grid it cannot take) run one launch each
+    // media without a ragged kernel (or with a grid it cannot take) run one batch call each
     std::vector<size_t> fused;
     for (size_t k = 0; k < n_media; k++) {
       Medium* m = ms[k];
@@ -45,242 +177,274 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     }
     if (fused.empty()) return;
     std::lock_guard<std::mutex> lock(g_ragged.mu);
-    std::vector<cudaStream_t> clusterSync;   // streams holding the read-back of cluster propagations
-    struct PendingCopy {
-      double2* dst;
-      const double2* src;
-      size_t bytes;
-      cudaStream_t st;
-    };
-    std::vector<PendingCopy> pendingD2H;
-    auto flushD2H = [&] {
-      for (const PendingCopy& c : pendingD2H)
-        ck(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, c.st), "ragged output");
-      pendingD2H.clear();
-    };
-    {
-      // room for every medium, so cluster propagations of different solver groups never share it
-      size_t inAll = 0, outAll = 0;
-      for (size_t k : fused) {
-        inAll += ms[k]->N;
-        outAll += (size_t)ms[k]->nSignal * ms[k]->N;
-      }
-      g_ragged.cin.reserve(inAll);
-      g_ragged.cout.reserve(outAll);
-      g_ragged.hin.reserve(inAll);
-      g_ragged.hout.reserve(outAll);
+    for (size_t k : fused) ms[k]->ensureDevice();
+    const int sms = Medium::smCount();
+
+    // ---- plan: a form per medium (the RK4 propagator decision first: it changes the step cost) ----
+    std::vector<bool> withProp(n_media, false), needBuild(n_media, false);
+    for (size_t k : fused) {
+      Medium* m = ms[k];
+      withProp[k] = m->raggedPropagator();
+      needBuild[k] = withProp[k] && !(m->propVersion == m->pumpVersion && m->prop.p);
     }
-    // every input is staged in page-locked memory first, so no copy below waits on earlier work
-    std::vector<size_t> hinOff(n_media, 0), houtOff(n_media, 0);
-    {
-      size_t io = 0, oo = 0;
-      for (size_t k : fused) {
-        hinOff[k] = io;
-        houtOff[k] = oo;
-        std::memcpy(g_ragged.hin.p + io, inputs[k], ms[k]->N * sizeof(double2));
-        io += ms[k]->N;
-        oo += (size_t)ms[k]->nSignal * ms[k]->N;
-      }
+    std::vector<Job> jobs;
+    for (size_t k : fused) {
+      Medium* m = ms[k];
+      Job j{k, {-1, -1, -1}};
+      const double steps = (double)(m->nZ > 1 ? m->nZ - 1 : 1);
+      j.t[kOne] = step_us(kOne, m->N, m->nSignal, withProp[k]) * steps;
+      // four CTAs: one point per thread on the spread grids, four points per thread from 1024 points
+      const bool c4 = (m->spreadGrid() && m->findKernel(kKindCluster, m->solver, 1)) || m->clusterGrid();
+      if (c4) j.t[kC4] = step_us(kC4, m->N, m->nSignal, withProp[k]) * steps;
+      if (m->wideGrid() && m->findKernel(kKindCluster, m->solver + kSpreadWideKey, 1))
+        j.t[kW8] = step_us(kW8, m->N, m->nSignal, withProp[k]) * steps;
+      jobs.push_back(j);
     }
-    size_t cio = 0, coo = 0;
-    // one launch per solver present in the set
-    std::map<int, std::vector<size_t>> bySolver;
-    for (size_t k : fused) bySolver[ms[k]->solver].push_back(k);
+    // bisection on the makespan between the longest medium in its fastest form and every medium on
+    // one SM one after another; a few SMs are left for the placement of the clusters
+    const int budget = std::max(1, sms - 4);
+    double lo = 0, hi = 0;
+    for (const Job& j : jobs) {
+      lo = std::max(lo, j.best());
+      hi += j.t[kOne] >= 0 ? j.t[kOne] : j.best();
+    }
+    Plan plan;
+    if (plan_for(jobs, hi, budget, &plan)) {
+      for (int it = 0; it < 40 && hi - lo > 0.002 * hi; it++) {
+        const double mid = 0.5 * (lo + hi);
+        Plan p;
+        if (plan_for(jobs, mid, budget, &p)) {
+          plan = p;
+          hi = mid;
+        } else {
+          lo = mid;
+        }
+      }
+    } else {
+      // no plan fits the SMs at once (more cluster-only media than they hold): every medium in its
+      // fastest form, each cluster medium in a slot of its own, the slots queueing for SMs
+      plan = Plan{};
+      plan.form.assign(jobs.size(), kOne);
+      for (size_t i = 0; i < jobs.size(); i++) {
+        int f = kOne;
+        for (int c = 0; c < kForms; c++)
+          if (jobs[i].t[c] >= 0 && (jobs[i].t[f] < 0 || jobs[i].t[c] < jobs[i].t[f])) f = c;
+        plan.form[i] = f;
+        if (f != kOne) {
+          plan.slots.push_back({i});
+          plan.slotForm.push_back(f);
+        }
+      }
+      plan.poolSMs = sms;
+    }
+
+    // ---- buffers, staging and the ragged launches' items (nothing is allocated inside the graph) ----
+    std::vector<size_t> inOff(n_media, 0), outOff(n_media, 0);
+    size_t inAll = 0, outAll = 0;
+    for (size_t k : fused) {
+      inOff[k] = inAll;
+      outOff[k] = outAll;
+      inAll += ms[k]->N;
+      outAll += (size_t)ms[k]->nSignal * ms[k]->N;
+    }
+    g_ragged.in.reserve(inAll);
+    g_ragged.out.reserve(outAll);
+    g_ragged.hin.reserve(inAll);
+    g_ragged.hout.reserve(outAll);
+    for (size_t k : fused) std::memcpy(g_ragged.hin.p + inOff[k], inputs[k], ms[k]->N * sizeof(double2));
+    for (size_t k : fused)
+      if (withProp[k]) ms[k]->reservePropagator();
+    auto rowArgs = [&](Medium* m, size_t k, int R) {
+      PropArgs a = m->baseArgs(R);
+      a.inKind = 1;
+      a.inTime = in_time_domain ? 1 : 0;
+      a.in = g_ragged.in.p + inOff[k];
+      a.inStride = (long long)m->N;
+      a.inChannels = 1;
+      a.inputMode = 0;
+      a.nOut = (int)m->nSignal;
+      for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
+      a.out = g_ragged.out.p + outOff[k];
+      a.outStride = (long long)m->nSignal * m->N;
+      return a;
+    };
+    // one ragged launch per solver among the one-SM media, largest first; the launches share the
+    // plan's one-SM CTAs in proportion to their work
+    std::map<int, std::vector<size_t>> bySolver;   // job indices
+    double poolWork = 0;
+    for (size_t i = 0; i < jobs.size(); i++)
+      if (plan.form[i] == kOne) {
+        bySolver[ms[jobs[i].k]->solver].push_back(i);
+        poolWork += jobs[i].t[kOne];
+      }
+    struct RaggedLaunch {
+      const KernelEntry* ke;
+      int grid, block, first, count;
+      size_t smem;
+    };
+    std::vector<RaggedLaunch> raggedLaunches;
+    std::vector<PropArgs> items;
+    std::vector<size_t> itemJob;   // job index of every item
     for (auto& kv : bySolver) {
-      std::vector<size_t>& ks = kv.second;
-      for (size_t k : ks) ms[k]->ensureDevice();
-      // largest first (cost ~ nZSteps * modes * N log N)
-      std::sort(ks.begin(), ks.end(), [&](size_t x, size_t y) {
-        auto cost = [&](Medium* m) { return (double)m->nZ * m->nSignal * m->N * std::log2((double)m->N); };
-        return cost(ms[x]) > cost(ms[y]);
-      });
-      // The costliest media on grids of 1024+ points run as cluster-distributed propagations (4 SMs
-      // each, on their own streams, concurrently with the ragged launch of the others) while the
-      // clusters leave the ragged launch about one SM per two remaining media: it claims its media
-      // largest first from a work counter, so the smallest ones queue behind the others.
-      std::vector<size_t> clustered;
-      std::vector<bool> wide(n_media, false);
-      {
-        const int sms = Medium::smCount();
-        std::vector<size_t> others;
-        for (size_t k : ks) {
-          Medium* m = ms[k];
-          const bool eligible = m->useCluster && is_pow2((int)m->N) && m->N >= 1024 && m->N <= (uint)kMaxFFT &&
-                                m->findKernel(kKindCluster, m->solver, Medium::kClusterSize) != nullptr;
-          const size_t rest = ks.size() - clustered.size() - 1;   // the ragged launch's media if this one joins
-          if (eligible && (clustered.size() + 1) * Medium::kClusterSize + (rest + 1) / 2 <= (size_t)sms)
-            clustered.push_back(k);
-          else
-            others.push_back(k);   // still largest first
-        }
-        ks.swap(others);
-        // the costliest of them on 2048- and 4096-point grids take eight CTAs (one point per thread,
-        // twice the SMs) while the SMs allow, largest first
-        size_t used = clustered.size() * Medium::kClusterSize + (ks.size() + 1) / 2;
-        for (size_t k : clustered) {
-          Medium* m = ms[k];
-          if (m->wideGrid() && m->findKernel(kKindCluster, m->solver + kSpreadWideKey, 1) &&
-              used + (8 - Medium::kClusterSize) <= (size_t)sms) {
-            wide[k] = true;
-            used += 8 - Medium::kClusterSize;
-          }
-        }
+      std::vector<size_t>& js = kv.second;
+      std::sort(js.begin(), js.end(), [&](size_t a, size_t b) { return jobs[a].t[kOne] > jobs[b].t[kOne]; });
+      size_t maxN = 0;
+      double work = 0;
+      for (size_t i : js) {
+        maxN = std::max<size_t>(maxN, ms[jobs[i].k]->N);
+        work += jobs[i].t[kOne];
       }
-      if (!clustered.empty()) {
-        // Each cluster propagation runs on its medium's own stream: input copy (page-locked source),
-        // propagation, and -- after the ragged launch of the other media is queued, below -- the
-        // read-back.  No stream waits on another: CUDA maps the streams onto a few hardware queues,
-        // and a cross-stream wait at the head of one would hold back whatever shares its queue.
-        size_t io = cio, oo = coo;
-        for (size_t k : clustered) {
-          Medium* m = ms[k];
-          ck(cudaMemcpyAsync(g_ragged.cin.p + io, g_ragged.hin.p + hinOff[k], m->N * sizeof(double2),
-                             cudaMemcpyHostToDevice, m->stream),
-             "ragged input");
-          PropArgs a = m->baseArgs(m->chooseR());
-          a.inKind = 1;
-          a.inTime = in_time_domain ? 1 : 0;
-          a.in = g_ragged.cin.p + io;
-          a.inStride = (long long)m->N;
-          a.inChannels = 1;
-          a.inputMode = 0;
-          a.nOut = (int)m->nSignal;
-          for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
-          a.out = g_ragged.cout.p + oo;
-          a.outStride = (long long)m->nSignal * m->N;
-          m->raggedWide = wide[k];
-          try {
-            m->propagate(a, 1, m->raggedPropagator());
-          } catch (...) {
-            m->raggedWide = false;
-            throw;
-          }
-          m->raggedWide = false;
-          pendingD2H.push_back({g_ragged.hout.p + houtOff[k], g_ragged.cout.p + oo,
-                                (size_t)m->nSignal * m->N * sizeof(double2), m->stream});
-          clusterSync.push_back(m->stream);
-          io += m->N;
-          oo += (size_t)m->nSignal * m->N;
-        }
-        cio = io;
-        coo = oo;
-      }
-      if (ks.empty()) {
-        flushD2H();
-        continue;
-      }
-      size_t inTot = 0, outTot = 0, maxN = 0;
-      for (size_t k : ks) {
-        inTot += ms[k]->N;
-        outTot += (size_t)ms[k]->nSignal * ms[k]->N;
-        maxN = std::max<size_t>(maxN, ms[k]->N);
-      }
-      Medium* lead = ms[ks[0]];
-      cudaStream_t st = lead->stream;
-      // pump-driven solvers: each medium's per-point RK4 matrices when Medium::raggedPropagator wants
-      // them, built on the launch's stream just before it (each build is parallel over all steps and
-      // points of its medium); the media run as cluster propagations build theirs on their own streams
-      std::vector<bool> withProp(n_media, false);
-      for (size_t k : ks) {
-        Medium* m = ms[k];
-        if (m->raggedPropagator()) {
-          m->buildPropagator(8, st);
-          withProp[k] = true;
-        }
-      }
+      Medium* lead = ms[jobs[js[0]].k];
       // N/4 threads per medium when the largest grid allows it (four warps from N = 512), else N/8
       const KernelEntry* k4 = maxN / 4 <= 512 ? lead->findKernel(kKindRagged, kv.first, 4) : nullptr;
       const KernelEntry* ke = k4 ? k4 : lead->findKernel(kKindRagged, kv.first, 8);
       const int Rg = ke->R;
-      g_ragged.in.reserve(inTot);
-      g_ragged.out.reserve(outTot);
-      g_ragged.items.reserve(ks.size());
-      g_ragged.counter.reserve(1);
-      std::vector<PropArgs> items(ks.size());
-      std::vector<size_t> outOff(ks.size());
-      size_t io = 0, oo = 0;
-      for (size_t q = 0; q < ks.size(); q++) {
-        Medium* m = ms[ks[q]];
-        ck(cudaMemcpyAsync(g_ragged.in.p + io, g_ragged.hin.p + hinOff[ks[q]], m->N * sizeof(double2),
-                           cudaMemcpyHostToDevice, st),
-           "ragged input");
-        PropArgs a = m->baseArgs(Rg);
+      RaggedLaunch rl{ke, 0, (int)((maxN / Rg + 31) / 32 * 32), (int)items.size(), (int)js.size(), 0};
+      for (size_t i : js) {
+        Medium* m = ms[jobs[i].k];
+        PropArgs a = rowArgs(m, jobs[i].k, Rg);
         a.nInst = 1;
         a.ipc = 1;
-        a.inKind = 1;
-        a.inTime = in_time_domain ? 1 : 0;
-        a.in = g_ragged.in.p + io;
-        a.inStride = (long long)m->N;
-        a.inChannels = 1;
-        a.inputMode = 0;
-        a.nOut = (int)m->nSignal;
-        for (int mm = 0; mm < (int)m->nSignal; mm++) a.outModes[mm] = mm;
-        a.out = g_ragged.out.p + oo;
-        a.outStride = (long long)m->nSignal * m->N;
-        a.prop = withProp[ks[q]] ? m->prop.p : nullptr;
-        items[q] = a;
-        outOff[q] = oo;
-        io += m->N;
-        oo += (size_t)m->nSignal * m->N;
+        a.prop = withProp[jobs[i].k] ? m->prop.p : nullptr;
+        items.push_back(a);
+        itemJob.push_back(i);
       }
-      g_ragged.hitems.reserve(items.size());
-      std::memcpy(g_ragged.hitems.p, items.data(), items.size() * sizeof(PropArgs));
-      ck(cudaMemcpyAsync(g_ragged.items.p, g_ragged.hitems.p, items.size() * sizeof(PropArgs), cudaMemcpyHostToDevice,
-                         st),
-         "ragged items");
-      ck(cudaMemsetAsync(g_ragged.counter.p, 0, sizeof(unsigned long long), st), "ragged counter");
-      int block = (int)((maxN / Rg + 31) / 32 * 32);
-      int dev = 0, sms = 1;
-      ck(cudaGetDevice(&dev), "device");
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      // One CTA per SM: every medium is a sequential march bound by its SM's FP64 units, so a second
-      // resident CTA (of this launch or of a cluster propagation running beside it) would only halve
-      // both.  Asking for more than half of the SM's shared memory keeps the others off.
-      size_t smem = 0;
+      // One CTA per SM: every medium is a sequential march bound by its SM's FP64 units.  Asking for
+      // more than half of the SM's shared memory keeps other CTAs off its SM.
       cudaFuncAttributes fa;
-      ck(exclusive_smem(ke->fn, maxN * sizeof(double2), &smem, &fa), "smem attribute");
-      if (smem == 0) throw Unsupported("ragged kernel does not fit on an SM");
-      if (block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
-      int active = 0;
-      ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, ke->fn, block, smem), "occupancy");
-      if (active < 1) throw Unsupported("ragged kernel does not fit on an SM");
-      const int nItems = (int)ks.size();
-      // launched as clusters of four CTAs (each CTA still runs its own media): the hardware places a
-      // cluster on four SMs of one GPC, so the ragged CTAs take whole groups of four SMs and do not
-      // break up the groups that the cluster propagations launched beside them need
-      const int grid = (std::min(nItems, sms * active) + Medium::kClusterSize - 1) / Medium::kClusterSize *
-                       Medium::kClusterSize;
-      PropArgs* itemsD = g_ragged.items.p;
-      unsigned long long* ctr = g_ragged.counter.p;
-      int nIt = nItems;
-      void* args[] = {(void*)&itemsD, (void*)&nIt, (void*)&ctr};
-      if (lead->timeKernels) {
-        if (!lead->ev0) ck(cudaEventCreate(&lead->ev0), "event");
-        if (!lead->ev1) ck(cudaEventCreate(&lead->ev1), "event");
-        ck(cudaEventRecord(lead->ev0, st), "event");
-      }
-      ck(launch_clustered(ke->fn, grid, block, smem, st, Medium::kClusterSize, args), "ragged launch");
-      lead->launches++;
-      if (lead->timeKernels) {
-        ck(cudaEventRecord(lead->ev1, st), "event");
-        ck(cudaEventSynchronize(lead->ev1), "event");
-        float ms_ = 0;
-        ck(cudaEventElapsedTime(&ms_, lead->ev0, lead->ev1), "event");
-        lead->kernelMs += ms_;
-        lead->kernelCount++;
-      }
-      flushD2H();   // the cluster propagations' outputs (the ragged launch is queued by now)
-      for (size_t q = 0; q < ks.size(); q++) {
-        Medium* m = ms[ks[q]];
-        ck(cudaMemcpyAsync(g_ragged.hout.p + houtOff[ks[q]], g_ragged.out.p + outOff[q],
-                           (size_t)m->nSignal * m->N * sizeof(double2), cudaMemcpyDeviceToHost, st),
-           "ragged output");
-      }
-      ck(cudaStreamSynchronize(st), "ragged batch");
+      ck(exclusive_smem(ke->fn, maxN * sizeof(double2), &rl.smem, &fa), "smem attribute");
+      if (rl.smem == 0) throw Unsupported("ragged kernel does not fit on an SM");
+      if (rl.block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
+      const int share = (int)std::ceil(plan.poolSMs * (poolWork > 0 ? work / poolWork : 1.0));
+      // clusters of four CTAs: the ragged CTAs take whole groups of four SMs and leave the groups that
+      // the cluster slots need
+      rl.grid = (std::min<int>((int)js.size(), std::max(1, share)) + Medium::kClusterSize - 1) /
+                Medium::kClusterSize * Medium::kClusterSize;
+      raggedLaunches.push_back(rl);
     }
-    for (cudaStream_t st : clusterSync) ck(cudaStreamSynchronize(st), "ragged batch (clusters)");
+    g_ragged.items.reserve(std::max<size_t>(items.size(), 1));
+    g_ragged.hitems.reserve(std::max<size_t>(items.size(), 1));
+    if (!items.empty()) std::memcpy(g_ragged.hitems.p, items.data(), items.size() * sizeof(PropArgs));
+    g_ragged.counters.reserve(std::max<size_t>(raggedLaunches.size(), 1));
+    const size_t nStreams = 1 + plan.slots.size() + raggedLaunches.size();
+    g_ragged.ensureStreams(nStreams);
+    cudaStream_t origin = g_ragged.streams[0];
+
+    // ---- the call: one input copy, the slots and ragged launches on their streams, one output copy --
+    auto record = [&] {
+      ck(cudaMemcpyAsync(g_ragged.in.p, g_ragged.hin.p, inAll * sizeof(double2), cudaMemcpyHostToDevice, origin),
+         "ragged inputs");
+      if (!items.empty())
+        ck(cudaMemcpyAsync(g_ragged.items.p, g_ragged.hitems.p, items.size() * sizeof(PropArgs),
+                           cudaMemcpyHostToDevice, origin),
+           "ragged items");
+      if (!raggedLaunches.empty())
+        ck(cudaMemsetAsync(g_ragged.counters.p, 0, raggedLaunches.size() * sizeof(unsigned long long), origin),
+           "ragged counters");
+      ck(cudaEventRecord(g_ragged.events[0], origin), "ragged fork");
+      size_t si = 1;
+      for (size_t s = 0; s < plan.slots.size(); s++, si++) {
+        cudaStream_t st = g_ragged.streams[si];
+        ck(cudaStreamWaitEvent(st, g_ragged.events[0], 0), "ragged fork");
+        for (size_t i : plan.slots[s]) {
+          const size_t k = jobs[i].k;
+          Medium* m = ms[k];
+          const cudaStream_t own = m->stream;
+          m->stream = st;
+          m->raggedWide = plan.slotForm[s] == kW8;
+          try {
+            m->propagate(rowArgs(m, k, m->chooseR()), 1, withProp[k]);
+          } catch (...) {
+            m->stream = own;
+            m->raggedWide = false;
+            throw;
+          }
+          m->stream = own;
+          m->raggedWide = false;
+        }
+      }
+      for (size_t r = 0; r < raggedLaunches.size(); r++, si++) {
+        const RaggedLaunch& rl = raggedLaunches[r];
+        cudaStream_t st = g_ragged.streams[si];
+        ck(cudaStreamWaitEvent(st, g_ragged.events[0], 0), "ragged fork");
+        // the one-SM media's RK4 matrices, each built in parallel over all steps and points just before
+        for (int q = rl.first; q < rl.first + rl.count; q++) {
+          const size_t k = jobs[itemJob[q]].k;
+          if (needBuild[k]) ms[k]->buildPropagator(8, st);
+        }
+        PropArgs* itemsD = g_ragged.items.p + rl.first;
+        unsigned long long* ctr = g_ragged.counters.p + r;
+        int nIt = rl.count;
+        void* args[] = {(void*)&itemsD, (void*)&nIt, (void*)&ctr};
+        ck(launch_clustered(rl.ke->fn, rl.grid, rl.block, rl.smem, st, Medium::kClusterSize, args), "ragged launch");
+      }
+      for (size_t j = 1; j < si; j++) {
+        ck(cudaEventRecord(g_ragged.events[j], g_ragged.streams[j]), "ragged join");
+        ck(cudaStreamWaitEvent(origin, g_ragged.events[j], 0), "ragged join");
+      }
+      ck(cudaMemcpyAsync(g_ragged.hout.p, g_ragged.out.p, outAll * sizeof(double2), cudaMemcpyDeviceToHost, origin),
+         "ragged outputs");
+    };
+
+    // ---- one CUDA graph per plan: every host value the launches read goes into its key ----
+    bool useGraph = true;
+    GraphKey key;
+    key.add(in_time_domain).add(inAll).add(outAll).add(g_ragged.in.p).add(g_ragged.out.p).add(g_ragged.hin.p);
+    key.add(g_ragged.hout.p).add(g_ragged.items.p).add(g_ragged.hitems.p).add(g_ragged.counters.p);
+    for (size_t k : fused) {
+      Medium* m = ms[k];
+      useGraph = useGraph && m->useGraph && !m->timeKernels;
+      key.add(m).add((bool)withProp[k]).add((bool)needBuild[k]).add(m->prop.p).add(m->useCluster).add(m->ctaPerSM);
+      key.add(m->usePropagator).add(m->precision);
+      add_prop_key(key, rowArgs(m, k, m->chooseR()));
+    }
+    for (size_t s = 0; s < plan.slots.size(); s++) {
+      key.add(plan.slotForm[s]).add(plan.slots[s].size());
+      for (size_t i : plan.slots[s]) key.add(jobs[i].k);
+    }
+    for (const RaggedLaunch& rl : raggedLaunches) key.add(rl.ke->fn).add(rl.grid).add(rl.block).add(rl.smem);
+    for (const PropArgs& a : items) add_prop_key(key, a);
+    // a plan is captured the second time it comes (a one-off plan runs directly), then replayed
+    bool replayed = false;
+    if (useGraph && key.bytes == g_ragged.lastKey) {
+      replayed = g_ragged.graphs.run(key, origin, record);
+    } else {
+      record();
+    }
+    g_ragged.lastKey = key.bytes;
+    ck(cudaStreamSynchronize(origin), "ragged batch");
+    // host-side state of what ran: the matrices built; one launch per propagation, build and ragged
+    // launch (credited to the launch's largest medium)
+    for (size_t k : fused) {
+      Medium* m = ms[k];
+      m->launches = 0;
+      if (needBuild[k]) {
+        m->propVersion = m->pumpVersion;
+        if (replayed) m->propBuilds++;
+        m->launches++;
+      }
+    }
+    for (size_t i = 0; i < jobs.size(); i++)
+      if (plan.form[i] != kOne) ms[jobs[i].k]->launches++;
+    for (const RaggedLaunch& rl : raggedLaunches) ms[jobs[itemJob[rl.first]].k]->launches++;
+    g_lastRagged = RaggedStats{plan.makespan, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays};
+    for (int f : plan.slotForm) (f == kW8 ? g_lastRagged.slotsW8 : g_lastRagged.slotsC4)++;
+    for (const RaggedLaunch& rl : raggedLaunches) g_lastRagged.raggedCTAs += rl.grid;
     for (size_t k : fused)
-      std::memcpy(outputs[k], g_ragged.hout.p + houtOff[k], (size_t)ms[k]->nSignal * ms[k]->N * sizeof(double2));
+      std::memcpy(outputs[k], g_ragged.hout.p + outOff[k], (size_t)ms[k]->nSignal * ms[k]->N * sizeof(double2));
+  });
+}
+
+nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
+                                long* graph_captures, long* graph_replays) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lock(g_ragged.mu);
+    if (makespan_estimate_us) *makespan_estimate_us = g_lastRagged.makespan;
+    if (slots_c4) *slots_c4 = g_lastRagged.slotsC4;
+    if (slots_w8) *slots_w8 = g_lastRagged.slotsW8;
+    if (ragged_ctas) *ragged_ctas = g_lastRagged.raggedCTAs;
+    if (graph_captures) *graph_captures = g_lastRagged.captures;
+    if (graph_replays) *graph_replays = g_lastRagged.replays;
   });
 }
 

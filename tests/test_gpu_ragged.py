@@ -57,15 +57,12 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
         assert cases.rel_l2(o, t[0]) < TOL
 
 
-def test_ragged_set_with_cluster_propagations(nlm, oracle):
-    """The costliest media on grids of 1024+ points run as cluster propagations beside the ragged
-    launch of the others (one point per thread on four CTAs at 1024 points, on eight at 2048); every
-    output matches the oracle."""
+def _sfg_set(nlm, oracle, shapes, seed=21):
     kw0 = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=0.4, beta2s=-0.3, beta2o=0, beta1=0, beta1s=1.2,
                beta1o=0, beta3=0, beta3s=0.05, beta3o=0, diffBeta0=0, tMax=10)
-    rng = np.random.default_rng(21)
+    rng = np.random.default_rng(seed)
     media, refs, ins = [], [], []
-    for n, zp in ((2048, 14), (1024, 12), (256, 10), (128, 8), (1024, 6)):
+    for n, zp in shapes:
         kw = dict(kw0, tPrecision=n, zPrecision=zp)
         t = np.fft.fftshift(np.linspace(-10, 10, n, endpoint=False))
         pump = np.exp(-t ** 2 / 2)
@@ -76,14 +73,49 @@ def test_ragged_set_with_cluster_propagations(nlm, oracle):
         media.append(m)
         refs.append(r)
         ins.append(cases.noise(rng, n, 1e-2))
+    return media, refs, ins
+
+
+def test_ragged_set_with_cluster_propagations(nlm, oracle):
+    """The planner gives the longest march its fastest form (the 2048-point medium: one point per
+    thread on eight CTAs) and every other medium the form of least SM time that finishes within the
+    makespan; every output matches the oracle."""
+    media, refs, ins = _sfg_set(nlm, oracle, ((2048, 14), (1024, 12), (256, 10), (128, 8), (1024, 6)))
     outs = nlm.ragged_batch(media, ins)
-    for m in media:
-        s, n = m._last_schedule(), m._dims["nFreqs"]
-        want = {1024: (4, 1, 256), 2048: (8, 1, 256)}.get(n)
-        if want:
-            assert (s["grid"], s["R"], s["block"]) == want
-        else:
-            assert (s["grid"], s["R"]) not in ((4, 1), (8, 1), (4, 4))
+    plan = nlm.ragged_last_plan()
+    assert plan["slots_w8"] >= 1 and plan["makespan_estimate_ms"] > 0
+    s = media[0]._last_schedule()
+    assert (s["grid"], s["R"], s["block"]) == (8, 1, 256)
     for r, x, o in zip(refs, ins, outs):
         f, _ = r.propagate(x[None, :], False, 0)
         assert cases.rel_l2(o, f[0]) < TOL
+
+
+def test_ragged_call_replays_its_graph(nlm, oracle):
+    """The whole call (input copy, cluster slots, ragged launch, output copy) is captured once its plan
+    repeats and then replayed: the same outputs bit for bit, and a new pump is seen by the replay."""
+    media, refs, ins = _sfg_set(nlm, oracle, ((2048, 10), (1024, 8), (512, 9), (256, 6), (128, 7), (128, 5)), seed=5)
+    for m in media:
+        m._set_schedule(use_propagator=0)   # the DiffEq in every call: one plan throughout
+    first = nlm.ragged_batch(media, ins)
+    before = nlm.ragged_last_plan()
+    again = [nlm.ragged_batch(media, ins) for _ in range(3)]
+    after = nlm.ragged_last_plan()
+    assert after["graph_captures"] >= before["graph_captures"] + 1
+    assert after["graph_replays"] >= before["graph_replays"] + 2
+    for outs in again:
+        for o, o1 in zip(outs, first):
+            assert np.array_equal(o, o1)
+    for r, x, o in zip(refs, ins, first):
+        f, _ = r.propagate(x[None, :], False, 0)
+        assert cases.rel_l2(o, f[0]) < TOL
+    # a new pump (same buffers) is read by the replayed graph
+    t = np.fft.fftshift(np.linspace(-10, 10, 1024, endpoint=False))
+    media[1].setPump(np.exp(-t ** 2 / 3) + 0j)
+    refs[1].set_pump_custom(np.exp(-t ** 2 / 3) + 0j)
+    media[1].runPumpSimulation()
+    refs[1].run_pump_simulation()
+    outs = nlm.ragged_batch(media, ins)
+    f, _ = refs[1].propagate(ins[1][None, :], False, 0)
+    assert cases.rel_l2(outs[1], f[0]) < TOL
+    assert nlm.ragged_last_plan()["graph_replays"] > after["graph_replays"]
