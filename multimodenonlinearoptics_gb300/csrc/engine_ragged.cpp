@@ -6,7 +6,7 @@
 //   c4   -- a 4-CTA cluster on four SMs (one point per thread up to 1024 points, four from 2048);
 //   w8   -- an 8-CTA cluster on eight SMs, one point per thread (2048 and 4096 points).
 // The larger forms finish a medium sooner but spend more SM time on it.  The planner picks a target
-// makespan T by bisection: every medium takes the form of least SM time that finishes within T;
+// makespan T (the smallest feasible one, scanned upward): every medium takes the form of least SM time that finishes within T;
 // cluster-form media are packed first-fit, largest first, into slots (a stream running its media one
 // after another on 4 or 8 SMs); the one-SM media share the ragged launch.  T is feasible when the
 // slots and the ragged launch fit on the SMs at once.  The call is then enqueued on those streams
@@ -62,16 +62,24 @@ struct Plan {
   double makespan = 0;
 };
 
+// Largest-first list schedule of `times` (descending) on m one-SM CTAs: its makespan.  The ragged
+// launch's CTAs claim media in that order from a counter, which is this schedule.
+double lpt_makespan(const std::vector<double>& times, int m) {
+  std::vector<double> load((size_t)m, 0.0);
+  for (double t : times) *std::min_element(load.begin(), load.end()) += t;
+  return *std::max_element(load.begin(), load.end());
+}
+
 // Plan for target makespan T (us); false when the slots and the ragged launch need more than `sms` SMs.
 bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
   Plan p;
   p.form.assign(jobs.size(), -1);
-  std::vector<double> slotLoad;
-  double pool = 0, poolMax = 0;
+  std::vector<double> slotLoad, pool;
   // largest first (by the time of the fastest form)
   std::vector<size_t> order(jobs.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = i;
   std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a].best() > jobs[b].best(); });
+  int used = 0;
   for (size_t i : order) {
     const Job& j = jobs[i];
     // the form of least SM time that finishes within T
@@ -81,8 +89,7 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
     if (f < 0) return false;
     p.form[i] = f;
     if (f == kOne) {
-      pool += j.t[f];
-      poolMax = std::max(poolMax, j.t[f]);
+      pool.push_back(j.t[f]);
       continue;
     }
     size_t s = 0;
@@ -92,21 +99,23 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
       slotLoad.push_back(0);
       p.slotForm.push_back(f);
       p.slots.emplace_back();
+      used += kFormSMs[f];
     }
     slotLoad[s] += j.t[f];
     p.slots[s].push_back(i);
   }
-  // the ragged launch's CTAs take their media largest first from a counter: with m CTAs the last
-  // medium starts by pool / m and runs at most poolMax more
-  int m = 0;
-  if (pool > 0) {
-    const double room = T - poolMax;
-    m = room > 0 ? (int)std::ceil(pool / room) : sms + 1;
-    m = std::max(m, 1);
-  }
-  int used = m;
-  for (int f : p.slotForm) used += kFormSMs[f];
   if (used > sms) return false;
+  // the fewest one-SM CTAs whose largest-first schedule of the pool fits within T
+  int m = 0;
+  if (!pool.empty()) {
+    std::sort(pool.begin(), pool.end(), std::greater<double>());
+    double sum = 0;
+    for (double t : pool) sum += t;
+    m = std::max(1, (int)std::ceil(sum / T));
+    const int most = std::min<int>(sms - used, (int)pool.size());
+    while (m <= most && lpt_makespan(pool, m) > T) m++;
+    if (m > most) return false;
+  }
   p.poolSMs = m;
   p.makespan = T;
   *out = p;
@@ -208,19 +217,13 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       lo = std::max(lo, j.best());
       hi += j.t[kOne] >= 0 ? j.t[kOne] : j.best();
     }
+    // feasibility need not be monotonic in T (a medium at the edge of T moves between forms), so the
+    // targets are scanned upward in steps of 1 % and the first feasible one is taken
     Plan plan;
-    if (plan_for(jobs, hi, budget, &plan)) {
-      for (int it = 0; it < 40 && hi - lo > 0.002 * hi; it++) {
-        const double mid = 0.5 * (lo + hi);
-        Plan p;
-        if (plan_for(jobs, mid, budget, &p)) {
-          plan = p;
-          hi = mid;
-        } else {
-          lo = mid;
-        }
-      }
-    } else {
+    bool planned = false;
+    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.01) planned = plan_for(jobs, T, budget, &plan);
+    if (!planned) planned = plan_for(jobs, hi, budget, &plan);
+    if (!planned) {
       // no plan fits the SMs at once (more cluster-only media than they hold): every medium in its
       // fastest form, each cluster medium in a slot of its own, the slots queueing for SMs
       plan = Plan{};
