@@ -573,13 +573,21 @@ def measure_configs(nlm, torch, cpu=True):
         nlm.ragged_batch(media, ins)
         wall_direct.append(time.perf_counter() - t0)
     steps = sum(m._dims["nZSteps"] for m in media)
+    for m in media:
+        m._set_cluster(1)
+        m._set_schedule(use_propagator=-1)
+    for m in media:
+        m.runPumpSimulation()
+    nlm.ragged_batch(media, ins)
+    plan = nlm.ragged_last_plan()
     res["ragged_chi2sfg_64_media"] = {"gpu_wall_ms": 1e3 * min(wall), "media": len(media), "total_z_steps": steps,
                                       "n_freqs": sorted({m._dims["nFreqs"] for m in media}),
                                       "pumps": "rerun before each call: every medium propagates with its DiffEq "
                                                "(RK4 matrices are built only for a pump used again)",
                                       "gpu_wall_ms_pumps_kept": 1e3 * min(wall_kept),
-                                      "form": "the costliest media on grids of 1024+ points as 4-CTA cluster "
-                                              "propagations beside one ragged launch of the others",
+                                      "form": "each medium on one SM in a ragged launch or on a 4- or 8-SM cluster "
+                                              "slot, planned for the makespan; the call replayed as a CUDA graph",
+                                      "plan": plan,
                                       "gpu_wall_ms_one_cta_per_medium": 1e3 * min(wall_one),
                                       "gpu_wall_ms_one_cta_diffeq_form": 1e3 * min(wall_direct)}
     # the oracle of configuration 3 (all 64 media at their full step counts) in spawned processes, and

@@ -158,10 +158,12 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
 /* The plan of the last nlm_ragged_batch call: its estimated makespan (microseconds), the cluster
- * slots of four and eight SMs, the CTAs of its one-SM ragged launches, and the CUDA-graph captures and
- * replays of ragged calls so far.  No counterpart in the reference (measurement support). */
+ * slots of four and eight SMs, the CTAs of its one-SM ragged launches, the CUDA-graph captures and
+ * replays of ragged calls so far, and the SMs the plan could use (those clusters of four can hold at
+ * once; the environment variable NLM_RAGGED_CLUSTER_SMS overrides the measured figure).  No
+ * counterpart in the reference (measurement support). */
 nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
-                                long* graph_captures, long* graph_replays);
+                                long* graph_captures, long* graph_replays, int* sm_budget);
 
 /* --- gradients (no counterpart in the reference) -------------------------------------------
  * Reverse-mode gradients of a functional L of the output spectra of a Chi2PDC batch with respect to

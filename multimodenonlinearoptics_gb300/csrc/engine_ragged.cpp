@@ -12,6 +12,9 @@
 // slots and the ragged launch fit on the SMs at once.  The call is then enqueued on those streams
 // (inputs in one copy, outputs in one copy) and captured into a CUDA graph, replayed by later calls
 // with the same plan.
+#include <cstdlib>
+#include <map>
+
 #include "engine.h"
 
 using nlm::guarded;
@@ -45,6 +48,7 @@ double step_us(int form, uint N, uint modes, bool prop) {
 
 struct Job {
   size_t k;                  // index in the call's media
+  int cls;                   // ragged launch class: media of one solver and one grid share a launch
   double t[kForms];          // estimated march time per form (us); < 0: form not available
   double best() const {
     double b = -1;
@@ -59,6 +63,7 @@ struct Plan {
   std::vector<std::vector<size_t>> slots;   // cluster slots: job indices in launch order
   std::vector<int> slotForm;
   int poolSMs = 0;                          // CTAs of the ragged launches
+  std::map<int, int> classCTAs;             // per ragged launch class: its fewest CTAs (multiple of 4)
   double makespan = 0;
 };
 
@@ -74,7 +79,7 @@ double lpt_makespan(const std::vector<double>& times, int m) {
 bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
   Plan p;
   p.form.assign(jobs.size(), -1);
-  std::vector<double> slotLoad, pool;
+  std::vector<double> slotLoad;
   // largest first (by the time of the fastest form)
   std::vector<size_t> order(jobs.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = i;
@@ -88,10 +93,7 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
       if (j.t[c] >= 0 && j.t[c] <= T && (f < 0 || j.t[c] * kFormSMs[c] < j.t[f] * kFormSMs[f])) f = c;
     if (f < 0) return false;
     p.form[i] = f;
-    if (f == kOne) {
-      pool.push_back(j.t[f]);
-      continue;
-    }
+    if (f == kOne) continue;
     size_t s = 0;
     for (; s < slotLoad.size(); s++)
       if (p.slotForm[s] == f && slotLoad[s] + j.t[f] <= T) break;
@@ -105,22 +107,56 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
     p.slots[s].push_back(i);
   }
   if (used > sms) return false;
-  // the fewest one-SM CTAs whose largest-first schedule of the pool fits within T
+  // per ragged launch class (the CTAs of a launch are sized for its grid), the fewest one-SM CTAs
+  // whose largest-first schedule fits within T, in clusters of four
+  std::map<int, std::vector<double>> byClass;
+  for (size_t i : order)
+    if (p.form[i] == kOne) byClass[jobs[i].cls].push_back(jobs[i].t[kOne]);
   int m = 0;
-  if (!pool.empty()) {
+  for (auto& kv : byClass) {
+    std::vector<double>& pool = kv.second;
     std::sort(pool.begin(), pool.end(), std::greater<double>());
     double sum = 0;
     for (double t : pool) sum += t;
-    m = std::max(1, (int)std::ceil(sum / T));
-    const int most = std::min<int>(sms - used, (int)pool.size());
-    while (m <= most && lpt_makespan(pool, m) > T) m++;
-    if (m > most) return false;
+    int mc = std::max(1, (int)std::ceil(sum / T));
+    while (mc < (int)pool.size() && lpt_makespan(pool, mc) > T) mc++;
+    if (lpt_makespan(pool, mc) > T) return false;
+    mc = (mc + 3) / 4 * 4;
+    p.classCTAs[kv.first] = mc;
+    m += mc;
   }
+  if (used + m > sms) return false;
   p.poolSMs = m;
   p.makespan = T;
   *out = p;
   return true;
 }
+
+// SMs that clusters of four CTAs, each CTA alone on its SM, can hold at once: every cluster sits in
+// one GPC, so the SMs of a GPC beyond a multiple of four stay out of reach (on a GB300 with 19 SMs per
+// GPC, 128 of the 152).  Measured once per process with the occupancy API on `fn`.
+// NLM_RAGGED_CLUSTER_SMS overrides the measured figure.
+int cluster_capacity_sms(const void* fn, int sms) {
+  static int cached = 0;
+  if (cached) return cached;
+  if (const char* env = std::getenv("NLM_RAGGED_CLUSTER_SMS")) {
+    const int v = std::atoi(env);
+    if (v >= 4) return cached = std::min(v, sms);
+  }
+  size_t smem = 0;
+  int cap = sms - 4;
+  if (exclusive_smem(fn, 1024 * sizeof(double2), &smem) == cudaSuccess && smem) {
+    cudaLaunchAttribute attr;
+    cudaLaunchConfig_t cfg = cluster_config(4 * sms, 128, smem, nullptr, 4, &attr);
+    int n = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, fn, &cfg);
+    if (e == cudaSuccess && n > 0) cap = std::min(cap, 4 * n);
+    else cudaGetLastError();
+  }
+  cached = cap;
+  return cached;
+}
+int g_capacityUsed = 0;
 
 }  // namespace
 
@@ -158,8 +194,9 @@ struct RaggedStats {
   double makespan;
   int slotsC4, slotsW8, raggedCTAs;
   long captures, replays;
+  int budget;
 };
-static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0};
+static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0, 0};
 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
                             double* const* outputs) {
@@ -199,7 +236,9 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     std::vector<Job> jobs;
     for (size_t k : fused) {
       Medium* m = ms[k];
-      Job j{k, {-1, -1, -1}};
+      int lg = 0;
+      while ((1u << lg) < m->N) lg++;
+      Job j{k, m->solver * 64 + lg, {-1, -1, -1}};
       const double steps = (double)(m->nZ > 1 ? m->nZ - 1 : 1);
       j.t[kOne] = step_us(kOne, m->N, m->nSignal, withProp[k]) * steps;
       // four CTAs: one point per thread on the spread grids, four points per thread from 1024 points
@@ -209,9 +248,12 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         j.t[kW8] = step_us(kW8, m->N, m->nSignal, withProp[k]) * steps;
       jobs.push_back(j);
     }
-    // bisection on the makespan between the longest medium in its fastest form and every medium on
-    // one SM one after another; a few SMs are left for the placement of the clusters
-    const int budget = std::max(1, sms - 4);
+    // the makespan lies between the longest medium in its fastest form and every medium on one SM one
+    // after another; the plan may use the SMs that clusters of four can hold at once (the slots and
+    // the ragged launches are all launched as clusters)
+    const int budget = std::max(4, cluster_capacity_sms(ms[fused[0]]->findKernel(kKindRagged, ms[fused[0]]->solver, 8)->fn,
+                                                        sms));
+    g_capacityUsed = budget;
     double lo = 0, hi = 0;
     for (const Job& j : jobs) {
       lo = std::max(lo, j.best());
@@ -236,9 +278,21 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         if (f != kOne) {
           plan.slots.push_back({i});
           plan.slotForm.push_back(f);
+        } else {
+          plan.classCTAs[jobs[i].cls] += 1;
         }
       }
-      plan.poolSMs = sms;
+      plan.poolSMs = 0;
+      for (auto& kv : plan.classCTAs) plan.poolSMs += (kv.second = (kv.second + 3) / 4 * 4);
+    }
+
+    // The plan's one-SM CTAs are the fewest that fit its target; the SMs the slots leave free all go to
+    // the ragged launches (one CTA per medium at most), a margin against the estimates.
+    int leftover = 0;
+    {
+      int slotSMs = 0;
+      for (int f : plan.slotForm) slotSMs += kFormSMs[f];
+      leftover = std::max(0, (budget - slotSMs - plan.poolSMs) / 4 * 4);
     }
 
     // ---- buffers, staging and the ragged launches' items (nothing is allocated inside the graph) ----
@@ -271,13 +325,13 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       a.outStride = (long long)m->nSignal * m->N;
       return a;
     };
-    // one ragged launch per solver among the one-SM media, largest first; the launches share the
-    // plan's one-SM CTAs in proportion to their work
-    std::map<int, std::vector<size_t>> bySolver;   // job indices
+    // one ragged launch per class (solver and grid) among the one-SM media, largest first, each with the
+    // plan's CTAs for it and a share of the SMs left over (in proportion to its work)
+    std::map<int, std::vector<size_t>> byClass;   // job indices
     double poolWork = 0;
     for (size_t i = 0; i < jobs.size(); i++)
       if (plan.form[i] == kOne) {
-        bySolver[ms[jobs[i].k]->solver].push_back(i);
+        byClass[jobs[i].cls].push_back(i);
         poolWork += jobs[i].t[kOne];
       }
     struct RaggedLaunch {
@@ -288,8 +342,9 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     std::vector<RaggedLaunch> raggedLaunches;
     std::vector<PropArgs> items;
     std::vector<size_t> itemJob;   // job index of every item
-    for (auto& kv : bySolver) {
+    for (auto& kv : byClass) {
       std::vector<size_t>& js = kv.second;
+      const int solver = ms[jobs[js[0]].k]->solver;
       std::sort(js.begin(), js.end(), [&](size_t a, size_t b) { return jobs[a].t[kOne] > jobs[b].t[kOne]; });
       size_t maxN = 0;
       double work = 0;
@@ -299,8 +354,8 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       Medium* lead = ms[jobs[js[0]].k];
       // N/4 threads per medium when the largest grid allows it (four warps from N = 512), else N/8
-      const KernelEntry* k4 = maxN / 4 <= 512 ? lead->findKernel(kKindRagged, kv.first, 4) : nullptr;
-      const KernelEntry* ke = k4 ? k4 : lead->findKernel(kKindRagged, kv.first, 8);
+      const KernelEntry* k4 = maxN / 4 <= 512 ? lead->findKernel(kKindRagged, solver, 4) : nullptr;
+      const KernelEntry* ke = k4 ? k4 : lead->findKernel(kKindRagged, solver, 8);
       const int Rg = ke->R;
       RaggedLaunch rl{ke, 0, (int)((maxN / Rg + 31) / 32 * 32), (int)items.size(), (int)js.size(), 0};
       for (size_t i : js) {
@@ -318,11 +373,11 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       ck(exclusive_smem(ke->fn, maxN * sizeof(double2), &rl.smem, &fa), "smem attribute");
       if (rl.smem == 0) throw Unsupported("ragged kernel does not fit on an SM");
       if (rl.block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
-      const int share = (int)std::ceil(plan.poolSMs * (poolWork > 0 ? work / poolWork : 1.0));
-      // clusters of four CTAs: the ragged CTAs take whole groups of four SMs and leave the groups that
-      // the cluster slots need
-      rl.grid = (std::min<int>((int)js.size(), std::max(1, share)) + Medium::kClusterSize - 1) /
-                Medium::kClusterSize * Medium::kClusterSize;
+      // launched in clusters of four CTAs: the ragged CTAs take whole groups of four SMs and leave the
+      // groups that the cluster slots need
+      const int extra = (int)((double)leftover * (poolWork > 0 ? work / poolWork : 1.0)) / 4 * 4;
+      const int most = ((int)js.size() + 3) / 4 * 4;
+      rl.grid = std::min(most, std::max(4, plan.classCTAs[kv.first] + extra));
       raggedLaunches.push_back(rl);
     }
     g_ragged.items.reserve(std::max<size_t>(items.size(), 1));
@@ -430,7 +485,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (size_t i = 0; i < jobs.size(); i++)
       if (plan.form[i] != kOne) ms[jobs[i].k]->launches++;
     for (const RaggedLaunch& rl : raggedLaunches) ms[jobs[itemJob[rl.first]].k]->launches++;
-    g_lastRagged = RaggedStats{plan.makespan, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays};
+    g_lastRagged = RaggedStats{plan.makespan, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays, budget};
     for (int f : plan.slotForm) (f == kW8 ? g_lastRagged.slotsW8 : g_lastRagged.slotsC4)++;
     for (const RaggedLaunch& rl : raggedLaunches) g_lastRagged.raggedCTAs += rl.grid;
     for (size_t k : fused)
@@ -439,9 +494,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
 }
 
 nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
-                                long* graph_captures, long* graph_replays) {
+                                long* graph_captures, long* graph_replays, int* sm_budget) {
   return guarded([&] {
     std::lock_guard<std::mutex> lock(g_ragged.mu);
+    if (sm_budget) *sm_budget = g_lastRagged.budget;
     if (makespan_estimate_us) *makespan_estimate_us = g_lastRagged.makespan;
     if (slots_c4) *slots_c4 = g_lastRagged.slotsC4;
     if (slots_w8) *slots_w8 = g_lastRagged.slotsW8;

@@ -62,7 +62,7 @@ def _load():
         "nlm_batch": (i, [vp, P(d), sz, sz, i, i, u, u, P(u8), sz, P(d)]),
         "nlm_batch_device": (i, [vp, vp, sz, sz, i, i, u, u, P(u8), sz, vp]),
         "nlm_ragged_batch": (i, [P(vp), sz, P(P(d)), i, P(P(d))]),
-        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long)]),
+        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i)]),
         "nlm_get_grid": (i, [vp, i, u, P(P(d)), P(sz), P(sz)]),
         "nlm_get_axis": (i, [vp, i, u, P(P(d)), P(sz)]),
         "nlm_cascade_create": (i, [P(vp), sz, P(u), P(sz), sz, i, P(vp)]),
@@ -158,14 +158,15 @@ def ragged_batch(media, inputs, inTimeDomain=False):
 
 def ragged_last_plan():
     """The plan of the last ragged_batch call (no counterpart in the reference): estimated makespan
-    (ms), cluster slots of four and eight SMs, CTAs of the one-SM ragged launches, and the CUDA-graph
-    captures and replays of ragged calls so far."""
+    (ms), cluster slots of four and eight SMs, CTAs of the one-SM ragged launches, the CUDA-graph
+    captures and replays of ragged calls so far, and the SMs the plan could use."""
     ms, c4, w8, ctas = ctypes.c_double(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    cap, rep = ctypes.c_long(), ctypes.c_long()
+    cap, rep, budget = ctypes.c_long(), ctypes.c_long(), ctypes.c_int()
     _check(_lib.nlm_ragged_last_plan(ctypes.byref(ms), ctypes.byref(c4), ctypes.byref(w8), ctypes.byref(ctas),
-                                     ctypes.byref(cap), ctypes.byref(rep)))
+                                     ctypes.byref(cap), ctypes.byref(rep), ctypes.byref(budget)))
     return {"makespan_estimate_ms": ms.value / 1e3, "slots_c4": c4.value, "slots_w8": w8.value,
-            "ragged_ctas": ctas.value, "graph_captures": cap.value, "graph_replays": rep.value}
+            "ragged_ctas": ctas.value, "graph_captures": cap.value, "graph_replays": rep.value,
+            "sm_budget": budget.value}
 
 
 def fp64_peak_tflops():
