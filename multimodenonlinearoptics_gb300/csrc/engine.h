@@ -1562,14 +1562,32 @@ struct Medium {
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
     if (wideLaunch(a) && nInst * 8 <= smCount())
-      if (const KernelEntry* kw = findKernel(kKindCluster, solver + kSpreadWideKey, 1)) return kw;
+      if (const KernelEntry* kw = findKernel(kKindCluster, solver + kSpreadWideKey, 1)) return fusedSpread(kw, 8);
     if (nInst * kClusterSize > smCount()) return nullptr;
     // the spread grids: one point per thread (the Chi2PDC reverse sweep has the same form,
     // adjoint_spread.cu; Chi3GNLSE, whose forward stores stage values, has no spread kernel)
     if (spreadGrid() && !a.stages)
-      if (const KernelEntry* ks = findKernel(kKindCluster, solver, 1)) return ks;
+      if (const KernelEntry* ks = findKernel(kKindCluster, solver, 1)) return fusedSpread(ks, kClusterSize);
     if (N < 1024) return nullptr;
     return findKernel(kKindCluster, solver, kClusterSize);
+  }
+
+  // The kernel of a multi-mode solver that transforms its modes together (kKindSpreadFused), in place of
+  // the one-point-per-thread cluster kernel k of C CTAs, when its buffers fit in shared memory.
+  const KernelEntry* fusedSpread(const KernelEntry* k, int C) const {
+    if (nSignal < 2) return k;
+    const KernelEntry* kf = findKernel(kKindSpreadFused, k->key, 1);
+    if (!kf) return k;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, kf->fn) != cudaSuccess) {
+      cudaGetLastError();
+      return k;
+    }
+    const long long need = spread_smem_per_point_k(C, (int)nSignal) * (long long)(N / C) * (long long)sizeof(double2);
+    return need + (long long)fa.sharedSizeBytes <= optin ? kf : k;
   }
 
   void launchCluster(const KernelEntry* k, PropArgs a, long long nInst) {
@@ -1587,7 +1605,9 @@ struct Medium {
     // CTAs of a ragged launch
     size_t smem = 0;
     cudaFuncAttributes fa;
-    const size_t need = (size_t)(spread ? spread_smem_per_point(C) : 5LL) * M * sizeof(double2);
+    const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(C, (int)nSignal)
+                               : (spread ? spread_smem_per_point(C) : 5LL);
+    const size_t need = (size_t)perPoint * M * sizeof(double2);
     ck(exclusive_smem(k->fn, need, &smem, &fa), "smem attribute");
     if (smem == 0) throw Unsupported("grid too large for the cluster kernel");
     const long long clusters = std::min<long long>(nInst, smCount() / C);

@@ -33,8 +33,8 @@ constexpr int kFormSMs[kForms] = {1, 4, 8};
 // the table's end, smaller ones take the 128-point time (latency-bound); other solvers scale with
 // their mode count.
 constexpr double kStepUs[2][kForms][5] = {
-    {{26.3, 27.8, 34.7, 67.8, 137.6}, {9.6, 10.8, 13.7, 24.4, 41.7}, {0, 0, 0, 0, 30.7}},
-    {{18.3, 19.7, 27.8, 51.8, 99.3}, {7.6, 8.8, 11.7, 20.0, 33.6}, {0, 0, 0, 0, 26.6}}};
+    {{26.4, 27.9, 34.8, 67.9, 137.8}, {8.8, 9.7, 11.6, 21.8, 41.8}, {0, 0, 0, 0, 27.4}},
+    {{18.4, 19.9, 27.8, 51.8, 99.5}, {6.7, 7.6, 9.4, 17.2, 33.7}, {0, 0, 0, 0, 23.4}}};
 
 double step_us(int form, uint N, uint modes, bool prop) {
   int lg = 0;

@@ -31,6 +31,7 @@ void add_kernels_gen_b(std::vector<KernelEntry>& t);
 void add_kernels_gen_c(std::vector<KernelEntry>& t);
 void add_kernels_gen_d(std::vector<KernelEntry>& t);
 void add_kernels_gen_e(std::vector<KernelEntry>& t);
+void add_kernels_spread_fused(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -58,6 +59,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_gen_c(table);
     add_kernels_gen_d(table);
     add_kernels_gen_e(table);
+    add_kernels_spread_fused(table);
   });
   *count = (int)table.size();
   return table.data();

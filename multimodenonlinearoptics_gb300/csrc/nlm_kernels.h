@@ -98,7 +98,8 @@ enum KernelKind : int {
   kKindAdjoint = 4,    // k_adjoint_pdc<R>                   key = solver id; args (PropArgs, AdjArgs)
   kKindRagged = 5,     // k_propagate_ragged<Solver, R>      key = solver id; args (items, nItems, work)
   kKindLinearFF = 6,   // k_propagate_linear_ff<R, SMALL>    key = M + 10 SMALL; args (PropArgs, FFTables)
-  kKindCluster = 7     // k_propagate_cluster<Solver, C>     key = solver id, R = C; cluster launch
+  kKindCluster = 7,    // k_propagate_cluster<Solver, C>     key = solver id, R = C; cluster launch
+  kKindSpreadFused = 8 // k_propagate_spread<Solver, C, M>   key as kKindCluster (R = 1): modes transformed together
 };
 
 // Float-float copies (float4 {re.hi, re.lo, im.hi, im.lo} per complex value) of the tables of a
@@ -139,6 +140,9 @@ cudaError_t launch_pump_chi3_cluster(double2* pumpFreq, double2* pumpTime, const
 // double2 values per point of the CTA: M-point twiddles, two exchange buffers, two halves of C receive
 // rows.
 constexpr long long spread_smem_per_point(int C) { return 3 + 2LL * C; }
+// The same for the kernels that transform their K modes together (kKindSpreadFused): twiddles, two
+// K-field exchange buffers, two halves of C x K receive rows.
+constexpr long long spread_smem_per_point_k(int C, int K) { return 1 + 2LL * K + 2LL * C * K; }
 constexpr long long kSpreadSmemPerPoint = spread_smem_per_point(4);
 // Registry key offset of the instantiations for the general plan (FFTPlanH::gen == 1): grids that are
 // not powers of two (kKindDirect, kKindLinear, kKindGnlse).

@@ -42,8 +42,9 @@ struct SpreadFFT {
 };
 
 // Sets up the spread transform of this CTA: the M-point twiddles (every C-th entry of the N-point
-// table `tw`) and this thread's cluster twiddle.  Ends with a CTA barrier.
-template <int C = kSpreadC>
+// table `tw`) and this thread's cluster twiddle.  Ends with a CTA barrier.  K: fields transformed
+// together (spread_fwd_k, spread_inv_store_k), which sizes the exchange and receive buffers.
+template <int C = kSpreadC, int K = 1>
 __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const double2* __restrict__ tw, int M,
                                             int rank) {
   f.M = M;
@@ -54,7 +55,7 @@ __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const d
   f.base = 0;
   double2* twM = smem;
   f.buf = smem + M;
-  f.recv = smem + 3 * M;
+  f.recv = smem + (1 + 2 * K) * M;
   for (int k = threadIdx.x; k < M; k += blockDim.x) twM[k] = tw[(long long)k * C];
   f.twM = twM;
   f.twC = tw[(long long)rank * f.j];
@@ -94,20 +95,9 @@ __device__ __forceinline__ double2 spread_local(SpreadFFT& f, double2 x) {
   return x;
 }
 
-// C-point DFT over the cluster's CTAs: thread j of every CTA pushes y to column j of row `rank` in all
-// C CTAs; after the barrier thread j of CTA r returns sum_c W_C^(+-r c) recv[c][j].
-template <bool INV, int C = kSpreadC>
-__device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::cluster_group& cl) {
-  static_assert(C == 4 || C == 8, "four or eight CTAs");
-  const int M = f.M;
-  double2* half = f.recv + (long long)f.phase * C * M;
-#pragma unroll
-  for (int v = 0; v < C; v++) *cl.map_shared_rank(half + f.rank * M + f.j, f.base + v) = y;
-  cl.sync();
-  double2 r[C];
-#pragma unroll
-  for (int c = 0; c < C; c++) r[c] = half[c * M + f.j];
-  f.phase ^= 1;
+// C-point DFT of the values r[c] of this thread's column: sum_c W_C^(+-rank c) r[c].
+template <bool INV, int C>
+__device__ __forceinline__ double2 spread_combine(const SpreadFFT& f, const double2 (&r)[C]) {
   const int rk = f.rank;
   const double sg = (rk & 1) ? -1.0 : 1.0;   // W_C^(r C/2) = (-1)^r
   // W_4^(+-r) b for the four quarter turns: 1, -i, -1, i (forward); conjugates for the inverse
@@ -133,10 +123,113 @@ __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::
     const double2 q2 = quarter(u[2]), q3 = quarter(u[3]);
     const double2 v0 = make_double2(u[0].x + q2.x, u[0].y + q2.y);
     const double2 v1 = make_double2(u[1].x + q3.x, u[1].y + q3.y);
-    const double2 w = f.twM[rk * (M / 8)];      // W_8^r = W_M^(r M / 8)
+    const double2 w = f.twM[rk * (f.M / 8)];    // W_8^r = W_M^(r M / 8)
     const double wy = INV ? -w.y : w.y;
     return make_double2(fma(-wy, v1.y, fma(w.x, v1.x, v0.x)), fma(wy, v1.x, fma(w.x, v1.y, v0.y)));
   }
+}
+
+// C-point DFT over the cluster's CTAs: thread j of every CTA pushes y to column j of row `rank` in all
+// C CTAs; after the barrier thread j of CTA r returns sum_c W_C^(+-r c) recv[c][j].
+template <bool INV, int C = kSpreadC>
+__device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::cluster_group& cl) {
+  static_assert(C == 4 || C == 8, "four or eight CTAs");
+  const int M = f.M;
+  double2* half = f.recv + (long long)f.phase * C * M;
+#pragma unroll
+  for (int v = 0; v < C; v++) *cl.map_shared_rank(half + f.rank * M + f.j, f.base + v) = y;
+  cl.sync();
+  double2 r[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) r[c] = half[c * M + f.j];
+  f.phase ^= 1;
+  return spread_combine<INV, C>(f, r);
+}
+
+// ---- K fields at once (the modes of a multi-mode solver): the same transforms with one barrier per
+// stage and one cluster barrier per exchange for all K, and K independent chains in flight per thread.
+// Buffers: [2][K][M] exchange, [2][C][K][M] receive.
+template <bool INV, int K>
+__device__ __forceinline__ void spread_local_k(SpreadFFT& f, double2 (&x)[K]) {
+  const int M = f.M, t = f.j, half = M >> 1;
+  {
+    double2* b = f.buf + f.sel * K * M;
+#pragma unroll
+    for (int m = 0; m < K; m++) b[m * M + t] = x[m];
+    __syncthreads();
+    const int p = t >> 1;
+    const double s = (t & 1) ? -1.0 : 1.0;
+#pragma unroll
+    for (int m = 0; m < K; m++) {
+      const double2 e = b[m * M + p], o = b[m * M + p + half];
+      x[m] = make_double2(fma(s, o.x, e.x), fma(s, o.y, e.y));
+    }
+    f.sel ^= 1;
+  }
+  for (int L = 2, shift = 1; L < M; L <<= 1, shift++) {
+    double2* b = f.buf + f.sel * K * M;
+#pragma unroll
+    for (int m = 0; m < K; m++) b[m * M + t] = x[m];
+    __syncthreads();
+    const int kp = t & (2 * L - 1);
+    const int k = kp & (L - 1);
+    const int src = k + L * (t >> (shift + 1));
+    const double2 w = f.twM[kp * (half >> shift)];
+    const double wy = INV ? -w.y : w.y;
+#pragma unroll
+    for (int m = 0; m < K; m++) {
+      const double2 e = b[m * M + src], o = b[m * M + src + half];
+      x[m].x = fma(-wy, o.y, fma(w.x, o.x, e.x));
+      x[m].y = fma(wy, o.x, fma(w.x, o.y, e.y));
+    }
+    f.sel ^= 1;
+  }
+}
+
+template <bool INV, int C, int K>
+__device__ __forceinline__ void spread_exchange_k(SpreadFFT& f, double2 (&y)[K], cg::cluster_group& cl) {
+  static_assert(C == 4 || C == 8, "four or eight CTAs");
+  const int M = f.M;
+  double2* half = f.recv + (long long)f.phase * C * K * M;
+#pragma unroll
+  for (int v = 0; v < C; v++) {
+    double2* dst = cl.map_shared_rank(half + (long long)f.rank * K * M + f.j, f.base + v);
+#pragma unroll
+    for (int m = 0; m < K; m++) dst[m * M] = y[m];
+  }
+  cl.sync();
+#pragma unroll
+  for (int m = 0; m < K; m++) {
+    double2 r[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) r[c] = half[((long long)c * K + m) * M + f.j];
+    y[m] = spread_combine<INV, C>(f, r);
+  }
+  f.phase ^= 1;
+}
+
+// time-domain ownership -> frequency-domain ownership, K fields
+template <int C, int K>
+__device__ __forceinline__ void spread_fwd_k(SpreadFFT& f, double2 (&x)[K], cg::cluster_group& cl) {
+  spread_local_k<false, K>(f, x);
+#pragma unroll
+  for (int m = 0; m < K; m++) x[m] = cmul(x[m], f.twC);
+  spread_exchange_k<false, C, K>(f, x, cl);
+}
+
+// frequency-domain ownership -> time-domain ownership (unscaled), K fields; store(m, v) receives each
+// field's frequency-domain value right after the exchange's cluster barrier (see spread_inv_store)
+template <int C, int K, class Store>
+__device__ __forceinline__ void spread_inv_store_k(SpreadFFT& f, double2 (&x)[K], cg::cluster_group& cl, Store store) {
+  double2 y[K];
+#pragma unroll
+  for (int m = 0; m < K; m++) y[m] = x[m];
+  spread_exchange_k<true, C, K>(f, y, cl);
+#pragma unroll
+  for (int m = 0; m < K; m++) store(m, x[m]);
+#pragma unroll
+  for (int m = 0; m < K; m++) x[m] = cmulc(y[m], f.twC);
+  spread_local_k<true, K>(f, x);
 }
 
 // n bare cluster barriers: the transform slots of a group that has no transform to do while the other

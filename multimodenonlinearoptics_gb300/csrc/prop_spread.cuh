@@ -46,17 +46,47 @@ __global__ void __launch_bounds__(kMaxThreads) k_pump_chi3_spread(double2* __res
   pt[last + tn] = cscale(spread_inv_store<C>(f, x, cl, [&](double2 v) { pf[last + fk] = v; }), invN);
 }
 
+// All MD modes: time -> frequency domain; K = MD together, K = 1 one after another.
+template <int C, int K, int MD>
+__device__ __forceinline__ void spread_fwd_all(SpreadFFT& f, double2 (&x)[MD], cg::cluster_group& cl) {
+  if constexpr (K > 1) {
+    spread_fwd_k<C, MD>(f, x, cl);
+  } else {
+#pragma unroll
+    for (int m = 0; m < MD; m++) x[m] = spread_fwd<C>(f, x[m], cl);
+  }
+}
+
+// All MD modes: frequency -> time domain, store(m, v) given each mode's spectrum after its exchange.
+template <int C, int K, int MD, class Store>
+__device__ __forceinline__ void spread_inv_all(SpreadFFT& f, double2 (&x)[MD], cg::cluster_group& cl, Store store) {
+  if constexpr (K > 1) {
+    spread_inv_store_k<C, MD>(f, x, cl, store);
+  } else {
+#pragma unroll
+    for (int m = 0; m < MD; m++) {
+      const int mm = m;
+      x[m] = spread_inv_store<C>(f, x[m], cl, [&](double2 v) { store(mm, v); });
+    }
+  }
+}
+
 // One propagation per cluster (clusters take instances in turn); a.plan.N = M, a.tw the N-point table.
-// Point-wise work: the pump-driven solvers' RK4 matrices (a.prop) or the solver's DiffEq.
-template <class S, int C>
+// Point-wise work: the pump-driven solvers' RK4 matrices (a.prop) or the solver's DiffEq.  K = 1: the
+// modes' transforms one after another; K = the solver's mode count: all modes in each transform
+// together (spread_fwd_k, spread_inv_store_k: one barrier per stage and one cluster barrier per
+// exchange for all of them), with K times the exchange and receive buffers.  Either way every mode
+// goes through the same operations, so the results are identical.
+template <class S, int C, int K = 1>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs a) {
   constexpr int MD = S::kM, P = S::kP > 0 ? S::kP : 1;
+  static_assert(K == 1 || K == MD, "modes one at a time or all together");
   extern __shared__ double2 smem[];
   cg::cluster_group cl = cg::this_cluster();
   SpreadFFT f;
   const int rank = (int)cl.block_rank();
   const int M = a.plan.N;
-  spread_init<C>(f, smem, a.tw, M, rank);
+  spread_init<C, K>(f, smem, a.tw, M, rank);
   const int N = M * C;
   const int tn = rank + C * f.j;
   const int fk = f.j + M * rank;
@@ -72,14 +102,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs
       if (m == a.inputMode) seg = 0;
       else if (a.inputMode < 1 && m < a.inChannels) seg = m;
       x[m] = seg >= 0 ? row[(long long)seg * N + (a.inTime ? tn : fk)] : czero();
-      if (a.inTime) x[m] = spread_fwd<C>(f, x[m], cl);
-      x[m] = cmul(x[m], __ldg(a.half + (long long)m * N + fk));
     }
+    if (a.inTime) spread_fwd_all<C, K, MD>(f, x, cl);
 #pragma unroll
-    for (int m = 0; m < MD; m++)
-      x[m] = spread_inv_store<C>(f, x[m], cl, [&](double2 v) {
-        if (a.gridF) a.gridF[m * ms + fk] = cscale(v, (double)N);
-      });
+    for (int m = 0; m < MD; m++) x[m] = cmul(x[m], __ldg(a.half + (long long)m * N + fk));
+    spread_inv_all<C, K, MD>(f, x, cl, [&](int m, double2 v) {
+      if (a.gridF) a.gridF[m * ms + fk] = cscale(v, (double)N);
+    });
     if (a.gridT) {
 #pragma unroll
       for (int m = 0; m < MD; m++) a.gridT[m * ms + tn] = x[m];
@@ -134,29 +163,39 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs
       const bool last = i == a.nZ - 1;
       const double2* table = last ? a.dlast : a.dstep;
       const bool wantTime = !last || a.inTime || a.gridT != nullptr;
+      spread_fwd_all<C, K, MD>(f, x, cl);
 #pragma unroll
-      for (int m = 0; m < MD; m++) {
-        x[m] = cmul(spread_fwd<C>(f, x[m], cl), __ldg(table + (long long)m * N + fk));
-        auto storeF = [&](double2 v) {
-          if (a.gridF) a.gridF[m * ms + (long long)i * N + fk] = cscale(v, (double)N);
-        };
-        if (wantTime) {
-          x[m] = spread_inv_store<C>(f, x[m], cl, storeF);
-          if (a.gridT) a.gridT[m * ms + (long long)i * N + tn] = x[m];
-        } else {
-          storeF(x[m]);
+      for (int m = 0; m < MD; m++) x[m] = cmul(x[m], __ldg(table + (long long)m * N + fk));
+      auto storeF = [&](int m, double2 v) {
+        if (a.gridF) a.gridF[m * ms + (long long)i * N + fk] = cscale(v, (double)N);
+      };
+      if (wantTime) {
+        spread_inv_all<C, K, MD>(f, x, cl, storeF);
+        if (a.gridT) {
+#pragma unroll
+          for (int m = 0; m < MD; m++) a.gridT[m * ms + (long long)i * N + tn] = x[m];
         }
-        if (ckRow && !last && i % a.ckK == 0) ckRow[((long long)(i / a.ckK) * MD + m) * N + tn] = x[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < MD; m++) storeF(m, x[m]);
+      }
+      if (ckRow && !last && i % a.ckK == 0) {
+#pragma unroll
+        for (int m = 0; m < MD; m++) ckRow[((long long)(i / a.ckK) * MD + m) * N + tn] = x[m];
       }
     }
     if (a.nZ == 1) {
+      spread_fwd_all<C, K, MD>(f, x, cl);
 #pragma unroll
       for (int m = 0; m < MD; m++) {
-        x[m] = cmul(spread_fwd<C>(f, x[m], cl), __ldg(a.back + (long long)m * N + fk));
+        x[m] = cmul(x[m], __ldg(a.back + (long long)m * N + fk));
         if (a.gridF) a.gridF[m * ms + fk] = cscale(x[m], (double)N);
-        if (a.inTime || a.gridT) {
-          x[m] = spread_inv<C>(f, x[m], cl);
-          if (a.gridT) a.gridT[m * ms + tn] = x[m];
+      }
+      if (a.inTime || a.gridT) {
+        spread_inv_all<C, K, MD>(f, x, cl, [&](int, double2) {});
+        if (a.gridT) {
+#pragma unroll
+          for (int m = 0; m < MD; m++) a.gridT[m * ms + tn] = x[m];
         }
       }
     }

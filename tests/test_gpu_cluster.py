@@ -143,6 +143,27 @@ def test_cluster_chi3_pump_march(nlm, oracle, n):
     assert cases.rel_l2(med.pumpFreq, one.pumpFreq) < 1e-12
 
 
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE" and n not in ("Chi3", "Chi2PDC")])
+def test_wide_spread_every_multimode_solver(nlm, oracle, name):
+    """runSignalSimulation of every multi-mode solver on 2048 points: eight CTAs with one point per
+    thread, the modes in each transform together where their buffers fit (two modes), one after another
+    otherwise (three and four), against the oracle's full grids."""
+    kw = dict(cases.CASES[name], tPrecision=2048, tMax=cases.CASES[name]["tMax"] * 8)
+    med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw)
+    if name not in cases.FULLY_NONLINEAR:
+        med.runPumpSimulation()
+        ref.run_pump_simulation()
+    modes = med._dims["nSignalModes"]
+    a = cases.noise(np.random.default_rng(7), 2048 * modes, 0.3)
+    med.runSignalSimulation(a, True, 0)
+    ref.run_signal_simulation(a, True, 0)
+    sched = med._last_schedule()
+    assert sched["grid"] == 8 and sched["R"] == 1 and sched["block"] == 256
+    for m in range(modes):
+        assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
+        assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
+
+
 @pytest.mark.parametrize("n", [128, 256, 512, 1024, 2048, 4096])
 @pytest.mark.parametrize("name", ["Chi2PDC", "Chi3", "Chi2SFG"])
 def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):

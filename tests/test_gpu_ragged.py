@@ -10,9 +10,10 @@ TOL = 1e-9
 
 @pytest.mark.parametrize("use_prop", [1, -1, 0])
 def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
-    """use_prop 1: every (pump-driven) medium's RK4 matrices are built before the one launch (one
-    build launch per medium); 0: the launch evaluates the DiffEq; -1 (the default): the DiffEq on the
-    first call after a pump change, the matrices built on the second and reused from the third."""
+    """All media on one SM each (clusters off): one ragged launch per solver and grid.  use_prop 1:
+    every (pump-driven) medium's RK4 matrices are built before its launch (one build launch per
+    medium); 0: the launches evaluate the DiffEq; -1 (the default): the DiffEq on the first call after a
+    pump change, the matrices built on the second and reused from the third."""
     from multimodenonlinearoptics_gb300.workloads import ragged_media_params
     params = ragged_media_params(seed=11, count=6)
     media, refs, ins = [], [], []
@@ -37,13 +38,14 @@ def test_ragged_launch_matches_oracle(nlm, oracle, use_prop):
         m._set_schedule(use_propagator=use_prop)
         m._set_cluster(0)                                   # every medium in the ragged launch
     outs = nlm.ragged_batch(media, ins)
-    # one launch per solver in the set (plus the propagator builds)
-    assert sum(m._launch_count() for m in media) == 2 + (len(media) if use_prop == 1 else 0)
+    # one ragged launch per solver and grid in the set (plus the propagator builds)
+    classes = len({(type(m).__name__, m._dims["nFreqs"]) for m in media})
+    assert sum(m._launch_count() for m in media) == classes + (len(media) if use_prop == 1 else 0)
     if use_prop == -1:
         again = nlm.ragged_batch(media, ins)
-        assert sum(m._launch_count() for m in media) == 2 + len(media)
+        assert sum(m._launch_count() for m in media) == classes + len(media)
         third = nlm.ragged_batch(media, ins)
-        assert sum(m._launch_count() for m in media) == 2
+        assert sum(m._launch_count() for m in media) == classes
         for o, o2, o3 in zip(outs, again, third):
             assert cases.rel_l2(o2, o) < 1e-13 and np.array_equal(o3, o2)
     for m, r, x, o in zip(media, refs, ins, outs):
