@@ -13,6 +13,8 @@ self-contained command for ncu.
 * gnlse_grad  gradient of the band energy (omega in [2, 4]) with respect to the input spectral phase
 * signal      one Chi2PDC runSignalSimulation (full grids) on the Green's medium at N=2048
 * gnlse_signal  one Chi3GNLSE runSignalSimulation (full grids) on the GNLSE medium at N=4096
+* ragged_wide  one 2048-point Chi2SFG runSignalSimulation with the ragged set's parameters (DiffEq form):
+               the eight-CTA march that sets the ragged set's makespan
 """
 
 import argparse
@@ -170,6 +172,15 @@ def _run(name, z_precision, rows, reps):
                             **dict(GREEN_CONFIG, tPrecision=2048, zPrecision=z_precision or 500))
             m.runPumpSimulation()
             m.runSignalSimulation((np.random.default_rng(2048).standard_normal(2048) + 0j) * 0.1)
+        elif name == "ragged_wide":
+            kw = dict(relativeLength=1, nlLength=1, nlLengthOrig=1, beta2=0.4, beta2s=-0.3, beta2o=0, beta1=0,
+                      beta1s=1.2, beta1o=0, beta3=0, beta3s=0.05, beta3o=0, diffBeta0=0, tMax=10, tPrecision=2048,
+                      zPrecision=z_precision or 200)
+            t = np.fft.fftshift(np.linspace(-10, 10, 2048, endpoint=False))
+            m = nlm.Chi2SFG(customPump=np.exp(-t ** 2 / 2), poling=[3, 4, 3], **kw)
+            m._set_schedule(use_propagator=0)
+            m.runPumpSimulation()
+            m.runSignalSimulation((np.random.default_rng(1).standard_normal(2048) + 0j) * 1e-3)
         elif name == "gnlse_signal":
             m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
             m.runSignalSimulation(gnlse_rows(1)[0])
@@ -192,7 +203,7 @@ def _run(name, z_precision, rows, reps):
 def main():
     ap = argparse.ArgumentParser(description="run one benchmark workload on cuda:0")
     ap.add_argument("name", choices=["green", "cascade", "chi3", "chi3_pump", "ragged", "adjoint", "adjoint_cluster", "gnlse",
-                                     "gnlse_grad", "signal", "gnlse_signal"])
+                                     "gnlse_grad", "signal", "gnlse_signal", "ragged_wide"])
     ap.add_argument("--zprecision", type=int, default=0, help="zPrecision override (0: the workload's own)")
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")
     ap.add_argument("--reps", type=int, default=1)
