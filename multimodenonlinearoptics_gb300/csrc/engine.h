@@ -1809,8 +1809,38 @@ struct Medium {
         lastTuned = 1;
       }
     }
-    const long long units = paired ? (nInst + 1) / 2 : nInst;   // thread groups' work items
+    long long units = paired ? (nInst + 1) / 2 : nInst;   // thread groups' work items
     if (!lastTuned) s = schedule(k, units, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
+    // Paired rows run in waves of one pair per resident thread group.  When the last wave would leave
+    // groups idle, the pairs fill whole waves and the rows left over run one per thread group in one
+    // more wave of the single-row kernel (a pair takes about 1.56 rows' time): 1024 rows of 4096
+    // points on 152 SMs take 3 pair waves and one single wave (5.7 row times) instead of 4 pair waves
+    // (6.2).
+    const KernelEntry* kTail = nullptr;
+    Schedule sTail{};
+    PropArgs aTail{};
+    if (paired && !lastTuned && !plainOne) {
+      const long long wave = (long long)smCount() * s.ctas * s.ipc;
+      const long long fullPairs = units / wave * wave;
+      const long long rest = nInst - 2 * fullPairs;
+      if (fullPairs > 0 && rest > 0 && units % wave != 0) {
+        if (const KernelEntry* k1 = findKernel(kKindGnlse, solver, a.R)) {
+          const Schedule s1 = schedule(k1, rest, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
+          if ((long long)s1.grid * s1.ipc >= rest) {   // the rest in one wave
+            kTail = k1;
+            sTail = s1;
+            aTail = a;
+            aTail.instBase = a.instBase + 2 * fullPairs;
+            aTail.nInst = rest;
+            aTail.ipc = s1.ipc;
+            aTail.work = nullptr;
+            a.nInst = 2 * fullPairs;
+            units = fullPairs;
+            s = schedule(k, units, a.R, ctaPerSM < 0 ? 0 : ctaPerSM);
+          }
+        }
+      }
+    }
     if (plainOne) s.grid = 1;
     lastSchedule = s;
     lastR = a.R;
@@ -1828,7 +1858,8 @@ struct Medium {
     double2* sp = nullptr;
     if (gnlse) {
       // per thread group: 2 (7 when paired) parts of T R values (N on the register plan)
-      scratch.reserve((size_t)s.grid * s.ipc * (paired ? 7 : 2) * ((size_t)a.plan.T * a.R));
+      const size_t slots = std::max((size_t)s.grid * s.ipc * (paired ? 7 : 2), (size_t)sTail.grid * sTail.ipc * 2);
+      scratch.reserve(slots * ((size_t)a.plan.T * a.R));
       sp = scratch.p;
     }
     // with kernel timing on, the tail runs after the timed region, outside the graph
@@ -1838,6 +1869,11 @@ struct Medium {
       if (gnlse) {
         void* args[] = {(void*)&a, (void*)&sp};
         ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
+        if (kTail) {
+          void* targs[] = {(void*)&aTail, (void*)&sp};
+          ck(cudaLaunchKernel(kTail->fn, dim3(sTail.grid), dim3(sTail.block), targs, sTail.smem, stream),
+             "propagate (single rows)");
+        }
       } else if (ff) {
         void* args[] = {(void*)&a, (void*)&ffT};
         ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "propagate");
@@ -1856,6 +1892,8 @@ struct Medium {
       GraphKey key;
       add_prop_key(key, a);
       key.add(s.grid).add(s.block).add(s.smem).add(k->fn).add(sp).add(ff);
+      key.add(kTail ? kTail->fn : nullptr).add(sTail.grid).add(sTail.block).add(sTail.smem);
+      if (kTail) add_prop_key(key, aTail);
       key.add(ffT.tw).add(ffT.dstep).add(ffT.dlast).add(ffT.half).add(ffT.back).add(ffT.prop);
       key.add(tailInside);
       if (tailInside && tailKey) key.bytes.insert(key.bytes.end(), tailKey->bytes.begin(), tailKey->bytes.end());
@@ -1863,7 +1901,7 @@ struct Medium {
     } else {
       record();
     }
-    launches++;
+    launches += kTail ? 2 : 1;
     if (timeKernels) {
       ck(cudaEventRecord(ev1, stream), "event");
       ck(cudaEventSynchronize(ev1), "event");

@@ -84,3 +84,22 @@ def test_paired_reverse_sweep(nlm, k):
     single = np.concatenate([grad(x[q:q + 100]) for q in range(0, 320, 100)])
     assert cases.rel_l2(paired, single) < 1e-11
     assert not np.array_equal(paired, single)
+
+
+def test_pair_waves_then_single_rows(nlm, oracle):
+    """400 rows of 4096 points on 152 SMs: 152 pairs fill one wave of the paired kernel, and the 96
+    rows left over run one per thread group in one wave of the single-row kernel (instead of a second,
+    part-empty pair wave).  Against the oracle; the tail rows equal the single-row kernel's bit for bit."""
+    from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG, gnlse_rows
+    kw = dict(GNLSE_CONFIG, relativeLength=0.002)
+    med, ref = nlm.Chi3GNLSE(**kw), oracle.Chi3GNLSE(**kw)
+    torch = pytest.importorskip("torch")
+    if torch.cuda.get_device_properties(0).multi_processor_count != 152:
+        pytest.skip("the wave arithmetic below is for 4096 points on 152 SMs")
+    x = gnlse_rows(400, seed=8)
+    med.batchSignalSimulation(x[:1], inTimeDomain=True)             # device tables (the Raman transform)
+    out = med.batchSignalSimulation(x, inTimeDomain=True)
+    assert med._launch_count() == 2                                 # the pair wave and the single-row wave
+    assert cases.rel_l2(out, ref.batch_signal_simulation(x, True)) < TOL
+    tail = med.batchSignalSimulation(x[304:], inTimeDomain=True)   # fewer rows than SMs: one-row kernel
+    assert np.array_equal(out[304:], tail)
