@@ -2219,6 +2219,26 @@ struct Medium {
         (gn && !kp && adjRows > smCount()) ? findKernel(kKindAdjoint, solver + 400, R) : nullptr;
     if (kq) k = kq;
     Schedule s = schedule(k, kq ? (adjRows + 1) / 2 : adjRows, R);
+    // as for the paired forward (Medium::propagate): whole waves of pairs, the rows left over in one
+    // wave of the single-row reverse sweep
+    const KernelEntry* kTail = nullptr;
+    Schedule sTail{};
+    long long headRows = adjRows;
+    if (kq) {
+      const long long pairs = (adjRows + 1) / 2, wave = (long long)smCount() * s.ctas * s.ipc;
+      const long long fullPairs = pairs / wave * wave, rest = adjRows - 2 * fullPairs;
+      if (fullPairs > 0 && rest > 0 && pairs % wave != 0) {
+        if (const KernelEntry* k1 = findKernel(kKindAdjoint, solver, R)) {
+          const Schedule s1 = schedule(k1, rest, R);
+          if ((long long)s1.grid * s1.ipc >= rest) {
+            kTail = k1;
+            sTail = s1;
+            headRows = 2 * fullPairs;
+            s = schedule(k, fullPairs, R);
+          }
+        }
+      }
+    }
     if (kp) {
       s.ipc = 1;
       s.block = (int)N / R;
@@ -2229,11 +2249,13 @@ struct Medium {
       adjSeg.reserve((size_t)adjRows * (2 * (size_t)adjK * 8 + 4) * N);   // per cluster: STG[2][K][8][N], 4 N
     } else {
       size_t perSlot = gn ? (size_t)(10 + (adjK > 1 ? 1 + 8 * adjK : 0)) * N : (size_t)adjK * N;
+      const size_t singleSlot = perSlot;
       if (kq) perSlot = 2 * (size_t)(16 + (adjK > 1 ? 1 + 8 * adjK : 0)) * N;   // two rows of the pair kernel's scratch
-      if (gn || adjK > 1) adjSeg.reserve((size_t)s.grid * s.ipc * perSlot);
+      if (gn || adjK > 1)
+        adjSeg.reserve(std::max((size_t)s.grid * s.ipc * perSlot, (size_t)sTail.grid * sTail.ipc * singleSlot));
     }
     PropArgs a = baseArgs(R);
-    a.nInst = adjRows;
+    a.nInst = headRows;
     a.ipc = s.ipc;
     a.work = nullptr;
     // segments between checkpoints are recomputed with the RK4 propagator matrices (built in parallel
@@ -2264,6 +2286,16 @@ struct Medium {
       ck(cudaLaunchKernel(k->fn, dim3(s.grid), dim3(s.block), args, s.smem, stream), "adjoint");
     }
     launches++;
+    if (kTail) {
+      PropArgs at = a;
+      at.instBase = headRows;
+      at.nInst = adjRows - headRows;
+      at.ipc = sTail.ipc;
+      void* targs[] = {(void*)&at, (void*)&d};
+      ck(cudaLaunchKernel(kTail->fn, dim3(sTail.grid), dim3(sTail.block), targs, sTail.smem, stream),
+         "adjoint (single rows)");
+      launches++;
+    }
     if (march) {
       ck(launch_adj_stage_grads(a, d, (int)N, adjRows, stream), "stage gradients");
       launches++;

@@ -103,3 +103,30 @@ def test_pair_waves_then_single_rows(nlm, oracle):
     assert cases.rel_l2(out, ref.batch_signal_simulation(x, True)) < TOL
     tail = med.batchSignalSimulation(x[304:], inTimeDomain=True)   # fewer rows than SMs: one-row kernel
     assert np.array_equal(out[304:], tail)
+
+
+@pytest.mark.parametrize("k", [1, 4])
+def test_reverse_sweep_waves_then_single_rows(nlm, k):
+    """400 rows of 4096 points: the reverse sweep too runs one wave of pairs and the 96 rows left over
+    one per thread group; the gradients equal those of 100-row sweeps on the same rows, to rounding."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.get_device_properties(0).multi_processor_count != 152:
+        pytest.skip("the wave arithmetic below is for 4096 points on 152 SMs")
+    from multimodenonlinearoptics_gb300.autograd import propagate_gnlse
+    from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG, gnlse_rows
+    kw = dict(GNLSE_CONFIG, relativeLength=0.002)
+    x = np.fft.fft(gnlse_rows(400, seed=12), axis=1)
+    n = x.shape[1]
+    weights = torch.linspace(0, 1, n, device="cuda", dtype=torch.float64)
+
+    def grad(rows_x):
+        med = nlm.Chi3GNLSE(**kw)
+        xt = torch.tensor(rows_x, device="cuda", requires_grad=True)
+        torch.sum(torch.abs(propagate_gnlse(med, xt, k)) ** 2 * weights).backward()
+        return xt.grad.cpu().numpy()
+
+    waves = grad(x)
+    chunks = np.concatenate([grad(x[q:q + 100]) for q in range(0, 400, 100)])
+    assert np.all(np.isfinite(waves))
+    assert cases.rel_l2(waves, chunks) < 1e-11
+    assert cases.rel_l2(waves[304:], chunks[304:]) < 1e-11
