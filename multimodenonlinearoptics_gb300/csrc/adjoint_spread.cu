@@ -148,11 +148,149 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe(const P
   }
 }
 
+// Three groups of four on clusters of twelve CTAs, for checkpoint intervals K > 1 with the RK4
+// propagator matrices built.  In k_adjoint_pdc_spread_pipe the reverse group also runs the transposed
+// stages of every step (about 90 FP64 operations per point), so the recomputing group, whose step is
+// 4 FMAs, waits at every shared barrier.  Here:
+//   ranks 4..7 (group 1) recompute the states of segment j-1 into STG, as there;
+//   ranks 0..3 (group 0) reverse segment j: the dispersion pair, then P^T per point (4 FMAs), storing
+//     the gradient after each step's RK4 in GP;
+//   ranks 8..11 (group 2) compute the stage-factor gradients of segment j+1, reversed in the previous
+//     iteration, from its states (STG) and stored gradients (GP): one step per slot, the loads and the
+//     forward stages before the slot's first barrier, the transposed stages after it.
+// So each slot carries about the same work in every group.  STG holds three segments (written by
+// group 1 at iteration it, read by group 0 at it+1 and by group 2 at it+2) and GP two.  After the
+// last iteration the three groups share the stage-factor gradients of segment 0, by steps.
+// Barriers per row: (nSeg + 1) (2K + 1) in the iterations, then one (the input gradient's transform
+// in group 0) and one after the shared work, in every group.  d.seg: [cluster][3 + 2][K][N].
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe3(const PropArgs a, const AdjArgs d) {
+  extern __shared__ double2 smem[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int crank = (int)cl.block_rank();
+  const int role = crank / kSpreadC;   // 0: reverse sweep, 1: recomputation, 2: stage-factor gradients
+  const int lr = crank - role * kSpreadC;
+  const int M = a.plan.N;
+  const int N = M * kSpreadC;
+  SpreadFFT f;
+  if (role < 2) {
+    spread_init(f, smem, a.tw, M, lr);
+    f.base = role * kSpreadC;
+  }
+  const int tn = lr + kSpreadC * (int)threadIdx.x, fk = (int)threadIdx.x + M * lr;
+  const int pc = lr * M + (int)threadIdx.x;   // the point of this thread's stage-factor gradients
+  const int K = d.K;
+  const long long clusterId = blockIdx.x / (3 * kSpreadC), nClusters = gridDim.x / (3 * kSpreadC);
+  const long long bufStride = (long long)K * N;
+  double2* STG = d.seg + clusterId * 5 * bufStride;
+  double2* GP = STG + 3 * bufStride;
+  const int nSeg = (a.nZ - 2) / K + 1;
+  // the forward stages of step i at point pc from the state before it (x)
+  auto stages = [&](int i, double2 x) {
+    const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
+    return pdc_stages(a, N, i, pc, c[0], c[1], c[2], x);
+  };
+  for (long long local = clusterId; local < a.nInst; local += nClusters) {
+    const long long inst = a.instBase + local;
+    const double2* ck = d.ckpt + inst * (long long)d.nCk * N;
+    double2 g = czero();
+    if (role == 0) g = cscale(d.gout[inst * (long long)N + fk], (double)N);
+    for (int it = 0; it <= nSeg; it++) {
+      if (role == 1) {
+        if (it < nSeg) {
+          const int jseg = nSeg - 1 - it, s0 = jseg * K, segEnd = min(s0 + K, a.nZ - 1);
+          double2* stg = STG + (long long)(it % 3) * bufStride;
+          double2 x = ck[(long long)jseg * N + tn];
+          stg[tn] = x;
+          for (int q = 1; q <= K; q++) {
+            const int i = s0 + q;
+            if (i < segEnd) {
+              x = pdc_step_point(a, N, i, tn, x);
+              x = spread_inv(f, cmul(spread_fwd(f, x, cl), __ldg(a.dstep + fk)), cl);
+              stg[(long long)q * N + tn] = x;
+            } else {
+              spread_idle(cl, 2);
+            }
+          }
+        } else {
+          spread_idle(cl, 2 * K);
+        }
+      } else if (role == 0) {
+        if (it >= 1) {
+          const int jseg = nSeg - it, s0 = jseg * K, segEnd = min(s0 + K, a.nZ - 1);
+          double2* gps = GP + (long long)(it & 1) * bufStride;
+          for (int q = 0; q < K; q++) {
+            const int i = segEnd - q;
+            if (i > s0) {
+              if (i < a.nZ - 1) g = spread_fwd(f, g, cl);
+              else cl.sync();
+              const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+              g = spread_inv(f, cmulc(g, __ldg(tab + fk)), cl);
+              gps[(long long)(i - 1 - s0) * N + tn] = g;
+              g = pdc_transpose_point(a, N, i, tn, g);
+            } else {
+              spread_idle(cl, 2);
+            }
+          }
+        } else {
+          spread_idle(cl, 2 * K);
+        }
+      } else {
+        if (it >= 2) {
+          const int jseg = nSeg - it + 1, s0 = jseg * K, segEnd = min(s0 + K, a.nZ - 1);
+          const double2* stg = STG + (long long)((it - 2) % 3) * bufStride;
+          const double2* gps = GP + (long long)((it - 1) & 1) * bufStride;
+          for (int q = 0; q < K; q++) {
+            const int i = s0 + 1 + q;
+            if (i <= segEnd) {
+              const double2 x = stg[(long long)(i - 1 - s0) * N + pc];
+              const double2 gp = gps[(long long)(i - 1 - s0) * N + pc];
+              const PdcStages st = stages(i, x);
+              cl.sync();
+              double2 ga0, ga1, ga2;
+              pdc_stages_reverse(st, x, gp, ga0, ga1, ga2);
+              pdc_store_ga(d, N, i, pc, ga0, ga1, ga2);
+              cl.sync();
+            } else {
+              spread_idle(cl, 2);
+            }
+          }
+        } else {
+          spread_idle(cl, 2 * K);
+        }
+      }
+      cl.sync();
+    }
+    if (role == 0) {
+      g = spread_fwd(f, g, cl);
+      d.gin[inst * (long long)N + fk] = cmulc(g, __ldg(a.half + fk));
+    } else {
+      cl.sync();
+    }
+    // segment 0 (reversed in the last iteration): its steps shared by the three groups
+    {
+      const int segEnd = min(K, a.nZ - 1);
+      const double2* stg = STG + (long long)((nSeg - 1) % 3) * bufStride;
+      const double2* gps = GP + (long long)(nSeg & 1) * bufStride;
+      for (int i = 1 + role; i <= segEnd; i += 3) {
+        const double2 x = stg[(long long)(i - 1) * N + pc];
+        const double2 gp = gps[(long long)(i - 1) * N + pc];
+        const PdcStages st = stages(i, x);
+        double2 ga0, ga1, ga2;
+        pdc_stages_reverse(st, x, gp, ga0, ga1, ga2);
+        pdc_store_ga(d, N, i, pc, ga0, ga1, ga2);
+      }
+    }
+    cl.sync();
+  }
+}
+
 void add_kernels_adjoint_spread(std::vector<KernelEntry>& t) {
   // key + 300: one propagation per cluster of four CTAs; key + 200: pipelined on eight; R = 1 point
   // per thread
   t.push_back({kKindAdjoint, kChi2PDC + 300, 1, (const void*)k_adjoint_pdc_spread});
   t.push_back({kKindAdjoint, kChi2PDC + 200, 1, (const void*)k_adjoint_pdc_spread_pipe});
+  // key + 500: three groups on twelve CTAs (checkpoints with the propagator matrices)
+  t.push_back({kKindAdjoint, kChi2PDC + 500, 1, (const void*)k_adjoint_pdc_spread_pipe3});
 }
 
 }  // namespace nlm

@@ -268,7 +268,35 @@ def test_sqrt_checkpoints_at_config_size(nlm):
     target = cases.noise(rng, 512, 1.0).reshape(1, 512)
     target /= np.linalg.norm(target)
     a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
-    b = _engine_grads(nlm, kw, x, f0, d, target, interval=int(np.ceil(np.sqrt(nz - 1))))
+    k = int(np.ceil(np.sqrt(nz - 1)))
+    b = _engine_grads(nlm, kw, x, f0, d, target, interval=k)
+    assert b[4]._last_schedule()["grid"] == 12          # three groups of four CTAs
+    for ga, gb in zip(a[1:4], b[1:4]):
+        assert cases.rel_l2(gb, ga) < 1e-11
+    # the two-group form on eight CTAs (the transposed stages inside the reverse steps)
+    import os
+    os.environ["NLM_ADJOINT_CTAS"] = "8"
+    try:
+        c = _engine_grads(nlm, kw, x, f0, d, target, interval=k)
+    finally:
+        del os.environ["NLM_ADJOINT_CTAS"]
+    assert c[4]._last_schedule()["grid"] == 8
+    for gb, gc in zip(b[1:4], c[1:4]):
+        assert cases.rel_l2(gb, gc) < 1e-11
+
+
+@pytest.mark.parametrize("interval", [2, 13, 20, 40])
+def test_twelve_cta_sweep_segment_counts(nlm, interval):
+    """The three-group sweep with one segment (interval 40 > nZSteps - 1), two, several, and the shortest
+    interval, on 256 points and 3 rows (stage-factor gradients accumulated over rows): the gradients
+    of every-state storage."""
+    kw = dict(KW, tPrecision=256, zPrecision=15)
+    nz = nlm.Chi2PDC(**kw)._dims["nZSteps"]
+    assert 20 < nz - 1 < 40
+    x, f0, d, target = _problem(256, nz, rows=3, seed=interval)
+    a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
+    b = _engine_grads(nlm, kw, x, f0, d, target, interval=interval)
+    assert b[4]._last_schedule()["grid"] % 12 == 0
     for ga, gb in zip(a[1:4], b[1:4]):
         assert cases.rel_l2(gb, ga) < 1e-11
 
@@ -359,7 +387,10 @@ def test_pdc_cluster_sweep(nlm, oracle, n):
             res[cluster, k] = _engine_grads(nlm, kw, x, f0, d, target, interval=k, cluster=cluster)
             if cluster:
                 sched = res[cluster, k][4]._last_schedule()
-                assert sched["grid"] == (8 if k == 1 else 16)
+                # interval 7 on the spread grids: three groups on twelve CTAs (the propagator matrices
+                # are built), else two groups on eight
+                spread = cluster == 1 and n <= 1024
+                assert sched["grid"] == (8 if k == 1 else (24 if spread else 16))
                 assert sched["R"] == (1 if cluster == 1 and n <= 1024 else 4)
     for key in [(1, 7), (0, 1), (0, 7)] + ([(2, 1), (2, 7)] if n == 1024 else []):
         for ga, gb in zip(res[1, 1][1:4], res[key][1:4]):
