@@ -148,26 +148,35 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe(const P
   }
 }
 
-// Three groups of four on clusters of twelve CTAs, for checkpoint intervals K > 1 with the RK4
-// propagator matrices built.  In k_adjoint_pdc_spread_pipe the reverse group also runs the transposed
-// stages of every step (about 90 FP64 operations per point), so the recomputing group, whose step is
-// 4 FMAs, waits at every shared barrier.  Here:
+// Stage-factor gradient groups beside the pipelined sweep, on clusters of 4 (2 + G) CTAs, for
+// checkpoint intervals K > 1 with the RK4 propagator matrices built.  In k_adjoint_pdc_spread_pipe the
+// reverse group also runs the transposed stages of every step (about 90 FP64 operations per point),
+// so the recomputing group, whose step is 4 FMAs, waits at every shared barrier.  Here:
 //   ranks 4..7 (group 1) recompute the states of segment j-1 into STG, as there;
 //   ranks 0..3 (group 0) reverse segment j: the dispersion pair, then P^T per point (4 FMAs), storing
 //     the gradient after each step's RK4 in GP;
-//   ranks 8..11 (group 2) compute the stage-factor gradients of segment j+1, reversed in the previous
-//     iteration, from its states (STG) and stored gradients (GP): one step per slot, the loads and the
-//     forward stages before the slot's first barrier, the transposed stages after it.
-// So each slot carries about the same work in every group.  STG holds three segments (written by
-// group 1 at iteration it, read by group 0 at it+1 and by group 2 at it+2) and GP two.  After the
-// last iteration the three groups share the stage-factor gradients of segment 0, by steps.
-// Barriers per row: (nSeg + 1) (2K + 1) in the iterations, then one (the input gradient's transform
-// in group 0) and one after the shared work, in every group.  d.seg: [cluster][3 + 2][K][N].
-__global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe3(const PropArgs a, const AdjArgs d) {
+//   ranks 8.. (groups 2 .. 1 + G) compute the stage-factor gradients of segment j+1, reversed in the
+//     previous iteration, from its states (STG) and stored gradients (GP).  Group 2 + s takes the steps
+//     q = s mod G of the segment (q = 0 .. K-1): the loads and forward stages of step q in slot q, its
+//     transposed stages and stores in slot q + 1 (or after the last slot), both before the slot's
+//     first barrier.  That interval holds two local transforms in groups 0 and 1 (the inverse of the
+//     previous slot, the forward of this one); the one between the slot's two barriers holds only the
+//     cluster exchange.
+// Per slot a point costs about 76 FP64 instructions in groups 0 and 1 and 90 / G in each stage group;
+// the FP64 issue rate of an SM is fixed per scheduler, so G = 2 (sixteen CTAs) keeps the stage groups
+// off the critical path and G = 1 (twelve) is the form for GPUs without 16-CTA clusters.  STG holds
+// three segments (written by group 1 at iteration it, read by group 0 at it+1 and by the stage groups
+// at it+2) and GP two.  After the last iteration all groups share the stage-factor gradients of
+// segment 0, by steps.  Barriers per row: (nSeg + 1) (2K + 1) in the iterations, then one (the input
+// gradient's transform in group 0) and one after the shared work, in every group.
+// d.seg: [cluster][3 + 2][K][N].
+template <int G>
+__global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_stage(const PropArgs a, const AdjArgs d) {
+  constexpr int kGroups = 2 + G;
   extern __shared__ double2 smem[];
   cg::cluster_group cl = cg::this_cluster();
   const int crank = (int)cl.block_rank();
-  const int role = crank / kSpreadC;   // 0: reverse sweep, 1: recomputation, 2: stage-factor gradients
+  const int role = crank / kSpreadC;   // 0: reverse sweep, 1: recomputation, 2..: stage-factor gradients
   const int lr = crank - role * kSpreadC;
   const int M = a.plan.N;
   const int N = M * kSpreadC;
@@ -179,15 +188,28 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe3(const 
   const int tn = lr + kSpreadC * (int)threadIdx.x, fk = (int)threadIdx.x + M * lr;
   const int pc = lr * M + (int)threadIdx.x;   // the point of this thread's stage-factor gradients
   const int K = d.K;
-  const long long clusterId = blockIdx.x / (3 * kSpreadC), nClusters = gridDim.x / (3 * kSpreadC);
+  const long long clusterId = blockIdx.x / (kGroups * kSpreadC), nClusters = gridDim.x / (kGroups * kSpreadC);
   const long long bufStride = (long long)K * N;
   double2* STG = d.seg + clusterId * 5 * bufStride;
   double2* GP = STG + 3 * bufStride;
   const int nSeg = (a.nZ - 2) / K + 1;
-  // the forward stages of step i at point pc from the state before it (x)
-  auto stages = [&](int i, double2 x) {
+  // a stage group's step in flight: its forward stages, state and gradient (step 0: none)
+  PdcStages st{};
+  double2 sx = czero(), sg = czero();
+  int si = 0;
+  auto stageLoad = [&](const double2* stg, const double2* gps, int i, int s0) {
+    sx = stg[(long long)(i - 1 - s0) * N + pc];
+    sg = gps[(long long)(i - 1 - s0) * N + pc];
     const double2* c = a.coef + (long long)(i - 1) * 3 * a.nCoef;
-    return pdc_stages(a, N, i, pc, c[0], c[1], c[2], x);
+    st = pdc_stages(a, N, i, pc, c[0], c[1], c[2], sx);
+    si = i;
+  };
+  auto stageFinish = [&]() {
+    if (si == 0) return;
+    double2 ga0, ga1, ga2;
+    pdc_stages_reverse(st, sx, sg, ga0, ga1, ga2);
+    pdc_store_ga(d, N, si, pc, ga0, ga1, ga2);
+    si = 0;
   };
   for (long long local = clusterId; local < a.nInst; local += nClusters) {
     const long long inst = a.instBase + local;
@@ -236,24 +258,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe3(const 
         }
       } else {
         if (it >= 2) {
+          const int sub = role - 2;
           const int jseg = nSeg - it + 1, s0 = jseg * K, segEnd = min(s0 + K, a.nZ - 1);
           const double2* stg = STG + (long long)((it - 2) % 3) * bufStride;
           const double2* gps = GP + (long long)((it - 1) & 1) * bufStride;
           for (int q = 0; q < K; q++) {
+            stageFinish();   // the step loaded in an earlier slot
             const int i = s0 + 1 + q;
-            if (i <= segEnd) {
-              const double2 x = stg[(long long)(i - 1 - s0) * N + pc];
-              const double2 gp = gps[(long long)(i - 1 - s0) * N + pc];
-              const PdcStages st = stages(i, x);
-              cl.sync();
-              double2 ga0, ga1, ga2;
-              pdc_stages_reverse(st, x, gp, ga0, ga1, ga2);
-              pdc_store_ga(d, N, i, pc, ga0, ga1, ga2);
-              cl.sync();
-            } else {
-              spread_idle(cl, 2);
-            }
+            if (q % G == sub && i <= segEnd) stageLoad(stg, gps, i, s0);
+            spread_idle(cl, 2);
           }
+          stageFinish();
         } else {
           spread_idle(cl, 2 * K);
         }
@@ -266,18 +281,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe3(const 
     } else {
       cl.sync();
     }
-    // segment 0 (reversed in the last iteration): its steps shared by the three groups
+    // segment 0 (reversed in the last iteration): its steps shared by all groups
     {
       const int segEnd = min(K, a.nZ - 1);
       const double2* stg = STG + (long long)((nSeg - 1) % 3) * bufStride;
       const double2* gps = GP + (long long)(nSeg & 1) * bufStride;
-      for (int i = 1 + role; i <= segEnd; i += 3) {
-        const double2 x = stg[(long long)(i - 1) * N + pc];
-        const double2 gp = gps[(long long)(i - 1) * N + pc];
-        const PdcStages st = stages(i, x);
-        double2 ga0, ga1, ga2;
-        pdc_stages_reverse(st, x, gp, ga0, ga1, ga2);
-        pdc_store_ga(d, N, i, pc, ga0, ga1, ga2);
+      for (int i = 1 + role; i <= segEnd; i += kGroups) {
+        stageLoad(stg, gps, i, 0);
+        stageFinish();
       }
     }
     cl.sync();
@@ -289,8 +300,10 @@ void add_kernels_adjoint_spread(std::vector<KernelEntry>& t) {
   // per thread
   t.push_back({kKindAdjoint, kChi2PDC + 300, 1, (const void*)k_adjoint_pdc_spread});
   t.push_back({kKindAdjoint, kChi2PDC + 200, 1, (const void*)k_adjoint_pdc_spread_pipe});
-  // key + 500: three groups on twelve CTAs (checkpoints with the propagator matrices)
-  t.push_back({kKindAdjoint, kChi2PDC + 500, 1, (const void*)k_adjoint_pdc_spread_pipe3});
+  // key + 500 / + 600: stage-factor gradients in one / two groups of their own, on twelve / sixteen
+  // CTAs (checkpoints with the propagator matrices)
+  t.push_back({kKindAdjoint, kChi2PDC + 500, 1, (const void*)k_adjoint_pdc_spread_stage<1>});
+  t.push_back({kKindAdjoint, kChi2PDC + 600, 1, (const void*)k_adjoint_pdc_spread_stage<2>});
 }
 
 }  // namespace nlm

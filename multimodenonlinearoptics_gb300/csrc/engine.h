@@ -2137,33 +2137,37 @@ struct Medium {
     // steps), in at most three waves of clusters
     int group = C;
     long long clusters = adjRows;
-    // with the propagator matrices: three groups on twelve CTAs (the stage-factor gradients on their
-    // own four SMs beside the recomputation and the reverse steps), a non-portable cluster size;
-    // NLM_ADJOINT_CTAS=8 keeps the two-group form
-    bool three = false;
-    const char* ctas = std::getenv("NLM_ADJOINT_CTAS");
-    if (adjK > 1 && spread && a.prop && !(ctas && std::atoi(ctas) == 8)) {
-      if (const KernelEntry* k3 = findKernel(kKindAdjoint, solver + 500, Rk)) {
-        size_t smem3 = 0;
-        cudaFuncAttributes fa3;
-        ck(exclusive_smem(k3->fn, need, &smem3, &fa3), "smem attribute");
-        int fit = 0;
-        if (smem3 && cudaFuncSetAttribute(k3->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
-          fit = maxActiveClusters(k3->fn, 3 * C, T, smem3);
-        else
-          cudaGetLastError();
-        if (fit >= 1 && adjRows <= 3LL * fit) {
-          const long long waves = (adjRows + fit - 1) / fit;
-          clusters = (adjRows + waves - 1) / waves;
-          group = 3 * C;
-          k = k3;
-          smem = smem3;
-          fa = fa3;
-          three = true;
-        }
+    // with the propagator matrices: the stage-factor gradients in a group of their own beside the
+    // recomputation and the reverse steps, on twelve CTAs (a non-portable cluster size).  Measured on
+    // the N=512, nZSteps=2000 problem with 45-step segments, two such groups on sixteen CTAs are no
+    // faster (grad/fwd 2.10 both, 2.56 on eight).  NLM_ADJOINT_CTAS = 16 / 8 selects those forms.
+    bool staged = false;
+    const char* ctasEnv = std::getenv("NLM_ADJOINT_CTAS");
+    const int ctasWant = ctasEnv ? std::atoi(ctasEnv) : 12;
+    for (int G = 1; G <= 2 && adjK > 1 && spread && a.prop && !staged; G++) {
+      const int size = (2 + G) * C;
+      if (size != ctasWant) continue;
+      const KernelEntry* k3 = findKernel(kKindAdjoint, solver + 400 + 100 * G, Rk);
+      if (!k3) continue;
+      size_t smem3 = 0;
+      cudaFuncAttributes fa3;
+      ck(exclusive_smem(k3->fn, need, &smem3, &fa3), "smem attribute");
+      int fit = 0;
+      if (smem3 && cudaFuncSetAttribute(k3->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+        fit = maxActiveClusters(k3->fn, size, T, smem3);
+      else
+        cudaGetLastError();
+      if (fit >= 1 && adjRows <= 3LL * fit) {
+        const long long waves = (adjRows + fit - 1) / fit;
+        clusters = (adjRows + waves - 1) / waves;
+        group = size;
+        k = k3;
+        smem = smem3;
+        fa = fa3;
+        staged = true;
       }
     }
-    if (adjK > 1 && !three) {
+    if (adjK > 1 && !staged) {
       if (const KernelEntry* kp = findKernel(kKindAdjoint, solver + 200, Rk)) {
         size_t smemP = 0;
         cudaFuncAttributes faP;
@@ -2179,8 +2183,8 @@ struct Medium {
         }
       }
     }
-    // [cluster][1 or 2][K][N]; three groups: [cluster][3 + 2][K][N]
-    if (adjK > 1) adjSeg.reserve((size_t)clusters * (three ? 5 : group / C) * adjK * N);
+    // [cluster][1 or 2][K][N]; with stage groups: [cluster][3 + 2][K][N]
+    if (adjK > 1) adjSeg.reserve((size_t)clusters * (staged ? 5 : group / C) * adjK * N);
     AdjArgs d{};
     d.gout = gout;
     d.ckpt = ckpt.p;

@@ -1,6 +1,8 @@
 """Gradients of the reverse sweep (Chi2PDC) against central finite differences of the engine's own
 forward and of the oracle's forward (the reference's algorithm with its poling array replaced by a
 continuous profile)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -270,24 +272,25 @@ def test_sqrt_checkpoints_at_config_size(nlm):
     a = _engine_grads(nlm, kw, x, f0, d, target, interval=1)
     k = int(np.ceil(np.sqrt(nz - 1)))
     b = _engine_grads(nlm, kw, x, f0, d, target, interval=k)
-    assert b[4]._last_schedule()["grid"] == 12          # three groups of four CTAs
+    assert b[4]._last_schedule()["grid"] == 12          # a stage-gradient group beside the sweep
     for ga, gb in zip(a[1:4], b[1:4]):
         assert cases.rel_l2(gb, ga) < 1e-11
-    # the two-group form on eight CTAs (the transposed stages inside the reverse steps)
-    import os
-    os.environ["NLM_ADJOINT_CTAS"] = "8"
-    try:
-        c = _engine_grads(nlm, kw, x, f0, d, target, interval=k)
-    finally:
-        del os.environ["NLM_ADJOINT_CTAS"]
-    assert c[4]._last_schedule()["grid"] == 8
-    for gb, gc in zip(b[1:4], c[1:4]):
-        assert cases.rel_l2(gb, gc) < 1e-11
+    # two stage groups on sixteen CTAs; the two-group form on eight CTAs (the transposed stages inside
+    # the reverse steps)
+    for cap in (16, 8):
+        os.environ["NLM_ADJOINT_CTAS"] = str(cap)
+        try:
+            c = _engine_grads(nlm, kw, x, f0, d, target, interval=k)
+        finally:
+            del os.environ["NLM_ADJOINT_CTAS"]
+        assert c[4]._last_schedule()["grid"] == cap
+        for gb, gc in zip(b[1:4], c[1:4]):
+            assert cases.rel_l2(gb, gc) < 1e-11
 
 
 @pytest.mark.parametrize("interval", [2, 13, 20, 40])
-def test_twelve_cta_sweep_segment_counts(nlm, interval):
-    """The three-group sweep with one segment (interval 40 > nZSteps - 1), two, several, and the shortest
+def test_stage_group_sweep_segment_counts(nlm, interval):
+    """The sweeps with stage-gradient groups (sixteen and twelve CTAs) with one segment (interval 40 > nZSteps - 1), two, several, and the shortest
     interval, on 256 points and 3 rows (stage-factor gradients accumulated over rows): the gradients
     of every-state storage."""
     kw = dict(KW, tPrecision=256, zPrecision=15)
@@ -299,6 +302,14 @@ def test_twelve_cta_sweep_segment_counts(nlm, interval):
     assert b[4]._last_schedule()["grid"] % 12 == 0
     for ga, gb in zip(a[1:4], b[1:4]):
         assert cases.rel_l2(gb, ga) < 1e-11
+    os.environ["NLM_ADJOINT_CTAS"] = "16"
+    try:
+        c = _engine_grads(nlm, kw, x, f0, d, target, interval=interval)
+    finally:
+        del os.environ["NLM_ADJOINT_CTAS"]
+    assert c[4]._last_schedule()["grid"] % 16 == 0
+    for ga, gc in zip(a[1:4], c[1:4]):
+        assert cases.rel_l2(gc, ga) < 1e-11
 
 
 def test_gnlse_pipelined_and_one_cta_sweeps_agree(nlm):
