@@ -158,12 +158,14 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
 /* The plan of the last nlm_ragged_batch call: its estimated makespan (microseconds), the cluster
- * slots of four and eight SMs, the CTAs of its one-SM ragged launches, the CUDA-graph captures and
- * replays of ragged calls so far, and the SMs the plan could use (those clusters of four can hold at
- * once; the environment variable NLM_RAGGED_CLUSTER_SMS overrides the measured figure).  No
- * counterpart in the reference (measurement support). */
-nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
-                                long* graph_captures, long* graph_replays, int* sm_budget);
+ * slots of four, eight and sixteen SMs, the CTAs of its one-SM ragged launches, the CUDA-graph
+ * captures and replays of ragged calls so far, the SMs the plan could use (those clusters of four can
+ * hold at once; the environment variable NLM_RAGGED_CLUSTER_SMS overrides the measured figure) and
+ * the sixteen-SM slots that can run at once (NLM_RAGGED_W16_SLOTS overrides it; 0 when no medium of
+ * the call has that form).  No counterpart in the reference (measurement support). */
+nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* slots_w16,
+                                int* ragged_ctas, long* graph_captures, long* graph_replays, int* sm_budget,
+                                int* w16_capacity);
 
 /* --- gradients (no counterpart in the reference) -------------------------------------------
  * Reverse-mode gradients of a functional L of the output spectra of a Chi2PDC batch with respect to
@@ -257,9 +259,11 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
  * Chi2PDC reverse sweeps) and the Chi3 pump march use clusters with one point per thread instead;
  * on 2048 and 4096 points, full-grid propagations, the costliest ragged media and the Chi3 pump
  * march use eight CTAs with one point per thread.
- * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  Also used by
- * nlm_ragged_batch for the costliest media.  Other values: NLM_ERR_VALUE.  No counterpart in the
- * reference. */
+ * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  3: as 1, with
+ * sixteen CTAs (a non-portable cluster size) in place of eight for those 2048- and 4096-point
+ * launches where the solver has that form.  nlm_ragged_batch plans each medium's form among those
+ * its mode allows (1 and 3: one, four, eight or sixteen CTAs).  Other values: NLM_ERR_VALUE.  No
+ * counterpart in the reference. */
 nlm_status nlm_set_cluster(nlm_medium* m, int enable);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float

@@ -22,7 +22,8 @@ CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_
                 "nlm_noalloc.cu", "adjoint.cu", "prop_ragged.cu", "adjoint_gnlse.cu", "prop_ff.cu", "prop_direct_c.cu", "prop_cluster.cu", "prop_cluster_b.cu", "prop_cluster_gnlse.cu", "prop_cluster_pump.cu", "prop_spread.cu", "prop_spread_b.cu",
                 "adjoint_gnlse_cluster.cu", "adjoint_cluster.cu", "adjoint_spread.cu",
                 "greens_quadrature.cu", "prop_gen_a.cu", "prop_gen_b.cu",
-                "prop_gen_c.cu", "prop_gen_d.cu", "prop_gen_e.cu", "prop_spread_fused.cu"]
+                "prop_gen_c.cu", "prop_gen_d.cu", "prop_gen_e.cu", "prop_spread_fused.cu",
+                "prop_spread_w16.cu"]
 CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]
 
 

@@ -672,7 +672,7 @@ nlm_status nlm_set_schedule(nlm_medium* h, int cta_per_sm, int use_propagator, i
 nlm_status nlm_set_cluster(nlm_medium* h, int enable) {
   return guarded([&] {
     Medium* m = M(h);
-    if (enable < 0 || enable > 2) throw std::invalid_argument("cluster mode must be 0, 1 or 2");
+    if (enable < 0 || enable > 3) throw std::invalid_argument("cluster mode must be 0, 1, 2 or 3");
     m->useCluster = enable;
     for (Medium* c : m->media) c->useCluster = m->useCluster;
   });

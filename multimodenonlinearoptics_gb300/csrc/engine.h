@@ -1542,26 +1542,49 @@ struct Medium {
   // A grid whose single propagations run on a 4-CTA cluster with one point per thread (prop_spread.cu):
   // M = N/4 threads per CTA gives one to eight warps per SM, where the four-points-per-thread cluster
   // form would give at most two (or, below 1024 points, is not built) and one CTA has one SM's FP64.
+  // cluster mode 3 is mode 1 with sixteen CTAs in place of eight on 2048 and 4096 points
   bool spreadGrid() const {
-    return useCluster == 1 && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;
+    return (useCluster == 1 || useCluster == 3) && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;
   }
   // 2048- and 4096-point grids: one point per thread on eight CTAs (prop_spread_b.cu), twice the SMs of
   // the four-points-per-thread cluster, for the launches that no reverse sweep pairs with (full grids,
   // the media of ragged batches marked by raggedWide) and the Chi3 pump march.
   bool wideGrid() const {
-    return useCluster == 1 && is_pow2((int)N) && N > kSpreadMaxN && N <= kWideMaxN;
+    return (useCluster == 1 || useCluster == 3) && is_pow2((int)N) && N > kSpreadMaxN && N <= kWideMaxN;
   }
   bool wideLaunch(const PropArgs& a) const {
-    return wideGrid() && !a.ckpt && !a.stages && (a.gridF || a.gridT || raggedWide);
+    return wideGrid() && !a.ckpt && !a.stages && (a.gridF || a.gridT || raggedWide || raggedW16);
+  }
+  // Grids that also take eight CTAs with one point per thread: from 1024 points (128 per CTA) when a
+  // ragged plan gives a 1024-point medium that form, or in cluster mode 3
+  bool w8Grid() const {
+    return (useCluster == 1 || useCluster == 3) && is_pow2((int)N) && N >= kSpreadMaxN && N <= kWideMaxN;
+  }
+  bool w8Launch(const PropArgs& a) const {
+    if (!w8Grid() || a.ckpt || a.stages) return false;
+    if (N > kSpreadMaxN) return wideLaunch(a);
+    return raggedWide || (useCluster == 3 && (a.gridF || a.gridT));
   }
   bool raggedWide = false;   // set by nlm_ragged_batch around the propagation of a medium given 8 CTAs
+  bool raggedW16 = false;    // ... given 16 CTAs
+
+  // The sixteen-CTA kernel of this medium (prop_spread_w16.cu): single-mode solvers, and multi-mode
+  // solvers in the mode-fused form where its buffers fit in shared memory; nullptr otherwise.
+  const KernelEntry* w16Kernel() const {
+    if (!wideGrid()) return nullptr;
+    if (nSignal < 2) return findKernel(kKindCluster, solver + kSpreadW16Key, 1);
+    const KernelEntry* kf = findKernel(kKindSpreadFused, solver + kSpreadW16Key, 1);
+    return kf && fusedFits(kf, 16) ? kf : nullptr;
+  }
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
     // checkpointed forwards (the adjoint's, Chi2PDC and Chi3GNLSE) run on clusters too: their reverse
     // sweeps have cluster forms that read the same checkpoints
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
-    if (wideLaunch(a) && nInst * 8 <= smCount())
+    if (wideLaunch(a) && (useCluster == 3 || raggedW16) && nInst * 16 <= smCount())
+      if (const KernelEntry* k16 = w16Kernel()) return k16;
+    if (w8Launch(a) && nInst * 8 <= smCount())
       if (const KernelEntry* kw = findKernel(kKindCluster, solver + kSpreadWideKey, 1)) return fusedSpread(kw, 8);
     if (nInst * kClusterSize > smCount()) return nullptr;
     // the spread grids: one point per thread (the Chi2PDC reverse sweep has the same form,
@@ -1577,22 +1600,26 @@ struct Medium {
   const KernelEntry* fusedSpread(const KernelEntry* k, int C) const {
     if (nSignal < 2) return k;
     const KernelEntry* kf = findKernel(kKindSpreadFused, k->key, 1);
-    if (!kf) return k;
+    return kf && fusedFits(kf, C) ? kf : k;
+  }
+  // whether the mode-fused kernel kf of C CTAs fits its buffers in one CTA's shared memory
+  bool fusedFits(const KernelEntry* kf, int C) const {
     int dev = 0, optin = 0;
     cudaFuncAttributes fa;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
         cudaFuncGetAttributes(&fa, kf->fn) != cudaSuccess) {
       cudaGetLastError();
-      return k;
+      return false;
     }
     const long long need = spread_smem_per_point_k(C, (int)nSignal) * (long long)(N / C) * (long long)sizeof(double2);
-    return need + (long long)fa.sharedSizeBytes <= optin ? kf : k;
+    return need + (long long)fa.sharedSizeBytes <= optin;
   }
 
   void launchCluster(const KernelEntry* k, PropArgs a, long long nInst) {
-    const bool spread = k->R == 1;   // one point per thread (prop_spread.cu, prop_spread_b.cu)
-    const int C = k->key >= kSpreadWideKey ? 8 : kClusterSize;
+    const bool spread = k->R == 1;   // one point per thread (prop_spread.cu, prop_spread_b.cu, prop_spread_w16.cu)
+    const int C = k->key >= kSpreadW16Key ? 16 : k->key >= kSpreadWideKey ? 8 : kClusterSize;
+    if (C > 8) ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1), "cluster size");
     const int M = (int)N / C;
     a.plan = make_plan(M, spread ? 1 : C);
     a.R = spread ? 1 : C;

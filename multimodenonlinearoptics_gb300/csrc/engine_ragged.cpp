@@ -1,10 +1,11 @@
 // engine_ragged.cpp -- nlm_ragged_batch: one call over a ragged set of media (different grids and step
 // counts), scheduled for its makespan over the SMs and captured into a CUDA graph.
 //
-// Every medium is a sequential z march; it can run in one of three forms:
+// Every medium is a sequential z march; it can run in one of four forms:
 //   one  -- one CTA (one SM) in the ragged launch, whose CTAs claim media largest first;
 //   c4   -- a 4-CTA cluster on four SMs (one point per thread up to 1024 points, four from 2048);
-//   w8   -- an 8-CTA cluster on eight SMs, one point per thread (2048 and 4096 points).
+//   w8   -- an 8-CTA cluster on eight SMs, one point per thread (2048 and 4096 points);
+//   w16  -- a 16-CTA cluster (a non-portable size) on sixteen SMs, one point per thread.
 // The larger forms finish a medium sooner but spend more SM time on it.  The planner picks a target
 // makespan T (the smallest feasible one, scanned upward): every medium takes the form of least SM time that finishes within T;
 // cluster-form media are packed first-fit, largest first, into slots (a stream running its media one
@@ -24,17 +25,17 @@ namespace {
 
 using namespace nlm;
 
-enum Form { kOne = 0, kC4 = 1, kW8 = 2, kForms = 3 };
-constexpr int kFormSMs[kForms] = {1, 4, 8};
+enum Form { kOne = 0, kC4 = 1, kW8 = 2, kW16 = 3, kForms = 4 };
+constexpr int kFormSMs[kForms] = {1, 4, 8, 16};
 
 // Per-step time (microseconds) of a two-mode pump-driven medium (Chi2SFG) in each form on a GB300,
 // measured with one propagation of 1199 steps per form: [RK4 propagator used][form][log2 N - 7] for
-// N = 128 .. 2048.  Zero: the form does not exist for that grid.  Larger grids scale as N log2 N from
+// N = 128 .. 2048 (eight CTAs from 1024 points, sixteen at 2048).  Zero: the form does not exist for that grid.  Larger grids scale as N log2 N from
 // the table's end, smaller ones take the 128-point time (latency-bound); other solvers scale with
 // their mode count.
 constexpr double kStepUs[2][kForms][5] = {
-    {{26.4, 27.9, 34.8, 67.9, 137.8}, {8.8, 9.7, 11.6, 21.8, 41.8}, {0, 0, 0, 0, 27.4}},
-    {{18.4, 19.9, 27.8, 51.8, 99.5}, {6.7, 7.6, 9.4, 17.2, 33.7}, {0, 0, 0, 0, 23.4}}};
+    {{26.4, 27.9, 34.8, 67.9, 137.8}, {8.8, 9.7, 11.6, 21.8, 41.8}, {0, 0, 0, 14.6, 27.4}, {0, 0, 0, 0, 21.1}},
+    {{18.4, 19.9, 27.8, 51.8, 99.5}, {6.7, 7.6, 9.4, 17.2, 33.7}, {0, 0, 0, 12.8, 23.4}, {0, 0, 0, 0, 19.2}}};
 
 double step_us(int form, uint N, uint modes, bool prop) {
   int lg = 0;
@@ -76,7 +77,8 @@ double lpt_makespan(const std::vector<double>& times, int m) {
 }
 
 // Plan for target makespan T (us); false when the slots and the ragged launch need more than `sms` SMs.
-bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
+// maxW16: the sixteen-CTA slots that can run at once (one per GPC that holds sixteen SMs).
+bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, Plan* out) {
   Plan p;
   p.form.assign(jobs.size(), -1);
   std::vector<double> slotLoad;
@@ -84,27 +86,40 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, Plan* out) {
   std::vector<size_t> order(jobs.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = i;
   std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a].best() > jobs[b].best(); });
-  int used = 0;
+  int used = 0, w16 = 0;
   for (size_t i : order) {
     const Job& j = jobs[i];
-    // the form of least SM time that finishes within T
-    int f = -1;
+    // the forms that finish within T, least SM time first; a slot form takes the first slot of its
+    // form with room, or a new slot (sixteen-CTA slots up to maxW16)
+    int forms[kForms], nf = 0;
     for (int c = 0; c < kForms; c++)
-      if (j.t[c] >= 0 && j.t[c] <= T && (f < 0 || j.t[c] * kFormSMs[c] < j.t[f] * kFormSMs[f])) f = c;
-    if (f < 0) return false;
-    p.form[i] = f;
-    if (f == kOne) continue;
-    size_t s = 0;
-    for (; s < slotLoad.size(); s++)
-      if (p.slotForm[s] == f && slotLoad[s] + j.t[f] <= T) break;
-    if (s == slotLoad.size()) {
-      slotLoad.push_back(0);
-      p.slotForm.push_back(f);
-      p.slots.emplace_back();
-      used += kFormSMs[f];
+      if (j.t[c] >= 0 && j.t[c] <= T) forms[nf++] = c;
+    std::sort(forms, forms + nf, [&](int a, int b) { return j.t[a] * kFormSMs[a] < j.t[b] * kFormSMs[b]; });
+    bool placed = false;
+    for (int q = 0; q < nf && !placed; q++) {
+      const int f = forms[q];
+      if (f == kOne) {
+        p.form[i] = f;
+        placed = true;
+        break;
+      }
+      size_t s = 0;
+      for (; s < slotLoad.size(); s++)
+        if (p.slotForm[s] == f && slotLoad[s] + j.t[f] <= T) break;
+      if (s == slotLoad.size()) {
+        if (f == kW16 && w16 >= maxW16) continue;
+        slotLoad.push_back(0);
+        p.slotForm.push_back(f);
+        p.slots.emplace_back();
+        used += kFormSMs[f];
+        if (f == kW16) w16++;
+      }
+      slotLoad[s] += j.t[f];
+      p.slots[s].push_back(i);
+      p.form[i] = f;
+      placed = true;
     }
-    slotLoad[s] += j.t[f];
-    p.slots[s].push_back(i);
+    if (!placed) return false;
   }
   if (used > sms) return false;
   // per ragged launch class (the CTAs of a launch are sized for its grid), the fewest one-SM CTAs
@@ -157,6 +172,34 @@ int cluster_capacity_sms(const void* fn, int sms) {
   return cached;
 }
 int g_capacityUsed = 0;
+std::map<std::vector<double>, Plan> g_planCache;   // recent sets' plans (under the ragged workspace's mutex)
+
+// Sixteen-CTA clusters of medium m's kernel (prop_spread_w16.cu), each CTA alone on its SM, that fit
+// on the device at once: one per GPC of sixteen SMs or more.  Measured once per process with the
+// occupancy API; NLM_RAGGED_W16_SLOTS overrides the figure (0 turns the form off).
+int w16_capacity(Medium* m) {
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  if (const char* env = std::getenv("NLM_RAGGED_W16_SLOTS")) return cached = std::max(0, std::atoi(env));
+  cached = 0;
+  const KernelEntry* k = m->w16Kernel();
+  if (!k) return cached;
+  const int M = (int)m->N / 16;
+  const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(16, (int)m->nSignal)
+                                                         : spread_smem_per_point(16);
+  size_t smem = 0;
+  if (exclusive_smem(k->fn, (size_t)perPoint * M * sizeof(double2), &smem) != cudaSuccess || smem == 0 ||
+      cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return cached;
+  }
+  cudaLaunchAttribute attr;
+  cudaLaunchConfig_t cfg = cluster_config(16, M, smem, nullptr, 16, &attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k->fn, &cfg) == cudaSuccess) cached = n;
+  else cudaGetLastError();
+  return cached;
+}
 
 }  // namespace
 
@@ -192,11 +235,11 @@ static RaggedWorkspace g_ragged;
 // What the last call planned and ran (nlm_ragged_last_plan).
 struct RaggedStats {
   double makespan;
-  int slotsC4, slotsW8, raggedCTAs;
+  int slotsC4, slotsW8, slotsW16, raggedCTAs;
   long captures, replays;
-  int budget;
+  int budget, w16Capacity;
 };
-static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0, 0};
+static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0, 0, 0, 0};
 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
                             double* const* outputs) {
@@ -238,16 +281,23 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       Medium* m = ms[k];
       int lg = 0;
       while ((1u << lg) < m->N) lg++;
-      Job j{k, m->solver * 64 + lg, {-1, -1, -1}};
+      Job j{k, m->solver * 64 + lg, {-1, -1, -1, -1}};
       const double steps = (double)(m->nZ > 1 ? m->nZ - 1 : 1);
       j.t[kOne] = step_us(kOne, m->N, m->nSignal, withProp[k]) * steps;
       // four CTAs: one point per thread on the spread grids, four points per thread from 1024 points
       const bool c4 = (m->spreadGrid() && m->findKernel(kKindCluster, m->solver, 1)) || m->clusterGrid();
       if (c4) j.t[kC4] = step_us(kC4, m->N, m->nSignal, withProp[k]) * steps;
-      if (m->wideGrid() && m->findKernel(kKindCluster, m->solver + kSpreadWideKey, 1))
+      if (m->w8Grid() && m->findKernel(kKindCluster, m->solver + kSpreadWideKey, 1))
         j.t[kW8] = step_us(kW8, m->N, m->nSignal, withProp[k]) * steps;
+      if (m->w16Kernel()) j.t[kW16] = step_us(kW16, m->N, m->nSignal, withProp[k]) * steps;
       jobs.push_back(j);
     }
+    int maxW16 = 0;
+    for (const Job& j : jobs)
+      if (j.t[kW16] >= 0) {
+        maxW16 = w16_capacity(ms[j.k]);
+        break;
+      }
     // the makespan lies between the longest medium in its fastest form and every medium on one SM one
     // after another; the plan may use the SMs that clusters of four can hold at once (the slots and
     // the ragged launches are all launched as clusters)
@@ -260,11 +310,27 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       hi += j.t[kOne] >= 0 ? j.t[kOne] : j.best();
     }
     // feasibility need not be monotonic in T (a medium at the edge of T moves between forms), so the
-    // targets are scanned upward in steps of 1 % and the first feasible one is taken
+    // targets are scanned upward in steps of 0.25 % and the first feasible one is taken.  The plans of
+    // recent sets are kept: a repeated call (the same estimates, budget and slot capacity) reuses its
+    // plan without the scan.
+    std::vector<double> planKey{(double)budget, (double)maxW16};
+    for (const Job& j : jobs) {
+      planKey.push_back((double)j.cls);
+      planKey.insert(planKey.end(), j.t, j.t + kForms);
+    }
     Plan plan;
     bool planned = false;
-    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.01) planned = plan_for(jobs, T, budget, &plan);
-    if (!planned) planned = plan_for(jobs, hi, budget, &plan);
+    auto cached = g_planCache.find(planKey);
+    if (cached != g_planCache.end()) {
+      plan = cached->second;
+      planned = true;
+    }
+    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.0025) planned = plan_for(jobs, T, budget, maxW16, &plan);
+    if (!planned) planned = plan_for(jobs, hi, budget, maxW16, &plan);
+    if (planned && cached == g_planCache.end()) {
+      if (g_planCache.size() >= 16) g_planCache.erase(g_planCache.begin());
+      g_planCache[planKey] = plan;
+    }
     if (!planned) {
       // no plan fits the SMs at once (more cluster-only media than they hold): every medium in its
       // fastest form, each cluster medium in a slot of its own, the slots queueing for SMs
@@ -410,15 +476,16 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
           const cudaStream_t own = m->stream;
           m->stream = st;
           m->raggedWide = plan.slotForm[s] == kW8;
+          m->raggedW16 = plan.slotForm[s] == kW16;
           try {
             m->propagate(rowArgs(m, k, m->chooseR()), 1, withProp[k]);
           } catch (...) {
             m->stream = own;
-            m->raggedWide = false;
+            m->raggedWide = m->raggedW16 = false;
             throw;
           }
           m->stream = own;
-          m->raggedWide = false;
+          m->raggedWide = m->raggedW16 = false;
         }
       }
       for (size_t r = 0; r < raggedLaunches.size(); r++, si++) {
@@ -485,22 +552,27 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (size_t i = 0; i < jobs.size(); i++)
       if (plan.form[i] != kOne) ms[jobs[i].k]->launches++;
     for (const RaggedLaunch& rl : raggedLaunches) ms[jobs[itemJob[rl.first]].k]->launches++;
-    g_lastRagged = RaggedStats{plan.makespan, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays, budget};
-    for (int f : plan.slotForm) (f == kW8 ? g_lastRagged.slotsW8 : g_lastRagged.slotsC4)++;
+    g_lastRagged =
+        RaggedStats{plan.makespan, 0, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays, budget, maxW16};
+    for (int f : plan.slotForm)
+      (f == kW16 ? g_lastRagged.slotsW16 : f == kW8 ? g_lastRagged.slotsW8 : g_lastRagged.slotsC4)++;
     for (const RaggedLaunch& rl : raggedLaunches) g_lastRagged.raggedCTAs += rl.grid;
     for (size_t k : fused)
       std::memcpy(outputs[k], g_ragged.hout.p + outOff[k], (size_t)ms[k]->nSignal * ms[k]->N * sizeof(double2));
   });
 }
 
-nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* ragged_ctas,
-                                long* graph_captures, long* graph_replays, int* sm_budget) {
+nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* slots_w16,
+                                int* ragged_ctas, long* graph_captures, long* graph_replays, int* sm_budget,
+                                int* w16_capacity) {
   return guarded([&] {
     std::lock_guard<std::mutex> lock(g_ragged.mu);
     if (sm_budget) *sm_budget = g_lastRagged.budget;
+    if (w16_capacity) *w16_capacity = g_lastRagged.w16Capacity;
     if (makespan_estimate_us) *makespan_estimate_us = g_lastRagged.makespan;
     if (slots_c4) *slots_c4 = g_lastRagged.slotsC4;
     if (slots_w8) *slots_w8 = g_lastRagged.slotsW8;
+    if (slots_w16) *slots_w16 = g_lastRagged.slotsW16;
     if (ragged_ctas) *ragged_ctas = g_lastRagged.raggedCTAs;
     if (graph_captures) *graph_captures = g_lastRagged.captures;
     if (graph_replays) *graph_replays = g_lastRagged.replays;

@@ -147,8 +147,9 @@ constexpr long long kSpreadSmemPerPoint = spread_smem_per_point(4);
 // Registry key offset of the instantiations for the general plan (FFTPlanH::gen == 1): grids that are
 // not powers of two (kKindDirect, kKindLinear, kKindGnlse).
 constexpr int kGenKey = 2000;
-// Registry key offset (kKindCluster) of the one-point-per-thread kernels on eight CTAs.
+// Registry key offset (kKindCluster) of the one-point-per-thread kernels on eight CTAs, and on sixteen.
 constexpr int kSpreadWideKey = 800;
+constexpr int kSpreadW16Key = 900;
 
 // Chi3 pump march on a 4-CTA cluster with one point per thread (prop_spread.cu); N = 4 M, M a power of
 // two from 32 to 1024.

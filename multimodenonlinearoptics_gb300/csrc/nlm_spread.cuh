@@ -5,7 +5,8 @@
 // give a grid of N points N/16 threads per CTA: below N = 2048 that is fewer than four warps per SM,
 // so some schedulers idle.  Here every CTA holds M = N/4 points, one per thread: N = 512 gives four
 // warps on each of the four SMs, four times the FP64 issue of one SM.  With C = 8 CTAs (M = N/8) the
-// same form doubles the SMs of a 2048- or 4096-point propagation.  The transforms:
+// same form doubles the SMs of a 2048- or 4096-point propagation, and C = 16 (a non-portable cluster
+// size) doubles them again for the longest marches of a ragged batch.  The transforms:
 //   time domain:       CTA c, thread j  <->  point n = c + C j
 //   frequency domain:  CTA c, thread j  <->  bin   k = j + M c
 // forward:  M-point DFT over j of the CTA's strided points (radix-2 Stockham through shared memory,
@@ -115,7 +116,7 @@ __device__ __forceinline__ double2 spread_combine(const SpreadFFT& f, const doub
     const double2 a = make_double2(fma(sg, r[2].x, r[0].x), fma(sg, r[2].y, r[0].y));
     const double2 b = quarter(make_double2(fma(sg, r[3].x, r[1].x), fma(sg, r[3].y, r[1].y)));
     return make_double2(a.x + b.x, a.y + b.y);
-  } else {
+  } else if constexpr (C == 8) {
     // u_c = r_c + (-1)^r r_(c+4); v0 = u0 + W_4^r u2, v1 = u1 + W_4^r u3; out = v0 + W_8^r v1
     double2 u[4];
 #pragma unroll
@@ -126,6 +127,29 @@ __device__ __forceinline__ double2 spread_combine(const SpreadFFT& f, const doub
     const double2 w = f.twM[rk * (f.M / 8)];    // W_8^r = W_M^(r M / 8)
     const double wy = INV ? -w.y : w.y;
     return make_double2(fma(-wy, v1.y, fma(w.x, v1.x, v0.x)), fma(wy, v1.x, fma(w.x, v1.y, v0.y)));
+  } else {
+    // sixteen CTAs: u_c = r_c + (-1)^r r_(c+8) (c < 8); w_c = u_c + W_4^r u_(c+4) (c < 4);
+    // y_c = w_c + W_8^r w_(c+2) (c < 2); out = y_0 + W_16^r y_1
+    static_assert(C == 16, "four, eight or sixteen CTAs");
+    double2 u[8], w[4];
+#pragma unroll
+    for (int c = 0; c < 8; c++) u[c] = make_double2(fma(sg, r[c + 8].x, r[c].x), fma(sg, r[c + 8].y, r[c].y));
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const double2 q4 = quarter(u[c + 4]);
+      w[c] = make_double2(u[c].x + q4.x, u[c].y + q4.y);
+    }
+    const double2 w8 = f.twM[(rk & 7) * (f.M / 8)];   // W_8^r
+    const double w8y = INV ? -w8.y : w8.y;
+    double2 y[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++)
+      y[c] = make_double2(fma(-w8y, w[c + 2].y, fma(w8.x, w[c + 2].x, w[c].x)),
+                          fma(w8y, w[c + 2].x, fma(w8.x, w[c + 2].y, w[c].y)));
+    const double2 w16 = f.twM[rk * (f.M / 16)];       // W_16^r = W_M^(r M / 16)
+    const double w16y = INV ? -w16.y : w16.y;
+    return make_double2(fma(-w16y, y[1].y, fma(w16.x, y[1].x, y[0].x)),
+                        fma(w16y, y[1].x, fma(w16.x, y[1].y, y[0].y)));
   }
 }
 
@@ -133,7 +157,7 @@ __device__ __forceinline__ double2 spread_combine(const SpreadFFT& f, const doub
 // C CTAs; after the barrier thread j of CTA r returns sum_c W_C^(+-r c) recv[c][j].
 template <bool INV, int C = kSpreadC>
 __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::cluster_group& cl) {
-  static_assert(C == 4 || C == 8, "four or eight CTAs");
+  static_assert(C == 4 || C == 8 || C == 16, "four, eight or sixteen CTAs");
   const int M = f.M;
   double2* half = f.recv + (long long)f.phase * C * M;
 #pragma unroll
@@ -188,7 +212,7 @@ __device__ __forceinline__ void spread_local_k(SpreadFFT& f, double2 (&x)[K]) {
 
 template <bool INV, int C, int K>
 __device__ __forceinline__ void spread_exchange_k(SpreadFFT& f, double2 (&y)[K], cg::cluster_group& cl) {
-  static_assert(C == 4 || C == 8, "four or eight CTAs");
+  static_assert(C == 4 || C == 8 || C == 16, "four, eight or sixteen CTAs");
   const int M = f.M;
   double2* half = f.recv + (long long)f.phase * C * K * M;
 #pragma unroll

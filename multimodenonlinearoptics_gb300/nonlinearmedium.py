@@ -62,7 +62,7 @@ def _load():
         "nlm_batch": (i, [vp, P(d), sz, sz, i, i, u, u, P(u8), sz, P(d)]),
         "nlm_batch_device": (i, [vp, vp, sz, sz, i, i, u, u, P(u8), sz, vp]),
         "nlm_ragged_batch": (i, [P(vp), sz, P(P(d)), i, P(P(d))]),
-        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i)]),
+        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i), P(i)]),
         "nlm_get_grid": (i, [vp, i, u, P(P(d)), P(sz), P(sz)]),
         "nlm_get_axis": (i, [vp, i, u, P(P(d)), P(sz)]),
         "nlm_cascade_create": (i, [P(vp), sz, P(u), P(sz), sz, i, P(vp)]),
@@ -158,15 +158,17 @@ def ragged_batch(media, inputs, inTimeDomain=False):
 
 def ragged_last_plan():
     """The plan of the last ragged_batch call (no counterpart in the reference): estimated makespan
-    (ms), cluster slots of four and eight SMs, CTAs of the one-SM ragged launches, the CUDA-graph
-    captures and replays of ragged calls so far, and the SMs the plan could use."""
-    ms, c4, w8, ctas = ctypes.c_double(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    cap, rep, budget = ctypes.c_long(), ctypes.c_long(), ctypes.c_int()
-    _check(_lib.nlm_ragged_last_plan(ctypes.byref(ms), ctypes.byref(c4), ctypes.byref(w8), ctypes.byref(ctas),
-                                     ctypes.byref(cap), ctypes.byref(rep), ctypes.byref(budget)))
+    (ms), cluster slots of four, eight and sixteen SMs, CTAs of the one-SM ragged launches, the
+    CUDA-graph captures and replays of ragged calls so far, the SMs the plan could use and the
+    sixteen-SM slots that can run at once."""
+    ms, c4, w8, w16, ctas = ctypes.c_double(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    cap, rep, budget, w16cap = ctypes.c_long(), ctypes.c_long(), ctypes.c_int(), ctypes.c_int()
+    _check(_lib.nlm_ragged_last_plan(ctypes.byref(ms), ctypes.byref(c4), ctypes.byref(w8), ctypes.byref(w16),
+                                     ctypes.byref(ctas), ctypes.byref(cap), ctypes.byref(rep), ctypes.byref(budget),
+                                     ctypes.byref(w16cap)))
     return {"makespan_estimate_ms": ms.value / 1e3, "slots_c4": c4.value, "slots_w8": w8.value,
-            "ragged_ctas": ctas.value, "graph_captures": cap.value, "graph_replays": rep.value,
-            "sm_budget": budget.value}
+            "slots_w16": w16.value, "ragged_ctas": ctas.value, "graph_captures": cap.value,
+            "graph_replays": rep.value, "sm_budget": budget.value, "w16_capacity": w16cap.value}
 
 
 def fp64_peak_tflops():
@@ -356,8 +358,10 @@ class _NonlinearMedium:
 
     def _set_cluster(self, enable):
         """Spread each propagation of small launches over a 4-CTA cluster: 1 (default) with one point
-        per thread on 128..1024-point grids (and the Chi3 pump march there), 2 with
-        four points per thread only (grids of 1024 points and more), 0 one CTA per propagation."""
+        per thread on 128..1024-point grids (and the Chi3 pump march there), and on eight CTAs for
+        full grids of 2048 and 4096 points; 3 the same with sixteen CTAs in place of eight where the
+        solver has that form; 2 four points per thread only (grids of 1024 points and more); 0 one CTA
+        per propagation."""
         _check(_lib.nlm_set_cluster(self._h(), int(enable)))
 
     def _set_precision(self, precision):

@@ -164,6 +164,86 @@ def test_wide_spread_every_multimode_solver(nlm, oracle, name):
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
 
 
+@pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
+def test_sixteen_cta_spread_every_solver(nlm, oracle, name):
+    """Cluster mode 3: runSignalSimulation on 2048 points over sixteen CTAs with one point per thread
+    (128 threads each; multi-mode solvers with their modes in each transform together, up to three
+    modes), against the oracle's full grids and the eight-CTA form."""
+    kw = dict(cases.CASES[name], tPrecision=2048, tMax=cases.CASES[name]["tMax"] * 8)
+    med, ref, w8 = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
+    med._set_cluster(3)
+    if name not in cases.FULLY_NONLINEAR:
+        for m in (med, w8):
+            m.runPumpSimulation()
+        ref.run_pump_simulation()
+    modes = med._dims["nSignalModes"]
+    a = cases.noise(np.random.default_rng(17), 2048 * modes, 0.3)
+    for in_time in (True, False):
+        med.runSignalSimulation(a, in_time, 0)
+        w8.runSignalSimulation(a, in_time, 0)
+        ref.run_signal_simulation(a, in_time, 0)
+        sched = med._last_schedule()
+        # four modes: the mode-fused buffers of sixteen CTAs do not fit, and eight CTAs run it
+        ctas = 16 if modes <= 3 else 8
+        assert sched["grid"] == ctas and sched["R"] == 1 and sched["block"] == 2048 // ctas
+        assert w8._last_schedule()["grid"] == 8
+        for m in range(modes):
+            assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
+            assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
+            assert cases.rel_l2(med.signalTimes(m), w8.signalTimes(m)) < 1e-12, m
+
+
+@pytest.mark.parametrize("name", ["Chi2PDC", "Chi2SFG"])
+def test_eight_cta_spread_at_1024(nlm, oracle, name):
+    """Cluster mode 3 on 1024 points: eight CTAs of 128 threads (the form a ragged plan gives its long
+    1024-point marches), both input domains, against the oracle and the four-CTA form."""
+    kw = dict(MEDIA[name], tPrecision=1024)
+    med, ref, c4 = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
+    med._set_cluster(3)
+    for m in (med, c4):
+        m.runPumpSimulation()
+    ref.run_pump_simulation()
+    modes = med._dims["nSignalModes"]
+    a = cases.noise(np.random.default_rng(21), 1024, 0.2)
+    for in_time in (True, False):
+        med.runSignalSimulation(a, in_time)
+        c4.runSignalSimulation(a, in_time)
+        ref.run_signal_simulation(a, in_time)
+        sched = med._last_schedule()
+        assert sched["grid"] == 8 and sched["block"] == 128 and c4._last_schedule()["grid"] == 4
+        for m in range(modes):
+            assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
+            assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL
+            assert cases.rel_l2(med.signalFreqs(m), c4.signalFreqs(m)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_sixteen_cta_spread_single_mode(nlm, oracle, n):
+    """Cluster mode 3 on Chi2PDC at 2048 and 4096 points (256 threads per CTA at 4096), both input
+    domains, against the oracle; a 4096-point two-mode medium, whose mode-fused buffers do not fit,
+    keeps eight CTAs."""
+    kw = dict(MEDIA["Chi2PDC"], tPrecision=n)
+    med, ref = nlm.Chi2PDC(**kw), oracle.Chi2PDC(**kw)
+    med._set_cluster(3)
+    med.runPumpSimulation()
+    ref.run_pump_simulation()
+    a = cases.noise(np.random.default_rng(n + 5), n, 0.2)
+    for in_time in (True, False):
+        med.runSignalSimulation(a, in_time)
+        ref.run_signal_simulation(a, in_time)
+        sched = med._last_schedule()
+        assert sched["grid"] == 16 and sched["block"] == n // 16
+        assert cases.rel_l2(med.signalTimes(0), ref.signal_time[0]) < TOL
+        assert cases.rel_l2(med.signalFreqs(0), ref.signal_freq[0]) < TOL
+    if n == 4096:
+        kw2 = dict(MEDIA["Chi2SFG"], tPrecision=n)
+        m2 = nlm.Chi2SFG(**kw2)
+        m2._set_cluster(3)
+        m2.runPumpSimulation()
+        m2.runSignalSimulation(cases.noise(np.random.default_rng(3), n, 0.2))
+        assert m2._last_schedule()["grid"] == 8
+
+
 @pytest.mark.parametrize("n", [128, 256, 512, 1024, 2048, 4096])
 @pytest.mark.parametrize("name", ["Chi2PDC", "Chi3", "Chi2SFG"])
 def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
