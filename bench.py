@@ -585,8 +585,9 @@ def measure_configs(nlm, torch, cpu=True):
                                       "pumps": "rerun before each call: every medium propagates with its DiffEq "
                                                "(RK4 matrices are built only for a pump used again)",
                                       "gpu_wall_ms_pumps_kept": 1e3 * min(wall_kept),
-                                      "form": "each medium on one SM in a ragged launch or on a 4- or 8-SM cluster "
-                                              "slot, planned for the makespan; the call replayed as a CUDA graph",
+                                      "form": "each medium on one SM in a ragged launch or on a 4-, 8- or 16-SM "
+                                              "cluster slot, planned for the makespan; the call replayed as a CUDA "
+                                              "graph",
                                       "plan": plan,
                                       "gpu_wall_ms_one_cta_per_medium": 1e3 * min(wall_one),
                                       "gpu_wall_ms_one_cta_diffeq_form": 1e3 * min(wall_direct)}
