@@ -175,8 +175,8 @@ nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int
  * nlm_set_poling_profile: replace the domain pattern by d(z) on the nZSteps grid (the values the
  *   reference keeps in its protected _poling array, src/_NonlinearMedium.cpp:470-503).
  * nlm_adjoint_forward: propagate rows x N input spectra (device) to rows x N output spectra (device),
- *   storing the states every checkpoint_interval steps (<= 0: every step when that fits in a quarter of
- *   the free device memory, at most 64 GB, else every ceil(sqrt(nZSteps-1)) steps, the segments
+ *   storing the states every checkpoint_interval steps (<= 0: every step when that fits in 40 % of the
+ *   free device memory, at most 96 GB, else every ceil(sqrt(nZSteps-1)) steps, the segments
  *   being recomputed in the reverse sweep).
  *   Chi3GNLSE with checkpoint_interval <= 0 on a grid of 1024..8192 points, with rows x 4 <= SMs and
  *   the stage values of every step within a quarter of the free device memory (and 64 GB): the

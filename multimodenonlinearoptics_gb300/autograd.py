@@ -58,8 +58,8 @@ class Chi2PDCPropagation(torch.autograd.Function):
 def propagate_pdc(medium, signal_in, pump_spectrum, poling, checkpoint_interval=0):
     """Output spectra (last z row, FFT order) of a Chi2PDC medium; differentiable in all three inputs.
 
-    checkpoint_interval: 0 chooses (every step when the trajectory fits in a quarter of the free device
-    memory, at most 64 GB, else every ceil(sqrt(nZSteps-1)) steps with recomputation of the segments
+    checkpoint_interval: 0 chooses (every step when the trajectory fits in 40 % of the free device
+    memory, at most 96 GB, else every ceil(sqrt(nZSteps-1)) steps with recomputation of the segments
     in the reverse sweep).
     """
     return Chi2PDCPropagation.apply(medium, signal_in, pump_spectrum, poling, checkpoint_interval)

@@ -1992,15 +1992,15 @@ struct Medium {
     }
     int K = interval;
     if (K <= 0) {
-      // every state while the states fit in a quarter of the free device memory (at most 64 GB),
-      // else every ceil(sqrt(steps)) steps
+      // every state while the states fit in 40 % of the free device memory (at most 96 GB: 1024 rows of
+      // 4096 points over 999 steps take 67 GB), else every ceil(sqrt(steps)) steps
       const double bytes = (double)rows * steps * N * sizeof(double2);
       size_t freeB = 0, totalB = 0;
       if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess) {
         cudaGetLastError();
         freeB = 0;
       }
-      K = bytes <= std::max(1e9, std::min(0.25 * (double)freeB, 64e9)) ? 1 : (int)std::ceil(std::sqrt((double)steps));
+      K = bytes <= std::max(1e9, std::min(0.4 * (double)freeB, 96e9)) ? 1 : (int)std::ceil(std::sqrt((double)steps));
     }
     const int nCk = (int)((steps + K - 1) / K);
     ckpt.reserve((size_t)rows * nCk * N);
