@@ -404,10 +404,11 @@ def measure_configs(nlm, torch, cpu=True):
         kw = dict(CONFIG, tPrecision=n, zPrecision=500)
         a = (np.random.default_rng(n).standard_normal(n) + 0j) * 0.1
         row = {"n_freqs": n}
-        # mode 1: one point per thread (four CTAs at 1024 points, eight at 2048); mode 2: four points
-        # per thread on four CTAs, the only cluster form at 8192 points
-        forms = ((0, "one_cta_ms"), (1, "spread_ms"), (2, "cluster_ms")) if n <= 2048 else \
-            ((0, "one_cta_ms"), (1, "cluster_ms"))
+        # mode 1 (default): one point per thread in the widest form (eight CTAs at 1024 points, sixteen
+        # at 2048); mode 3: one point per thread on four CTAs at 1024 points, eight at 2048; mode 2:
+        # four points per thread on four CTAs, the only cluster form at 8192 points
+        forms = ((0, "one_cta_ms"), (1, "spread_ms"), (3, "spread_half_ctas_ms"), (2, "cluster_ms")) \
+            if n <= 2048 else ((0, "one_cta_ms"), (1, "cluster_ms"))
         for use, label in forms:
             m = nlm.Chi2PDC(poling=np.ones(N_DOMAINS), **kw)
             m._set_cluster(use)
@@ -816,13 +817,13 @@ def measure_ff(nlm, torch, args, stream, flush, C64, S64, f64_value, f64_kernel_
 
 def _over_spread(value, configs):
     """Batched throughput over the fastest one-propagation form: one runSignalSimulation of the same
-    medium (N=1024, 1000 steps) spread over a 4-CTA cluster, which also writes both full grids."""
+    medium (N=1024, 1000 steps) spread over an 8-CTA cluster, which also writes both full grids."""
     try:
         ms = configs["single_propagation"]["chi2pdc_run_signal_n1024"]["spread_ms"]
     except (KeyError, TypeError):
         return None
     return {"value": value / (1e3 / ms), "plain_spread_propagations_per_s": 1e3 / ms,
-            "form": "runSignalSimulation on a 4-CTA cluster, one point per thread (full grids written)"}
+            "form": "runSignalSimulation on an 8-CTA cluster, one point per thread (full grids written)"}
 
 
 def run_ours(args):

@@ -257,13 +257,14 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
  * shared memory); so do the Chi3 pump march and the reverse sweeps of nlm_adjoint_backward (on 4
  * or, pipelined, 8 CTAs) on such grids.  On grids of 128 to 1024 points, such launches (and the
  * Chi2PDC reverse sweeps) and the Chi3 pump march use clusters with one point per thread instead;
- * on 2048 and 4096 points, full-grid propagations, the costliest ragged media and the Chi3 pump
- * march use eight CTAs with one point per thread.
- * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  3: as 1, with
- * sixteen CTAs (a non-portable cluster size) in place of eight for those 2048- and 4096-point
- * launches where the solver has that form.  nlm_ragged_batch plans each medium's form among those
- * its mode allows (1 and 3: one, four, eight or sixteen CTAs).  Other values: NLM_ERR_VALUE.  No
- * counterpart in the reference. */
+ * full-grid propagations (runSignalSimulation) take the widest one-point-per-thread form: eight CTAs
+ * at 1024 points, sixteen (a non-portable cluster size) at 2048 and 4096 points where the solver
+ * has that form (single-mode solvers; multi-mode ones whose mode-fused buffers fit), eight otherwise;
+ * the Chi3 pump march uses eight CTAs on 2048 and 4096 points.
+ * 3: as 1 without the widest forms (full grids on four CTAs up to 1024 points, eight above).
+ * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  nlm_ragged_batch plans
+ * each medium's form among those its mode allows (1: one, four, eight or sixteen CTAs; 3: one, four
+ * or eight).  Other values: NLM_ERR_VALUE.  No counterpart in the reference. */
 nlm_status nlm_set_cluster(nlm_medium* m, int enable);
 /* Arithmetic of the single-mode precomputed-propagator kernel (Chi3, Chi2PDC Green's functions
  * and batches on power-of-two grids up to 4096 points): 0 = FP64 (default), 1 = double-float

@@ -1542,7 +1542,8 @@ struct Medium {
   // A grid whose single propagations run on a 4-CTA cluster with one point per thread (prop_spread.cu):
   // M = N/4 threads per CTA gives one to eight warps per SM, where the four-points-per-thread cluster
   // form would give at most two (or, below 1024 points, is not built) and one CTA has one SM's FP64.
-  // cluster mode 3 is mode 1 with sixteen CTAs in place of eight on 2048 and 4096 points
+  // cluster mode 3 is mode 1 without the widest forms (sixteen CTAs on 2048 and 4096 points, eight on
+  // 1024): four CTAs up to 1024 points and eight above, as a reference for them
   bool spreadGrid() const {
     return (useCluster == 1 || useCluster == 3) && is_pow2((int)N) && N >= kSpreadMinN && N <= kSpreadMaxN;
   }
@@ -1555,23 +1556,24 @@ struct Medium {
   bool wideLaunch(const PropArgs& a) const {
     return wideGrid() && !a.ckpt && !a.stages && (a.gridF || a.gridT || raggedWide || raggedW16);
   }
-  // Grids that also take eight CTAs with one point per thread: from 1024 points (128 per CTA) when a
-  // ragged plan gives a 1024-point medium that form, or in cluster mode 3
+  // Grids that take eight CTAs with one point per thread: 2048 and 4096 points, and in cluster mode 1
+  // also 1024 points (128 per CTA) for full grids and the ragged media a plan gives that form
   bool w8Grid() const {
-    return (useCluster == 1 || useCluster == 3) && is_pow2((int)N) && N >= kSpreadMaxN && N <= kWideMaxN;
+    return wideGrid() || (useCluster == 1 && N == kSpreadMaxN);
   }
   bool w8Launch(const PropArgs& a) const {
     if (!w8Grid() || a.ckpt || a.stages) return false;
     if (N > kSpreadMaxN) return wideLaunch(a);
-    return raggedWide || (useCluster == 3 && (a.gridF || a.gridT));
+    return raggedWide || a.gridF || a.gridT;
   }
   bool raggedWide = false;   // set by nlm_ragged_batch around the propagation of a medium given 8 CTAs
   bool raggedW16 = false;    // ... given 16 CTAs
 
-  // The sixteen-CTA kernel of this medium (prop_spread_w16.cu): single-mode solvers, and multi-mode
-  // solvers in the mode-fused form where its buffers fit in shared memory; nullptr otherwise.
+  // The sixteen-CTA kernel of this medium (prop_spread_w16.cu; cluster mode 1): single-mode solvers,
+  // and multi-mode solvers in the mode-fused form where its buffers fit in shared memory; nullptr
+  // otherwise.
   const KernelEntry* w16Kernel() const {
-    if (!wideGrid()) return nullptr;
+    if (useCluster != 1 || !wideGrid()) return nullptr;
     if (nSignal < 2) return findKernel(kKindCluster, solver + kSpreadW16Key, 1);
     const KernelEntry* kf = findKernel(kKindSpreadFused, solver + kSpreadW16Key, 1);
     return kf && fusedFits(kf, 16) ? kf : nullptr;
@@ -1582,7 +1584,9 @@ struct Medium {
     // sweeps have cluster forms that read the same checkpoints
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
-    if (wideLaunch(a) && (useCluster == 3 || raggedW16) && nInst * 16 <= smCount())
+    // full grids and the ragged media given sixteen SMs: the sixteen-CTA form (mode 1); a ragged medium
+    // given eight SMs keeps eight
+    if (wideLaunch(a) && !raggedWide && nInst * 16 <= smCount())
       if (const KernelEntry* k16 = w16Kernel()) return k16;
     if (w8Launch(a) && nInst * 8 <= smCount())
       if (const KernelEntry* kw = findKernel(kKindCluster, solver + kSpreadWideKey, 1)) return fusedSpread(kw, 8);

@@ -52,7 +52,8 @@ def test_cluster_two_modes_match_oracle(nlm, oracle, name, n):
     a = cases.noise(np.random.default_rng(3), n, 0.2)
     med.runSignalSimulation(a)
     ref.run_signal_simulation(a)
-    assert med._last_schedule()["grid"] == (8 if n > 1024 else 4)   # full grids: eight CTAs from 2048
+    # full grids: eight CTAs (two modes fused; sixteen CTAs would not hold their buffers at 4096)
+    assert med._last_schedule()["grid"] == 8
     for m in range(2):
         assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL
@@ -80,8 +81,9 @@ def test_cluster_equals_one_cta_kernels(nlm):
 @pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
 def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
-    """runSignalSimulation of each DiffEq solver on a 1024-point grid runs on a 4-CTA cluster, with one
-    point per thread (mode 1, the default) or four (mode 2), and matches the oracle's full grids."""
+    """runSignalSimulation of each DiffEq solver on a 1024-point grid runs on a cluster: eight CTAs with
+    one point per thread (mode 1, the default) or four CTAs with four (mode 2), and matches the oracle's
+    full grids."""
     kw = dict(cases.CASES[name], tPrecision=1024)
     med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**cases.oracle_kwargs(name) | {"tPrecision": 1024})
     med._set_cluster(mode)
@@ -92,8 +94,9 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
     med.runSignalSimulation(a, True, 0)
     ref.run_signal_simulation(a, True, 0)
     sched = med._last_schedule()
-    assert sched["grid"] == 4 and sched["R"] == (1 if mode == 1 else 4)
-    assert sched["block"] == (256 if mode == 1 else 64)
+    # full grids at 1024 points: eight CTAs of 128 threads (mode 1), four of 64 with four points each
+    assert sched["grid"] == (8 if mode == 1 else 4) and sched["R"] == (1 if mode == 1 else 4)
+    assert sched["block"] == (128 if mode == 1 else 64)
     for m in range(med._dims["nSignalModes"]):
         assert cases.rel_l2(med.signalTimes(m), ref.signal_time[m]) < TOL, m
         assert cases.rel_l2(med.signalFreqs(m), ref.signal_freq[m]) < TOL, m
@@ -145,11 +148,12 @@ def test_cluster_chi3_pump_march(nlm, oracle, n):
 
 @pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE" and n not in ("Chi3", "Chi2PDC")])
 def test_wide_spread_every_multimode_solver(nlm, oracle, name):
-    """runSignalSimulation of every multi-mode solver on 2048 points: eight CTAs with one point per
-    thread, the modes in each transform together where their buffers fit (two modes), one after another
+    """runSignalSimulation of every multi-mode solver on 2048 points in cluster mode 3: eight CTAs with
+    one point per thread, the modes in each transform together where their buffers fit (two modes), one after another
     otherwise (three and four), against the oracle's full grids."""
     kw = dict(cases.CASES[name], tPrecision=2048, tMax=cases.CASES[name]["tMax"] * 8)
     med, ref = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw)
+    med._set_cluster(3)                                  # eight CTAs (mode 1 takes sixteen where it can)
     if name not in cases.FULLY_NONLINEAR:
         med.runPumpSimulation()
         ref.run_pump_simulation()
@@ -166,12 +170,12 @@ def test_wide_spread_every_multimode_solver(nlm, oracle, name):
 
 @pytest.mark.parametrize("name", [n for n in cases.CASES if n != "Chi3GNLSE"])
 def test_sixteen_cta_spread_every_solver(nlm, oracle, name):
-    """Cluster mode 3: runSignalSimulation on 2048 points over sixteen CTAs with one point per thread
-    (128 threads each; multi-mode solvers with their modes in each transform together, up to three
-    modes), against the oracle's full grids and the eight-CTA form."""
+    """runSignalSimulation on 2048 points over sixteen CTAs with one point per thread (the default for
+    full grids; 128 threads each; multi-mode solvers with their modes in each transform together, up
+    to three modes), against the oracle's full grids and the eight-CTA form (cluster mode 3)."""
     kw = dict(cases.CASES[name], tPrecision=2048, tMax=cases.CASES[name]["tMax"] * 8)
     med, ref, w8 = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
-    med._set_cluster(3)
+    w8._set_cluster(3)
     if name not in cases.FULLY_NONLINEAR:
         for m in (med, w8):
             m.runPumpSimulation()
@@ -195,11 +199,11 @@ def test_sixteen_cta_spread_every_solver(nlm, oracle, name):
 
 @pytest.mark.parametrize("name", ["Chi2PDC", "Chi2SFG"])
 def test_eight_cta_spread_at_1024(nlm, oracle, name):
-    """Cluster mode 3 on 1024 points: eight CTAs of 128 threads (the form a ragged plan gives its long
-    1024-point marches), both input domains, against the oracle and the four-CTA form."""
+    """Full grids on 1024 points: eight CTAs of 128 threads (also the form a ragged plan gives its long
+    1024-point marches), both input domains, against the oracle and the four-CTA form (mode 3)."""
     kw = dict(MEDIA[name], tPrecision=1024)
     med, ref, c4 = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
-    med._set_cluster(3)
+    c4._set_cluster(3)
     for m in (med, c4):
         m.runPumpSimulation()
     ref.run_pump_simulation()
@@ -219,12 +223,11 @@ def test_eight_cta_spread_at_1024(nlm, oracle, name):
 
 @pytest.mark.parametrize("n", [2048, 4096])
 def test_sixteen_cta_spread_single_mode(nlm, oracle, n):
-    """Cluster mode 3 on Chi2PDC at 2048 and 4096 points (256 threads per CTA at 4096), both input
-    domains, against the oracle; a 4096-point two-mode medium, whose mode-fused buffers do not fit,
-    keeps eight CTAs."""
+    """Full grids of Chi2PDC at 2048 and 4096 points on sixteen CTAs (256 threads per CTA at 4096), both
+    input domains, against the oracle; a 4096-point two-mode medium, whose mode-fused buffers do not
+    fit, keeps eight CTAs."""
     kw = dict(MEDIA["Chi2PDC"], tPrecision=n)
     med, ref = nlm.Chi2PDC(**kw), oracle.Chi2PDC(**kw)
-    med._set_cluster(3)
     med.runPumpSimulation()
     ref.run_pump_simulation()
     a = cases.noise(np.random.default_rng(n + 5), n, 0.2)
@@ -238,7 +241,6 @@ def test_sixteen_cta_spread_single_mode(nlm, oracle, n):
     if n == 4096:
         kw2 = dict(MEDIA["Chi2SFG"], tPrecision=n)
         m2 = nlm.Chi2SFG(**kw2)
-        m2._set_cluster(3)
         m2.runPumpSimulation()
         m2.runSignalSimulation(cases.noise(np.random.default_rng(3), n, 0.2))
         assert m2._last_schedule()["grid"] == 8
@@ -252,6 +254,7 @@ def test_spread_signal_grids_match_oracle(nlm, oracle, name, n):
     other transform order)."""
     kw = dict(MEDIA[name], tPrecision=n)
     med, ref, one = getattr(nlm, name)(**kw), getattr(oracle, name)(**kw), getattr(nlm, name)(**kw)
+    med._set_cluster(3)                                  # four CTAs to 1024 points, eight above
     one._set_cluster(0)
     for m in (med, one):
         m.runPumpSimulation()
