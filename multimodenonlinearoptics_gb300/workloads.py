@@ -14,7 +14,8 @@ self-contained command for ncu.
 * signal      one Chi2PDC runSignalSimulation (full grids) on the Green's medium at N=2048
 * gnlse_signal  one Chi3GNLSE runSignalSimulation (full grids) on the GNLSE medium at N=4096
 * ragged_wide  one 2048-point Chi2SFG runSignalSimulation with the ragged set's parameters (DiffEq form):
-               the eight-CTA march that sets the ragged set's makespan
+               the march of the ragged set's longest media, on sixteen CTAs (--cluster 1, the
+               default for full grids) or eight (--cluster 3)
 """
 
 import argparse
@@ -109,7 +110,7 @@ def gnlse_rows(rows, n=4096, seed=5):
         * 1e-4 / np.sqrt(2)
 
 
-def _run(name, z_precision, rows, reps):
+def _run(name, z_precision, rows, reps, cluster=1):
     import torch
     from . import nonlinearmedium as nlm
     from .autograd import propagate_gnlse
@@ -179,6 +180,7 @@ def _run(name, z_precision, rows, reps):
             t = np.fft.fftshift(np.linspace(-10, 10, 2048, endpoint=False))
             m = nlm.Chi2SFG(customPump=np.exp(-t ** 2 / 2), poling=[3, 4, 3], **kw)
             m._set_schedule(use_propagator=0)
+            m._set_cluster(cluster)
             m.runPumpSimulation()
             m.runSignalSimulation((np.random.default_rng(1).standard_normal(2048) + 0j) * 1e-3)
         elif name == "gnlse_signal":
@@ -207,10 +209,12 @@ def main():
     ap.add_argument("--zprecision", type=int, default=0, help="zPrecision override (0: the workload's own)")
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")
     ap.add_argument("--reps", type=int, default=1)
+    ap.add_argument("--cluster", type=int, default=1,
+                    help="cluster mode of the ragged_wide medium (1: sixteen CTAs, 3: eight)")
     args = ap.parse_args()
     from . import build_ext
     build_ext.build()
-    _run(args.name, args.zprecision, args.rows, args.reps)
+    _run(args.name, args.zprecision, args.rows, args.reps, args.cluster)
 
 
 if __name__ == "__main__":
