@@ -235,6 +235,58 @@ def test_green_benchmark_config_full_size_properties(nlm):
     assert cases.rel_l2(out, np.fft.fftshift(med.signalFreq[-1])) < 1e-9
 
 
+def test_dispersion_known_answers(nlm):
+    """The reference's dispersion checks (tests/01 - Dispersion.py) on the engine: with no nonlinearity
+    a Gaussian exp(-t^2/2) under beta2 = 1 keeps |A(z, t)| = (1 + z^2)^(-1/4) exp(-t^2 / (2 (1 + z^2)))
+    (Agrawal's dispersion-length broadening), in the pump march and in the signal march (full grids
+    of 2048 points on clusters); a group-velocity mismatch beta1 = 4 (beta1s = -4) moves the pump
+    (signal) by 20 over L = 5."""
+    m = nlm.Chi3(relativeLength=5, nlLength=np.inf, beta2=1, pulseType=0, tPrecision=2048, zPrecision=100, tMax=50)
+    tau = m.tau
+
+    def exact(z):
+        return (1 + z * z) ** -0.25 * np.exp(-tau ** 2 / (2 * (1 + z * z)))
+    m.runPumpSimulation()
+    pt = m.pumpTime
+    assert np.max(np.abs(np.abs(pt[-1]) - exact(5.0))) < 1e-12
+    for i in range(1, 5):
+        r = int((pt.shape[0] - 1) * i / 5)
+        assert np.max(np.abs(np.abs(pt[r]) - exact(5.0 * r / (pt.shape[0] - 1)))) < 2e-3
+    m.runSignalSimulation(np.exp(-0.5 * tau ** 2) + 0j)
+    assert np.max(np.abs(np.abs(m.signalTime[-1]) - exact(5.0))) < 1e-12
+    w = nlm.Chi2PDC(relativeLength=5, nlLength=np.inf, beta2=1, beta2s=-1, pulseType=0, beta1=4, beta1s=-4,
+                    tPrecision=2048, zPrecision=100, tMax=50)
+    w.runPumpSimulation()
+    w.runSignalSimulation(np.exp(-0.5 * tau ** 2) + 0j)
+    for grid, shift in ((w.pumpTime, 20.0), (w.signalTime, 20.0)):
+        p = np.abs(grid[-1]) ** 2
+        assert abs(abs(np.sum(tau * p) / np.sum(p)) - shift) < 1e-9
+    # opposite walk-off: the pump and the signal move apart by 40
+    pp, ps = np.abs(w.pumpTime[-1]) ** 2, np.abs(w.signalTime[-1]) ** 2
+    assert abs(abs(np.sum(tau * pp) / np.sum(pp) - np.sum(tau * ps) / np.sum(ps)) - 40.0) < 1e-8
+
+
+def test_soliton_and_green_known_answers(nlm):
+    """On the engine: an N=1 soliton keeps |A| along the pump march (tests/03 - Nonlinear Propagation --
+    Solitons.py:42-48); the Green's function of a Chi2PDC medium is symplectic, C C^H - S S^H = I and
+    C S^T = S C^T (tests/05 - Hosaka.py:115-121), and reproduces a propagation through
+    a(L) = C a + S a* (tests/04 - Green's Function.py:98-111)."""
+    m = nlm.Chi3(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, tMax=20, tPrecision=256, zPrecision=100)
+    m.runPumpSimulation()
+    assert np.max(np.abs(np.abs(m.pumpTime[-1]) - np.abs(m.pumpTime[0]))) < 1e-4
+    g = nlm.Chi2PDC(relativeLength=1, nlLength=0.5, beta2=1, beta2s=0.5, beta1s=2, beta3s=0.1, tMax=20,
+                    tPrecision=256, zPrecision=20, poling=np.ones(20))
+    C, S = g.computeGreensFunction()
+    n = C.shape[0]
+    # RK4 is symplectic only to its truncation error: 7.7e-9 and 1.4e-9 in the oracle at this size
+    assert np.abs(C @ C.conj().T - S @ S.conj().T - np.eye(n)).max() < 1e-7
+    assert np.abs(C @ S.T - S @ C.T).max() < 1e-7
+    a = cases.noise(np.random.default_rng(0), n, 1.0)
+    g.runSignalSimulation(a, False)
+    out = C @ np.fft.fftshift(a) + S @ np.fft.fftshift(a.conj())
+    assert cases.rel_l2(out, np.fft.fftshift(g.signalFreq[-1])) < 1e-12
+
+
 def test_chi3_soliton_config(nlm, oracle):
     """Chi3 N=1 soliton pump + seeded-noise signal (N=512, nZSteps=200) against the oracle."""
     kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=512, zPrecision=200)

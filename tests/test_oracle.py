@@ -52,6 +52,35 @@ def test_soliton_is_stationary(oracle):
     assert np.max(np.abs(np.abs(m.pump_time[0][-1]) - np.abs(m.pump_time[0][0]))) < 1e-4
 
 
+def test_gaussian_dispersion_known_answer(oracle):
+    """Dispersion length (tests/01 - Dispersion.py, "Dispersion Length"): a Gaussian exp(-t^2/2) under
+    beta2 = 1 with no nonlinearity keeps |A(z, t)| = (1 + z^2)^(-1/4) exp(-t^2 / (2 (1 + z^2))), whose
+    width follows Agrawal's T(z) = T0 (1 + (z/L_d)^2)^(1/2); the last pump row (z = 5) to rounding,
+    the rows at z = 1..4 to the sampling of the row grid."""
+    m = oracle.Chi3(relativeLength=5, nlLength=np.inf, beta2=1, pulseType=0, tPrecision=2048, zPrecision=100,
+                    tMax=50)
+    m.run_pump_simulation()
+    pt = np.asarray(m.pump_time[0])
+    tau = m.tau
+
+    def exact(z):
+        return (1 + z * z) ** -0.25 * np.exp(-tau ** 2 / (2 * (1 + z * z)))
+    assert np.max(np.abs(np.abs(pt[-1]) - exact(5.0))) < 1e-12
+    for i in range(1, 5):
+        r = int((pt.shape[0] - 1) * i / 5)
+        assert np.max(np.abs(np.abs(pt[r]) - exact(5.0 * r / (pt.shape[0] - 1)))) < 2e-3
+
+
+def test_group_delay_known_answer(oracle):
+    """A group-velocity mismatch beta1 = 4 moves the pump by beta1 L = 20 over L = 5 (tests/01 -
+    Dispersion.py, "Qualitative test"), its envelope unchanged by the walk-off."""
+    m = oracle.Chi2PDC(relativeLength=5, nlLength=np.inf, beta2=1, beta2s=-1, pulseType=0, beta1=4, beta1s=-4,
+                       tPrecision=2048, zPrecision=100, tMax=50)
+    m.run_pump_simulation()
+    p = np.abs(np.asarray(m.pump_time[0][-1])) ** 2
+    assert abs(abs(np.sum(m.tau * p) / np.sum(p)) - 20.0) < 1e-9
+
+
 def test_green_consistency_and_symplectic(oracle):
     """a(L) = C a + S a* reproduces runSignalSimulation (tests/04 - Green's Function.py:98-111);
     C C^H - S S^H = I and C S^T = S C^T (tests/05 - Hosaka.py:115-121)."""
