@@ -1574,9 +1574,35 @@ struct Medium {
   // otherwise.
   const KernelEntry* w16Kernel() const {
     if (useCluster != 1 || !wideGrid()) return nullptr;
-    if (nSignal < 2) return findKernel(kKindCluster, solver + kSpreadW16Key, 1);
-    const KernelEntry* kf = findKernel(kKindSpreadFused, solver + kSpreadW16Key, 1);
-    return kf && fusedFits(kf, 16) ? kf : nullptr;
+    const KernelEntry* k = nSignal < 2 ? findKernel(kKindCluster, solver + kSpreadW16Key, 1)
+                                       : findKernel(kKindSpreadFused, solver + kSpreadW16Key, 1);
+    if (!k || (nSignal >= 2 && !fusedFits(k, 16))) return nullptr;
+    return w16Clusters(k) > 0 ? k : nullptr;
+  }
+  // 16-CTA clusters of kernel k for this grid, each CTA alone on its SM, that the device holds at once
+  // (0 where none fits, e.g. on a partition without a GPC of sixteen SMs).  Queried once per kernel and
+  // grid with the occupancy API.
+  int w16Clusters(const KernelEntry* k) const {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, uint>, int> known;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(k->fn, N);
+    auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    const int M = (int)N / 16;
+    const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(16, (int)nSignal)
+                                                           : spread_smem_per_point(16);
+    size_t smem = 0;
+    int n = 0;
+    if (exclusive_smem(k->fn, (size_t)perPoint * M * sizeof(double2), &smem) == cudaSuccess && smem &&
+        cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+      cudaLaunchAttribute attr;
+      cudaLaunchConfig_t cfg = cluster_config(16, M, smem, nullptr, 16, &attr);
+      if (cudaOccupancyMaxActiveClusters(&n, k->fn, &cfg) != cudaSuccess) n = 0;
+    }
+    cudaGetLastError();
+    known[key] = n;
+    return n;
   }
 
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {

@@ -174,31 +174,13 @@ int cluster_capacity_sms(const void* fn, int sms) {
 int g_capacityUsed = 0;
 std::map<std::vector<double>, Plan> g_planCache;   // recent sets' plans (under the ragged workspace's mutex)
 
-// Sixteen-CTA clusters of medium m's kernel (prop_spread_w16.cu), each CTA alone on its SM, that fit
-// on the device at once: one per GPC of sixteen SMs or more.  Measured once per process with the
-// occupancy API; NLM_RAGGED_W16_SLOTS overrides the figure (0 turns the form off).
+// Sixteen-SM slots that can run at once: the 16-CTA clusters of medium m's kernel (prop_spread_w16.cu)
+// that fit on the device, one per GPC of sixteen SMs or more.  NLM_RAGGED_W16_SLOTS overrides the
+// figure (0 turns the form off).
 int w16_capacity(Medium* m) {
-  static int cached = -1;
-  if (cached >= 0) return cached;
-  if (const char* env = std::getenv("NLM_RAGGED_W16_SLOTS")) return cached = std::max(0, std::atoi(env));
-  cached = 0;
+  if (const char* env = std::getenv("NLM_RAGGED_W16_SLOTS")) return std::max(0, std::atoi(env));
   const KernelEntry* k = m->w16Kernel();
-  if (!k) return cached;
-  const int M = (int)m->N / 16;
-  const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(16, (int)m->nSignal)
-                                                         : spread_smem_per_point(16);
-  size_t smem = 0;
-  if (exclusive_smem(k->fn, (size_t)perPoint * M * sizeof(double2), &smem) != cudaSuccess || smem == 0 ||
-      cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-    cudaGetLastError();
-    return cached;
-  }
-  cudaLaunchAttribute attr;
-  cudaLaunchConfig_t cfg = cluster_config(16, M, smem, nullptr, 16, &attr);
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k->fn, &cfg) == cudaSuccess) cached = n;
-  else cudaGetLastError();
-  return cached;
+  return k ? m->w16Clusters(k) : 0;
 }
 
 }  // namespace
