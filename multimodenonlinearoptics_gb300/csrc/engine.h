@@ -2198,20 +2198,24 @@ struct Medium {
     // recomputation and the reverse steps, on twelve CTAs (a non-portable cluster size).  Measured on
     // the N=512, nZSteps=2000 problem with 45-step segments, two such groups on sixteen CTAs are no
     // faster (grad/fwd 2.10 both, 2.56 on eight).  NLM_ADJOINT_CTAS = 16 / 8 selects those forms.
+    // At 2048 points the same kernels hold one point per thread with 512 threads per CTA (the forward's
+    // checkpoints are time-domain rows, whatever form wrote them).
     bool staged = false;
     const char* ctasEnv = std::getenv("NLM_ADJOINT_CTAS");
     const int ctasWant = ctasEnv ? std::atoi(ctasEnv) : 12;
-    for (int G = 1; G <= 2 && adjK > 1 && spread && a.prop && !staged; G++) {
+    const bool pointGrid = spread || (useCluster == 1 && N == 2 * kSpreadMaxN);
+    int T1 = T, R1 = Rk;
+    for (int G = 1; G <= 2 && adjK > 1 && pointGrid && a.prop && !staged; G++) {
       const int size = (2 + G) * C;
       if (size != ctasWant) continue;
-      const KernelEntry* k3 = findKernel(kKindAdjoint, solver + 400 + 100 * G, Rk);
+      const KernelEntry* k3 = findKernel(kKindAdjoint, solver + 400 + 100 * G, 1);
       if (!k3) continue;
       size_t smem3 = 0;
       cudaFuncAttributes fa3;
-      ck(exclusive_smem(k3->fn, need, &smem3, &fa3), "smem attribute");
+      ck(exclusive_smem(k3->fn, (size_t)kSpreadSmemPerPoint * M * sizeof(double2), &smem3, &fa3), "smem attribute");
       int fit = 0;
       if (smem3 && cudaFuncSetAttribute(k3->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
-        fit = maxActiveClusters(k3->fn, size, T, smem3);
+        fit = maxActiveClusters(k3->fn, size, M, smem3);
       else
         cudaGetLastError();
       if (fit >= 1 && adjRows <= 3LL * fit) {
@@ -2222,6 +2226,10 @@ struct Medium {
         smem = smem3;
         fa = fa3;
         staged = true;
+        T1 = M;
+        R1 = 1;
+        a.plan = make_plan(M, 1);
+        a.R = 1;
       }
     }
     if (adjK > 1 && !staged) {
@@ -2256,11 +2264,11 @@ struct Medium {
       d.gp = adjGPS.p;
     }
     void* args[] = {(void*)&a, (void*)&d};
-    lastSchedule = Schedule{(int)(group * clusters), T, 1, smem, 1, 1};
-    lastR = Rk;
+    lastSchedule = Schedule{(int)(group * clusters), T1, 1, smem, 1, 1};
+    lastR = R1;
     lastTuned = 0;
     lastRegs = fa.numRegs;
-    ck(launch_clustered(k->fn, (int)(group * clusters), T, smem, stream, group, args), "adjoint (cluster)");
+    ck(launch_clustered(k->fn, (int)(group * clusters), T1, smem, stream, group, args), "adjoint (cluster)");
     launches++;
     if (march) {
       ck(launch_adj_stage_grads(a, d, (int)N, adjRows, stream), "stage gradients");

@@ -382,7 +382,7 @@ def test_gnlse_cluster_sweep(nlm, n):
     assert abs(adj - fd) < 1e-6 * abs(fd)
 
 
-@pytest.mark.parametrize("n", [512, 1024, 4096])
+@pytest.mark.parametrize("n", [512, 1024, 2048, 4096])
 def test_pdc_cluster_sweep(nlm, oracle, n):
     """Few rows on grids of 256+ points: the checkpointed forward runs on 4-CTA clusters (one point per
     thread up to 1024 points, four above; cluster mode 2 keeps four at 1024), and so does the reverse
@@ -398,11 +398,11 @@ def test_pdc_cluster_sweep(nlm, oracle, n):
             res[cluster, k] = _engine_grads(nlm, kw, x, f0, d, target, interval=k, cluster=cluster)
             if cluster:
                 sched = res[cluster, k][4]._last_schedule()
-                # interval 7 on the spread grids: three groups on twelve CTAs (the propagator matrices
-                # are built), else two groups on eight
-                spread = cluster == 1 and n <= 1024
-                assert sched["grid"] == (8 if k == 1 else (24 if spread else 16))
-                assert sched["R"] == (1 if cluster == 1 and n <= 1024 else 4)
+                # interval 7 up to 2048 points in mode 1: three groups on twelve CTAs with one point per
+                # thread (the propagator matrices are built), else two groups on eight
+                staged = cluster == 1 and n <= 2048 and k > 1
+                assert sched["grid"] == (8 if k == 1 else (24 if staged else 16))
+                assert sched["R"] == (1 if (cluster == 1 and n <= 1024) or staged else 4)
     for key in [(1, 7), (0, 1), (0, 7)] + ([(2, 1), (2, 7)] if n == 1024 else []):
         for ga, gb in zip(res[1, 1][1:4], res[key][1:4]):
             assert cases.rel_l2(gb, ga) < 1e-11
