@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread(const PropAr
   const int M = a.plan.N;
   spread_init(f, smem, a.tw, M, rank);
   const int N = M * kSpreadC;
-  const int tn = rank + kSpreadC * f.j, fk = f.j + M * rank;
+  const int tn = rank + kSpreadC * f.t, fk = f.j + M * rank;
   const int K = d.K;
   const long long clusterId = blockIdx.x / kSpreadC, nClusters = gridDim.x / kSpreadC;
   double2* seg = K > 1 ? d.seg + clusterId * (long long)K * N : nullptr;
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_pipe(const P
   spread_init(f, smem, a.tw, M, crank - role * kSpreadC);
   f.base = role * kSpreadC;
   const int N = M * kSpreadC;
-  const int tn = f.rank + kSpreadC * f.j, fk = f.j + M * f.rank;
+  const int tn = f.rank + kSpreadC * f.t, fk = f.j + M * f.rank;
   const int K = d.K;
   const long long clusterId = blockIdx.x / (2 * kSpreadC), nClusters = gridDim.x / (2 * kSpreadC);
   const long long bufStride = (long long)K * N;
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_pdc_spread_stage(const 
     spread_init(f, smem, a.tw, M, lr);
     f.base = role * kSpreadC;
   }
-  const int tn = lr + kSpreadC * (int)threadIdx.x, fk = (int)threadIdx.x + M * lr;
+  const int tn = lr + kSpreadC * spread_time_index((int)threadIdx.x, M), fk = (int)threadIdx.x + M * lr;
   const int pc = lr * M + (int)threadIdx.x;   // the point of this thread's stage-factor gradients
   const int K = d.K;
   const long long clusterId = blockIdx.x / (kGroups * kSpreadC), nClusters = gridDim.x / (kGroups * kSpreadC);

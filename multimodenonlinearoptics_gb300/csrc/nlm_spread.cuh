@@ -7,19 +7,28 @@
 // warps on each of the four SMs, four times the FP64 issue of one SM.  With C = 8 CTAs (M = N/8) the
 // same form doubles the SMs of a 2048- or 4096-point propagation, and C = 16 (a non-portable cluster
 // size) doubles them again for the longest marches of a ragged batch.  The transforms:
-//   time domain:       CTA c, thread j  <->  point n = c + C j
+//   time domain:       CTA c, thread j  <->  point n = c + C t(j),  t(j) = g + G l
 //   frequency domain:  CTA c, thread j  <->  bin   k = j + M c
-// forward:  M-point DFT over j of the CTA's strided points (radix-2 Stockham through shared memory,
-//           one output per thread and stage: out = e + W o as two FMAs per component), twiddle
-//           exp(-2 pi i c j / N), then the C-point DFT over the CTAs: every thread pushes its value to
-//           all C CTAs through distributed shared memory, one cluster barrier, and each thread
-//           combines the C values of its own column for its CTA's output row;
+// with l = j mod 32 (lane), g = j / 32 (warp) and G = M / 32 warps: the time ownership strides the
+// CTA's points over the lanes so that each warp's 32 points are one decimated sub-sequence.
+// forward:  the M-point DFT over the CTA's strided points as 32 x G: a 32-point DFT inside each warp
+//           (lanes exchange through shuffles: no shared memory, no barrier), the twiddle W_M^(g l),
+//           then a G-point DFT across the warps (radix-2 Stockham through shared memory, one barrier
+//           per stage: log2 G of them); then the twiddle exp(-2 pi i c j / N) and the C-point DFT
+//           over the CTAs: every thread pushes its value to all C CTAs through distributed shared
+//           memory, one cluster barrier, and each thread combines the C values of its own column for
+//           its CTA's output row;
 // inverse:  the C-point inverse DFT over the CTAs first, the conjugate twiddle, then the local inverse
-//           DFT (unscaled; 1/N is in the tables).
+//           (the G-point DFT across warps, the conjugate W_M^(g l), the 32-point DFT in the warps;
+//           unscaled, 1/N is in the tables).
+// A transform of M = 128 points thus has two CTA barriers where a Stockham pass per radix-2 stage had
+// seven.  Each output costs 4 FP64 instructions per radix-2 stage in both parts (the warp stage writes
+// a +- W b for both lanes of a pair as A + (+-W) B, the sign and operand order chosen per lane).
 // Shared memory: M twiddles, two M-point exchange buffers (alternating, one barrier per stage: a thread
 // writes a buffer only after the barrier that every reader of that buffer's previous contents has
 // passed), and two halves of C x M cluster receive buffers (alternating per transform: a CTA writes a
 // half only after the cluster barrier that its readers passed after their last read of it).
+// M is a power of two of at least 32.
 #pragma once
 #include <cooperative_groups.h>
 
@@ -38,6 +47,7 @@ struct SpreadFFT {
   double2* buf;         // [2][M] exchange buffers of the local transform
   double2* recv;        // [2][C][M] cluster receive buffers
   int M, rank, j;
+  int l, g, t;          // lane, warp and local time index g + (M / 32) l of this thread
   int sel, phase;       // next exchange buffer / receive half
   int base;             // cluster rank of the group's first CTA (clusters holding two groups of four)
 };
@@ -51,6 +61,9 @@ __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const d
   f.M = M;
   f.rank = rank;
   f.j = threadIdx.x;
+  f.l = f.j & 31;
+  f.g = f.j >> 5;
+  f.t = f.g + (M >> 5) * f.l;
   f.sel = 0;
   f.phase = 0;
   f.base = 0;
@@ -63,37 +76,109 @@ __device__ __forceinline__ void spread_init(SpreadFFT& f, double2* smem, const d
   __syncthreads();
 }
 
-// M-point DFT over the CTA's threads: thread t holds element t on entry and bin t on return.
-// Stage L -> 2L: y'[k' + 2L p] = y[k + L p] + W_2L^k' y[k + L p + M/2], k = k' mod L.
+// Local time index of thread j of a CTA of M threads (the time ownership above).
+__device__ __forceinline__ int spread_time_index(int j, int M) { return (j >> 5) + (M >> 5) * (j & 31); }
+
+__device__ __forceinline__ double2 spread_shfl(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ double2 spread_shfl_xor(double2 v, int s) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, s), __shfl_xor_sync(0xffffffffu, v.y, s));
+}
+// v or -v through the sign bit (integer operations, no FP64 instruction)
+__device__ __forceinline__ double spread_neg_if(double v, bool neg) {
+  return __hiloint2double(__double2hiint(v) ^ (neg ? (int)0x80000000 : 0), __double2loint(v));
+}
+
+// 32-point DFT over the lanes of a warp: lane l holds element l on entry and bin l on return.  Each
+// lane first takes the element of its bit-reversed lane; then five radix-2 decimation-in-time stages
+// (s = 1 .. 16) pair lane l with l ^ s: the lower lane computes a + W b, the upper a - W b, both as
+// A + (+-W) B with W = W_2s^(l mod s) (conjugated for the inverse) from the M-point table.
+// Stage s = 1 (W = 1): own + partner below, partner - own above.  Stage s = 2 (W = 1 or W_4 = -i, +i
+// for the inverse): the product W B is a swap of B's components with a sign, so both stages cost 2
+// FP64 instructions per output.
 template <bool INV>
-__device__ __forceinline__ double2 spread_local(SpreadFFT& f, double2 x) {
-  const int M = f.M, t = f.j, half = M >> 1;
-  // first stage: W_2^k' = +-1
-  {
-    double2* b = f.buf + f.sel * M;
-    b[t] = x;
-    __syncthreads();
-    const int p = t >> 1;
-    const double2 e = b[p], o = b[p + half];
-    const double s = (t & 1) ? -1.0 : 1.0;
-    x = make_double2(fma(s, o.x, e.x), fma(s, o.y, e.y));
-    f.sel ^= 1;
+__device__ __forceinline__ double2 spread_warp_stage(double2 x, const double2* __restrict__ twM, int M, int l, int s) {
+  const double2 p = spread_shfl_xor(x, s);
+  const bool up = (l & s) != 0;
+  if (s == 1) {
+    const double sg = up ? -1.0 : 1.0;
+    return make_double2(fma(sg, x.x, p.x), fma(sg, x.y, p.y));
   }
-  for (int L = 2, shift = 1; L < M; L <<= 1, shift++) {
+  const double2 a = up ? p : x, b = up ? x : p;
+  if (s == 2) {
+    // W B with W = (-i)^(l & 1) (forward) or i^(l & 1) (inverse), then +- by the lane's position
+    const bool rot = (l & 1) != 0;
+    const double bx = rot ? spread_neg_if(b.y, INV) : b.x, by = rot ? spread_neg_if(b.x, !INV) : b.y;
+    const double sg = up ? -1.0 : 1.0;
+    return make_double2(fma(sg, bx, a.x), fma(sg, by, a.y));
+  }
+  const double2 w = twM[(l & (s - 1)) * (M / (2 * s))];
+  const double wx = spread_neg_if(w.x, up), wy = spread_neg_if(w.y, up != INV);
+  return make_double2(fma(-wy, b.y, fma(wx, b.x, a.x)), fma(wy, b.x, fma(wx, b.y, a.y)));
+}
+
+template <bool INV>
+__device__ __forceinline__ double2 spread_warp_dft(const SpreadFFT& f, double2 x) {
+  const int l = f.l, M = f.M;
+  x = spread_shfl(x, (int)(__brev((unsigned)l) >> 27));
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) x = spread_warp_stage<INV>(x, f.twM, M, l, s);
+  return x;
+}
+
+// One output e + W_2L^kp o of a Stockham stage across the warps; W_2 = -1 and W_4 = -i (i for the
+// inverse) as component swaps and signs (2 FP64 instructions), 4 otherwise.
+template <bool INV>
+__device__ __forceinline__ double2 spread_cross_stage(double2 e, double2 o, const double2* __restrict__ twM, int M, int kp,
+                                                      int L) {
+  if (L <= 2) {
+    // W = (-i)^q, q = kp (L = 2) or 2 kp (L = 1): 1, -i, -1, i (conjugates for the inverse)
+    const int q = (L == 1 ? 2 * kp : kp) & 3;
+    const bool swap = (q & 1) != 0;
+    const double ox = swap ? o.y : o.x, oy = swap ? o.x : o.y;
+    // the real and imaginary signs of W o: q = 0 (+,+), 1 (+,-), 2 (-,-), 3 (-,+); inverse: 1 and 3 swap
+    const int qq = INV ? (4 - q) & 3 : q;
+    const double sx = (qq == 2 || qq == 3) ? -1.0 : 1.0, sy = (qq == 1 || qq == 2) ? -1.0 : 1.0;
+    return make_double2(fma(sx, ox, e.x), fma(sy, oy, e.y));
+  }
+  const double2 w = twM[kp * (M / (2 * L))];
+  const double wy = INV ? -w.y : w.y;
+  return make_double2(fma(-wy, o.y, fma(w.x, o.x, e.x)), fma(wy, o.x, fma(w.x, o.y, e.y)));
+}
+
+// G-point DFT across the warps (G = M / 32) for every lane: thread (g, l) holds element g of its lane's
+// sequence on entry and bin g on return.  Radix-2 Stockham stages L -> 2L through shared memory:
+// y'[k' + 2L p] = y[k + L p] + W_2L^k' y[k + L p + G/2], k = k' mod L, element e of lane l at e 32 + l.
+template <bool INV>
+__device__ __forceinline__ double2 spread_cross_warp(SpreadFFT& f, double2 x) {
+  const int M = f.M, G = M >> 5, g = f.g, l = f.l, half = G >> 1;
+  for (int L = 1, shift = 0; L < G; L <<= 1, shift++) {
     double2* b = f.buf + f.sel * M;
-    b[t] = x;
+    b[f.j] = x;
     __syncthreads();
-    const int kp = t & (2 * L - 1);
-    const int k = kp & (L - 1);
-    const int src = k + L * (t >> (shift + 1));
-    const double2 e = b[src], o = b[src + half];
-    const double2 w = f.twM[kp * (half >> shift)];   // W_2L^k' = W_M^(k' M / 2L)
-    const double wy = INV ? -w.y : w.y;
-    x.x = fma(-wy, o.y, fma(w.x, o.x, e.x));
-    x.y = fma(wy, o.x, fma(w.x, o.y, e.y));
+    const int kp = g & (2 * L - 1);
+    const int src = (kp & (L - 1)) + L * (g >> (shift + 1));
+    const double2 e = b[src * 32 + l], o = b[(src + half) * 32 + l];
+    x = spread_cross_stage<INV>(e, o, f.twM, M, kp, L);
     f.sel ^= 1;
   }
   return x;
+}
+
+// M-point DFT over the CTA's threads: thread j holds element t(j) on entry and bin j on return
+// (forward); the inverse maps bins back to elements (unscaled).
+template <bool INV>
+__device__ __forceinline__ double2 spread_local(SpreadFFT& f, double2 x) {
+  const double2 w = f.twM[f.g * f.l];   // W_M^(g l)
+  if (!INV) {
+    x = spread_warp_dft<false>(f, x);
+    x = cmul(x, w);
+    return spread_cross_warp<false>(f, x);
+  }
+  x = spread_cross_warp<true>(f, x);
+  x = cmulc(x, w);
+  return spread_warp_dft<true>(f, x);
 }
 
 // C-point DFT of the values r[c] of this thread's column: sum_c W_C^(+-rank c) r[c].
@@ -174,40 +259,48 @@ __device__ __forceinline__ double2 spread_exchange(SpreadFFT& f, double2 y, cg::
 // stage and one cluster barrier per exchange for all K, and K independent chains in flight per thread.
 // Buffers: [2][K][M] exchange, [2][C][K][M] receive.
 template <bool INV, int K>
+__device__ __forceinline__ void spread_warp_dft_k(const SpreadFFT& f, double2 (&x)[K]) {
+  const int l = f.l, M = f.M;
+  const int src = (int)(__brev((unsigned)l) >> 27);
+#pragma unroll
+  for (int m = 0; m < K; m++) x[m] = spread_shfl(x[m], src);
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1)
+#pragma unroll
+    for (int m = 0; m < K; m++) x[m] = spread_warp_stage<INV>(x[m], f.twM, M, l, s);
+}
+
+template <bool INV, int K>
+__device__ __forceinline__ void spread_cross_warp_k(SpreadFFT& f, double2 (&x)[K]) {
+  const int M = f.M, G = M >> 5, g = f.g, l = f.l, half = G >> 1;
+  for (int L = 1, shift = 0; L < G; L <<= 1, shift++) {
+    double2* b = f.buf + f.sel * K * M;
+#pragma unroll
+    for (int m = 0; m < K; m++) b[m * M + f.j] = x[m];
+    __syncthreads();
+    const int kp = g & (2 * L - 1);
+    const int src = (kp & (L - 1)) + L * (g >> (shift + 1));
+#pragma unroll
+    for (int m = 0; m < K; m++)
+      x[m] = spread_cross_stage<INV>(b[m * M + src * 32 + l], b[m * M + (src + half) * 32 + l], f.twM, M, kp, L);
+    f.sel ^= 1;
+  }
+}
+
+template <bool INV, int K>
 __device__ __forceinline__ void spread_local_k(SpreadFFT& f, double2 (&x)[K]) {
-  const int M = f.M, t = f.j, half = M >> 1;
-  {
-    double2* b = f.buf + f.sel * K * M;
+  const double2 w = f.twM[f.g * f.l];
+  if (!INV) {
+    spread_warp_dft_k<false, K>(f, x);
 #pragma unroll
-    for (int m = 0; m < K; m++) b[m * M + t] = x[m];
-    __syncthreads();
-    const int p = t >> 1;
-    const double s = (t & 1) ? -1.0 : 1.0;
-#pragma unroll
-    for (int m = 0; m < K; m++) {
-      const double2 e = b[m * M + p], o = b[m * M + p + half];
-      x[m] = make_double2(fma(s, o.x, e.x), fma(s, o.y, e.y));
-    }
-    f.sel ^= 1;
+    for (int m = 0; m < K; m++) x[m] = cmul(x[m], w);
+    spread_cross_warp_k<false, K>(f, x);
+    return;
   }
-  for (int L = 2, shift = 1; L < M; L <<= 1, shift++) {
-    double2* b = f.buf + f.sel * K * M;
+  spread_cross_warp_k<true, K>(f, x);
 #pragma unroll
-    for (int m = 0; m < K; m++) b[m * M + t] = x[m];
-    __syncthreads();
-    const int kp = t & (2 * L - 1);
-    const int k = kp & (L - 1);
-    const int src = k + L * (t >> (shift + 1));
-    const double2 w = f.twM[kp * (half >> shift)];
-    const double wy = INV ? -w.y : w.y;
-#pragma unroll
-    for (int m = 0; m < K; m++) {
-      const double2 e = b[m * M + src], o = b[m * M + src + half];
-      x[m].x = fma(-wy, o.y, fma(w.x, o.x, e.x));
-      x[m].y = fma(wy, o.x, fma(w.x, o.y, e.y));
-    }
-    f.sel ^= 1;
-  }
+  for (int m = 0; m < K; m++) x[m] = cmulc(x[m], w);
+  spread_warp_dft_k<true, K>(f, x);
 }
 
 template <bool INV, int C, int K>

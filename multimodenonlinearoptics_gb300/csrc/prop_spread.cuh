@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_pump_chi3_spread(double2* __res
   const int rank = (int)cl.block_rank();
   spread_init<C>(f, smem, tw, M, rank);
   const int N = M * C;
-  const int tn = rank + C * f.j;          // time-domain point of this thread
+  const int tn = rank + C * f.t;          // time-domain point of this thread
   const int fk = f.j + M * rank;          // frequency bin of this thread
   const double invN = 1.0 / N;
   const double2 hp = halfP[fk], dp = dstepP[fk];
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_spread(const PropArgs
   const int M = a.plan.N;
   spread_init<C, K>(f, smem, a.tw, M, rank);
   const int N = M * C;
-  const int tn = rank + C * f.j;
+  const int tn = rank + C * f.t;
   const int fk = f.j + M * rank;
   const long long clusterId = blockIdx.x / C, nClusters = gridDim.x / C;
   const long long ms = (long long)a.nZ * N;

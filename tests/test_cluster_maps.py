@@ -2,12 +2,15 @@
 
 One point per thread (`nlm_spread.cuh`):
 
-multimodenonlinearoptics_gb300/csrc/nlm_spread.cuh spreads an N-point transform over C = 4 or 8 CTAs
-of M = N / C threads: thread j of CTA c holds time point c + C j and frequency bin j + M c.  The local
-M-point DFT is a radix-2 Stockham pass per stage (output t = e + W o with e = y[k + L p], o = e's
-partner M/2 further, W = twM[k' M / 2L]); the C-point DFT across the CTAs combines the received
-column per output row (4 points: a + W_4^r b; 8 points: v0 + W_8^r v1).  This test executes exactly
-those index expressions for every thread, checks every shared-memory index against its buffer, and
+multimodenonlinearoptics_gb300/csrc/nlm_spread.cuh spreads an N-point transform over C = 4, 8 or 16
+CTAs of M = N / C threads: thread j of CTA c (lane l = j mod 32, warp g = j / 32, G = M / 32 warps)
+holds time point c + C (g + G l) and frequency bin j + M c.  The local M-point DFT is 32 x G: a 32-point
+DFT in each warp (the lanes take their bit-reversed lane's element by a shuffle, then five radix-2
+decimation-in-time stages pair lane l with l ^ s through shuffles, each lane computing A + (+-W) B),
+the twiddle W_M^(g l), then a G-point radix-2 Stockham DFT across the warps through shared memory; the
+C-point DFT across the CTAs combines the received column per output row (4 points: a + W_4^r b; 8
+points: v0 + W_8^r v1; 16 points: y0 + W_16^r y1).  This test executes exactly those index
+expressions for every thread, checks every shared-memory and table index against its buffer, and
 compares the result with numpy's FFT: forward, and the unscaled inverse round trip.
 
 Four points per thread (`nlm_cluster.cuh`, C = R = 4): thread j of CTA c, register v holds time point
@@ -22,25 +25,84 @@ import numpy as np
 import pytest
 
 
-def _local(x, tw_m, inverse):
-    """spread_local: thread t holds element t on entry and bin t on return."""
-    m = x.size
-    half = m >> 1
-    t = np.arange(m)
-    p = t >> 1
-    assert p.max() + half < m
-    x = x[p] + np.where(t & 1, -1.0, 1.0) * x[p + half]
-    big_l, shift = 2, 1
-    while big_l < m:
-        kp = t & (2 * big_l - 1)
-        src = (kp & (big_l - 1)) + big_l * (t >> (shift + 1))
-        widx = kp * (half >> shift)
-        assert src.min() >= 0 and src.max() < half and widx.max() < m
-        w = np.conj(tw_m[widx]) if inverse else tw_m[widx]
-        x = x[src] + w * x[src + half]
+def _brev5(lane):
+    return int(format(lane, "05b")[::-1], 2)
+
+
+def _warp_dft(vals, tw_m, inverse):
+    """spread_warp_dft: lane l holds element l on entry and bin l on return."""
+    m = tw_m.size
+    x = np.array([vals[_brev5(lane)] for lane in range(32)])
+    s = 1
+    while s < 32:
+        p = x[np.arange(32) ^ s]
+        out = np.empty(32, complex)
+        for lane in range(32):
+            up = (lane & s) != 0
+            if s == 1:                                  # W = 1: own + partner, partner - own
+                out[lane] = p[lane] + (-1 if up else 1) * x[lane]
+                continue
+            a, b = (p[lane], x[lane]) if up else (x[lane], p[lane])
+            if s == 2:                                  # W = 1 or -i (i inverse) as a component swap
+                if lane & 1:
+                    b = complex(-b.imag, b.real) if inverse else complex(b.imag, -b.real)
+                out[lane] = a + (-1 if up else 1) * b
+                continue
+            idx = (lane & (s - 1)) * (m // (2 * s))
+            assert idx < m
+            w = np.conj(tw_m[idx]) if inverse else tw_m[idx]
+            out[lane] = a + (-w if up else w) * b
+        x = out
+        s *= 2
+    return x
+
+
+def _cross_warp(vals, tw_m, inverse):
+    """spread_cross_warp: vals[g][l]; the G-point DFT over g for every lane (Stockham, shared memory
+    element e of lane l at e 32 + l)."""
+    g_count, m = vals.shape[0], tw_m.size
+    y = vals.copy()
+    big_l, shift = 1, 0
+    g = np.arange(g_count)
+    while big_l < g_count:
+        kp = g & (2 * big_l - 1)
+        src = (kp & (big_l - 1)) + big_l * (g >> (shift + 1))
+        assert (src + g_count // 2).max() * 32 + 31 < m
+        if big_l <= 2:                                   # W = (-i)^q as a swap and signs
+            q = (2 * kp if big_l == 1 else kp) & 3
+            qq = (4 - q) & 3 if inverse else q
+            o = y[src + g_count // 2]
+            swap = (q & 1)[:, None] != 0
+            ox = np.where(swap, o.imag, o.real)
+            oy = np.where(swap, o.real, o.imag)
+            sx = np.where((qq == 2) | (qq == 3), -1.0, 1.0)[:, None]
+            sy = np.where((qq == 1) | (qq == 2), -1.0, 1.0)[:, None]
+            y = y[src] + sx * ox + 1j * sy * oy
+        else:
+            w = tw_m[kp * (m // (2 * big_l))]
+            w = np.conj(w) if inverse else w
+            y = y[src] + w[:, None] * y[src + g_count // 2]
         big_l <<= 1
         shift += 1
-    return x
+    return y
+
+
+def _local(x, tw_m, inverse):
+    """spread_local: x[j] is thread j's value; forward: thread j holds element t(j), returns bin j."""
+    m = tw_m.size
+    g_count = m // 32
+    gl = np.array([[tw_m[g * lane] for lane in range(32)] for g in range(g_count)])
+    v = x.reshape(g_count, 32)
+    if not inverse:
+        w = np.array([_warp_dft(v[g], tw_m, False) for g in range(g_count)]) * gl
+        return _cross_warp(w, tw_m, False).reshape(m)
+    z = _cross_warp(v, tw_m, True) * np.conj(gl)
+    return np.array([_warp_dft(z[g], tw_m, True) for g in range(g_count)]).reshape(m)
+
+
+def _time_index(j, m):
+    """spread_time_index: the local time element of thread j."""
+    return (j >> 5) + (m >> 5) * (j & 31)
 
 
 def _quarter(q, b):
@@ -56,11 +118,19 @@ def _exchange(rows, tw_m, inverse):
         q = (4 - (r & 3)) & 3 if inverse else r & 3
         if c_count == 4:
             out[r] = rows[0] + sg * rows[2] + _quarter(q, rows[1] + sg * rows[3])
-        else:
+        elif c_count == 8:
             u = [rows[c] + sg * rows[c + 4] for c in range(4)]
             v0, v1 = u[0] + _quarter(q, u[2]), u[1] + _quarter(q, u[3])
             w = tw_m[r * (m // 8)]
             out[r] = v0 + (np.conj(w) if inverse else w) * v1
+        else:
+            u = [rows[c] + sg * rows[c + 8] for c in range(8)]
+            w4 = [u[c] + _quarter(q, u[c + 4]) for c in range(4)]
+            w8 = tw_m[(r & 7) * (m // 8)]
+            w8 = np.conj(w8) if inverse else w8
+            y = [w4[c] + w8 * w4[c + 2] for c in range(2)]
+            w16 = tw_m[r * (m // 16)]
+            out[r] = y[0] + (np.conj(w16) if inverse else w16) * y[1]
     return out
 
 
@@ -74,7 +144,8 @@ def spread_forward(x, c_count):
     n = x.size
     tw, tw_m, m = _tables(n, c_count)
     j = np.arange(m)
-    rows = np.array([_local(x[c + c_count * j], tw_m, False) * tw[c * j] for c in range(c_count)])
+    t = _time_index(j, m)
+    rows = np.array([_local(x[c + c_count * t], tw_m, False) * tw[c * j] for c in range(c_count)])
     y = _exchange(rows, tw_m, False)
     out = np.empty(n, complex)
     for c in range(c_count):
@@ -86,14 +157,16 @@ def spread_inverse(xf, c_count):
     n = xf.size
     tw, tw_m, m = _tables(n, c_count)
     j = np.arange(m)
+    t = _time_index(j, m)
     y = _exchange(np.array([xf[j + m * c] for c in range(c_count)]), tw_m, True)
     out = np.empty(n, complex)
     for c in range(c_count):
-        out[c + c_count * j] = _local(y[c] * np.conj(tw[c * j]), tw_m, True)
+        out[c + c_count * t] = _local(y[c] * np.conj(tw[c * j]), tw_m, True)
     return out
 
 
-@pytest.mark.parametrize("c_count,n", [(4, 128), (4, 256), (4, 512), (4, 1024), (8, 2048), (8, 4096), (8, 256)])
+@pytest.mark.parametrize("c_count,n", [(4, 128), (4, 256), (4, 512), (4, 1024), (4, 2048), (8, 1024), (8, 2048),
+                                       (8, 4096), (16, 2048), (16, 4096)])
 def test_spread_transform_matches_numpy(c_count, n):
     rng = np.random.default_rng(n + c_count)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
@@ -104,10 +177,17 @@ def test_spread_transform_matches_numpy(c_count, n):
     assert np.max(np.abs(back - x)) <= 1e-12 * np.max(np.abs(x))
 
 
+def test_time_ownership_is_a_permutation():
+    """Every local time element is held by exactly one thread (M = 32 .. 512)."""
+    for m in (32, 64, 128, 256, 512):
+        assert np.array_equal(np.sort(_time_index(np.arange(m), m)), np.arange(m))
+
+
 def test_shared_memory_layout():
     """Twiddles (M), two exchange buffers (2M) and two halves of C receive rows (2CM) per CTA, as
-    spread_smem_per_point in nlm_kernels.h; within 227 KB for the largest launch (N=4096 on 8 CTAs)."""
-    for c_count, n in ((4, 1024), (8, 4096)):
+    spread_smem_per_point in nlm_kernels.h; within 227 KB for the largest launches (N=4096 on 8 and
+    16 CTAs)."""
+    for c_count, n in ((4, 1024), (8, 4096), (16, 4096)):
         m = n // c_count
         values = m * (1 + 2 + 2 * c_count)
         assert values * 16 <= 227 * 1024
