@@ -34,8 +34,8 @@ constexpr int kFormSMs[kForms] = {1, 4, 8, 16};
 // the table's end, smaller ones take the 128-point time (latency-bound); other solvers scale with
 // their mode count.
 constexpr double kStepUs[2][kForms][5] = {
-    {{26.4, 27.9, 34.8, 67.9, 137.8}, {8.8, 9.7, 11.6, 21.8, 41.8}, {0, 0, 0, 14.6, 27.4}, {0, 0, 0, 0, 21.1}},
-    {{18.4, 19.9, 27.8, 51.8, 99.5}, {6.7, 7.6, 9.4, 17.2, 33.7}, {0, 0, 0, 12.8, 23.4}, {0, 0, 0, 0, 19.2}}};
+    {{26.4, 27.9, 34.8, 67.9, 137.8}, {9.8, 10.5, 12.0, 21.0, 41.8}, {0, 0, 0, 14.3, 25.5}, {0, 0, 0, 0, 20.6}},
+    {{18.4, 19.9, 27.8, 51.8, 99.5}, {7.7, 8.5, 10.0, 16.9, 33.7}, {0, 0, 0, 12.5, 21.5}, {0, 0, 0, 0, 19.3}}};
 
 double step_us(int form, uint N, uint modes, bool prop) {
   int lg = 0;

@@ -170,14 +170,14 @@ __device__ __forceinline__ double2 spread_cross_warp(SpreadFFT& f, double2 x) {
 // (forward); the inverse maps bins back to elements (unscaled).
 template <bool INV>
 __device__ __forceinline__ double2 spread_local(SpreadFFT& f, double2 x) {
-  const double2 w = f.twM[f.g * f.l];   // W_M^(g l)
+  const double2 w = f.twM[f.g * f.l];   // W_M^(g l); 1 in warp 0 (a warp-uniform branch skips it)
   if (!INV) {
     x = spread_warp_dft<false>(f, x);
-    x = cmul(x, w);
+    if (f.g > 0) x = cmul(x, w);
     return spread_cross_warp<false>(f, x);
   }
   x = spread_cross_warp<true>(f, x);
-  x = cmulc(x, w);
+  if (f.g > 0) x = cmulc(x, w);
   return spread_warp_dft<true>(f, x);
 }
 
@@ -292,14 +292,16 @@ __device__ __forceinline__ void spread_local_k(SpreadFFT& f, double2 (&x)[K]) {
   const double2 w = f.twM[f.g * f.l];
   if (!INV) {
     spread_warp_dft_k<false, K>(f, x);
+    if (f.g > 0)
 #pragma unroll
-    for (int m = 0; m < K; m++) x[m] = cmul(x[m], w);
+      for (int m = 0; m < K; m++) x[m] = cmul(x[m], w);
     spread_cross_warp_k<false, K>(f, x);
     return;
   }
   spread_cross_warp_k<true, K>(f, x);
+  if (f.g > 0)
 #pragma unroll
-  for (int m = 0; m < K; m++) x[m] = cmulc(x[m], w);
+    for (int m = 0; m < K; m++) x[m] = cmulc(x[m], w);
   spread_warp_dft_k<true, K>(f, x);
 }
 
