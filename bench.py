@@ -434,7 +434,8 @@ def measure_configs(nlm, torch, cpu=True):
     t = np.fft.fftshift(np.linspace(-50, 50, 4096, endpoint=False))
     a = 3 / np.cosh(t) + 0j
     row = {"n_freqs": 4096}
-    for use, label in ((0, "one_cta_ms"), (1, "cluster_ms")):
+    # mode 1: one point per thread on sixteen CTAs; mode 2: four points per thread on four CTAs
+    for use, label in ((0, "one_cta_ms"), (1, "spread_ms"), (2, "cluster_ms")):
         m = nlm.Chi3GNLSE(**kw)
         m._set_cluster(use)
         m.runSignalSimulation(a)

@@ -104,9 +104,10 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
 
 @pytest.mark.parametrize("n,t_max", [(1024, 50), (4096, 50), (8192, 100)])
 def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
-    """Chi3GNLSE on a 4-CTA cluster (all 16 stage transforms and the dispersion pair as cluster
-    FFTs): full grids of one propagation and a small batch, against the oracle and the one-CTA kernel
-    (N=8192 has no one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
+    """Chi3GNLSE on clusters (all 16 stage transforms and the dispersion pair as cluster FFTs): full
+    grids of one propagation (one point per thread on 8 or 16 CTAs; four points per thread on four at
+    8192) and a small batch (four CTAs per row), against the oracle and the one-CTA kernel (N=8192 has
+    no one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
     self-steepening) over 0.2 of its length with its z step (1999 steps); at N=8192 the time window
     doubles so that the RK4 step stays stable for the self-steepening term at the highest frequency."""
     from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG
@@ -116,12 +117,16 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     a = 3.0 / np.cosh(t) + cases.noise(np.random.default_rng(n), n, 1e-4)
     med.runSignalSimulation(a)
     ref.run_signal_simulation(a)
-    assert med._last_schedule()["grid"] == 4 and med._last_schedule()["R"] == 4
+    # full grids: one point per thread on eight CTAs at 1024 points, sixteen at 4096; four points per
+    # thread on four CTAs at 8192
+    s = med._last_schedule()
+    assert (s["grid"], s["R"]) == {1024: (8, 1), 4096: (16, 1), 8192: (4, 4)}[n]
     assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
     assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
     x = np.fft.fft(a)[None, :] * np.exp(1j * np.arange(3))[:, None]
     out = med.batchSignalSimulation(x, inTimeDomain=False)
-    assert med._last_schedule()["grid"] == 12
+    s = med._last_schedule()
+    assert s["grid"] == 12 and s["R"] == (1 if n <= 1024 else 4)   # a small batch: four CTAs per row
     assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
     if n <= 4096:
         one = nlm.Chi3GNLSE(**kw)
