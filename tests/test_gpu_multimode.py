@@ -168,3 +168,20 @@ def test_large_polar_and_vectors(dc, mm, oracle_mm):
     d, left, right = mm.blochMessiahVecs(z)
     assert _rel(left @ np.diag(d) @ right, z) < 1e-12
     assert _rel(np.sort(d), np.sort(np.linalg.svd(z, compute_uv=False))) < 1e-13
+
+
+@pytest.mark.parametrize("phi,tol", [(0.1, 1e-3), (0.4, 1.5e-2)])
+def test_squeezing_known_answer(nlm, mm, phi, tol):
+    """The reference's Shirasaki notebook (tests/08 - Shirasaki.py): a Gaussian pulse in a Chi3 fibre
+    over a nonlinear phase phi, squeezed below shot noise as Haus's formula
+    1 + 2 phi^2 / sqrt 3 - (2 phi^3 / sqrt 3 + sqrt 2 phi) / sqrt(1 + phi^2) predicts for small phi,
+    through the engine's Green's function and the GPU consumers (quadrature matrix, covariance,
+    local-oscillator squeezing)."""
+    m = nlm.Chi3(relativeLength=phi, nlLength=1, beta2=-1, pulseType=0, tPrecision=512, zPrecision=200)
+    C, S = m.computeGreensFunction()
+    Z = mm.calcQuadratureGreens(C, S)
+    cov = mm.calcCovarianceMtx(Z, tol=1e-2)
+    v = np.real(np.asarray(mm.calcLOSqueezing(cov, m.pumpTime[-1], tol=1e-2)))
+    haus = 1 + 2 * phi ** 2 / np.sqrt(3) - (2 * phi ** 3 / np.sqrt(3) + np.sqrt(2) * phi) / np.sqrt(1 + phi ** 2)
+    assert abs(v[0] - haus) < tol * haus
+    assert v[1] > 1.0                                   # the conjugate quadrature is anti-squeezed

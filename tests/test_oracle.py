@@ -105,6 +105,19 @@ def test_weak_gain_pdc_matches_pump_spectrum(oracle):
     assert np.argmax(s_diag) in (31, 32, 33)
 
 
+def test_squeezing_known_answer(oracle):
+    """Shirasaki notebook (tests/08 - Shirasaki.py): the squeezed quadrature of a Gaussian pulse in a
+    Chi3 fibre over a nonlinear phase 0.1 follows Haus's formula (to 2e-4 here), through the Green's
+    function and the restated consumers."""
+    from oracle import multimode_oracle as M
+    phi = 0.1
+    m = oracle.Chi3(relativeLength=phi, nlLength=1, beta2=-1, pulseType=0, tPrecision=512, zPrecision=200)
+    C, S = m.compute_greens_function()
+    v = np.real(M.lo_squeezing(M.covariance(M.quadrature_greens(C, S)), m.pump_time[0][-1], tol=1e-2))
+    haus = 1 + 2 * phi ** 2 / np.sqrt(3) - (2 * phi ** 3 / np.sqrt(3) + np.sqrt(2) * phi) / np.sqrt(1 + phi ** 2)
+    assert abs(v[0] - haus) < 1e-3 * haus and v[1] > 1.0
+
+
 def _rel(a, b):
     a, b = np.asarray(a), np.asarray(b)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
