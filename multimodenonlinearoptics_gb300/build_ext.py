@@ -23,7 +23,8 @@ CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_
                 "adjoint_gnlse_cluster.cu", "adjoint_cluster.cu", "adjoint_spread.cu",
                 "greens_quadrature.cu", "prop_gen_a.cu", "prop_gen_b.cu",
                 "prop_gen_c.cu", "prop_gen_d.cu", "prop_gen_e.cu", "prop_spread_fused.cu",
-                "prop_spread_w16.cu", "prop_gnlse_spread.cu"]
+                "prop_spread_w16.cu", "prop_gnlse_spread.cu",
+                "adjoint_gnlse_spread.cu"]
 CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]
 
 

@@ -25,6 +25,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/nlm_capi.h"
@@ -1579,25 +1580,27 @@ struct Medium {
     if (!k || (nSignal >= 2 && !fusedFits(k, 16))) return nullptr;
     return w16Clusters(k) > 0 ? k : nullptr;
   }
-  // 16-CTA clusters of kernel k for this grid, each CTA alone on its SM, that the device holds at once
-  // (0 where none fits, e.g. on a partition without a GPC of sixteen SMs).  Queried once per kernel and
-  // grid with the occupancy API.
-  int w16Clusters(const KernelEntry* k) const {
+  int w16Clusters(const KernelEntry* k) const { return spreadClusters(k, 16); }
+  // C-CTA clusters of the one-point-per-thread kernel k for this grid, each CTA alone on its SM, that
+  // the device holds at once (0 where none fits, e.g. sixteen CTAs on a partition without a GPC of
+  // sixteen SMs).  A cluster sits in one GPC, so this can be well below SMs / C.  Queried once per
+  // kernel, grid and C with the occupancy API.
+  int spreadClusters(const KernelEntry* k, int C) const {
     static std::mutex mu;
-    static std::map<std::pair<const void*, uint>, int> known;
+    static std::map<std::tuple<const void*, uint, int>, int> known;
     std::lock_guard<std::mutex> lock(mu);
-    const auto key = std::make_pair(k->fn, N);
+    const auto key = std::make_tuple(k->fn, N, C);
     auto it = known.find(key);
     if (it != known.end()) return it->second;
-    const int M = (int)N / 16;
-    const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(16, (int)nSignal)
-                                                           : spread_smem_per_point(16);
+    const int M = (int)N / C;
+    const long long perPoint = k->kind == kKindSpreadFused ? spread_smem_per_point_k(C, (int)nSignal)
+                                                           : spread_smem_per_point(C);
     size_t smem = 0;
     int n = 0;
     if (exclusive_smem(k->fn, (size_t)perPoint * M * sizeof(double2), &smem) == cudaSuccess && smem &&
-        cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        (C <= 8 || cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)) {
       cudaLaunchAttribute attr;
-      cudaLaunchConfig_t cfg = cluster_config(16, M, smem, nullptr, 16, &attr);
+      cudaLaunchConfig_t cfg = cluster_config(C, M, smem, nullptr, C, &attr);
       if (cudaOccupancyMaxActiveClusters(&n, k->fn, &cfg) != cudaSuccess) n = 0;
     }
     cudaGetLastError();
@@ -1605,11 +1608,32 @@ struct Medium {
     return n;
   }
 
+  // Chi3GNLSE launches of few rows in cluster mode 1: the CTAs per row of the one-point-per-thread form
+  // (prop_gnlse_spread.cu) whose clusters hold every row at once, the most first (16, 8, 4) with at
+  // least 128 threads per CTA (at most 256 on sixteen CTAs, 512 otherwise); 0 when none applies (then
+  // four points per thread on four CTAs).  The stored-stage reverse sweep takes the same form.
+  int gnlseSpreadC(long long rows) const {
+    if (solver != kChi3GNLSE || useCluster != 1 || !is_pow2((int)N)) return 0;
+    for (int C : {16, 8, 4}) {
+      const int M = (int)N / C;
+      if (M < 128 || M > (C == 16 ? 256 : 512) || rows * C > smCount()) continue;
+      const KernelEntry* k = C == 16 ? findKernel(kKindCluster, solver + kSpreadW16Key, 1)
+                                     : findKernel(kKindCluster, C == 8 ? solver + kSpreadWideKey : solver, 1);
+      if (!k || !findKernel(kKindAdjoint, solver + 500, C)) continue;
+      if (spreadClusters(k, C) < rows) continue;
+      return C;
+    }
+    return 0;
+  }
+
   const KernelEntry* clusterKernel(const PropArgs& a, long long nInst, bool plainOne) const {
     // checkpointed forwards (the adjoint's, Chi2PDC and Chi3GNLSE) run on clusters too: their reverse
     // sweeps have cluster forms that read the same checkpoints
     if (!useCluster || plainOne || a.inKind != 1) return nullptr;
     if (!is_pow2((int)N) || N > (uint)kMaxFFT) return nullptr;
+    if (const int Cs = gnlseSpreadC(nInst))
+      return Cs == 16 ? findKernel(kKindCluster, solver + kSpreadW16Key, 1)
+                      : findKernel(kKindCluster, Cs == 8 ? solver + kSpreadWideKey : solver, 1);
     // full grids and the ragged media given sixteen SMs: the sixteen-CTA form (mode 1); a ragged medium
     // given eight SMs keeps eight
     if (wideLaunch(a) && !raggedWide && nInst * 16 <= smCount())
@@ -2074,6 +2098,39 @@ struct Medium {
 
   // Reverse sweep over the stored stage values: one propagation per 4-CTA cluster.
   void adjointStored(const double2* gout, double2* gin) {
+    // the form of the forward that stored the stages: one point per thread on Cs CTAs, or four points
+    // per thread on four
+    const int Cs = gnlseSpreadC(adjRows);
+    if (Cs) {
+      const KernelEntry* k = findKernel(kKindAdjoint, solver + 500, Cs);
+      if (!k) throw Unsupported("no stored-stage adjoint kernel");
+      const int M = (int)N / Cs;
+      size_t smem = 0;
+      cudaFuncAttributes fa;
+      ck(exclusive_smem(k->fn, (size_t)spread_smem_per_point(Cs) * M * sizeof(double2), &smem, &fa), "smem attribute");
+      if (smem == 0) throw Unsupported("grid too large for the cluster adjoint");
+      if (Cs > 8) ck(cudaFuncSetAttribute(k->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1), "cluster size");
+      PropArgs a = baseArgs(kClusterSize);
+      a.plan = make_plan(M, 1);
+      a.R = 1;
+      a.nInst = adjRows;
+      a.ipc = 1;
+      a.work = nullptr;
+      a.stages = adjStages.p;
+      AdjArgs d{};
+      d.gout = gout;
+      d.gin = gin;
+      const long long clusters = std::min<long long>(adjRows, smCount() / Cs);
+      void* args[] = {(void*)&a, (void*)&d};
+      lastSchedule = Schedule{(int)(Cs * clusters), M, 1, smem, 1, 1};
+      lastR = 1;
+      lastTuned = 0;
+      lastRegs = fa.numRegs;
+      ck(launch_clustered(k->fn, (int)(Cs * clusters), M, smem, stream, Cs, args), "adjoint (stored stages)");
+      launches++;
+      ck(cudaStreamSynchronize(stream), "adjoint");
+      return;
+    }
     constexpr int C = kClusterSize;
     const KernelEntry* k = findKernel(kKindAdjoint, solver + 300, C);
     if (!k) throw Unsupported("no stored-stage adjoint kernel");

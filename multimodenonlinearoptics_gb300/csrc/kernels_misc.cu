@@ -34,6 +34,7 @@ void add_kernels_gen_e(std::vector<KernelEntry>& t);
 void add_kernels_spread_fused(std::vector<KernelEntry>& t);
 void add_kernels_spread_w16(std::vector<KernelEntry>& t);
 void add_kernels_gnlse_spread(std::vector<KernelEntry>& t);
+void add_kernels_adjoint_gnlse_spread(std::vector<KernelEntry>& t);
 
 const KernelEntry* kernel_table(int* count) {
   static std::vector<KernelEntry> table;
@@ -64,6 +65,7 @@ const KernelEntry* kernel_table(int* count) {
     add_kernels_spread_fused(table);
     add_kernels_spread_w16(table);
     add_kernels_gnlse_spread(table);
+    add_kernels_adjoint_gnlse_spread(table);
   });
   *count = (int)table.size();
   return table.data();

@@ -334,9 +334,9 @@ def test_gnlse_pipelined_and_one_cta_sweeps_agree(nlm):
 
 @pytest.mark.parametrize("n", [1024, 4096])
 def test_gnlse_cluster_sweep(nlm, n):
-    """Few rows on grids of 1024+ points: the forward runs on 4-CTA clusters.  With the interval chosen
-    by the engine (0) it stores the stage values of every step and the reverse sweep reads them on
-    4-CTA clusters; with an explicit checkpoint interval the reverse sweep runs on clusters of eight CTAs
+    """Few rows on grids of 1024+ points: the forward runs on clusters.  With the interval chosen by the
+    engine (0) it stores the stage values of every step and the reverse sweep reads them on clusters of
+    the same form (one point per thread on 8 or 16 CTAs; four points per thread on four in mode 2); with an explicit checkpoint interval the reverse sweep runs on clusters of eight CTAs
     (four reverse the current segment while four recompute the next).  Gradients agree with the one-CTA
     sweeps for intervals 1 and one that leaves a short last segment, and match a directional central
     difference of the engine's forward."""
@@ -361,13 +361,17 @@ def test_gnlse_cluster_sweep(nlm, n):
 
     g = {}
     g[1, 0], sched = grad(1, 0)
+    # stored stages: the forward and the reverse sweep with one point per thread on eight CTAs per row
+    # at 1024 points, sixteen at 4096
+    assert sched["grid"] == (8 if n == 1024 else 16) * rows and sched["R"] == 1
+    g[2, 0], sched = grad(2, 0)                       # four points per thread on four CTAs per row
     assert sched["grid"] == 4 * rows and sched["R"] == 4
     for k in (1, k_short):
         g[1, k], sched = grad(1, k)
         assert sched["grid"] == 8 * rows and sched["R"] == 4
         g[0, k], sched = grad(0, k)
         assert sched["grid"] not in (4 * rows, 8 * rows)
-    for key in ((1, 1), (1, k_short), (0, 1), (0, k_short)):
+    for key in ((2, 0), (1, 1), (1, k_short), (0, 1), (0, k_short)):
         assert cases.rel_l2(g[key], g[1, 0]) < 1e-10
     med = nlm.Chi3GNLSE(**kw)
     w = weights.cpu().numpy()

@@ -105,9 +105,9 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
 @pytest.mark.parametrize("n,t_max", [(1024, 50), (4096, 50), (8192, 100)])
 def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     """Chi3GNLSE on clusters (all 16 stage transforms and the dispersion pair as cluster FFTs): full
-    grids of one propagation (one point per thread on 8 or 16 CTAs; four points per thread on four at
-    8192) and a small batch (four CTAs per row), against the oracle and the one-CTA kernel (N=8192 has
-    no one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
+    grids of one propagation and a small batch (one point per thread on 8 or 16 CTAs per row; four
+    points per thread on four at 8192), against the oracle and the one-CTA kernel (N=8192 has no
+    one-CTA GNLSE kernel).  The medium is the GNLSE benchmark's (N=3 soliton, Raman,
     self-steepening) over 0.2 of its length with its z step (1999 steps); at N=8192 the time window
     doubles so that the RK4 step stays stable for the self-steepening term at the highest frequency."""
     from multimodenonlinearoptics_gb300.workloads import GNLSE_CONFIG
@@ -126,7 +126,9 @@ def test_cluster_gnlse_matches_oracle(nlm, oracle, n, t_max):
     x = np.fft.fft(a)[None, :] * np.exp(1j * np.arange(3))[:, None]
     out = med.batchSignalSimulation(x, inTimeDomain=False)
     s = med._last_schedule()
-    assert s["grid"] == 12 and s["R"] == (1 if n <= 1024 else 4)   # a small batch: four CTAs per row
+    # a small batch: one point per thread on eight CTAs per row at 1024 points, sixteen at 4096; four
+    # points per thread on four CTAs at 8192
+    assert (s["grid"], s["R"]) == {1024: (24, 1), 4096: (48, 1), 8192: (12, 4)}[n]
     assert cases.rel_l2(out, ref.batch_signal_simulation(x, False)) < TOL
     if n <= 4096:
         one = nlm.Chi3GNLSE(**kw)
