@@ -251,7 +251,8 @@ struct GraphCache {
     }
     ck(cudaStreamEndCapture(stream, &g), "graph capture");
     cudaGraphExec_t ex = nullptr;
-    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    // node priorities: launches captured from prioritised streams keep their priority in the graph
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     ck(e, "graph instantiate");
     if (entries.size() >= kMaxEntries) {

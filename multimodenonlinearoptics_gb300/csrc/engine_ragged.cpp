@@ -195,21 +195,37 @@ struct RaggedWorkspace {
   nlm::PinnedBuf<double2> hin, hout;            // host staging of the inputs and outputs
   nlm::PinnedBuf<nlm::PropArgs> hitems;
   nlm::DevBuf<unsigned long long> counters;     // one work counter per ragged launch
-  std::vector<cudaStream_t> streams;            // [0]: origin; then one per slot and ragged launch
+  // The cluster slots' streams have the device's highest priority and the ragged launches' the lowest:
+  // CTAs of the slots (and of each slot's next medium) are placed first wherever both wait for SMs, so
+  // the one-SM CTAs never hold the GPC room a slot's cluster needs.
+  cudaStream_t origin = nullptr;
+  std::vector<cudaStream_t> slotStreams, poolStreams;
   std::vector<cudaEvent_t> events;
   nlm::GraphCache graphs;
   std::vector<unsigned char> lastKey;           // the previous call's plan
-  void ensureStreams(size_t n) {
-    while (streams.size() < n) {
-      cudaStream_t st = nullptr;
-      ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "ragged stream");
-      streams.push_back(st);
-    }
-    while (events.size() < n) {
+  // [0]: origin; then one per slot and one per ragged launch
+  std::vector<cudaStream_t> callStreams(size_t nSlots, size_t nPool) {
+    int least = 0, greatest = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    if (!origin) ck(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking), "ragged stream");
+    auto grow = [](std::vector<cudaStream_t>& v, size_t n, int prio) {
+      while (v.size() < n) {
+        cudaStream_t st = nullptr;
+        ck(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio), "ragged stream");
+        v.push_back(st);
+      }
+    };
+    grow(slotStreams, nSlots, greatest);
+    grow(poolStreams, nPool, least);
+    while (events.size() < 1 + nSlots + nPool) {
       cudaEvent_t e = nullptr;
       ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "ragged event");
       events.push_back(e);
     }
+    std::vector<cudaStream_t> out{origin};
+    out.insert(out.end(), slotStreams.begin(), slotStreams.begin() + (long)nSlots);
+    out.insert(out.end(), poolStreams.begin(), poolStreams.begin() + (long)nPool);
+    return out;
   }
 };
 static RaggedWorkspace g_ragged;
@@ -432,9 +448,8 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     g_ragged.hitems.reserve(std::max<size_t>(items.size(), 1));
     if (!items.empty()) std::memcpy(g_ragged.hitems.p, items.data(), items.size() * sizeof(PropArgs));
     g_ragged.counters.reserve(std::max<size_t>(raggedLaunches.size(), 1));
-    const size_t nStreams = 1 + plan.slots.size() + raggedLaunches.size();
-    g_ragged.ensureStreams(nStreams);
-    cudaStream_t origin = g_ragged.streams[0];
+    const std::vector<cudaStream_t> streams = g_ragged.callStreams(plan.slots.size(), raggedLaunches.size());
+    cudaStream_t origin = streams[0];
 
     // ---- the call: one input copy, the slots and ragged launches on their streams, one output copy --
     auto record = [&] {
@@ -450,7 +465,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       ck(cudaEventRecord(g_ragged.events[0], origin), "ragged fork");
       size_t si = 1;
       for (size_t s = 0; s < plan.slots.size(); s++, si++) {
-        cudaStream_t st = g_ragged.streams[si];
+        cudaStream_t st = streams[si];
         ck(cudaStreamWaitEvent(st, g_ragged.events[0], 0), "ragged fork");
         for (size_t i : plan.slots[s]) {
           const size_t k = jobs[i].k;
@@ -472,7 +487,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       }
       for (size_t r = 0; r < raggedLaunches.size(); r++, si++) {
         const RaggedLaunch& rl = raggedLaunches[r];
-        cudaStream_t st = g_ragged.streams[si];
+        cudaStream_t st = streams[si];
         ck(cudaStreamWaitEvent(st, g_ragged.events[0], 0), "ragged fork");
         // the one-SM media's RK4 matrices, each built in parallel over all steps and points just before
         for (int q = rl.first; q < rl.first + rl.count; q++) {
@@ -486,7 +501,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         ck(launch_clustered(rl.ke->fn, rl.grid, rl.block, rl.smem, st, Medium::kClusterSize, args), "ragged launch");
       }
       for (size_t j = 1; j < si; j++) {
-        ck(cudaEventRecord(g_ragged.events[j], g_ragged.streams[j]), "ragged join");
+        ck(cudaEventRecord(g_ragged.events[j], streams[j]), "ragged join");
         ck(cudaStreamWaitEvent(origin, g_ragged.events[j], 0), "ragged join");
       }
       ck(cudaMemcpyAsync(g_ragged.hout.p, g_ragged.out.p, outAll * sizeof(double2), cudaMemcpyDeviceToHost, origin),
