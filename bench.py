@@ -547,6 +547,7 @@ def measure_configs(nlm, torch, cpu=True):
     ins = [p[3] for p in params]
     nlm.ragged_batch(media, ins)
     wall, wall_kept, wall_direct = [], [], []
+    dev, dev_kept = [], []         # the calls' device time (CUDA events on the engine's stream)
     for _ in range(3):
         for m in media:            # new pumps before every timed call
             m.runPumpSimulation()
@@ -554,11 +555,13 @@ def measure_configs(nlm, torch, cpu=True):
         t0 = time.perf_counter()
         nlm.ragged_batch(media, ins)
         wall.append(time.perf_counter() - t0)
+        dev.append(nlm.ragged_last_plan()["gpu_ms"])
     for _ in range(3):             # the same pumps again: the RK4 matrices are built, then reused
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ragged_out = nlm.ragged_batch(media, ins)
         wall_kept.append(time.perf_counter() - t0)
+        dev_kept.append(nlm.ragged_last_plan()["gpu_ms"])
     wall_one = []
     for m in media:
         m._set_cluster(0)
@@ -587,6 +590,10 @@ def measure_configs(nlm, torch, cpu=True):
                                       "pumps": "rerun before each call: every medium propagates with its DiffEq "
                                                "(RK4 matrices are built only for a pump used again)",
                                       "gpu_wall_ms_pumps_kept": 1e3 * min(wall_kept),
+                                      "device_ms": min(dev), "device_ms_pumps_kept": min(dev_kept),
+                                      "timing": "wall: the API call (host conversion, one input and one output "
+                                                "copy, the graph); device: CUDA events on the engine's stream "
+                                                "around the enqueued work",
                                       "form": "each medium on one SM in a ragged launch or on a 4-, 8- or 16-SM "
                                               "cluster slot, planned for the makespan; the call replayed as a CUDA "
                                               "graph",

@@ -162,10 +162,11 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
  * captures and replays of ragged calls so far, the SMs the plan could use (those clusters of four can
  * hold at once; the environment variable NLM_RAGGED_CLUSTER_SMS overrides the measured figure) and
  * the sixteen-SM slots that can run at once (NLM_RAGGED_W16_SLOTS overrides it; 0 when no medium of
- * the call has that form).  No counterpart in the reference (measurement support). */
+ * the call has that form), and the call's device time (milliseconds, CUDA events on its stream around
+ * the enqueued work).  No counterpart in the reference (measurement support). */
 nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* slots_w16,
                                 int* ragged_ctas, long* graph_captures, long* graph_replays, int* sm_budget,
-                                int* w16_capacity);
+                                int* w16_capacity, double* gpu_ms);
 
 /* --- gradients (no counterpart in the reference) -------------------------------------------
  * Reverse-mode gradients of a functional L of the output spectra of a Chi2PDC batch with respect to

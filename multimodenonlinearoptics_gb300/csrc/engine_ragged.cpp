@@ -201,6 +201,7 @@ struct RaggedWorkspace {
   cudaStream_t origin = nullptr;
   std::vector<cudaStream_t> slotStreams, poolStreams;
   std::vector<cudaEvent_t> events;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;        // timing events around the call on the origin stream
   nlm::GraphCache graphs;
   std::vector<unsigned char> lastKey;           // the previous call's plan
   // [0]: origin; then one per slot and one per ragged launch
@@ -236,8 +237,9 @@ struct RaggedStats {
   int slotsC4, slotsW8, slotsW16, raggedCTAs;
   long captures, replays;
   int budget, w16Capacity;
+  double gpuMs;   // device time of the call on its origin stream (CUDA events around the launch)
 };
-static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0, 0, 0, 0};
+static RaggedStats g_lastRagged{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs, int in_time_domain,
                             double* const* outputs) {
@@ -528,13 +530,19 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (const PropArgs& a : items) add_prop_key(key, a);
     // a plan is captured the second time it comes (a one-off plan runs directly), then replayed
     bool replayed = false;
+    if (!g_ragged.t0) ck(cudaEventCreate(&g_ragged.t0), "ragged timing");
+    if (!g_ragged.t1) ck(cudaEventCreate(&g_ragged.t1), "ragged timing");
+    ck(cudaEventRecord(g_ragged.t0, origin), "ragged timing");
     if (useGraph && key.bytes == g_ragged.lastKey) {
       replayed = g_ragged.graphs.run(key, origin, record);
     } else {
       record();
     }
+    ck(cudaEventRecord(g_ragged.t1, origin), "ragged timing");
     g_ragged.lastKey = key.bytes;
     ck(cudaStreamSynchronize(origin), "ragged batch");
+    float gpuMs = 0;
+    ck(cudaEventElapsedTime(&gpuMs, g_ragged.t0, g_ragged.t1), "ragged timing");
     // host-side state of what ran: the matrices built; one launch per propagation, build and ragged
     // launch (credited to the launch's largest medium)
     for (size_t k : fused) {
@@ -549,8 +557,8 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (size_t i = 0; i < jobs.size(); i++)
       if (plan.form[i] != kOne) ms[jobs[i].k]->launches++;
     for (const RaggedLaunch& rl : raggedLaunches) ms[jobs[itemJob[rl.first]].k]->launches++;
-    g_lastRagged =
-        RaggedStats{plan.makespan, 0, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays, budget, maxW16};
+    g_lastRagged = RaggedStats{plan.makespan, 0, 0, 0, 0, g_ragged.graphs.captures, g_ragged.graphs.replays,
+                               budget, maxW16, (double)gpuMs};
     for (int f : plan.slotForm)
       (f == kW16 ? g_lastRagged.slotsW16 : f == kW8 ? g_lastRagged.slotsW8 : g_lastRagged.slotsC4)++;
     for (const RaggedLaunch& rl : raggedLaunches) g_lastRagged.raggedCTAs += rl.grid;
@@ -561,11 +569,12 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
 
 nlm_status nlm_ragged_last_plan(double* makespan_estimate_us, int* slots_c4, int* slots_w8, int* slots_w16,
                                 int* ragged_ctas, long* graph_captures, long* graph_replays, int* sm_budget,
-                                int* w16_capacity) {
+                                int* w16_capacity, double* gpu_ms) {
   return guarded([&] {
     std::lock_guard<std::mutex> lock(g_ragged.mu);
     if (sm_budget) *sm_budget = g_lastRagged.budget;
     if (w16_capacity) *w16_capacity = g_lastRagged.w16Capacity;
+    if (gpu_ms) *gpu_ms = g_lastRagged.gpuMs;
     if (makespan_estimate_us) *makespan_estimate_us = g_lastRagged.makespan;
     if (slots_c4) *slots_c4 = g_lastRagged.slotsC4;
     if (slots_w8) *slots_w8 = g_lastRagged.slotsW8;

@@ -62,7 +62,8 @@ def _load():
         "nlm_batch": (i, [vp, P(d), sz, sz, i, i, u, u, P(u8), sz, P(d)]),
         "nlm_batch_device": (i, [vp, vp, sz, sz, i, i, u, u, P(u8), sz, vp]),
         "nlm_ragged_batch": (i, [P(vp), sz, P(P(d)), i, P(P(d))]),
-        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i), P(i)]),
+        "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i), P(i),
+                                     P(d)]),
         "nlm_get_grid": (i, [vp, i, u, P(P(d)), P(sz), P(sz)]),
         "nlm_get_axis": (i, [vp, i, u, P(P(d)), P(sz)]),
         "nlm_cascade_create": (i, [P(vp), sz, P(u), P(sz), sz, i, P(vp)]),
@@ -159,16 +160,18 @@ def ragged_batch(media, inputs, inTimeDomain=False):
 def ragged_last_plan():
     """The plan of the last ragged_batch call (no counterpart in the reference): estimated makespan
     (ms), cluster slots of four, eight and sixteen SMs, CTAs of the one-SM ragged launches, the
-    CUDA-graph captures and replays of ragged calls so far, the SMs the plan could use and the
-    sixteen-SM slots that can run at once."""
+    CUDA-graph captures and replays of ragged calls so far, the SMs the plan could use, the
+    sixteen-SM slots that can run at once and the call's device time (ms)."""
     ms, c4, w8, w16, ctas = ctypes.c_double(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     cap, rep, budget, w16cap = ctypes.c_long(), ctypes.c_long(), ctypes.c_int(), ctypes.c_int()
+    gpu = ctypes.c_double()
     _check(_lib.nlm_ragged_last_plan(ctypes.byref(ms), ctypes.byref(c4), ctypes.byref(w8), ctypes.byref(w16),
                                      ctypes.byref(ctas), ctypes.byref(cap), ctypes.byref(rep), ctypes.byref(budget),
-                                     ctypes.byref(w16cap)))
+                                     ctypes.byref(w16cap), ctypes.byref(gpu)))
     return {"makespan_estimate_ms": ms.value / 1e3, "slots_c4": c4.value, "slots_w8": w8.value,
             "slots_w16": w16.value, "ragged_ctas": ctas.value, "graph_captures": cap.value,
-            "graph_replays": rep.value, "sm_budget": budget.value, "w16_capacity": w16cap.value}
+            "graph_replays": rep.value, "sm_budget": budget.value, "w16_capacity": w16cap.value,
+            "gpu_ms": gpu.value}
 
 
 def fp64_peak_tflops():
