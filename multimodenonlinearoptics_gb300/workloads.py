@@ -114,18 +114,23 @@ def _run(name, z_precision, rows, reps, cluster=1):
     import torch
     from . import nonlinearmedium as nlm
     from .autograd import propagate_gnlse
+
+    def c(m):   # the cluster mode of every medium of the workload
+        m._set_cluster(cluster)
+        return m
     for _ in range(reps):
         if name == "green":
-            green_medium(nlm, z_precision or 500).computeGreensFunction()
+            c(green_medium(nlm, z_precision or 500)).computeGreensFunction()
         elif name == "chi3":
-            m = nlm.Chi3(**CHI3_CONFIG)
+            m = c(nlm.Chi3(**CHI3_CONFIG))
             m.runPumpSimulation()
             m.runSignalSimulation(chi3_signal())
         elif name == "ragged":
             media, inputs = ragged_media(nlm)
-            nlm.ragged_batch(media, inputs)
+            nlm.ragged_batch([c(m) for m in media], inputs)
         elif name == "adjoint":
             med, x, d, target = adjoint_problem(nlm, z_precision or 1000)
+            c(med)
             nz = med._dims["nZSteps"]
             med._set_poling_profile(d)
             xin = torch.tensor(x.reshape(1, -1), dtype=torch.complex128, device="cuda")
@@ -145,14 +150,15 @@ def _run(name, z_precision, rows, reps, cluster=1):
         elif name == "cascade":
             kwa = dict(GREEN_CONFIG, zPrecision=z_precision or 100)
             kwb = dict(kwa, beta1s=-1, diffBeta0=0.2)
-            ma = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwa)
-            mb = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwb)
+            ma = c(nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwa))
+            mb = c(nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS), **kwb))
             nlm.Cascade([ma, mb], [{0: 0}], False).computeGreensFunction()
         elif name == "chi3_pump":
-            m = nlm.Chi3(**dict(CHI3_CONFIG, tPrecision=8192, tMax=40, beta3=0.02, zPrecision=z_precision or 500))
+            m = c(nlm.Chi3(**dict(CHI3_CONFIG, tPrecision=8192, tMax=40, beta3=0.02, zPrecision=z_precision or 500)))
             m.runPumpSimulation()
         elif name == "adjoint_cluster":
             med, x, d, target = adjoint_problem(nlm, z_precision or 1000, n=2048)
+            c(med)
             nz = med._dims["nZSteps"]
             med._set_poling_profile(d)
             xin = torch.tensor(x.reshape(1, -1), dtype=torch.complex128, device="cuda")
@@ -169,8 +175,8 @@ def _run(name, z_precision, rows, reps, cluster=1):
                                                      ctypes.c_void_p(gin.data_ptr()), ctypes.c_void_p(gp.data_ptr()),
                                                      nlm._dptr(gpol)))
         elif name == "signal":
-            m = nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS),
-                            **dict(GREEN_CONFIG, tPrecision=2048, zPrecision=z_precision or 500))
+            m = c(nlm.Chi2PDC(poling=np.ones(GREEN_DOMAINS),
+                              **dict(GREEN_CONFIG, tPrecision=2048, zPrecision=z_precision or 500)))
             m.runPumpSimulation()
             m.runSignalSimulation((np.random.default_rng(2048).standard_normal(2048) + 0j) * 0.1)
         elif name == "ragged_wide":
@@ -180,17 +186,17 @@ def _run(name, z_precision, rows, reps, cluster=1):
             t = np.fft.fftshift(np.linspace(-10, 10, 2048, endpoint=False))
             m = nlm.Chi2SFG(customPump=np.exp(-t ** 2 / 2), poling=[3, 4, 3], **kw)
             m._set_schedule(use_propagator=0)
-            m._set_cluster(cluster)
+            c(m)
             m.runPumpSimulation()
             m.runSignalSimulation((np.random.default_rng(1).standard_normal(2048) + 0j) * 1e-3)
         elif name == "gnlse_signal":
-            m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
+            m = c(nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111)))
             m.runSignalSimulation(gnlse_rows(1)[0])
         elif name == "gnlse":
-            m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
+            m = c(nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111)))
             m.batchSignalSimulation(gnlse_rows(rows or 304), inTimeDomain=True)
         elif name == "gnlse_grad":
-            m = nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111))
+            m = c(nlm.Chi3GNLSE(**dict(GNLSE_CONFIG, zPrecision=z_precision or 111)))
             x = torch.tensor(gnlse_rows(rows or 16), device="cuda")
             w = torch.tensor(m.omega, device="cuda")
             band = ((w >= 2) & (w <= 4)).to(torch.float64)
@@ -210,7 +216,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="rows of the GNLSE workloads (0: the workload's own)")
     ap.add_argument("--reps", type=int, default=1)
     ap.add_argument("--cluster", type=int, default=1,
-                    help="cluster mode of the ragged_wide medium (1: sixteen CTAs, 3: eight)")
+                    help="cluster mode of the workload's media (nlm_set_cluster: 1 default, 3 narrower "
+                         "one-point-per-thread forms, 2 four points per thread only, 0 one CTA)")
     args = ap.parse_args()
     from . import build_ext
     build_ext.build()
