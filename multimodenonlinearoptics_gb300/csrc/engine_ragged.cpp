@@ -2,17 +2,18 @@
 // counts), scheduled for its makespan over the SMs and captured into a CUDA graph.
 //
 // Every medium is a sequential z march; it can run in one of four forms:
-//   one  -- one CTA (one SM) in the ragged launch, whose CTAs claim media largest first;
+//   one  -- one CTA (one SM) in a ragged launch, whose CTAs claim media largest first;
 //   c4   -- a 4-CTA cluster on four SMs (one point per thread up to 1024 points, four from 2048);
-//   w8   -- an 8-CTA cluster on eight SMs, one point per thread (2048 and 4096 points);
+//   w8   -- an 8-CTA cluster on eight SMs, one point per thread (1024 to 4096 points);
 //   w16  -- a 16-CTA cluster (a non-portable size) on sixteen SMs, one point per thread.
 // The larger forms finish a medium sooner but spend more SM time on it.  The planner picks a target
-// makespan T (the smallest feasible one, scanned upward): every medium takes the form of least SM time that finishes within T;
-// cluster-form media are packed first-fit, largest first, into slots (a stream running its media one
-// after another on 4 or 8 SMs); the one-SM media share the ragged launch.  T is feasible when the
-// slots and the ragged launch fit on the SMs at once.  The call is then enqueued on those streams
-// (inputs in one copy, outputs in one copy) and captured into a CUDA graph, replayed by later calls
-// with the same plan.
+// makespan T (the smallest feasible one, scanned upward): every medium takes the form of least SM
+// time that finishes within T; cluster-form media are packed first-fit, largest first, into slots (a
+// stream running its media one after another on 4, 8 or 16 SMs); the one-SM media of each solver and
+// grid share a ragged launch.  T is feasible when the slots fit in the SMs clusters can hold at once
+// and the slots and the ragged launches together in the device's SMs.  The call is then enqueued on
+// those streams (inputs in one copy, outputs in one copy) and captured into a CUDA graph, replayed by
+// later calls with the same plan.
 #include <cstdlib>
 #include <map>
 
@@ -76,9 +77,10 @@ double lpt_makespan(const std::vector<double>& times, int m) {
   return *std::max_element(load.begin(), load.end());
 }
 
-// Plan for target makespan T (us); false when the slots and the ragged launch need more than `sms` SMs.
-// maxW16: the sixteen-CTA slots that can run at once (one per GPC that holds sixteen SMs).
-bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, Plan* out) {
+// Plan for target makespan T (us); false when the slots need more than `sms` SMs (the cluster budget)
+// or the slots and the ragged launches more than poolSms.  maxW16: the sixteen-CTA slots that can run
+// at once (one per GPC that holds sixteen SMs); gran: the ragged CTAs come in groups of gran.
+bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, int poolSms, int gran, Plan* out) {
   Plan p;
   p.form.assign(jobs.size(), -1);
   std::vector<double> slotLoad;
@@ -123,7 +125,7 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, Plan*
   }
   if (used > sms) return false;
   // per ragged launch class (the CTAs of a launch are sized for its grid), the fewest one-SM CTAs
-  // whose largest-first schedule fits within T, in clusters of four
+  // whose largest-first schedule fits within T, in groups of gran
   std::map<int, std::vector<double>> byClass;
   for (size_t i : order)
     if (p.form[i] == kOne) byClass[jobs[i].cls].push_back(jobs[i].t[kOne]);
@@ -136,11 +138,11 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, Plan*
     int mc = std::max(1, (int)std::ceil(sum / T));
     while (mc < (int)pool.size() && lpt_makespan(pool, mc) > T) mc++;
     if (lpt_makespan(pool, mc) > T) return false;
-    mc = (mc + 3) / 4 * 4;
+    mc = (mc + gran - 1) / gran * gran;
     p.classCTAs[kv.first] = mc;
     m += mc;
   }
-  if (used + m > sms) return false;
+  if (used + m > poolSms) return false;
   p.poolSMs = m;
   p.makespan = T;
   *out = p;
@@ -299,8 +301,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         break;
       }
     // the makespan lies between the longest medium in its fastest form and every medium on one SM one
-    // after another; the plan may use the SMs that clusters of four can hold at once (the slots and
-    // the ragged launches are all launched as clusters)
+    // after another; the slots may use the SMs that clusters of four can hold at once
     const int budget = std::max(4, cluster_capacity_sms(ms[fused[0]]->findKernel(kKindRagged, ms[fused[0]]->solver, 8)->fn,
                                                         sms));
     g_capacityUsed = budget;
@@ -313,7 +314,13 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     // targets are scanned upward in steps of 0.25 % and the first feasible one is taken.  The plans of
     // recent sets are kept: a repeated call (the same estimates, budget and slot capacity) reuses its
     // plan without the scan.
-    std::vector<double> planKey{(double)budget, (double)maxW16};
+    // The ragged launches run without clusters, so their CTAs take any SM the slots leave, the SMs of
+    // a GPC beyond its clusters' groups included: the slots must fit in the cluster budget, the slots
+    // and the ragged CTAs together in all the device's SMs.  NLM_RAGGED_POOL_CLUSTERS=1 launches them
+    // in clusters of four within the budget instead.
+    const bool clusteredPool = std::getenv("NLM_RAGGED_POOL_CLUSTERS") != nullptr;
+    const int gran = clusteredPool ? 4 : 1, poolBudget = clusteredPool ? budget : sms;
+    std::vector<double> planKey{(double)budget, (double)maxW16, (double)clusteredPool};
     for (const Job& j : jobs) {
       planKey.push_back((double)j.cls);
       planKey.insert(planKey.end(), j.t, j.t + kForms);
@@ -325,8 +332,9 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       plan = cached->second;
       planned = true;
     }
-    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.0025) planned = plan_for(jobs, T, budget, maxW16, &plan);
-    if (!planned) planned = plan_for(jobs, hi, budget, maxW16, &plan);
+    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.0025)
+      planned = plan_for(jobs, T, budget, maxW16, poolBudget, gran, &plan);
+    if (!planned) planned = plan_for(jobs, hi, budget, maxW16, poolBudget, gran, &plan);
     if (planned && cached == g_planCache.end()) {
       if (g_planCache.size() >= 16) g_planCache.erase(g_planCache.begin());
       g_planCache[planKey] = plan;
@@ -358,7 +366,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     {
       int slotSMs = 0;
       for (int f : plan.slotForm) slotSMs += kFormSMs[f];
-      leftover = std::max(0, (budget - slotSMs - plan.poolSMs) / 4 * 4);
+      leftover = std::max(0, (poolBudget - slotSMs - plan.poolSMs) / gran * gran);
     }
 
     // ---- buffers, staging and the ragged launches' items (nothing is allocated inside the graph) ----
@@ -439,11 +447,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       ck(exclusive_smem(ke->fn, maxN * sizeof(double2), &rl.smem, &fa), "smem attribute");
       if (rl.smem == 0) throw Unsupported("ragged kernel does not fit on an SM");
       if (rl.block > fa.maxThreadsPerBlock) throw Unsupported("ragged kernel cannot launch that many threads");
-      // launched in clusters of four CTAs: the ragged CTAs take whole groups of four SMs and leave the
-      // groups that the cluster slots need
-      const int extra = (int)((double)leftover * (poolWork > 0 ? work / poolWork : 1.0)) / 4 * 4;
-      const int most = ((int)js.size() + 3) / 4 * 4;
-      rl.grid = std::min(most, std::max(4, plan.classCTAs[kv.first] + extra));
+      // a share of the SMs the plan leaves free, in proportion to the launch's work
+      const int extra = (int)((double)leftover * (poolWork > 0 ? work / poolWork : 1.0)) / gran * gran;
+      const int most = ((int)js.size() + gran - 1) / gran * gran;
+      rl.grid = std::min(most, std::max(gran, plan.classCTAs[kv.first] + extra));
       raggedLaunches.push_back(rl);
     }
     g_ragged.items.reserve(std::max<size_t>(items.size(), 1));
@@ -500,7 +507,7 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
         unsigned long long* ctr = g_ragged.counters.p + r;
         int nIt = rl.count;
         void* args[] = {(void*)&itemsD, (void*)&nIt, (void*)&ctr};
-        ck(launch_clustered(rl.ke->fn, rl.grid, rl.block, rl.smem, st, Medium::kClusterSize, args), "ragged launch");
+        ck(launch_clustered(rl.ke->fn, rl.grid, rl.block, rl.smem, st, gran, args), "ragged launch");
       }
       for (size_t j = 1; j < si; j++) {
         ck(cudaEventRecord(g_ragged.events[j], streams[j]), "ragged join");
