@@ -102,12 +102,17 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
 
 // Two rows per thread group (rows 2q and 2q+1 of the launch).  The Raman convolution acts on the real
 // intensity rel |y|^2 with the transform of a real response, R~ (Hermitian), so the two rows'
-// convolutions run as one complex convolution: IFFT[R~ FFT[uA + i uB]] = conv(uA) + i conv(uB).  A row
-// then costs 14 transforms per step instead of 18 (4 stages x (1 shared Raman pair / 2 + steepening
-// pair) + the dispersion pair); the Raman result is taken real, as it is in exact arithmetic.  A
-// second row past the end of the launch propagates zeros and is not stored.
-// Scratch per slot: the two rows' states X, RK4 sums A and stage results K, and their real Raman
-// results (7 N complex values).
+// convolutions run as one complex convolution: IFFT[R~ FFT[uA + i uB]] = conv(uA) + i conv(uB); the
+// Raman result is taken real, as it is in exact arithmetic.
+// The RK4 sum is kept in the frequency domain: each stage's k is formed there (the self-steepening
+// operator) and needed back in time only as the next stage's input, so the last stage's inverse
+// transform is skipped; and the state's spectrum is kept from the previous step's dispersion, so the
+// step's end FFT[x + sum / 6] = X + FFT[sum] / 6 needs no transform.  A row then costs 12 transforms
+// per step instead of 18 (4 stages x (1 shared Raman pair / 2 + 2 steepening) - 1, + 1 inverse for the
+// dispersion step); in exact arithmetic the same step.  A second row past the end of the launch
+// propagates zeros and is not stored.
+// Scratch per slot: the two rows' states in time (X) and frequency (XF), RK4 sums in frequency (A) and
+// stage results in time (K), and their real Raman results (9 N complex values).
 template <int R>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const PropArgs a, double2* __restrict__ scratch) {
   extern __shared__ double2 smem[];
@@ -117,13 +122,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
   double2* bufs;
   const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
   double2* buf = bufs + (long long)g * N;
-  // slot: X of row 0 and 1, then A of row 0 and 1, then K of row 0 and 1 (N values each), then the
-  // two rows' real Raman results (N reals each, in the space of N complex values)
-  double2* slot = scratch + ((long long)blockIdx.x * a.ipc + g) * 7 * N;
-  auto U = [&](int r) { return reinterpret_cast<double*>(slot + 6 * N) + (long long)r * N; };
+  // slot: X, XF, A, K of row 0 and 1 (N values each), then the two rows' real Raman results (N reals
+  // each, in the space of N complex values)
+  double2* slot = scratch + ((long long)blockIdx.x * a.ipc + g) * 9 * N;
+  auto U = [&](int r) { return reinterpret_cast<double*>(slot + 8 * N) + (long long)r * N; };
   auto X = [&](int r) { return slot + (long long)r * N; };
-  auto A = [&](int r) { return slot + (long long)(2 + r) * N; };
-  auto K = [&](int r) { return slot + (long long)(4 + r) * N; };
+  auto XF = [&](int r) { return slot + (long long)(2 + r) * N; };
+  auto A = [&](int r) { return slot + (long long)(4 + r) * N; };
+  auto K = [&](int r) { return slot + (long long)(6 + r) * N; };
   const long long nPairs = (a.nInst + 1) / 2;
   const long long nGroups = (nPairs + a.ipc - 1) / a.ipc;
   __shared__ long long s_group;
@@ -135,6 +141,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
     for (int r = 0; r < 2; r++) {
       double2 x[1][R];
       load_input<1, R>(a, inst(r), active(r), j, x, buf, plan, tw);
+#pragma unroll
+      for (int v = 0; v < R; v++) XF(r)[j + v * T] = x[0][v];
       fft_regs<R, true>(x[0], buf, tw, plan, j);
 #pragma unroll
       for (int v = 0; v < R; v++) X(r)[j + v * T] = x[0][v];
@@ -165,7 +173,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
           U(0)[j + v * T] = u[v].x;
           U(1)[j + v * T] = u[v].y;
         }
-        // per row: times the field, then the self-steepening operator (g0 + g1 w)
+        // per row: times the field, then the self-steepening operator (g0 + g1 w): the stage's k in
+        // the frequency domain, added to the sum there; back in time for the next stage's input
 #pragma unroll 1
         for (int r = 0; r < 2; r++) {
           double2 w[R];
@@ -178,23 +187,36 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
           }
           fft_regs<R, false>(w, buf, tw, plan, j);
 #pragma unroll
-          for (int v = 0; v < R; v++) w[v] = cmul(w[v], __ldg(a.steep + j + v * T));
-          fft_regs<R, true>(w, buf, tw, plan, j);
-#pragma unroll
           for (int v = 0; v < R; v++) {
             const int t = j + v * T;
-            K(r)[t] = w[v];
+            w[v] = cmul(w[v], __ldg(a.steep + t));
             A(r)[t] = s == 0 ? w[v] : caxpy(A(r)[t], wgt, w[v]);
+          }
+          if (s < 3) {
+            fft_regs<R, true>(w, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) K(r)[j + v * T] = w[v];
           }
         }
       }
+      // the dispersion step on the spectrum of x + sum / 6: N (X + A / 6), X and A holding spectra whose
+      // unscaled inverse transform is the time-domain field (the tables carry the 1/N of each
+      // transform pair); then back to time
       const bool last = i == a.nZ - 1;
+      const double2* table = last ? a.dlast : a.dstep;
 #pragma unroll 1
       for (int r = 0; r < 2; r++) {
         double2 x[1][R];
 #pragma unroll
-        for (int v = 0; v < R; v++) x[0][v] = caxpy(X(r)[j + v * T], 1.0 / 6.0, A(r)[j + v * T]);
-        dispersion_step<1, R>(a, i, last, j, x, buf, plan, active(r), last ? a.dlast : a.dstep, tw);
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          x[0][v] = cmul(cscale(caxpy(XF(r)[t], 1.0 / 6.0, A(r)[t]), (double)N), __ldg(table + t));
+        }
+        if (!last) {
+#pragma unroll
+          for (int v = 0; v < R; v++) XF(r)[j + v * T] = x[0][v];
+        }
+        if (!last || a.inTime) fft_regs<R, true>(x[0], buf, tw, plan, j);
         if (!last) {
 #pragma unroll
           for (int v = 0; v < R; v++) X(r)[j + v * T] = x[0][v];
