@@ -86,7 +86,8 @@ nlm_status nlm::prepare_gnlse_noalloc(nlm_medium* h, const void* in, size_t rows
     // only the one-CTA kernel takes its scratch from the caller: grids it cannot hold (more than
     // 512 threads of R points, or a grid the fused kernels do not take) are rejected here
     m->checkGridStrict(R);
-    const KernelEntry* k = m->findKernel(kKindGnlse, m->solver, R);
+    // the form whose RK4 sum stays in time: two scratch parts per propagation
+    const KernelEntry* k = m->findKernel(kKindGnlse, m->solver + 700, R);
     if (!k) throw Unsupported("no one-CTA Chi3GNLSE kernel for a grid of " + std::to_string(m->N) + " points");
     Medium::Schedule s = m->schedule(k, (long long)rows, R);
     // the array bounds how many CTAs run at once (2 N values per resident propagation); more rows

@@ -1939,8 +1939,8 @@ struct Medium {
     }
     double2* sp = nullptr;
     if (gnlse) {
-      // per thread group: 2 (9 when paired) parts of T R values (N on the register plan)
-      const size_t slots = std::max((size_t)s.grid * s.ipc * (paired ? 9 : 2), (size_t)sTail.grid * sTail.ipc * 2);
+      // per thread group: 3 (9 when paired) parts of T R values (N on the register plan)
+      const size_t slots = std::max((size_t)s.grid * s.ipc * (paired ? 9 : 3), (size_t)sTail.grid * sTail.ipc * 3);
       scratch.reserve(slots * ((size_t)a.plan.T * a.R));
       sp = scratch.p;
     }

@@ -13,7 +13,13 @@
 namespace nlm {
 
 // GEN: the general plan (any N, padded ownership); the scratch slot then holds T R >= N values per part.
-template <int R, bool GEN = false>
+// FS: the RK4 sum kept in the frequency domain, as in k_propagate_gnlse_pair: each stage's k is formed
+// as a spectrum by the self-steepening operator and transformed back only as the next stage's input
+// (the fourth stage's inverse transform drops out), and the state's spectrum is kept from the previous
+// dispersion step, so FFT[x + sum / 6] = N (X + A / 6) needs no transform: 16 transforms per step
+// instead of 18, three scratch parts (X, its spectrum XF, the sum A) instead of two.  Without FS (the
+// allocation-free entry point, whose static array is sized for two parts) the sum stays in time.
+template <int R, bool GEN = false, bool FS = true>
 __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs a, double2* __restrict__ scratch) {
   extern __shared__ double2 smem[];
   const FFTPlanH& plan = a.plan;
@@ -22,9 +28,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
   double2* bufs;
   const double2* tw = stage_twiddles<R>(a.tw, smem, N, &bufs);
   double2* buf = bufs + (long long)g * N;
-  const long long NS = (long long)T * R;                                // N for a power-of-two plan
-  double2* X = scratch + ((long long)blockIdx.x * a.ipc + g) * 2 * NS;  // state (time domain)
-  double2* ACC = X + NS;                                                // k1 + 2 k2 + 2 k3 + k4
+  const long long NS = (long long)T * R;                                          // N for a power-of-two plan
+  double2* X = scratch + ((long long)blockIdx.x * a.ipc + g) * (FS ? 3 : 2) * NS;  // state (time domain)
+  double2* ACC = X + NS;                       // k1 + 2 k2 + 2 k3 + k4 (time domain; the spectrum with FS)
+  double2* XF = X + 2 * NS;                    // FS: the state's spectrum
   const long long nGroups = (a.nInst + a.ipc - 1) / a.ipc;
   __shared__ long long s_group;
   for (long long cg = blockIdx.x; cg < nGroups; cg = next_group(a, cg, &s_group)) {
@@ -35,6 +42,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
     load_input<1, R, GEN>(a, inst, active, j, x, buf, plan, tw);
     const long long ms = (long long)a.nZ * N;
     if (a.gridF) store_rows<1, R, GEN>(a.gridF, ms, 0, N, T, j, x, (double)N, active);
+    if (FS) {
+#pragma unroll
+      for (int v = 0; v < R; v++) XF[j + v * T] = x[0][v];
+    }
     fft_any<R, true, GEN>(x[0], buf, tw, plan, j);
     if (a.gridT) store_rows<1, R, GEN>(a.gridT, ms, 0, N, T, j, x, 1.0, active);
 #pragma unroll
@@ -66,18 +77,50 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse(const PropArgs 
         fft_any<R, false, GEN>(u, buf, tw, plan, j);
 #pragma unroll
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + j + v * T));
-        fft_any<R, true, GEN>(u, buf, tw, plan, j);
+        if (FS) {
 #pragma unroll
-        for (int v = 0; v < R; v++) {
-          k[v] = u[v];
-          const int t = j + v * T;
-          ACC[t] = s == 0 ? u[v] : caxpy(ACC[t], wgt, u[v]);
+          for (int v = 0; v < R; v++) {
+            const int t = j + v * T;
+            ACC[t] = s == 0 ? u[v] : caxpy(ACC[t], wgt, u[v]);
+          }
+          if (s < 3) {
+            fft_any<R, true, GEN>(u, buf, tw, plan, j);
+#pragma unroll
+            for (int v = 0; v < R; v++) k[v] = u[v];
+          }
+        } else {
+          fft_any<R, true, GEN>(u, buf, tw, plan, j);
+#pragma unroll
+          for (int v = 0; v < R; v++) {
+            k[v] = u[v];
+            const int t = j + v * T;
+            ACC[t] = s == 0 ? u[v] : caxpy(ACC[t], wgt, u[v]);
+          }
         }
       }
-#pragma unroll
-      for (int v = 0; v < R; v++) x[0][v] = caxpy(X[j + v * T], 1.0 / 6.0, ACC[j + v * T]);
       const bool last = i == a.nZ - 1;
-      dispersion_step<1, R, GEN>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      if (FS) {
+        // the dispersion step on the spectrum of x + sum / 6 (the tables carry each pair's 1/N)
+        const double2* table = last ? a.dlast : a.dstep;
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+          const int t = j + v * T;
+          x[0][v] = cmul(cscale(caxpy(XF[t], 1.0 / 6.0, ACC[t]), (double)N), __ldg(table + t));
+        }
+        if (a.gridF) store_rows<1, R, GEN>(a.gridF, ms, i, N, T, j, x, (double)N, active);
+        if (!last) {
+#pragma unroll
+          for (int v = 0; v < R; v++) XF[j + v * T] = x[0][v];
+        }
+        if (!last || a.inTime || a.gridT) {
+          fft_any<R, true, GEN>(x[0], buf, tw, plan, j);
+          if (a.gridT) store_rows<1, R, GEN>(a.gridT, ms, i, N, T, j, x, 1.0, active);
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < R; v++) x[0][v] = caxpy(X[j + v * T], 1.0 / 6.0, ACC[j + v * T]);
+        dispersion_step<1, R, GEN>(a, i, last, j, x, buf, plan, active, last ? a.dlast : a.dstep, tw);
+      }
       if (!last) {
 #pragma unroll
         for (int v = 0; v < R; v++) X[j + v * T] = x[0][v];
@@ -246,6 +289,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_pair(const Prop
 
 void add_kernels_gnlse(std::vector<KernelEntry>& t) {
   t.push_back({kKindGnlse, kChi3GNLSE, 8, (const void*)k_propagate_gnlse<8>});
+  // key + 700: the RK4 sum in time (two scratch parts), for the allocation-free entry point
+  t.push_back({kKindGnlse, kChi3GNLSE + 700, 8, (const void*)k_propagate_gnlse<8, false, false>});
   // key + kGenKey: grids that are not powers of two (general plan), up to 4096 and 8192 points
   t.push_back({kKindGnlse, kChi3GNLSE + kGenKey, 8, (const void*)k_propagate_gnlse<8, true>});
   t.push_back({kKindGnlse, kChi3GNLSE + kGenKey, 16, (const void*)k_propagate_gnlse<16, true>});
