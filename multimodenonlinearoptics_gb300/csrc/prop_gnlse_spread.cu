@@ -3,7 +3,7 @@
 //
 // A z step is 16 transforms inside the four RK4 stages,
 //     k = IFFT[(g0 + g1 w) FFT[ y * IFFT[R~ FFT[rel |y|^2]] ]],
-// plus the dispersion pair.  With four points per thread on four CTAs (prop_cluster_gnlse.cu) a
+// plus the dispersion pair; with the RK4 sum in the frequency domain, 16 in all.  With four points per thread on four CTAs (prop_cluster_gnlse.cu) a
 // single 4096-point propagation takes about 260 us per step; here it holds N / C points per CTA, one
 // per thread: sixteen CTAs of 256 threads at 4096 points (the full-grid form), eight of 256 at 2048.
 // The per-point tables (Raman response, self-steepening factors, dispersion) stay in registers.
@@ -36,6 +36,7 @@ __global__ void __launch_bounds__(C == 16 ? 256 : kMaxThreads) k_propagate_gnlse
     double2 x = has ? row[a.inTime ? tn : fk] : czero();
     if (a.inTime) x = spread_fwd<C>(f, x, cl);
     x = cmul(x, __ldg(a.half + fk));
+    double2 xf = x;   // the state's spectrum (whose unscaled inverse transform is x)
     x = spread_inv_store<C>(f, x, cl, [&](double2 v) {
       if (a.gridF) a.gridF[fk] = cscale(v, (double)N);
     });
@@ -46,6 +47,9 @@ __global__ void __launch_bounds__(C == 16 ? 256 : kMaxThreads) k_propagate_gnlse
     for (int i = 1; i < a.nZ; i++) {
       const double* rel = a.relInt + (long long)(i - 1) * 3;
       double2* stg = a.stages ? a.stages + ((inst * (a.nZ - 1) + i - 1) * 8LL) * N : nullptr;
+      // the RK4 sum in the frequency domain (k_propagate_gnlse_pair): each stage's k is formed as a
+      // spectrum and transformed back only as the next stage's input; the step's end is
+      // FFT[x + sum / 6] = N (xf + sum / 6), with no transform.  16 transforms per step.
       double2 k = czero(), acc = czero();
       for (int s = 0; s < 4; s++) {
         const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
@@ -59,14 +63,13 @@ __global__ void __launch_bounds__(C == 16 ? 256 : kMaxThreads) k_propagate_gnlse
         u = spread_inv<C>(f, cmul(u, ram), cl);
         if (stg) stg[(long long)(4 + s) * N + tn] = u;
         // times the field, then the self-steepening operator (g0 + g1 w)
-        u = spread_fwd<C>(f, cmul(u, y), cl);
-        u = spread_inv<C>(f, cmul(u, stp), cl);
-        k = u;
+        u = cmul(spread_fwd<C>(f, cmul(u, y), cl), stp);
         acc = s == 0 ? u : caxpy(acc, wgt, u);
+        if (s < 3) k = spread_inv<C>(f, u, cl);
       }
-      x = caxpy(x, 1.0 / 6.0, acc);
       const bool last = i == a.nZ - 1;
-      x = cmul(spread_fwd<C>(f, x, cl), last ? dla : dst);
+      x = cmul(cscale(caxpy(xf, 1.0 / 6.0, acc), (double)N), last ? dla : dst);
+      if (!last) xf = x;
       auto storeF = [&](double2 v) {
         if (a.gridF) a.gridF[(long long)i * N + fk] = cscale(v, (double)N);
       };
