@@ -377,28 +377,29 @@ __device__ __forceinline__ void pair_stages(const PropArgs& a, int i, int j, dou
   }
 }
 
-// One reverse step i for both rows: G (time domain after the step; frequency domain for the last
-// step) becomes the gradient with respect to the state before the step.
+// One reverse step i for both rows.  G holds the gradient with respect to the spectrum after the step
+// (the transform of the time-domain gradient; for the last step the output spectrum's gradient) and
+// becomes the one before it.  The step in the frequency domain: with H = N conj(D) G (D the step's
+// dispersion factors, which carry the 1/N of a transform pair), the gradient of stage s's spectrum k_s
+// is w_s H plus, for s < 3, the transform of the gradient its time-domain value gets through the next
+// stage's input; the self-steepening and Raman adjoints follow in time; and the spectrum before the
+// step gets H plus the transform of the time-domain gradient the stage inputs give the state.  Per
+// row 12 transforms (the fourth stage needs only the inverse, and no pair brackets the dispersion
+// step), where the time-domain form takes 14; in exact arithmetic the same gradient.
 template <int R>
 __device__ __forceinline__ void pair_reverse_step(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
                                                   PairRow (&row)[2]) {
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
   const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
+  // H (frequency domain) in GXP; the stage inputs' gradient sum (time domain) in GX
 #pragma unroll 1
   for (int r = 0; r < 2; r++) {
-    double2 g[R];
-#pragma unroll
-    for (int v = 0; v < R; v++) g[v] = row[r].G[j + v * T];
-    if (i < a.nZ - 1) fft_regs<R, false>(g, buf, tw, plan, j);
-#pragma unroll
-    for (int v = 0; v < R; v++) g[v] = cmulc(g[v], __ldg(tab + j + v * T));
-    fft_regs<R, true>(g, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) {
       const int t = j + v * T;
-      row[r].GX[t] = g[v];
-      row[r].GXP[t] = g[v];
+      row[r].GXP[t] = cscale(cmulc(row[r].G[t], __ldg(tab + t)), (double)N);
+      row[r].GX[t] = czero();
       row[r].GKE[t] = czero();
     }
   }
@@ -410,12 +411,19 @@ __device__ __forceinline__ void pair_reverse_step(const PropArgs& a, int i, int 
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
       double2 u[R];
+      if (s < 3) {
 #pragma unroll
-      for (int v = 0; v < R; v++) u[v] = caxpy(row[r].GKE[j + v * T], w, row[r].GXP[j + v * T]);   // g_k_s
-      fft_regs<R, false>(u, buf, tw, plan, j);
+        for (int v = 0; v < R; v++) u[v] = row[r].GKE[j + v * T];
+        fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+        for (int v = 0; v < R; v++) u[v] = caxpy(u[v], w, row[r].GXP[j + v * T]);   // g_k_s (spectrum)
+      } else {
+#pragma unroll
+        for (int v = 0; v < R; v++) u[v] = cscale(row[r].GXP[j + v * T], w);
+      }
 #pragma unroll
       for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
-      fft_regs<R, true>(u, buf, tw, plan, j);                                                 // g_u3
+      fft_regs<R, true>(u, buf, tw, plan, j);                                         // g_u3
 #pragma unroll
       for (int v = 0; v < R; v++) {
         const int t = j + v * T;
@@ -432,7 +440,7 @@ __device__ __forceinline__ void pair_reverse_step(const PropArgs& a, int i, int 
     fft_regs<R, false>(p, buf, tw, plan, j);
 #pragma unroll
     for (int v = 0; v < R; v++) p[v] = cmulc(p[v], __ldg(a.raman + j + v * T));
-    fft_regs<R, true>(p, buf, tw, plan, j);                                                   // g_u1 of both rows
+    fft_regs<R, true>(p, buf, tw, plan, j);                                           // g_u1 of both rows
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
 #pragma unroll
@@ -446,10 +454,15 @@ __device__ __forceinline__ void pair_reverse_step(const PropArgs& a, int i, int 
       }
     }
   }
+  // the spectrum before the step: H + FFT[the stage inputs' gradient]
 #pragma unroll 1
   for (int r = 0; r < 2; r++) {
+    double2 gv[R];
 #pragma unroll
-    for (int v = 0; v < R; v++) row[r].G[j + v * T] = row[r].GX[j + v * T];
+    for (int v = 0; v < R; v++) gv[v] = row[r].GX[j + v * T];
+    fft_regs<R, false>(gv, buf, tw, plan, j);
+#pragma unroll
+    for (int v = 0; v < R; v++) row[r].G[j + v * T] = cadd(gv[v], row[r].GXP[j + v * T]);
   }
 }
 
@@ -545,16 +558,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pair(const PropAr
       }
       segEnd = s0;
     }
+    // G: the gradient of the input spectrum times half a dispersion step (its transform)
 #pragma unroll 1
     for (int r = 0; r < 2; r++) {
-      double2 gv[R];
-#pragma unroll
-      for (int v = 0; v < R; v++) gv[v] = row[r].G[j + v * T];
-      fft_regs<R, false>(gv, buf, tw, plan, j);
       if (act[r]) {
 #pragma unroll
         for (int v = 0; v < R; v++)
-          d.gin[(inst0 + r) * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
+          d.gin[(inst0 + r) * (long long)N + j + v * T] = cmulc(row[r].G[j + v * T], __ldg(a.half + j + v * T));
       }
     }
     __syncthreads();
