@@ -287,10 +287,10 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pipe(const PropAr
 // Hermitian) maps real fields to real fields.  The forward's Raman input rel |y|^2 is real, and the
 // reverse step only uses Re L(g_u2) = L(Re g_u2): so two rows' Raman transforms run as one complex
 // pair, L(a + i b) = L(a) + i L(b).  Per row and step: 10 transforms to recompute the stages (4
-// shared Raman pairs, 3 self-steepening pairs) and 14 to reverse the step (the dispersion pair, 4 x
-// the self-steepening pair and 4 shared Raman pairs), against 14 + 18.  With checkpoint intervals
-// K > 1 the segment's forward recomputation (14 per row and step) stores the stage values of its K
-// steps and the reverse steps read them: 14 + 14 instead of 14 + 10 + 14.  Per-row scratch (each
+// shared Raman pairs, 3 self-steepening pairs) and 12 to reverse the step in the frequency domain
+// (7 for the self-steepening adjoints, 4 shared Raman pairs, one for the state), against 14 + 18.
+// With checkpoint intervals K > 1 the segment's forward recomputation (14 per row and step) stores
+// the stage values of its K steps and the reverse steps read them: 14 + 12 instead of 14 + 10 + 12.  Per-row scratch (each
 // thread touches only its own points): Y[4], U2[4] (real, stored as complex), K, GX, GXP, G, GY, GKE,
 // ZR (real, stored as complex), ACC: 16 N; for K > 1 also the state being recomputed and the stage
 // store STG[K][8]: (1 + 8 K) N.
