@@ -7,7 +7,7 @@
 //     g_u1 = Re F^H(conj(R') F g_u2),  g_y += 2 r g_u1 y,  g_x += g_y,  g_k_{s-1} += fac_s g_y.
 // For every step the stage inputs y_s and convolutions u2_s are recomputed from the state before the
 // step (14 transforms: the last stage's self-steepening pair is not needed), then the 16 transforms
-// of the reverse stages and the dispersion pair run.  States come from checkpoints every K steps;
+// of the reverse step run (gnlse_reverse_step: the gradient stays in the frequency domain).  States come from checkpoints every K steps;
 // segments between checkpoints are recomputed.
 // With K > 1 the segment's recomputation stores the stage values of its steps, which its reverse
 // steps then read.  Scratch per propagation slot: Y[4][N], U2[4][N], GX[N], GXP[N], and for K > 1 the
@@ -70,25 +70,25 @@ __device__ __forceinline__ void gnlse_stages(const PropArgs& a, int i, int j, do
   }
 }
 
-// One reverse step i: gv (this thread's points of g, time domain after the step) becomes the gradient
-// with respect to the state before the step.  Y/U2: the stage inputs y_s and convolutions u2_s of
-// step i; GX/GXP: per-propagation global scratch of N points each.
+// One reverse step i: gv (this thread's points of the gradient with respect to the spectrum after the
+// step) becomes the gradient with respect to the spectrum before it.  Y/U2: the stage inputs y_s and
+// convolutions u2_s of step i; GX/GXP: per-propagation global scratch of N points each.  The transpose
+// of the forward's frequency-domain RK4 sum: with H = N conj(D) g (D the step's dispersion factors,
+// which carry the 1/N of a transform pair), stage s's spectrum gets w_s H plus the transform of the
+// gradient its time-domain value takes through the next stage's input, and the spectrum before the
+// step H plus the transform of the stage inputs' gradient.  16 transforms per step where the
+// time-domain form takes 18; in exact arithmetic the same gradient.
 template <int R>
 __device__ __forceinline__ void gnlse_reverse_step(const PropArgs& a, int i, int j, double2* buf, const double2* tw,
                                                    const double2* Y, const double2* U2, double2* GX, double2* GXP,
                                                    double2 (&gv)[R]) {
   const FFTPlanH& plan = a.plan;
   const int N = plan.N, T = plan.T;
-  // dispersion half: g_x' = F^H(conj(table) F g)
-  if (i < a.nZ - 1) fft_regs<R, false>(gv, buf, tw, plan, j);
   const double2* tab = (i == a.nZ - 1) ? a.dlast : a.dstep;
 #pragma unroll
-  for (int v = 0; v < R; v++) gv[v] = cmulc(gv[v], __ldg(tab + j + v * T));
-  fft_regs<R, true>(gv, buf, tw, plan, j);
-#pragma unroll
   for (int v = 0; v < R; v++) {
-    GX[j + v * T] = gv[v];
-    GXP[j + v * T] = gv[v];
+    GXP[j + v * T] = cscale(cmulc(gv[v], __ldg(tab + j + v * T)), (double)N);   // H
+    GX[j + v * T] = czero();
   }
   const double* rel = a.relInt + (long long)(i - 1) * 3;
   double2 gke[R];
@@ -99,9 +99,16 @@ __device__ __forceinline__ void gnlse_reverse_step(const PropArgs& a, int i, int
     const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
     const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
     double2 u[R];
+    if (s < 3) {
 #pragma unroll
-    for (int v = 0; v < R; v++) u[v] = caxpy(gke[v], w, GXP[j + v * T]);   // g_k_s
-    fft_regs<R, false>(u, buf, tw, plan, j);
+      for (int v = 0; v < R; v++) u[v] = gke[v];
+      fft_regs<R, false>(u, buf, tw, plan, j);
+#pragma unroll
+      for (int v = 0; v < R; v++) u[v] = caxpy(u[v], w, GXP[j + v * T]);   // g_k_s (spectrum)
+    } else {
+#pragma unroll
+      for (int v = 0; v < R; v++) u[v] = cscale(GXP[j + v * T], w);
+    }
 #pragma unroll
     for (int v = 0; v < R; v++) u[v] = cmulc(u[v], __ldg(a.steep + j + v * T));
     fft_regs<R, true>(u, buf, tw, plan, j);                                   // g_u3
@@ -128,6 +135,9 @@ __device__ __forceinline__ void gnlse_reverse_step(const PropArgs& a, int i, int
   }
 #pragma unroll
   for (int v = 0; v < R; v++) gv[v] = GX[j + v * T];
+  fft_regs<R, false>(gv, buf, tw, plan, j);
+#pragma unroll
+  for (int v = 0; v < R; v++) gv[v] = cadd(gv[v], GXP[j + v * T]);
 }
 
 template <int R>
@@ -196,7 +206,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse(const PropArgs a,
       }
       segEnd = s0;
     }
-    fft_regs<R, false>(gv, buf, tw, plan, j);
+    // gv: the gradient of the input spectrum; times half a dispersion step
     if (active) {
 #pragma unroll
       for (int v = 0; v < R; v++)
@@ -274,7 +284,6 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_pipe(const PropAr
       cluster.sync();
     }
     if (role == 0) {
-      fft_regs<R, false>(gv, buf, tw, plan, j);
 #pragma unroll
       for (int v = 0; v < R; v++) d.gin[inst * (long long)N + j + v * T] = cmulc(gv[v], __ldg(a.half + j + v * T));
     }
