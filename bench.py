@@ -367,7 +367,9 @@ def measure_configs(nlm, torch, cpu=True):
     sig = (rng.standard_normal(512) + 1j * rng.standard_normal(512)) * 1e-3 / np.sqrt(2)
 
     def chi3_latency(mode):
-        # mode 1 (default): both marches on four SMs with one point per thread; 0: one CTA each
+        # mode 1 (default): the pump march and the signal side by side on one cluster of eight CTAs (four
+        # SMs each, one point per thread); 3: the same two marches one after the other on four SMs; 0:
+        # one CTA each
         m1 = nlm.Chi3(**kw1)
         m1._set_cluster(mode)
         m1.runPumpSimulation()
@@ -382,7 +384,9 @@ def measure_configs(nlm, torch, cpu=True):
         return 1e3 * min(lat), m1
 
     lat1, m1 = chi3_latency(1)
-    res["chi3_pump_signal_n512"] = {"gpu_latency_ms": lat1, "gpu_latency_ms_one_cta": chi3_latency(0)[0]}
+    res["chi3_pump_signal_n512"] = {"gpu_latency_ms": lat1, "form": "pump and signal pipelined on 8 CTAs",
+                                    "gpu_latency_ms_sequential_spread": chi3_latency(3)[0],
+                                    "gpu_latency_ms_one_cta": chi3_latency(0)[0]}
     if cpu:
         from oracle import nlm_oracle as O
         o1 = O.Chi3(**kw1)

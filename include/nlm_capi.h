@@ -261,8 +261,12 @@ nlm_status nlm_last_schedule(const nlm_medium* m, int* values);
  * full-grid propagations (runSignalSimulation) take the widest one-point-per-thread form: eight CTAs
  * at 1024 points, sixteen (a non-portable cluster size) at 2048 and 4096 points where the solver
  * has that form (single-mode solvers; multi-mode ones whose mode-fused buffers fit), eight otherwise;
- * the Chi3 pump march uses eight CTAs on 2048 and 4096 points.
- * 3: as 1 without the widest forms (full grids on four CTAs up to 1024 points, eight above).
+ * the Chi3 pump march uses eight CTAs on 2048 and 4096 points.  On 128 to 1024 points, a Chi3
+ * nlm_run_pump defers the pump march: the next nlm_run_signal runs it beside the signal on one
+ * cluster of eight CTAs (four each, the signal one pump step pair behind); any other call that reads
+ * the pump grids runs it alone first.
+ * 3: as 1 without the widest forms (full grids on four CTAs up to 1024 points, eight above) and
+ * without the deferred Chi3 pump march.
  * 2: the four-points-per-thread clusters only.  0: one CTA per propagation.  nlm_ragged_batch plans
  * each medium's form among those its mode allows (1: one, four, eight or sixteen CTAs; 3: one, four
  * or eight).  Other values: NLM_ERR_VALUE.  No counterpart in the reference. */

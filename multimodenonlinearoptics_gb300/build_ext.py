@@ -24,7 +24,7 @@ CUDA_SOURCES = ["prop_linear.cu", "prop_direct_a.cu", "prop_direct_b.cu", "prop_
                 "greens_quadrature.cu", "prop_gen_a.cu", "prop_gen_b.cu",
                 "prop_gen_c.cu", "prop_gen_d.cu", "prop_gen_e.cu", "prop_spread_fused.cu",
                 "prop_spread_w16.cu", "prop_gnlse_spread.cu",
-                "adjoint_gnlse_spread.cu"]
+                "adjoint_gnlse_spread.cu", "prop_chi3_pipe.cu"]
 CXX_SOURCES = ["engine.cpp", "engine_ragged.cpp"]
 
 

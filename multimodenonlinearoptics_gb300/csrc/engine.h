@@ -650,6 +650,13 @@ struct Medium {
   long long adjPumpVersion = -1;
   DevBuf<double2> scaleD;
   long long pumpVersion = 0, signalVersion = 0;
+  // A Chi3 pump march that runPump prepared but did not launch (spread grids of up to 1024 points): the
+  // next runSignal runs it beside the signal on one cluster of eight CTAs (prop_chi3_pipe.cu); any
+  // other use of the pump grids runs it alone first (flushPump).
+  struct DeferredPump {
+    DevBuf<double2> env, half, dstep, back, rel;
+    bool pending = false;
+  } deferredPump;
   GridMirror mPumpF, mPumpT, mSigF, mSigT;
   std::vector<std::vector<double>> pumpMirrorF, pumpMirrorT, sigMirrorF, sigMirrorT;
   std::vector<long long> pumpMirrorVerF, pumpMirrorVerT, sigMirrorVerF, sigMirrorVerT;
@@ -1190,6 +1197,17 @@ struct Medium {
       }
       rel[i] = make_double2(r.real(), r.imag());
     }
+    if (pipePumpGrid()) {
+      DeferredPump& q = deferredPump;
+      upload(q.env, e);
+      upload(q.half, hP);
+      upload(q.dstep, dP);
+      upload(q.back, bP);
+      upload(q.rel, rel);
+      ck(cudaStreamSynchronize(stream), "chi3 pump tables");
+      q.pending = true;
+      return;
+    }
     DevBuf<double2> de, dh, dd, db, dr;
     upload(de, e);
     upload(dh, hP);
@@ -1213,9 +1231,32 @@ struct Medium {
     ck(cudaStreamSynchronize(stream), "chi3 pump");
   }
 
+  // The Chi3 pump march runs beside the next signal propagation: cluster mode 1, 128..1024 points (the
+  // four-CTA spread form), one pump row per half step.
+  bool pipePumpGrid() const {
+    return solver == kChi3 && useCluster == 1 && spreadGrid() && nZ >= 2 && nZP == 2 * nZ - 1 && nSignal == 1;
+  }
+
+  PumpMarchArgs deferredPumpArgs() const {
+    const DeferredPump& q = deferredPump;
+    return PumpMarchArgs{pumpFreq.p, pumpTime.p, q.env.p, q.half.p, q.dstep.p, q.back.p, q.rel.p, (int)nZP};
+  }
+
+  // Runs a deferred pump march alone (four CTAs, k_pump_chi3_spread) and waits for it.
+  void flushPump() {
+    if (!deferredPump.pending) return;
+    deferredPump.pending = false;
+    const PumpMarchArgs p = deferredPumpArgs();
+    ck(launch_pump_chi3_spread(p.pf, p.pt, p.env, p.halfP, p.dstepP, p.backP, p.rel, p.nRows, (int)N, tw, stream),
+       "chi3 pump (spread)");
+    launches++;
+    ck(cudaStreamSynchronize(stream), "chi3 pump");
+  }
+
   // src/_NonlinearMedium.cpp:506-534
   void setPumpFrom(Medium& other, uint modeIndex, double delay, uint idx) {
     if (fnl || isCascade) throw std::runtime_error("Object does not have this method.");
+    flushPump();
     if (other.isCascade) throw std::invalid_argument("Medium does not have same time and frequency axes as this one");
     if (other.N != N || other.tMax != tMax)
       throw std::invalid_argument("Medium does not have same time and frequency axes as this one");
@@ -1479,7 +1520,14 @@ struct Medium {
     return best;
   }
 
-  PropArgs baseArgs(int R) const {
+  // The launch description every kernel starts from; a deferred pump march runs first, since the
+  // launch may read the pump grids.
+  PropArgs baseArgs(int R) {
+    flushPump();
+    return plainArgs(R);
+  }
+
+  PropArgs plainArgs(int R) const {
     PropArgs a{};
     a.plan = make_plan((int)N, R);
     a.R = R;
@@ -2523,7 +2571,8 @@ struct Medium {
     checkGrid(R);
     io.reserve(n);
     ck(cudaMemcpyAsync(io.p, in, n * sizeof(double2), cudaMemcpyHostToDevice, stream), "input upload");
-    PropArgs a = baseArgs(R);
+    const bool pipe = deferredPump.pending && pipePumpGrid() && n == N;
+    PropArgs a = pipe ? plainArgs(R) : baseArgs(R);
     a.inKind = 1;
     a.inTime = inTime ? 1 : 0;
     a.in = io.p;
@@ -2532,9 +2581,43 @@ struct Medium {
     a.inputMode = (a.inChannels > 1 || nSignal <= 1) ? 0 : (int)inputMode;
     a.gridF = sigFreq.p;
     a.gridT = sigTime.p;
-    propagate(a, 1, true);
+    if (pipe) launchPumpSignal(a);
+    else propagate(a, 1, true);
     ck(cudaStreamSynchronize(stream), "signal simulation");
     signalVersion++;
+  }
+
+  // The deferred Chi3 pump march and this signal propagation on one cluster of eight CTAs: the pump on
+  // four, the signal on the other four one pump step pair behind (the solver's DiffEq at every step, no
+  // RK4 matrices), M = N / 4 threads per CTA.
+  void launchPumpSignal(PropArgs a) {
+    const int M = (int)N / 4;
+    a.plan = make_plan(M, 1);
+    a.R = 1;
+    a.nInst = 1;
+    a.ipc = 1;
+    a.work = nullptr;
+    a.prop = nullptr;
+    const PumpMarchArgs p = deferredPumpArgs();
+    deferredPump.pending = false;
+    lastSchedule = Schedule{8, M, 1, (size_t)spread_smem_per_point(4) * M * sizeof(double2), 1, 1};
+    lastR = 1;
+    lastTuned = 0;
+    if (timeKernels) {
+      if (!ev0) ck(cudaEventCreate(&ev0), "event");
+      if (!ev1) ck(cudaEventCreate(&ev1), "event");
+      ck(cudaEventRecord(ev0, stream), "event");
+    }
+    ck(launch_chi3_pump_signal_spread(a, p, stream, &lastRegs), "chi3 pump + signal (cluster of eight)");
+    launches++;
+    if (timeKernels) {
+      ck(cudaEventRecord(ev1, stream), "event");
+      ck(cudaEventSynchronize(ev1), "event");
+      float ms = 0;
+      ck(cudaEventElapsedTime(&ms, ev0, ev1), "event");
+      kernelMs += ms;
+      kernelCount++;
+    }
   }
 
   // mode selection of computeGreensFunction, src/_NonlinearMedium.cpp:266-302
@@ -2785,6 +2868,7 @@ struct Medium {
       default: throw IndexError("vector::_M_range_check");
     }
     if (isCascade || idx >= count) throw IndexError("vector::_M_range_check: index out of range");
+    if (which <= 1) flushPump();
     store->resize(count);
     vers->resize(count, -2);
     std::vector<double>& h = (*store)[idx];

@@ -268,7 +268,10 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     }
     if (fused.empty()) return;
     std::lock_guard<std::mutex> lock(g_ragged.mu);
-    for (size_t k : fused) ms[k]->ensureDevice();
+    for (size_t k : fused) {
+      ms[k]->ensureDevice();
+      ms[k]->flushPump();   // before any capture: the launches below read the pump grids
+    }
     const int sms = Medium::smCount();
 
     // ---- plan: a form per medium (the RK4 propagator decision first: it changes the step cost) ----

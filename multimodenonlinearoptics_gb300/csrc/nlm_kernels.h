@@ -156,6 +156,24 @@ constexpr int kSpreadW16Key = 900;
 cudaError_t launch_pump_chi3_spread(double2* pumpFreq, double2* pumpTime, const double2* env, const double2* halfP,
                                     const double2* dstepP, const double2* backP, const double2* rel, int nRows, int N,
                                     const double2* tw, cudaStream_t s);
+
+// The Chi3 pump march's grids and per-point tables (k_pump_chi3_spread's arguments).
+struct PumpMarchArgs {
+  double2* pf;            // [nRows][N] frequency-domain grid
+  double2* pt;            // [nRows][N] time-domain grid
+  const double2* env;     // [N] time-domain envelope
+  const double2* halfP;   // [N] half a dispersion step
+  const double2* dstepP;  // [N] a dispersion step, 1/N folded in
+  const double2* backP;   // [N] half a step back (the last row)
+  const double2* rel;     // [nRows] nonlinear step factors
+  int nRows;
+};
+
+// The Chi3 pump march and one signal propagation (a: the signal's launch, a.pump = p.pt, a.nInst = 1)
+// pipelined on one cluster of eight CTAs (prop_chi3_pipe.cu); N = 4 M, M a power of two from 32 to
+// 1024, p.nRows = 2 a.nZ - 1.  regs (optional): the kernel's registers per thread.
+cudaError_t launch_chi3_pump_signal_spread(const PropArgs& a, const PumpMarchArgs& p, cudaStream_t s,
+                                           int* regs = nullptr);
 cudaError_t launch_green_epilogue(const double2* raw, long long rawStride, int N, int nIn, int nOut,
                                   const double2* blockScale, const uint8_t* blockShift, double2* C,
                                   double2* S, cudaStream_t s);

@@ -362,8 +362,10 @@ class _NonlinearMedium:
     def _set_cluster(self, enable):
         """Spread each propagation of small launches over a 4-CTA cluster: 1 (default) with one point
         per thread on 128..1024-point grids (and the Chi3 pump march there), full grids in the widest
-        form (eight CTAs at 1024 points, sixteen at 2048 and 4096 where the solver has it); 3 the same
-        without the widest forms (full grids on four CTAs up to 1024 points, eight above); 2 four
+        form (eight CTAs at 1024 points, sixteen at 2048 and 4096 where the solver has it), and a Chi3
+        runPumpSimulation followed by runSignalSimulation as one launch of both marches side by side on
+        eight CTAs; 3 the same without the widest forms (full grids on four CTAs up to 1024 points,
+        eight above) and with the two Chi3 marches one after the other; 2 four
         points per thread only (grids of 1024 points and more); 0 one CTA per propagation."""
         _check(_lib.nlm_set_cluster(self._h(), int(enable)))
 

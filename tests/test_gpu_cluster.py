@@ -93,6 +93,14 @@ def test_cluster_every_solver_matches_oracle(nlm, oracle, name, mode):
     a = cases.noise(np.random.default_rng(5), 1024, 0.3)
     med.runSignalSimulation(a, True, 0)
     ref.run_signal_simulation(a, True, 0)
+    if name == "Chi3" and mode == 1:
+        # right after runPumpSimulation: the pump march and the signal side by side, four CTAs of 256
+        # threads each; with the pump in place the signal alone takes the form below
+        sched = med._last_schedule()
+        assert sched["grid"] == 8 and sched["R"] == 1 and sched["block"] == 256
+        first = med.signalTime.copy()
+        med.runSignalSimulation(a, True, 0)
+        assert cases.rel_l2(med.signalTime, first) < 1e-12
     sched = med._last_schedule()
     # full grids at 1024 points: eight CTAs of 128 threads (mode 1), four of 64 with four points each
     assert sched["grid"] == (8 if mode == 1 else 4) and sched["R"] == (1 if mode == 1 else 4)
@@ -310,7 +318,57 @@ def test_spread_config_chi3_n512(nlm, oracle):
     a = cases.noise(np.random.default_rng(1), 512, 1e-3)
     med.runSignalSimulation(a, True)
     ref.run_signal_simulation(a, True)
-    assert med._last_schedule()["R"] == 1 and med._last_schedule()["grid"] == 4
+    # the pump march and the signal side by side on one cluster of eight CTAs
+    assert med._last_schedule()["R"] == 1 and med._last_schedule()["grid"] == 8
     assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(med.pumpFreq, ref.pump_freq[0]) < TOL
     assert cases.rel_l2(med.signalTime, ref.signal_time[0]) < TOL
     assert cases.rel_l2(med.signalFreq, ref.signal_freq[0]) < TOL
+
+
+@pytest.mark.parametrize("n,z,in_time", [(512, 200, True), (128, 2, True), (256, 17, False), (1024, 30, True)])
+def test_pipelined_chi3_pump_signal(nlm, oracle, n, z, in_time):
+    """runPumpSimulation then runSignalSimulation runs both marches on one cluster of eight CTAs (the
+    signal one pump step pair behind, with the solver's DiffEq).  Reading the pump grids between the
+    calls runs the pump march alone first, and the signal then takes the four-CTA kernel with the RK4
+    matrices.  Both orders: the pump grids alike to rounding (the same operations in both kernels; the
+    compiler may pair their multiply-adds differently), the signal grids too, all against the oracle;
+    from the two-step minimum (one phase) up to 1024 points."""
+    kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=n, zPrecision=z)
+    pipe, seq, ref = nlm.Chi3(**kw), nlm.Chi3(**kw), oracle.Chi3(**kw)
+    a = cases.noise(np.random.default_rng(n + z), n, 1e-3)
+    pipe.runPumpSimulation()
+    pipe.runSignalSimulation(a, in_time)
+    assert pipe._last_schedule()["grid"] == 8
+    seq.runPumpSimulation()
+    pump_t = seq.pumpTime                              # runs the march alone
+    seq.runSignalSimulation(a, in_time)
+    assert seq._last_schedule()["grid"] == (8 if n == 1024 else 4)   # eight CTAs of 128 at 1024 points
+    ref.run_pump_simulation()
+    ref.run_signal_simulation(a, in_time)
+    assert cases.rel_l2(pipe.pumpTime, pump_t) < 1e-13 and cases.rel_l2(pipe.pumpFreq, seq.pumpFreq) < 1e-13
+    assert cases.rel_l2(pipe.signalTime, seq.signalTime) < 1e-12
+    assert cases.rel_l2(pipe.signalFreq, seq.signalFreq) < 1e-12
+    assert cases.rel_l2(pipe.pumpTime, ref.pump_time[0]) < TOL
+    assert cases.rel_l2(pipe.signalTime, ref.signal_time[0]) < TOL
+    assert cases.rel_l2(pipe.signalFreq, ref.signal_freq[0]) < TOL
+
+
+def test_deferred_chi3_pump_other_uses(nlm, oracle):
+    """A pump march that runPumpSimulation deferred runs before anything else that reads the pump: a
+    Green's function without rerunning the pump, a batch, and a second runPumpSimulation in between
+    (which replaces the deferred march)."""
+    kw = dict(relativeLength=1, nlLength=1, beta2=-1, pulseType=1, beta3=0, tMax=20, tPrecision=256, zPrecision=40)
+    med, ref = nlm.Chi3(**kw), oracle.Chi3(**kw)
+    ref.run_pump_simulation()
+    med.runPumpSimulation()
+    med.runPumpSimulation()
+    C, S = med.computeGreensFunction(runPump=False)
+    Cr, Sr = ref.compute_greens_function(run_pump=False)
+    assert cases.rel_l2(C, Cr) < TOL and cases.rel_l2(S, Sr) < TOL
+    med.runPumpSimulation()
+    x = cases.noise(np.random.default_rng(3), 3 * 256, 1e-3).reshape(3, 256)
+    out = med.batchSignalSimulation(x, inTimeDomain=True, runPump=False)
+    want = ref.batch_signal_simulation(x, in_time_domain=True, run_pump=False)
+    assert cases.rel_l2(out, want) < TOL
+    assert cases.rel_l2(med.pumpTime, ref.pump_time[0]) < TOL
