@@ -127,6 +127,66 @@ __device__ __forceinline__ void reverse_step(const PropArgs& a, int i, int N, Cl
   }
 }
 
+// Reverse step i in the frequency domain, for the sweep over stored stages: g (this thread's bins of
+// the gradient with respect to the spectrum after the step) becomes the gradient with respect to the
+// spectrum before it.  The transpose of the forward's frequency-domain RK4 sum: with h = N conj(D) g
+// (D the dispersion factors, which carry the 1/N of a transform pair), stage s's spectrum gets w_s h
+// plus the transform of the gradient its time-domain value takes through the next stage's input, and
+// the spectrum before the step h plus the transform of the stage inputs' gradient.  16 transposes.
+template <int C>
+__device__ __forceinline__ void reverse_step_fs(const PropArgs& a, int i, int N, ClusterFFT<C>& f,
+                                                cg::cluster_group& cl, const int (&tn)[C], const int (&fk)[C],
+                                                double2 (&g)[C], const double2* Yi) {
+  const double2* tab = i == a.nZ - 1 ? a.dlast : a.dstep;
+  double2 h[C], gx[C], gke[C];
+#pragma unroll
+  for (int v = 0; v < C; v++) {
+    h[v] = cscale(cmulc(g[v], __ldg(tab + fk[v])), (double)N);
+    gx[v] = czero();
+    gke[v] = czero();
+  }
+  const double* rel = a.relInt + (long long)(i - 1) * 3;
+  for (int s = 3; s >= 0; s--) {
+    const double w = (s == 1 || s == 2) ? 2.0 / 6.0 : 1.0 / 6.0;
+    const double fac = s == 0 ? 0.0 : (s == 3 ? 1.0 : 0.5);
+    const double ri = __ldg(rel + (s == 0 ? 0 : (s == 3 ? 2 : 1)));
+    double2 u[C], gy[C];
+    if (s < 3) {
+#pragma unroll
+      for (int v = 0; v < C; v++) u[v] = gke[v];
+      cluster_fft_fwd<C>(f, u, cl);
+#pragma unroll
+      for (int v = 0; v < C; v++) u[v] = caxpy(u[v], w, h[v]);     // g_k_s (spectrum)
+    } else {
+#pragma unroll
+      for (int v = 0; v < C; v++) u[v] = cscale(h[v], w);
+    }
+#pragma unroll
+    for (int v = 0; v < C; v++) u[v] = cmulc(u[v], __ldg(a.steep + fk[v]));
+    cluster_fft_inv<C>(f, u, cl);                                   // g_u3
+#pragma unroll
+    for (int v = 0; v < C; v++) {
+      const double2 y = Yi[(long long)s * N + tn[v]], u2 = Yi[(long long)(4 + s) * N + tn[v]];
+      gy[v] = cmulc(u[v], u2);     // conj(u2) g_u3
+      u[v] = cmulc(u[v], y);       // g_u2 = conj(y) g_u3
+    }
+    cluster_fft_fwd<C>(f, u, cl);
+#pragma unroll
+    for (int v = 0; v < C; v++) u[v] = cmulc(u[v], __ldg(a.raman + fk[v]));
+    cluster_fft_inv<C>(f, u, cl);                                   // g_u1 (real part)
+#pragma unroll
+    for (int v = 0; v < C; v++) {
+      const double2 y = Yi[(long long)s * N + tn[v]];
+      gy[v] = caxpy(gy[v], 2.0 * ri * u[v].x, y);
+      gx[v] = cadd(gx[v], gy[v]);
+      gke[v] = cscale(gy[v], fac);
+    }
+  }
+  cluster_fft_fwd<C>(f, gx, cl);
+#pragma unroll
+  for (int v = 0; v < C; v++) g[v] = cadd(gx[v], h[v]);
+}
+
 }  // namespace
 
 // a.plan: the local M-point plan (M = N / C, C points per thread); a.tw: the N-point table.
@@ -254,8 +314,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_adjoint_gnlse_stored(const Prop
     const double2* go = d.gout + inst * (long long)N;
 #pragma unroll
     for (int v = 0; v < C; v++) g[v] = cscale(go[fk[v]], (double)N);
-    for (int i = a.nZ - 1; i >= 1; i--) reverse_step<C>(a, i, N, f, cl, tn, fk, g, stg + (long long)(i - 1) * 8 * N);
-    cluster_fft_fwd<C>(f, g, cl);
+    for (int i = a.nZ - 1; i >= 1; i--)
+      reverse_step_fs<C>(a, i, N, f, cl, tn, fk, g, stg + (long long)(i - 1) * 8 * N);
+    // g: the gradient of the input spectrum, times half a dispersion step
 #pragma unroll
     for (int v = 0; v < C; v++) d.gin[inst * (long long)N + fk[v]] = cmulc(g[v], __ldg(a.half + fk[v]));
   }

@@ -3,7 +3,9 @@
 //
 // A z step of the generalised NLSE is 16 transforms inside the four RK4 stages,
 //     k = IFFT[(g0 + g1 w) FFT[ y * IFFT[R~ FFT[rel |y|^2]] ]],
-// plus the dispersion pair; on one SM a single propagation at N=4096 runs about 0.9 ms per step.  Here
+// plus the dispersion pair; on one SM a single propagation at N=4096 runs about 0.9 ms per step.  The
+// stages' spectra are summed in the frequency domain, which drops the fourth stage's inverse transform
+// and the forward transform of the dispersion step: 16 transforms per step.  Here
 // every transform is the cluster's four-step FFT, and the state, the stage input and the RK4 sum stay
 // in registers (C points per thread), in the time-domain ownership of the cluster kernels.
 #include <vector>
@@ -53,6 +55,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
 #pragma unroll
       for (int v = 0; v < R; v++) a.gridF[fk(v)] = cscale(x[v], (double)N);
     }
+    double2 xf[R];   // the state's spectrum (whose unscaled inverse transform is x)
+#pragma unroll
+    for (int v = 0; v < R; v++) xf[v] = x[v];
     cluster_fft_inv<C>(f, x, cl);
     if (a.gridT) {
 #pragma unroll
@@ -67,6 +72,9 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
     for (int i = 1; i < a.nZ; i++) {
       const double* rel = a.relInt + (long long)(i - 1) * 3;
       double2* stg = a.stages ? a.stages + ((inst * (a.nZ - 1) + i - 1) * 8LL) * N : nullptr;
+      // the RK4 sum in the frequency domain (k_propagate_gnlse_pair): each stage's k is formed as a
+      // spectrum and transformed back only as the next stage's input; the step's end is
+      // FFT[x + sum / 6] = N (xf + sum / 6), with no transform.  16 transforms per step.
       double2 k[R], acc[R];
 #pragma unroll
       for (int v = 0; v < R; v++) k[v] = czero();
@@ -95,21 +103,23 @@ __global__ void __launch_bounds__(kMaxThreads) k_propagate_gnlse_cluster(const P
         for (int v = 0; v < R; v++) u[v] = cmul(u[v], y[v]);
         cluster_fft_fwd<C>(f, u, cl);
 #pragma unroll
-        for (int v = 0; v < R; v++) u[v] = cmul(u[v], __ldg(a.steep + fk(v)));
-        cluster_fft_inv<C>(f, u, cl);
-#pragma unroll
         for (int v = 0; v < R; v++) {
-          k[v] = u[v];
+          u[v] = cmul(u[v], __ldg(a.steep + fk(v)));
           acc[v] = s == 0 ? u[v] : caxpy(acc[v], wgt, u[v]);
         }
-      }
+        if (s < 3) {
+          cluster_fft_inv<C>(f, u, cl);
 #pragma unroll
-      for (int v = 0; v < R; v++) x[v] = caxpy(x[v], 1.0 / 6.0, acc[v]);
+          for (int v = 0; v < R; v++) k[v] = u[v];
+        }
+      }
       const bool last = i == a.nZ - 1;
       const double2* table = last ? a.dlast : a.dstep;
-      cluster_fft_fwd<C>(f, x, cl);
 #pragma unroll
-      for (int v = 0; v < R; v++) x[v] = cmul(x[v], __ldg(table + fk(v)));
+      for (int v = 0; v < R; v++) {
+        x[v] = cmul(cscale(caxpy(xf[v], 1.0 / 6.0, acc[v]), (double)N), __ldg(table + fk(v)));
+        if (!last) xf[v] = x[v];
+      }
       if (a.gridF) {
 #pragma unroll
         for (int v = 0; v < R; v++) a.gridF[(long long)i * N + fk(v)] = cscale(x[v], (double)N);
