@@ -157,6 +157,22 @@ nlm_status nlm_batch_device(nlm_medium* m, const void* inputs_dev, size_t rows, 
  * shortest makespan and runs as one CUDA graph, replayed while the plan stays the same. */
 nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const double* const* inputs,
                             int in_time_domain, double* const* outputs);
+/* nlm_ragged_batch's makespan planner alone, with no device work: n_media media given by their grid
+ * (n_freqs), signal mode count, nZSteps, whether the RK4 propagator matrices are used (propagator),
+ * ragged-launch class (media of one class share a launch: one solver and one grid) and available
+ * forms (bit 0: one SM in a ragged launch, bits 1-3: clusters of 4, 8 and 16 SMs); the SMs that
+ * cluster slots may use, the sixteen-SM slots that can run at once, the SMs for slots and ragged
+ * launches together and the ragged CTAs' granularity, as nlm_ragged_batch measures them.  Outputs: the
+ * makespan the plan was made for (microseconds; -1 when no plan fits the SMs at once, the slots then
+ * queueing), per medium its form (0-3) and cluster slot (-1: a ragged launch; a slot's media run one
+ * after another), the ragged launches' CTAs, and (times_us, n_media x 4) each medium's estimated
+ * march time in each form (microseconds, -1 where the form is not available), from the engine's
+ * GB300 per-step table.  No counterpart in the reference (scheduling support). */
+nlm_status nlm_ragged_plan(size_t n_media, const unsigned* n_freqs, const unsigned* n_modes,
+                           const unsigned* n_z_steps, const int* propagator, const int* launch_class,
+                           const unsigned* forms, int cluster_sms, int w16_slots, int pool_sms,
+                           int pool_granularity, double* makespan_us, int* form, int* slot,
+                           int* ragged_ctas, double* times_us);
 /* The plan of the last nlm_ragged_batch call: its estimated makespan (microseconds), the cluster
  * slots of four, eight and sixteen SMs, the CTAs of its one-SM ragged launches, the CUDA-graph
  * captures and replays of ragged calls so far, the SMs the plan could use (those clusters of four can

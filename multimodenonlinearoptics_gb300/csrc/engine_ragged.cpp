@@ -149,6 +149,40 @@ bool plan_for(const std::vector<Job>& jobs, double T, int sms, int maxW16, int p
   return true;
 }
 
+// The plan of a set.  The makespan lies between the longest medium in its fastest form and every
+// medium on one SM one after another.  Feasibility need not be monotonic in T (a medium at the edge of
+// T moves between forms), so the targets are scanned upward in steps of 0.25 % and the first feasible
+// one is taken.  When none fits the SMs at once (more cluster-only media than they hold), every medium
+// takes its fastest form, each cluster medium a slot of its own, and the slots queue for SMs: false.
+bool plan_set(const std::vector<Job>& jobs, int budget, int maxW16, int poolBudget, int gran, Plan* out) {
+  double lo = 0, hi = 0;
+  for (const Job& j : jobs) {
+    lo = std::max(lo, j.best());
+    hi += j.t[kOne] >= 0 ? j.t[kOne] : j.best();
+  }
+  for (double T = lo; lo > 0 && T <= hi * 1.0001; T *= 1.0025)
+    if (plan_for(jobs, T, budget, maxW16, poolBudget, gran, out)) return true;
+  if (plan_for(jobs, hi, budget, maxW16, poolBudget, gran, out)) return true;
+  Plan plan;
+  plan.form.assign(jobs.size(), kOne);
+  for (size_t i = 0; i < jobs.size(); i++) {
+    int f = kOne;
+    for (int c = 0; c < kForms; c++)
+      if (jobs[i].t[c] >= 0 && (jobs[i].t[f] < 0 || jobs[i].t[c] < jobs[i].t[f])) f = c;
+    plan.form[i] = f;
+    if (f != kOne) {
+      plan.slots.push_back({i});
+      plan.slotForm.push_back(f);
+    } else {
+      plan.classCTAs[jobs[i].cls] += 1;
+    }
+  }
+  plan.poolSMs = 0;
+  for (auto& kv : plan.classCTAs) plan.poolSMs += (kv.second = (kv.second + 3) / 4 * 4);
+  *out = plan;
+  return false;
+}
+
 // SMs that clusters of four CTAs, each CTA alone on its SM, can hold at once: every cluster sits in
 // one GPC, so the SMs of a GPC beyond a multiple of four stay out of reach (on a GB300 with 19 SMs per
 // GPC, 128 of the 152).  Measured once per process with the occupancy API on `fn`.
@@ -308,19 +342,11 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     const int budget = std::max(4, cluster_capacity_sms(ms[fused[0]]->findKernel(kKindRagged, ms[fused[0]]->solver, 8)->fn,
                                                         sms));
     g_capacityUsed = budget;
-    double lo = 0, hi = 0;
-    for (const Job& j : jobs) {
-      lo = std::max(lo, j.best());
-      hi += j.t[kOne] >= 0 ? j.t[kOne] : j.best();
-    }
-    // feasibility need not be monotonic in T (a medium at the edge of T moves between forms), so the
-    // targets are scanned upward in steps of 0.25 % and the first feasible one is taken.  The plans of
-    // recent sets are kept: a repeated call (the same estimates, budget and slot capacity) reuses its
-    // plan without the scan.
     // The ragged launches run without clusters, so their CTAs take any SM the slots leave, the SMs of
     // a GPC beyond its clusters' groups included: the slots must fit in the cluster budget, the slots
     // and the ragged CTAs together in all the device's SMs.  NLM_RAGGED_POOL_CLUSTERS=1 launches them
-    // in clusters of four within the budget instead.
+    // in clusters of four within the budget instead.  The plans of recent sets are kept: a repeated
+    // call (the same estimates, budget and slot capacity) reuses its plan without the scan.
     const bool clusteredPool = std::getenv("NLM_RAGGED_POOL_CLUSTERS") != nullptr;
     const int gran = clusteredPool ? 4 : 1, poolBudget = clusteredPool ? budget : sms;
     std::vector<double> planKey{(double)budget, (double)maxW16, (double)clusteredPool};
@@ -329,38 +355,12 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
       planKey.insert(planKey.end(), j.t, j.t + kForms);
     }
     Plan plan;
-    bool planned = false;
     auto cached = g_planCache.find(planKey);
     if (cached != g_planCache.end()) {
       plan = cached->second;
-      planned = true;
-    }
-    for (double T = lo; T <= hi * 1.0001 && !planned; T *= 1.0025)
-      planned = plan_for(jobs, T, budget, maxW16, poolBudget, gran, &plan);
-    if (!planned) planned = plan_for(jobs, hi, budget, maxW16, poolBudget, gran, &plan);
-    if (planned && cached == g_planCache.end()) {
+    } else if (plan_set(jobs, budget, maxW16, poolBudget, gran, &plan)) {
       if (g_planCache.size() >= 16) g_planCache.erase(g_planCache.begin());
       g_planCache[planKey] = plan;
-    }
-    if (!planned) {
-      // no plan fits the SMs at once (more cluster-only media than they hold): every medium in its
-      // fastest form, each cluster medium in a slot of its own, the slots queueing for SMs
-      plan = Plan{};
-      plan.form.assign(jobs.size(), kOne);
-      for (size_t i = 0; i < jobs.size(); i++) {
-        int f = kOne;
-        for (int c = 0; c < kForms; c++)
-          if (jobs[i].t[c] >= 0 && (jobs[i].t[f] < 0 || jobs[i].t[c] < jobs[i].t[f])) f = c;
-        plan.form[i] = f;
-        if (f != kOne) {
-          plan.slots.push_back({i});
-          plan.slotForm.push_back(f);
-        } else {
-          plan.classCTAs[jobs[i].cls] += 1;
-        }
-      }
-      plan.poolSMs = 0;
-      for (auto& kv : plan.classCTAs) plan.poolSMs += (kv.second = (kv.second + 3) / 4 * 4);
     }
 
     // The plan's one-SM CTAs are the fewest that fit its target; the SMs the slots leave free all go to
@@ -574,6 +574,44 @@ nlm_status nlm_ragged_batch(nlm_medium* const* media, size_t n_media, const doub
     for (const RaggedLaunch& rl : raggedLaunches) g_lastRagged.raggedCTAs += rl.grid;
     for (size_t k : fused)
       std::memcpy(outputs[k], g_ragged.hout.p + outOff[k], (size_t)ms[k]->nSignal * ms[k]->N * sizeof(double2));
+  });
+}
+
+nlm_status nlm_ragged_plan(size_t n_media, const unsigned* n_freqs, const unsigned* n_modes,
+                           const unsigned* n_z_steps, const int* propagator, const int* launch_class,
+                           const unsigned* forms, int cluster_sms, int w16_slots, int pool_sms, int pool_granularity,
+                           double* makespan_us, int* form, int* slot, int* ragged_ctas, double* times_us) {
+  return guarded([&] {
+    if (n_media == 0 || !n_freqs || !n_modes || !n_z_steps || !propagator || !launch_class || !forms)
+      throw std::invalid_argument("ragged plan: no media");
+    if (cluster_sms < 0 || w16_slots < 0 || pool_sms < 1 || pool_granularity < 1)
+      throw std::invalid_argument("ragged plan: invalid SM budgets");
+    std::vector<Job> jobs;
+    for (size_t k = 0; k < n_media; k++) {
+      if (n_freqs[k] < 2) throw std::invalid_argument("ragged plan: a grid needs at least 2 points");
+      Job j{k, launch_class[k], {-1, -1, -1, -1}};
+      const double steps = (double)(n_z_steps[k] > 1 ? n_z_steps[k] - 1 : 1);
+      for (int c = 0; c < kForms; c++) {
+        if (!((forms[k] >> c) & 1u)) continue;
+        const double t = step_us(c, n_freqs[k], n_modes[k], propagator[k] != 0);
+        if (t >= 0) j.t[c] = t * steps;
+      }
+      if (j.best() < 0) throw std::invalid_argument("ragged plan: a medium has no form for its grid");
+      if (times_us)
+        for (int c = 0; c < kForms; c++) times_us[k * kForms + c] = j.t[c];
+      jobs.push_back(j);
+    }
+    Plan plan;
+    const bool fits = plan_set(jobs, cluster_sms, w16_slots, pool_sms, pool_granularity, &plan);
+    if (makespan_us) *makespan_us = fits ? plan.makespan : -1.0;
+    if (ragged_ctas) *ragged_ctas = plan.poolSMs;
+    for (size_t k = 0; k < n_media; k++) {
+      if (form) form[k] = plan.form[k];
+      if (slot) slot[k] = -1;
+    }
+    if (slot)
+      for (size_t q = 0; q < plan.slots.size(); q++)
+        for (size_t i : plan.slots[q]) slot[i] = (int)q;
   });
 }
 

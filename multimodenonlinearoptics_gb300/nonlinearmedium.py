@@ -64,6 +64,7 @@ def _load():
         "nlm_ragged_batch": (i, [P(vp), sz, P(P(d)), i, P(P(d))]),
         "nlm_ragged_last_plan": (i, [P(d), P(i), P(i), P(i), P(i), P(ctypes.c_long), P(ctypes.c_long), P(i), P(i),
                                      P(d)]),
+        "nlm_ragged_plan": (i, [sz, P(u), P(u), P(u), P(i), P(i), P(u), i, i, i, i, P(d), P(i), P(i), P(i), P(d)]),
         "nlm_get_grid": (i, [vp, i, u, P(P(d)), P(sz), P(sz)]),
         "nlm_get_axis": (i, [vp, i, u, P(P(d)), P(sz)]),
         "nlm_cascade_create": (i, [P(vp), sz, P(u), P(sz), sz, i, P(vp)]),
@@ -172,6 +173,34 @@ def ragged_last_plan():
             "slots_w16": w16.value, "ragged_ctas": ctas.value, "graph_captures": cap.value,
             "graph_replays": rep.value, "sm_budget": budget.value, "w16_capacity": w16cap.value,
             "gpu_ms": gpu.value}
+
+
+def ragged_plan(n_freqs, n_modes, n_z_steps, propagator, launch_class, forms, cluster_sms=128, w16_slots=7,
+                pool_sms=152, pool_granularity=1):
+    """ragged_batch's makespan planner alone, with no device work (no counterpart in the reference).
+
+    Per medium: its grid, signal mode count, nZSteps, whether its RK4 matrices are used, its
+    ragged-launch class (one solver and one grid) and a mask of its available forms (bit 0 one SM,
+    bits 1-3 clusters of 4, 8 and 16 SMs).  The budgets default to a GB300's.  Returns the plan's
+    makespan in microseconds (None when no plan fits the SMs at once), each medium's form and cluster
+    slot (-1: a ragged launch), the ragged launches' CTAs and each medium's estimated march time per
+    form (microseconds, n x 4; -1 where the form is not available)."""
+    n = len(n_freqs)
+    arrs = [np.ascontiguousarray(v, dtype=t) for v, t in
+            ((n_freqs, np.uint32), (n_modes, np.uint32), (n_z_steps, np.uint32), (propagator, np.int32),
+             (launch_class, np.int32), (forms, np.uint32))]
+    if any(a.shape != (n,) for a in arrs):
+        raise ValueError("every per-medium array needs one entry per medium")
+    ms, ctas = ctypes.c_double(), ctypes.c_int()
+    form, slot, times = np.empty(n, np.int32), np.empty(n, np.int32), np.empty((n, 4), np.float64)
+    ptr = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    _check(_lib.nlm_ragged_plan(n, ptr(arrs[0], ctypes.c_uint), ptr(arrs[1], ctypes.c_uint),
+                                ptr(arrs[2], ctypes.c_uint), ptr(arrs[3], ctypes.c_int), ptr(arrs[4], ctypes.c_int),
+                                ptr(arrs[5], ctypes.c_uint), int(cluster_sms), int(w16_slots), int(pool_sms),
+                                int(pool_granularity), ctypes.byref(ms), ptr(form, ctypes.c_int),
+                                ptr(slot, ctypes.c_int), ctypes.byref(ctas), ptr(times, ctypes.c_double)))
+    return {"makespan_us": ms.value if ms.value >= 0 else None, "form": form, "slot": slot,
+            "ragged_ctas": ctas.value, "times_us": times}
 
 
 def fp64_peak_tflops():
