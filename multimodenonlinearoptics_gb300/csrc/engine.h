@@ -1242,13 +1242,14 @@ struct Medium {
     return PumpMarchArgs{pumpFreq.p, pumpTime.p, q.env.p, q.half.p, q.dstep.p, q.back.p, q.rel.p, (int)nZP};
   }
 
-  // Runs a deferred pump march alone (four CTAs, k_pump_chi3_spread) and waits for it.
+  // Runs a deferred pump march alone (four CTAs, k_pump_chi3_spread) and waits for it.  The march stays
+  // deferred if its launch fails, so the next reader tries again rather than reading stale grids.
   void flushPump() {
     if (!deferredPump.pending) return;
-    deferredPump.pending = false;
     const PumpMarchArgs p = deferredPumpArgs();
     ck(launch_pump_chi3_spread(p.pf, p.pt, p.env, p.halfP, p.dstepP, p.backP, p.rel, p.nRows, (int)N, tw, stream),
        "chi3 pump (spread)");
+    deferredPump.pending = false;
     launches++;
     ck(cudaStreamSynchronize(stream), "chi3 pump");
   }
@@ -2599,7 +2600,6 @@ struct Medium {
     a.work = nullptr;
     a.prop = nullptr;
     const PumpMarchArgs p = deferredPumpArgs();
-    deferredPump.pending = false;
     lastSchedule = Schedule{8, M, 1, (size_t)spread_smem_per_point(4) * M * sizeof(double2), 1, 1};
     lastR = 1;
     lastTuned = 0;
@@ -2609,6 +2609,7 @@ struct Medium {
       ck(cudaEventRecord(ev0, stream), "event");
     }
     ck(launch_chi3_pump_signal_spread(a, p, stream, &lastRegs), "chi3 pump + signal (cluster of eight)");
+    deferredPump.pending = false;   // only once launched: a failed launch leaves the march deferred
     launches++;
     if (timeKernels) {
       ck(cudaEventRecord(ev1, stream), "event");
